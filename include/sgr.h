@@ -1,0 +1,245 @@
+/*
+ * sgr.h - C ABI of the GB300 surfel rasteriser (libsgr.so).
+ *
+ * The library implements the differentiable 2D-Gaussian surfel rasteriser
+ * of PartGS in both of its variants ("plain": submodules/diff-surfel-
+ * rasterization, "part": submodules/diff-surfel-rasterization_part) and the
+ * superquadric-to-surfel binding that feeds it.  No C++ or torch type crosses
+ * this boundary: every argument is a plain pointer, an integer, a float or a
+ * struct of those.  Device pointers are CUDA global-memory addresses; every
+ * call enqueues its work on the caller's stream and never synchronises the
+ * host, so whole steps can be captured in a CUDA graph.
+ *
+ * Reference interfaces replaced (paths relative to the PartGS repository):
+ *   sgr_forward_geometry + sgr_forward_raster
+ *       -> _C.rasterize_gaussians           submodules/diff-surfel-rasterization/ext.cpp:16,
+ *          RasterizeGaussiansCUDA           submodules/diff-surfel-rasterization/rasterize_points.cu:39-134
+ *          (part variant: submodules/diff-surfel-rasterization_part/rasterize_points.cu:39-145)
+ *   sgr_backward
+ *       -> _C.rasterize_gaussians_backward  submodules/diff-surfel-rasterization/ext.cpp:17,
+ *          RasterizeGaussiansBackwardCUDA   submodules/diff-surfel-rasterization/rasterize_points.cu:136-233
+ *          (part variant: submodules/diff-surfel-rasterization_part/rasterize_points.cu:148-252)
+ *   sgr_mark_visible
+ *       -> _C.mark_visible                  submodules/diff-surfel-rasterization/ext.cpp:18,
+ *          markVisible                      submodules/diff-surfel-rasterization/rasterize_points.cu:235-254
+ *   sgr_bind_forward / sgr_bind_backward
+ *       -> BlockGaussianModel.prepare_scaling_rot and its autograd backward
+ *          games/block_mesh_splatting/scene/block_gaussian_model.py:178-256
+ *
+ * The reference forward sizes its scratch buffers from the number of
+ * (surfel, tile) keys, which it learns with a blocking device-to-host copy
+ * (cuda_rasterizer/rasterizer_impl.cu:282).  Here the forward is split in
+ * two calls instead: sgr_forward_geometry computes the key count on the
+ * device (and, if asked, copies it to pinned host memory); the caller sizes
+ * the key list from it, or passes a capacity it chose earlier, to
+ * sgr_forward_raster.  A key count above the capacity is reported through
+ * the device status word (SGR_FLAG_KEY_OVERFLOW), never by faulting.
+ */
+#ifndef SGR_H_INCLUDED
+#define SGR_H_INCLUDED
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SGR_ABI_VERSION 1
+
+/* status codes returned by every entry point */
+#define SGR_OK 0
+#define SGR_ERR_INVALID_ARGUMENT 1   /* a null pointer, a negative size or inconsistent tables */
+#define SGR_ERR_UNSUPPORTED 2        /* a combination the path does not define */
+#define SGR_ERR_SEMANTIC_CHANNELS 3  /* more than SGR_MAX_SEMANTICS semantic channels */
+#define SGR_ERR_WORKSPACE 4          /* a workspace smaller than sgr_query_sizes asked for */
+#define SGR_ERR_KEY_CAPACITY 5       /* key capacity above 2^31 - 1 or below zero */
+#define SGR_ERR_CUDA 6               /* a CUDA runtime call failed; see sgr_last_error_message */
+
+/* bits of the device status word (sgr_sizes.off_status), set by kernels */
+#define SGR_FLAG_KEY_OVERFLOW 1u     /* more (surfel, tile) keys than the key capacity */
+#define SGR_FLAG_PREFILTERED 2u      /* prefiltered was set but a surfel failed the near test
+                                        (the reference traps here, cuda_rasterizer/auxiliary.h:200-206) */
+
+#define SGR_VARIANT_PLAIN 0
+#define SGR_VARIANT_PART 1
+#define SGR_MAX_SEMANTICS 16         /* the part variant's fixed register array, P1 forward.cu:317 */
+#define SGR_TILE 16                  /* tile edge in pixels, cuda_rasterizer/config.h:15-16 */
+
+/* One scene: a contiguous range of surfels seen by a contiguous range of views. */
+typedef struct sgr_scene_desc {
+    int32_t surfel_offset;
+    int32_t surfel_count;
+    int32_t view_begin;
+    int32_t view_count;
+} sgr_scene_desc;
+
+/* One view.  record_offset is the first of this view's surfel_count per-view
+ * records; records of all views are packed back to back. */
+typedef struct sgr_view_desc {
+    int32_t scene;
+    int32_t record_offset;
+    float tanfovx;
+    float tanfovy;
+} sgr_view_desc;
+
+/* A batch of views over one or more scenes.  With one scene and one view
+ * this is exactly the reference's single-view call. */
+typedef struct sgr_batch {
+    int32_t variant;             /* SGR_VARIANT_PLAIN or SGR_VARIANT_PART */
+    int32_t num_scenes;
+    int32_t num_views;
+    int32_t height;              /* image size, shared by every view */
+    int32_t width;
+    int32_t num_surfels;         /* P: surfels of all scenes */
+    int32_t num_records;         /* R: sum over views of their scene's surfel count */
+    int32_t sh_degree;           /* active SH degree D */
+    int32_t sh_coeffs;           /* M coefficients per surfel; 0 when colors_precomp is given */
+    int32_t semantic_channels;   /* S, part variant only, 0..SGR_MAX_SEMANTICS */
+    int32_t prefiltered;
+    float scale_modifier;
+    /* device tables */
+    const sgr_scene_desc* scenes;    /* [num_scenes] */
+    const sgr_view_desc* views;      /* [num_views] */
+    const float* viewmatrix;         /* [V,16] world_view_transform, row-major as torch stores it */
+    const float* projmatrix;         /* [V,16] full_proj_transform */
+    const float* campos;             /* [V,3] */
+    const float* background;         /* [3] */
+    /* device surfel attributes, contiguous float32 */
+    const float* means3D;            /* [P,3] */
+    const float* scales;             /* [P,2] or NULL with transmat_precomp */
+    const float* rotations;          /* [P,4] (w,x,y,z) or NULL with transmat_precomp */
+    const float* opacities;          /* [P] */
+    const float* shs;                /* [P,M,3] or NULL */
+    const float* colors_precomp;     /* [P,3] or NULL */
+    const float* transmat_precomp;   /* [P,9] or NULL (single-view batches only) */
+    const float* semantics;          /* [P,S] or NULL */
+} sgr_batch;
+
+/* Workspace sizes and the layout of the geometry workspace. */
+typedef struct sgr_sizes {
+    size_t geom_bytes;           /* kept from the forward to the backward */
+    size_t list_bytes;           /* kept: the sorted (surfel, tile) list, key_capacity entries */
+    size_t fwd_scratch_bytes;    /* forward only */
+    size_t bwd_scratch_bytes;    /* backward only */
+    /* byte offsets inside the geometry workspace */
+    size_t off_records;          /* float4[R][5] per-view surfel records */
+    size_t off_radii;            /* int32[R] */
+    size_t off_tiles_touched;    /* uint32[R] */
+    size_t off_depth_order;      /* uint32[R] record ids in (view, depth, id) order */
+    size_t off_offsets;          /* uint64[R] inclusive scan of tiles_touched in that order */
+    size_t off_ranges;           /* uint32[V*tiles][2] per-tile [start, end) of the list */
+    size_t off_final_T;          /* float[V][3][H][W]: T, M1, M2 */
+    size_t off_n_contrib;        /* uint32[V][2][H][W]: last contributor, median contributor */
+    size_t off_status;           /* uint64 key count, uint32 status flags */
+    int32_t tiles_x, tiles_y;
+    int32_t tile_key_bits;
+} sgr_sizes;
+
+/* Per-view outputs of the forward.  color [V,3,H,W], others [V,7,H,W]
+ * (plain: expected depth, alpha, normal xyz, median depth, distortion) or
+ * [V,8,H,W] (part: the same plus median weight), semantic [V,S,H,W] (part),
+ * radii [R]. */
+typedef struct sgr_fwd_outputs {
+    float* color;
+    float* others;
+    float* semantic;
+    int32_t* radii;
+} sgr_fwd_outputs;
+
+/* Upstream gradients, same shapes as the forward outputs. */
+typedef struct sgr_bwd_inputs {
+    const float* dL_dcolor;
+    const float* dL_dothers;
+    const float* dL_dsemantic;   /* part variant, or NULL */
+} sgr_bwd_inputs;
+
+/* Gradients.  Per-surfel tensors are summed over the views of the surfel's
+ * scene; dL_dmeans2D and dL_dtransmat are per view record.  Every element
+ * is written (no zero-fill needed); NULL skips an output. */
+typedef struct sgr_bwd_outputs {
+    float* dL_dmeans2D;          /* [R,3] densification proxy (P0 backward.cu:626-629) */
+    float* dL_dcolors;           /* [P,3] */
+    float* dL_dopacity;          /* [P] */
+    float* dL_dmeans3D;          /* [P,3] */
+    float* dL_dtransmat;         /* [R,9] */
+    float* dL_dsh;               /* [P,M,3] */
+    float* dL_dscales;           /* [P,2] */
+    float* dL_drotations;        /* [P,4] */
+    float* dL_dsemantics;        /* [P,S] */
+} sgr_bwd_outputs;
+
+/* Library identity. */
+int sgr_abi_version(void);
+const char* sgr_status_string(int status);
+/* Message of the last failing CUDA call on this host thread ("" if none). */
+const char* sgr_last_error_message(void);
+
+/* Workspace sizes for a batch and a key capacity (0 when only the geometry
+ * phase will run).  Replaces the sizing in required<GeometryState> /
+ * required<ImageState> / required<BinningState>,
+ * cuda_rasterizer/rasterizer_impl.cu:155-194. */
+int sgr_query_sizes(const sgr_batch* batch, int64_t key_capacity, sgr_sizes* out);
+
+/* Phase 1 of the forward: per-view preprocess (transform, screen bounds,
+ * SH colour), depth order, key offsets and the key count.  If
+ * num_keys_host is not NULL it must be pinned host memory; the key count
+ * is copied there asynchronously on the stream.  fwd_scratch must hold
+ * sizes.fwd_scratch_bytes for key_capacity 0 or more. */
+int sgr_forward_geometry(const sgr_batch* batch, void* geom, void* fwd_scratch, size_t fwd_scratch_bytes,
+                         int64_t* num_keys_host, void* stream);
+
+/* Phase 2: key duplication, stable tile sort, tile ranges and the blend. */
+int sgr_forward_raster(const sgr_batch* batch, void* geom, void* lists, int64_t key_capacity,
+                       void* fwd_scratch, size_t fwd_scratch_bytes, const sgr_fwd_outputs* out, void* stream);
+
+/* Backward of both phases. */
+int sgr_backward(const sgr_batch* batch, const void* geom, const void* lists, int64_t key_capacity,
+                 void* bwd_scratch, size_t bwd_scratch_bytes, const sgr_bwd_inputs* in,
+                 const sgr_bwd_outputs* out, void* stream);
+
+/* Near-plane visibility of P points in one view (present: uint8[P]). */
+int sgr_mark_visible(int32_t P, const float* means3D, const float* viewmatrix, const float* projmatrix,
+                     uint8_t* present, void* stream);
+
+/* ---- superquadric binding ---------------------------------------------- */
+
+/* Shapes of the binding: B superquadrics, each with V vertices on an
+ * (eta, omega) parameter set, F triangles, N surfels per triangle. */
+typedef struct sgr_bind_args {
+    int32_t B, V, F, N;
+    float ratio_block_scene;     /* vertex scale of the unit superquadric */
+    float scale_block_min;       /* added to exp(sq_s) */
+    const float* sq_s;           /* [B,3] log semi-axes */
+    const float* sq_r;           /* [B,4] unnormalised quaternion (w,x,y,z) */
+    const float* sq_t;           /* [B,3] translation */
+    const float* sq_eps;         /* [B,2] exponent logits */
+    const float* eta;            /* [B,V] */
+    const float* omega;          /* [B,V] */
+    const int32_t* faces;        /* [B,F,3] vertex ids */
+    const float* sq_occ;         /* [B] occupancy logits */
+    const float* alpha;          /* [B*F,N,3] raw barycentric weights (relu + normalise inside) */
+    const float* scale;          /* [B,F*N] surfel scale factors */
+} sgr_bind_args;
+
+/* Forward: xyz [B*F*N,3], log_scaling [B*F*N,2], rotation [B*F*N,4]
+ * (the tensors prepare_scaling_rot stores in _xyz, _scaling, _rotation,
+ * block_gaussian_model.py:198-256) and opacity [B*F*N] (get_opacity,
+ * block_gaussian_model.py:107-109).  NULL skips an output. */
+int sgr_bind_forward(const sgr_bind_args* a, float* xyz, float* log_scaling, float* rotation, float* opacity,
+                     void* stream);
+
+/* Backward: from dL/d_xyz, dL/d_scaling (of the log scaling), dL/d_rotation
+ * and dL/d_opacity (each may be NULL for zero) to dL/dsq_s, dL/dsq_r,
+ * dL/dsq_t, dL/dsq_eps and dL/dsq_occ, which are overwritten.  scratch must
+ * hold sgr_bind_scratch_bytes(a) bytes. */
+size_t sgr_bind_scratch_bytes(const sgr_bind_args* a);
+int sgr_bind_backward(const sgr_bind_args* a, const float* d_xyz, const float* d_log_scaling,
+                      const float* d_rotation, const float* d_opacity, float* d_sq_s, float* d_sq_r,
+                      float* d_sq_t, float* d_sq_eps, float* d_sq_occ, void* scratch, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SGR_H_INCLUDED */

@@ -1,0 +1,335 @@
+// C ABI of the surfel rasteriser: argument checks, workspace layout and the
+// launch sequence of each phase.
+#include <cub/device/device_radix_sort.cuh>
+#include <cub/device/device_scan.cuh>
+
+#include <cstdio>
+#include <cstring>
+#include <string>
+
+#include "sgr_kernels.cuh"
+
+namespace sgr {
+namespace {
+
+thread_local std::string g_last_error;
+
+int cuda_fail(cudaError_t e, const char* what) {
+  g_last_error = std::string(what) + ": " + cudaGetErrorString(e);
+  return SGR_ERR_CUDA;
+}
+
+#define SGR_CUDA(call)                                  \
+  do {                                                  \
+    cudaError_t e_ = (call);                            \
+    if (e_ != cudaSuccess) return cuda_fail(e_, #call); \
+  } while (0)
+
+constexpr size_t kAlign = 256;
+size_t align_up(size_t x) { return (x + kAlign - 1) & ~(kAlign - 1); }
+
+int bit_length(unsigned long long n) {
+  int b = 0;
+  while (n) {
+    ++b;
+    n >>= 1;
+  }
+  return b;
+}
+
+// Byte layout of the forward scratch.
+struct ScratchLayout {
+  size_t depth_keys, depth_vals, depth_keys_sorted, temp_a, temp_a_bytes;
+  size_t keys, vals, keys_sorted, temp_b, temp_b_bytes;
+  size_t end_a, end;
+};
+
+int check_batch(const sgr_batch* b) {
+  if (!b) return SGR_ERR_INVALID_ARGUMENT;
+  if (b->variant != SGR_VARIANT_PLAIN && b->variant != SGR_VARIANT_PART) return SGR_ERR_INVALID_ARGUMENT;
+  if (b->num_scenes < 1 || b->num_views < 1 || b->height < 1 || b->width < 1) return SGR_ERR_INVALID_ARGUMENT;
+  if (b->num_surfels < 0 || b->num_records < 0) return SGR_ERR_INVALID_ARGUMENT;
+  if (b->semantic_channels < 0) return SGR_ERR_INVALID_ARGUMENT;
+  if (b->semantic_channels > SGR_MAX_SEMANTICS) return SGR_ERR_SEMANTIC_CHANNELS;
+  if (b->variant == SGR_VARIANT_PLAIN && b->semantic_channels != 0) return SGR_ERR_INVALID_ARGUMENT;
+  if (!b->scenes || !b->views || !b->viewmatrix || !b->projmatrix || !b->campos || !b->background)
+    return SGR_ERR_INVALID_ARGUMENT;
+  if (b->num_surfels > 0) {
+    if (!b->means3D || !b->opacities) return SGR_ERR_INVALID_ARGUMENT;
+    if ((b->shs == nullptr) == (b->colors_precomp == nullptr)) return SGR_ERR_INVALID_ARGUMENT;
+    if (b->transmat_precomp == nullptr && (!b->scales || !b->rotations)) return SGR_ERR_INVALID_ARGUMENT;
+    if (b->transmat_precomp != nullptr && b->num_views != 1) return SGR_ERR_UNSUPPORTED;
+    if (b->shs != nullptr && (b->sh_coeffs < 1 || b->sh_coeffs > kMaxShCoeffs)) return SGR_ERR_UNSUPPORTED;
+    if (b->shs != nullptr && (b->sh_degree < 0 || b->sh_degree > 3 || (b->sh_degree + 1) * (b->sh_degree + 1) > b->sh_coeffs))
+      return SGR_ERR_UNSUPPORTED;
+    if (b->semantic_channels > 0 && !b->semantics) return SGR_ERR_INVALID_ARGUMENT;
+    if ((size_t)reinterpret_cast<uintptr_t>(b->rotations) % 16 != 0) return SGR_ERR_INVALID_ARGUMENT;
+  }
+  return SGR_OK;
+}
+
+void tile_grid(const sgr_batch* b, int& gx, int& gy) {
+  gx = (b->width + kTile - 1) / kTile;
+  gy = (b->height + kTile - 1) / kTile;
+}
+
+int tile_key_bits(const sgr_batch* b) {
+  int gx, gy;
+  tile_grid(b, gx, gy);
+  return bit_length((unsigned long long)gx * gy * b->num_views);
+}
+
+int depth_key_bits(const sgr_batch* b) { return 32 + bit_length((unsigned long long)(b->num_views - 1)); }
+
+int scratch_layout(const sgr_batch* b, long long cap, ScratchLayout& L) {
+  const size_t R = (size_t)b->num_records;
+  size_t o = 0;
+  L.depth_keys = o; o = align_up(o + R * 8);
+  L.depth_vals = o; o = align_up(o + R * 4);
+  L.depth_keys_sorted = o; o = align_up(o + R * 8);
+  size_t sort_a = 0, scan_a = 0;
+  if (R > 0) {
+    SGR_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, sort_a, (const unsigned long long*)nullptr,
+                                             (unsigned long long*)nullptr, (const uint32_t*)nullptr,
+                                             (uint32_t*)nullptr, (int64_t)R, 0, depth_key_bits(b)));
+    SGR_CUDA(cub::DeviceScan::InclusiveSum(nullptr, scan_a, (unsigned long long*)nullptr,
+                                           (unsigned long long*)nullptr, (int64_t)R));
+  }
+  L.temp_a = o;
+  L.temp_a_bytes = std::max(sort_a, scan_a);
+  o = align_up(o + L.temp_a_bytes);
+  L.end_a = o;
+  const size_t K = (size_t)std::max(0LL, cap);
+  L.keys = o; o = align_up(o + K * 4);
+  L.vals = o; o = align_up(o + K * 4);
+  L.keys_sorted = o; o = align_up(o + K * 4);
+  size_t sort_b = 0;
+  if (K > 0)
+    SGR_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, sort_b, (const uint32_t*)nullptr, (uint32_t*)nullptr,
+                                             (const uint32_t*)nullptr, (uint32_t*)nullptr, (int64_t)K, 0,
+                                             std::max(1, tile_key_bits(b))));
+  L.temp_b = o;
+  L.temp_b_bytes = sort_b;
+  o = align_up(o + sort_b);
+  L.end = o;
+  return SGR_OK;
+}
+
+int sizes_impl(const sgr_batch* b, long long cap, sgr_sizes* s) {
+  int gx, gy;
+  tile_grid(b, gx, gy);
+  const size_t R = (size_t)b->num_records;
+  const size_t V = (size_t)b->num_views;
+  const size_t HW = (size_t)b->height * b->width;
+  size_t o = 0;
+  s->off_records = o; o = align_up(o + R * kRecF4 * 16);
+  s->off_radii = o; o = align_up(o + R * 4);
+  s->off_tiles_touched = o; o = align_up(o + R * 4);
+  s->off_depth_order = o; o = align_up(o + R * 4);
+  s->off_offsets = o; o = align_up(o + R * 8);
+  s->off_ranges = o; o = align_up(o + V * gx * gy * 8);
+  s->off_final_T = o; o = align_up(o + V * 3 * HW * 4);
+  s->off_n_contrib = o; o = align_up(o + V * 2 * HW * 4);
+  s->off_status = o; o = align_up(o + sizeof(Status));
+  s->geom_bytes = o;
+  s->list_bytes = align_up((size_t)std::max(0LL, cap) * 4);
+  ScratchLayout L;
+  int rc = scratch_layout(b, cap, L);
+  if (rc) return rc;
+  s->fwd_scratch_bytes = L.end;
+  s->bwd_scratch_bytes = align_up(R * kGradF * 4);
+  s->tiles_x = gx;
+  s->tiles_y = gy;
+  s->tile_key_bits = tile_key_bits(b);
+  return SGR_OK;
+}
+
+GeomView geom_view(const sgr_batch* b, const sgr_sizes& s, void* geom, void* scratch, const ScratchLayout* L) {
+  char* gp = static_cast<char*>(geom);
+  char* sp = static_cast<char*>(scratch);
+  GeomView g;
+  g.records = reinterpret_cast<float4*>(gp + s.off_records);
+  g.radii = reinterpret_cast<int*>(gp + s.off_radii);
+  g.tiles_touched = reinterpret_cast<uint32_t*>(gp + s.off_tiles_touched);
+  g.depth_order = reinterpret_cast<uint32_t*>(gp + s.off_depth_order);
+  g.offsets = reinterpret_cast<unsigned long long*>(gp + s.off_offsets);
+  g.ranges = reinterpret_cast<uint2*>(gp + s.off_ranges);
+  g.final_T = reinterpret_cast<float*>(gp + s.off_final_T);
+  g.n_contrib = reinterpret_cast<uint32_t*>(gp + s.off_n_contrib);
+  g.status = reinterpret_cast<Status*>(gp + s.off_status);
+  g.depth_keys = (sp && L) ? reinterpret_cast<unsigned long long*>(sp + L->depth_keys) : nullptr;
+  g.depth_vals = (sp && L) ? reinterpret_cast<uint32_t*>(sp + L->depth_vals) : nullptr;
+  g.depth_keys_sorted = (sp && L) ? reinterpret_cast<unsigned long long*>(sp + L->depth_keys_sorted) : nullptr;
+  g.tiles_x = s.tiles_x;
+  g.tiles_y = s.tiles_y;
+  return g;
+}
+
+__global__ void k_gather_counts(const uint32_t* __restrict__ order, const uint32_t* __restrict__ touched,
+                                unsigned long long* __restrict__ out, long long R) {
+  const long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j < R) out[j] = touched[order[j]];
+}
+
+int check_cap(long long cap) {
+  if (cap < 0 || cap > 0x7fffffffLL) return SGR_ERR_KEY_CAPACITY;
+  return SGR_OK;
+}
+
+}  // namespace
+}  // namespace sgr
+
+using namespace sgr;
+
+extern "C" {
+
+int sgr_abi_version(void) { return SGR_ABI_VERSION; }
+
+const char* sgr_status_string(int status) {
+  switch (status) {
+    case SGR_OK: return "ok";
+    case SGR_ERR_INVALID_ARGUMENT: return "invalid argument";
+    case SGR_ERR_UNSUPPORTED: return "unsupported combination of inputs";
+    case SGR_ERR_SEMANTIC_CHANNELS: return "more than 16 semantic channels";
+    case SGR_ERR_WORKSPACE: return "workspace smaller than sgr_query_sizes requires";
+    case SGR_ERR_KEY_CAPACITY: return "key capacity out of range";
+    case SGR_ERR_CUDA: return "CUDA runtime error";
+    default: return "unknown status";
+  }
+}
+
+const char* sgr_last_error_message(void) { return g_last_error.c_str(); }
+
+int sgr_query_sizes(const sgr_batch* batch, int64_t key_capacity, sgr_sizes* out) {
+  int rc = check_batch(batch);
+  if (rc) return rc;
+  if ((rc = check_cap(key_capacity))) return rc;
+  if (!out) return SGR_ERR_INVALID_ARGUMENT;
+  std::memset(out, 0, sizeof(*out));
+  return sizes_impl(batch, key_capacity, out);
+}
+
+int sgr_forward_geometry(const sgr_batch* batch, void* geom, void* fwd_scratch, size_t fwd_scratch_bytes,
+                         int64_t* num_keys_host, void* stream) {
+  int rc = check_batch(batch);
+  if (rc) return rc;
+  if (!geom) return SGR_ERR_INVALID_ARGUMENT;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  sgr_sizes s;
+  if ((rc = sizes_impl(batch, 0, &s))) return rc;
+  ScratchLayout L;
+  if ((rc = scratch_layout(batch, 0, L))) return rc;
+  if (fwd_scratch_bytes < L.end_a || (!fwd_scratch && L.end_a > 0)) return SGR_ERR_WORKSPACE;
+  GeomView g = geom_view(batch, s, geom, fwd_scratch, &L);
+  SGR_CUDA(cudaMemsetAsync(g.status, 0, sizeof(Status), st));
+  const long long R = batch->num_records;
+  if (R > 0) {
+    launch_preprocess(*batch, g, st);
+    SGR_CUDA(cudaGetLastError());
+    size_t tb = L.temp_a_bytes;
+    char* sp = static_cast<char*>(fwd_scratch);
+    SGR_CUDA(cub::DeviceRadixSort::SortPairs(sp + L.temp_a, tb, g.depth_keys, g.depth_keys_sorted, g.depth_vals,
+                                             g.depth_order, (int64_t)R, 0, depth_key_bits(batch), st));
+    k_gather_counts<<<(unsigned)((R + 255) / 256), 256, 0, st>>>(g.depth_order, g.tiles_touched, g.offsets, R);
+    SGR_CUDA(cudaGetLastError());
+    tb = L.temp_a_bytes;
+    SGR_CUDA(cub::DeviceScan::InclusiveSum(sp + L.temp_a, tb, g.offsets, g.offsets, (int64_t)R, st));
+    launch_store_key_count(g, R, st);
+    SGR_CUDA(cudaGetLastError());
+  }
+  if (num_keys_host)
+    SGR_CUDA(cudaMemcpyAsync(num_keys_host, &g.status->num_keys, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+  return SGR_OK;
+}
+
+int sgr_forward_raster(const sgr_batch* batch, void* geom, void* lists, int64_t key_capacity, void* fwd_scratch,
+                       size_t fwd_scratch_bytes, const sgr_fwd_outputs* out, void* stream) {
+  int rc = check_batch(batch);
+  if (rc) return rc;
+  if ((rc = check_cap(key_capacity))) return rc;
+  if (!geom || !out || !out->color || !out->others) return SGR_ERR_INVALID_ARGUMENT;
+  if (batch->variant == SGR_VARIANT_PART && batch->semantic_channels > 0 && !out->semantic)
+    return SGR_ERR_INVALID_ARGUMENT;
+  if (key_capacity > 0 && !lists) return SGR_ERR_INVALID_ARGUMENT;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  sgr_sizes s;
+  if ((rc = sizes_impl(batch, key_capacity, &s))) return rc;
+  ScratchLayout L;
+  if ((rc = scratch_layout(batch, key_capacity, L))) return rc;
+  if (fwd_scratch_bytes < L.end || (!fwd_scratch && L.end > 0)) return SGR_ERR_WORKSPACE;
+  GeomView g = geom_view(batch, s, geom, fwd_scratch, &L);
+  char* sp = static_cast<char*>(fwd_scratch);
+  uint32_t* keys = reinterpret_cast<uint32_t*>(sp + L.keys);
+  uint32_t* vals = reinterpret_cast<uint32_t*>(sp + L.vals);
+  uint32_t* keys_sorted = reinterpret_cast<uint32_t*>(sp + L.keys_sorted);
+  uint32_t* point_list = static_cast<uint32_t*>(lists);
+  const int NO = batch->variant == SGR_VARIANT_PLAIN ? 7 : 8;
+  const size_t HW = (size_t)batch->height * batch->width;
+  if (batch->num_surfels == 0) {
+    // the reference returns zero-filled images when there is nothing to draw
+    // (submodules/diff-surfel-rasterization/rasterize_points.cu:85-99)
+    SGR_CUDA(cudaMemsetAsync(out->color, 0, (size_t)batch->num_views * 3 * HW * 4, st));
+    SGR_CUDA(cudaMemsetAsync(out->others, 0, (size_t)batch->num_views * NO * HW * 4, st));
+    if (out->semantic && batch->semantic_channels > 0)
+      SGR_CUDA(cudaMemsetAsync(out->semantic, 0, (size_t)batch->num_views * batch->semantic_channels * HW * 4, st));
+    return SGR_OK;
+  }
+  SGR_CUDA(cudaMemsetAsync(g.ranges, 0, (size_t)batch->num_views * s.tiles_x * s.tiles_y * 8, st));
+  if (key_capacity > 0) {
+    launch_duplicate(*batch, g, keys, vals, key_capacity, st);
+    SGR_CUDA(cudaGetLastError());
+    const uint32_t pad = (s.tile_key_bits >= 32) ? 0xffffffffu : ((1u << s.tile_key_bits) - 1u);
+    launch_pad_keys(keys, key_capacity, g.status, pad, st);
+    SGR_CUDA(cudaGetLastError());
+    size_t tb = L.temp_b_bytes;
+    SGR_CUDA(cub::DeviceRadixSort::SortPairs(sp + L.temp_b, tb, keys, keys_sorted, vals, point_list,
+                                             (int64_t)key_capacity, 0, std::max(1, s.tile_key_bits), st));
+    launch_tile_ranges(keys_sorted, g.status, key_capacity, g.ranges, st);
+    SGR_CUDA(cudaGetLastError());
+  }
+  launch_render_fwd(*batch, g, point_list, *out, st);
+  SGR_CUDA(cudaGetLastError());
+  if (out->radii)
+    SGR_CUDA(cudaMemcpyAsync(out->radii, g.radii, (size_t)batch->num_records * 4, cudaMemcpyDeviceToDevice, st));
+  return SGR_OK;
+}
+
+int sgr_backward(const sgr_batch* batch, const void* geom, const void* lists, int64_t key_capacity, void* bwd_scratch,
+                 size_t bwd_scratch_bytes, const sgr_bwd_inputs* in, const sgr_bwd_outputs* out, void* stream) {
+  int rc = check_batch(batch);
+  if (rc) return rc;
+  if ((rc = check_cap(key_capacity))) return rc;
+  if (!geom || !in || !out || !in->dL_dcolor || !in->dL_dothers) return SGR_ERR_INVALID_ARGUMENT;
+  const int S = batch->variant == SGR_VARIANT_PART ? batch->semantic_channels : 0;
+  if (S > 0 && !in->dL_dsemantic) return SGR_ERR_INVALID_ARGUMENT;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  sgr_sizes s;
+  if ((rc = sizes_impl(batch, key_capacity, &s))) return rc;
+  if (bwd_scratch_bytes < s.bwd_scratch_bytes || (!bwd_scratch && s.bwd_scratch_bytes > 0)) return SGR_ERR_WORKSPACE;
+  GeomView g = geom_view(batch, s, const_cast<void*>(geom), nullptr, nullptr);
+  float* grads = static_cast<float*>(bwd_scratch);
+  const size_t P = (size_t)batch->num_surfels;
+  if (out->dL_dsemantics && S > 0) SGR_CUDA(cudaMemsetAsync(out->dL_dsemantics, 0, P * S * 4, st));
+  if (batch->num_records == 0) return SGR_OK;
+  SGR_CUDA(cudaMemsetAsync(grads, 0, (size_t)batch->num_records * kGradF * 4, st));
+  float* dsem = (S > 0) ? out->dL_dsemantics : nullptr;
+  if (S > 0 && !dsem) return SGR_ERR_INVALID_ARGUMENT;
+  launch_render_bwd(*batch, g, static_cast<const uint32_t*>(lists), *in, grads, dsem, st);
+  SGR_CUDA(cudaGetLastError());
+  launch_preprocess_bwd(*batch, g, grads, *out, st);
+  SGR_CUDA(cudaGetLastError());
+  return SGR_OK;
+}
+
+int sgr_mark_visible(int32_t P, const float* means3D, const float* viewmatrix, const float* projmatrix,
+                     uint8_t* present, void* stream) {
+  (void)projmatrix;
+  if (P < 0) return SGR_ERR_INVALID_ARGUMENT;
+  if (P == 0) return SGR_OK;
+  if (!means3D || !viewmatrix || !present) return SGR_ERR_INVALID_ARGUMENT;
+  launch_mark_visible(P, means3D, viewmatrix, present, static_cast<cudaStream_t>(stream));
+  SGR_CUDA(cudaGetLastError());
+  return SGR_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,543 @@
+// Backward kernels of the GB300 surfel rasteriser.
+#include "sgr_kernels.cuh"
+
+namespace sgr {
+
+// ---------------------------------------------------------------------------
+// blend backward (P0/cr/backward.cu:143-440, P1/cr/backward.cu:143-470)
+//
+// Same per-pixel recurrences as the reference: back to front over the
+// surfels before each pixel's last contributor, transmittance recovered by
+// division from the stored final T.  Differences in how the work is laid out:
+//  * the CTA starts at the largest last-contributor of its tile instead of
+//    the end of the tile's list (positions past it are skipped by every
+//    pixel in the reference);
+//  * the 18 per-fragment gradients of a warp's 32 pixels are summed with a
+//    transposed shuffle reduction, then one lane per value issues a single
+//    atomic add into the per-view gradient record (the reference issues up to
+//    16 atomics per pixel and fragment).
+// ---------------------------------------------------------------------------
+template <int VARIANT>
+__global__ void __launch_bounds__(kBlock) k_render_bwd(const sgr_batch b, GeomView g,
+                                                       const uint32_t* __restrict__ point_list,
+                                                       const sgr_bwd_inputs in, float* __restrict__ grads,
+                                                       float* __restrict__ dL_dsemantics) {
+  const int tiles_per_view = g.tiles_x * g.tiles_y;
+  const int tile = blockIdx.x;
+  const int v = tile / tiles_per_view;
+  const int t = tile - v * tiles_per_view;
+  const int ty = t / g.tiles_x, tx = t - ty * g.tiles_x;
+  const int W = b.width, H = b.height;
+  const int px = tx * kTile + (threadIdx.x & (kTile - 1));
+  const int py = ty * kTile + (threadIdx.x / kTile);
+  const bool inside = px < W && py < H;
+  const float pxf = (VARIANT == SGR_VARIANT_PLAIN) ? (float)px : (float)px + 0.5f;
+  const float pyf = (VARIANT == SGR_VARIANT_PLAIN) ? (float)py : (float)py + 0.5f;
+  const int lane = threadIdx.x & 31;
+  const int S = (VARIANT == SGR_VARIANT_PART) ? b.semantic_channels : 0;
+  const sgr_view_desc vd = b.views[v];
+  const int sid_base = b.scenes[vd.scene].surfel_offset - vd.record_offset;
+
+  __shared__ float4 s_rec[kRecF4][kBlock];
+  __shared__ uint32_t s_id[kBlock];
+  __shared__ float s_sem[(VARIANT == SGR_VARIANT_PART) ? SGR_MAX_SEMANTICS : 1][kBlock];
+  __shared__ int s_max[kBlock / 32];
+
+  const uint2 range = g.ranges[tile];
+  const size_t HW = (size_t)H * W;
+  const size_t pix = inside ? (size_t)py * W + px : 0;
+  const float* fT = g.final_T + (size_t)v * 3 * HW;
+  const uint32_t* nc = g.n_contrib + (size_t)v * 2 * HW;
+  const int NO = (VARIANT == SGR_VARIANT_PLAIN) ? 7 : 8;
+  const float* dpix = in.dL_dcolor + (size_t)v * 3 * HW;
+  const float* doth = in.dL_dothers + (size_t)v * NO * HW;
+
+  const float T_final = inside ? fT[pix] : 0.f;
+  float T = T_final;
+  const int last_contributor = inside ? (int)nc[pix] : 0;
+  const int median_contributor = inside ? (int)nc[pix + HW] : 0;
+  float dL_dpixel[3] = {0.f, 0.f, 0.f};
+  float dL_ddepth = 0.f, dL_daccum = 0.f, dL_dreg = 0.f, dL_dmedian = 0.f, dL_dmaxw = 0.f;
+  float dL_dnormal2D[3] = {0.f, 0.f, 0.f};
+  float dsem_pix[SGR_MAX_SEMANTICS];
+#pragma unroll
+  for (int c = 0; c < SGR_MAX_SEMANTICS; ++c) dsem_pix[c] = 0.f;
+  float final_D = 0.f, final_D2 = 0.f;
+  if (inside) {
+    for (int c = 0; c < 3; ++c) dL_dpixel[c] = dpix[pix + c * HW];
+    dL_ddepth = doth[pix];
+    dL_daccum = doth[pix + HW];
+    for (int c = 0; c < 3; ++c) dL_dnormal2D[c] = doth[pix + (2 + c) * HW];
+    dL_dmedian = doth[pix + 5 * HW];
+    dL_dreg = doth[pix + 6 * HW];
+    if (VARIANT == SGR_VARIANT_PART) {
+      dL_dmaxw = doth[pix + 7 * HW];
+      const float* ds = in.dL_dsemantic + (size_t)v * S * HW;
+      for (int c = 0; c < S; ++c) dsem_pix[c] = ds[pix + c * HW];
+    }
+    final_D = fT[pix + HW];
+    final_D2 = fT[pix + 2 * HW];
+  }
+  const float final_A = 1 - T_final;
+  const float* bg = b.background;
+  const float bg_dot = bg[0] * dL_dpixel[0] + bg[1] * dL_dpixel[1] + bg[2] * dL_dpixel[2];
+
+  float accum_rec[3] = {0.f, 0.f, 0.f}, last_color[3] = {0.f, 0.f, 0.f};
+  float accum_sem[SGR_MAX_SEMANTICS], last_sem[SGR_MAX_SEMANTICS];
+#pragma unroll
+  for (int c = 0; c < SGR_MAX_SEMANTICS; ++c) accum_sem[c] = last_sem[c] = 0.f;
+  float last_alpha = 0.f, last_depth = 0.f, accum_depth = 0.f, accum_alpha = 0.f, last_dL_dT = 0.f;
+  float last_normal[3] = {0.f, 0.f, 0.f}, accum_normal[3] = {0.f, 0.f, 0.f};
+
+  // largest last contributor of the tile: list positions at or past it are
+  // skipped by every pixel
+  {
+    int m = last_contributor;
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if (lane == 0) s_max[threadIdx.x / 32] = m;
+    __syncthreads();
+    m = 0;
+#pragma unroll
+    for (int w = 0; w < kBlock / 32; ++w) m = max(m, s_max[w]);
+    // every thread computed the same m; the loop bounds below are uniform
+    int hi = min(m, (int)(range.y - range.x));
+    for (; hi > 0; hi -= kBlock) {
+      const int n = min(kBlock, hi);
+      __syncthreads();
+      if ((int)threadIdx.x < n) {
+        const uint32_t r = point_list[range.x + hi - 1 - threadIdx.x];
+        s_id[threadIdx.x] = r;
+        const float4* rec = g.records + (size_t)r * kRecF4;
+#pragma unroll
+        for (int k = 0; k < kRecF4; ++k) s_rec[k][threadIdx.x] = rec[k];
+        if (VARIANT == SGR_VARIANT_PART) {
+          const float* sem = b.semantics + (size_t)(sid_base + (int)r) * S;
+          for (int c = 0; c < S; ++c) s_sem[c][threadIdx.x] = sem[c];
+        }
+      }
+      __syncthreads();
+      for (int j = 0; j < n; ++j) {
+        const int pos = hi - 1 - j;
+        float gv[32];
+#pragma unroll
+        for (int k = 0; k < 32; ++k) gv[k] = 0.f;
+        float gsem[32];
+        bool ok = inside && pos < last_contributor;
+        if (ok) {
+          const float4 r0 = s_rec[0][j], r1 = s_rec[1][j], r2 = s_rec[2][j];
+          const V3 Tu = v3(r0.x, r0.y, r0.z), Tv = v3(r0.w, r1.x, r1.y), Tw = v3(r1.z, r1.w, r2.x);
+          Frag fr;
+          intersect<VARIANT>(pxf, pyf, Tu, Tv, Tw, r2.y, r2.z, fr);
+          ok = fr.p.z != 0.0f && !(fr.depth < kNearP0);
+          const float power = -0.5f * fr.rho;
+          ok = ok && !(power > 0.0f);
+          const float G = expf(power);
+          const float alpha = fminf(0.99f, r2.w * G);
+          ok = ok && !(alpha < 1.0f / 255.0f);
+          if (ok) {
+            const float4 r3 = s_rec[3][j], r4 = s_rec[4][j];
+            T = T / (1.f - alpha);
+            const float wgt = alpha * T;
+            float dL_dalpha = 0.0f;
+            const float col[3] = {r4.x, r4.y, r4.z};
+#pragma unroll
+            for (int ch = 0; ch < 3; ++ch) {
+              accum_rec[ch] = last_alpha * last_color[ch] + (1.f - last_alpha) * accum_rec[ch];
+              last_color[ch] = col[ch];
+              dL_dalpha += (col[ch] - accum_rec[ch]) * dL_dpixel[ch];
+              gv[14 + ch] = wgt * dL_dpixel[ch];
+            }
+            if (VARIANT == SGR_VARIANT_PART) {
+              for (int c = 0; c < S; ++c) {
+                accum_sem[c] = last_alpha * last_sem[c] + (1.f - last_alpha) * accum_sem[c];
+                last_sem[c] = s_sem[c][j];
+              }
+            }
+            float dL_dz = 0.0f, dL_dweight = 0.f;
+            float m_d, dmd_dd;
+            if (VARIANT == SGR_VARIANT_PLAIN) {
+              m_d = kFarP0 / (kFarP0 - kNearP0) * (1 - kNearP0 / fr.depth);
+              dmd_dd = (kFarP0 * kNearP0) / ((kFarP0 - kNearP0) * fr.depth * fr.depth);
+            } else {
+              m_d = mapped_depth_p1(fr.depth);
+              dmd_dd = (float)((kFarP1 * kNearP1) / ((kFarP1 - kNearP1) * fr.depth * fr.depth));
+            }
+            if (pos == median_contributor - 1) {
+              dL_dz += dL_dmedian;
+              if (VARIANT == SGR_VARIANT_PART) dL_dweight += dL_dmaxw;
+            }
+            dL_dweight += (final_D2 + m_d * m_d * final_A - 2 * m_d * final_D) * dL_dreg;
+            dL_dalpha += dL_dweight - last_dL_dT;
+            last_dL_dT = dL_dweight * alpha + (1 - alpha) * last_dL_dT;
+            const float dL_dmd = 2.0f * (T * alpha) * (m_d * final_A - final_D) * dL_dreg;
+            dL_dz += dL_dmd * dmd_dd;
+            accum_depth = last_alpha * last_depth + (1.f - last_alpha) * accum_depth;
+            last_depth = fr.depth;
+            dL_dalpha += (fr.depth - accum_depth) * dL_ddepth;
+            // the reference adds last_alpha * 1.0 in double: one rounding of
+            // an exact sum, i.e. a plain float add
+            accum_alpha = __fadd_rn(last_alpha, __fmul_rn(1.f - last_alpha, accum_alpha));
+            dL_dalpha += (1 - accum_alpha) * dL_daccum;
+            const float nrm[3] = {r3.x, r3.y, r3.z};
+#pragma unroll
+            for (int ch = 0; ch < 3; ++ch) {
+              accum_normal[ch] = last_alpha * last_normal[ch] + (1.f - last_alpha) * accum_normal[ch];
+              last_normal[ch] = nrm[ch];
+              dL_dalpha += (nrm[ch] - accum_normal[ch]) * dL_dnormal2D[ch];
+              gv[11 + ch] = alpha * T * dL_dnormal2D[ch];
+            }
+            dL_dalpha *= T;
+            last_alpha = alpha;
+            dL_dalpha += (-T_final / (1.f - alpha)) * bg_dot;
+            const float dL_dG = r2.w * dL_dalpha;
+            dL_dz += alpha * T * dL_ddepth;
+            if (fr.use3d) {
+              const float dsx = dL_dG * -G * fr.sx + dL_dz * Tw.x;
+              const float dsy = dL_dG * -G * fr.sy + dL_dz * Tw.y;
+              const float dsx_pz = dsx / fr.p.z;
+              const float dsy_pz = dsy / fr.p.z;
+              const V3 dL_dp = v3(dsx_pz, dsy_pz, -(dsx_pz * fr.sx + dsy_pz * fr.sy));
+              const V3 dL_dk = cross3(fr.l, dL_dp);
+              const V3 dL_dl = cross3(dL_dp, fr.k);
+              gv[0] = -dL_dk.x; gv[1] = -dL_dk.y; gv[2] = -dL_dk.z;
+              gv[3] = -dL_dl.x; gv[4] = -dL_dl.y; gv[5] = -dL_dl.z;
+              gv[6] = pxf * dL_dk.x + pyf * dL_dl.x + dL_dz * fr.sx;
+              gv[7] = pxf * dL_dk.y + pyf * dL_dl.y + dL_dz * fr.sy;
+              gv[8] = pxf * dL_dk.z + pyf * dL_dl.z + dL_dz * 1.0f;
+            } else {
+              const float dG_ddelx = -G * kFilterInvSquareP0 * fr.dx;
+              const float dG_ddely = -G * kFilterInvSquareP0 * fr.dy;
+              gv[9] = dL_dG * dG_ddelx;
+              gv[10] = dL_dG * dG_ddely;
+              gv[8] = dL_dz;
+            }
+            gv[17] = G * dL_dalpha;
+            if (VARIANT == SGR_VARIANT_PART) {
+              for (int c = 0; c < S; ++c) gsem[c] = wgt * dsem_pix[c];
+            }
+          }
+        }
+        if (__any_sync(0xffffffffu, ok)) {
+          const float total = warp_transpose_sum(gv, lane);
+          const uint32_t r = s_id[j];
+          if (lane < kGradUsed && total != 0.f) atomicAdd(grads + (size_t)r * kGradF + lane, total);
+          if (VARIANT == SGR_VARIANT_PART && S > 0) {
+#pragma unroll
+            for (int c = 0; c < 32; ++c) gsem[c] = (ok && c < S) ? gsem[c] : 0.f;
+            const float st = warp_transpose_sum(gsem, lane);
+            if (lane < S && st != 0.f) atomicAdd(dL_dsemantics + (size_t)(sid_base + (int)r) * S + lane, st);
+          }
+        }
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// preprocess backward: one thread per surfel, summing over its scene's views
+// (P0/cr/backward.cu:443-630; P1/cr/backward.cu:473-671)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void sh_backward(int deg, const float* sh, V3 dir_orig, uint32_t clamped, V3 dL_dRGB_in,
+                                            float* dsh_acc, V3& dmean) {
+  const float len = sqrtf(dot3(dir_orig, dir_orig));
+  const V3 dir = v3(dir_orig.x / len, dir_orig.y / len, dir_orig.z / len);
+  V3 g = dL_dRGB_in;
+  g.x *= (clamped & 1u) ? 0 : 1;
+  g.y *= (clamped & 2u) ? 0 : 1;
+  g.z *= (clamped & 4u) ? 0 : 1;
+  auto c = [&](int k) { return v3(sh[3 * k], sh[3 * k + 1], sh[3 * k + 2]); };
+  auto add = [&](int k, float coef) {
+    dsh_acc[3 * k] += coef * g.x;
+    dsh_acc[3 * k + 1] += coef * g.y;
+    dsh_acc[3 * k + 2] += coef * g.z;
+  };
+  V3 dx = v3(0, 0, 0), dy = v3(0, 0, 0), dz = v3(0, 0, 0);
+  const float x = dir.x, y = dir.y, z = dir.z;
+  add(0, kShC0);
+  if (deg > 0) {
+    add(1, -kShC1 * y);
+    add(2, kShC1 * z);
+    add(3, -kShC1 * x);
+    dx = -kShC1 * c(3);
+    dy = -kShC1 * c(1);
+    dz = kShC1 * c(2);
+    if (deg > 1) {
+      const float xx = x * x, yy = y * y, zz = z * z;
+      const float xy = x * y, yz = y * z, xz = x * z;
+      add(4, kShC2[0] * xy);
+      add(5, kShC2[1] * yz);
+      add(6, kShC2[2] * (2.f * zz - xx - yy));
+      add(7, kShC2[3] * xz);
+      add(8, kShC2[4] * (xx - yy));
+      dx = dx + kShC2[0] * y * c(4) + kShC2[2] * 2.f * -x * c(6) + kShC2[3] * z * c(7) + kShC2[4] * 2.f * x * c(8);
+      dy = dy + kShC2[0] * x * c(4) + kShC2[1] * z * c(5) + kShC2[2] * 2.f * -y * c(6) + kShC2[4] * 2.f * -y * c(8);
+      dz = dz + kShC2[1] * y * c(5) + kShC2[2] * 2.f * 2.f * z * c(6) + kShC2[3] * x * c(7);
+      if (deg > 2) {
+        add(9, kShC3[0] * y * (3.f * xx - yy));
+        add(10, kShC3[1] * xy * z);
+        add(11, kShC3[2] * y * (4.f * zz - xx - yy));
+        add(12, kShC3[3] * z * (2.f * zz - 3.f * xx - 3.f * yy));
+        add(13, kShC3[4] * x * (4.f * zz - xx - yy));
+        add(14, kShC3[5] * z * (xx - yy));
+        add(15, kShC3[6] * x * (xx - 3.f * yy));
+        dx = dx + (kShC3[0] * c(9) * 3.f * 2.f * xy + kShC3[1] * c(10) * yz + kShC3[2] * c(11) * -2.f * xy +
+                   kShC3[3] * c(12) * -3.f * 2.f * xz + kShC3[4] * c(13) * (-3.f * xx + 4.f * zz - yy) +
+                   kShC3[5] * c(14) * 2.f * xz + kShC3[6] * c(15) * 3.f * (xx - yy));
+        dy = dy + (kShC3[0] * c(9) * 3.f * (xx - yy) + kShC3[1] * c(10) * xz +
+                   kShC3[2] * c(11) * (-3.f * yy + 4.f * zz - xx) + kShC3[3] * c(12) * -3.f * 2.f * yz +
+                   kShC3[4] * c(13) * -2.f * xy + kShC3[5] * c(14) * -2.f * yz + kShC3[6] * c(15) * -3.f * 2.f * xy);
+        dz = dz + (kShC3[1] * c(10) * xy + kShC3[2] * c(11) * 4.f * 2.f * yz +
+                   kShC3[3] * c(12) * 3.f * (2.f * zz - xx - yy) + kShC3[4] * c(13) * 4.f * 2.f * xz +
+                   kShC3[5] * c(14) * (xx - yy));
+      }
+    }
+  }
+  const V3 dL_ddir = v3(dot3(dx, g), dot3(dy, g), dot3(dz, g));
+  dmean = dmean + dnormvdv(dir_orig, dL_ddir);
+}
+
+template <int VARIANT>
+__global__ void __launch_bounds__(128) k_preprocess_bwd(const sgr_batch b, GeomView g, const float* __restrict__ grads,
+                                                        sgr_bwd_outputs out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= b.num_surfels) return;
+  const int s = find_scene(b.scenes, b.num_scenes, i);
+  const sgr_scene_desc sd = b.scenes[s];
+  const int local = i - sd.surfel_offset;
+  const int W = b.width, H = b.height;
+  const bool precomp = b.transmat_precomp != nullptr;
+  const V3 p = v3(b.means3D[3 * i + 0], b.means3D[3 * i + 1], b.means3D[3 * i + 2]);
+  float2 sc = make_float2(0.f, 0.f);
+  float4 q = make_float4(1.f, 0.f, 0.f, 0.f);
+  if (!precomp) {
+    sc = make_float2(b.scales[2 * i + 0], b.scales[2 * i + 1]);
+    q = reinterpret_cast<const float4*>(b.rotations)[i];
+  }
+  const int M = b.sh_coeffs;
+  const bool has_sh = b.shs != nullptr;
+  float sh[kMaxShCoeffs * 3];
+  float dsh[kMaxShCoeffs * 3];
+#pragma unroll
+  for (int k = 0; k < kMaxShCoeffs * 3; ++k) {
+    sh[k] = (has_sh && k < M * 3) ? b.shs[(size_t)i * M * 3 + k] : 0.f;
+    dsh[k] = 0.f;
+  }
+  const M3 R = quat_to_rot(q);
+  V3 dmean = v3(0, 0, 0), dcol = v3(0, 0, 0);
+  float dsx = 0.f, dsy = 0.f, dop = 0.f;
+  float4 drot = make_float4(0.f, 0.f, 0.f, 0.f);
+
+  for (int vi = 0; vi < sd.view_count; ++vi) {
+    const int v = sd.view_begin + vi;
+    const sgr_view_desc vd = b.views[v];
+    const int r = vd.record_offset + local;
+    const float* gr = grads + (size_t)r * kGradF;
+    const bool vis = g.radii[r] > 0;
+    float* o2 = out.dL_dmeans2D ? out.dL_dmeans2D + (size_t)r * 3 : nullptr;
+    float* oT = out.dL_dtransmat ? out.dL_dtransmat + (size_t)r * 9 : nullptr;
+    if (!vis) {
+      if (o2) o2[0] = o2[1] = o2[2] = 0.f;
+      if (oT) for (int k = 0; k < 9; ++k) oT[k] = gr[k];
+      continue;
+    }
+    const float* vm = b.viewmatrix + 16 * v;
+    const float* pm = b.projmatrix + 16 * v;
+    const float focal_x = W / (2.0f * vd.tanfovx);
+    const float focal_y = H / (2.0f * vd.tanfovy);
+    float dT[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) dT[k] = gr[k];
+    const float dm2x = gr[9], dm2y = gr[10];
+    const V3 dn = v3(gr[11], gr[12], gr[13]);
+    const V3 dc = v3(gr[14], gr[15], gr[16]);
+    dop += gr[17];
+    dcol = dcol + dc;
+    const float4 rc0 = g.records[(size_t)r * kRecF4 + 0];
+    const float4 rc1 = g.records[(size_t)r * kRecF4 + 1];
+    const float4 rc2 = g.records[(size_t)r * kRecF4 + 2];
+    const float4 rc4 = g.records[(size_t)r * kRecF4 + 4];
+    const float stored_depth = rc2.x;
+
+    if (VARIANT == SGR_VARIANT_PLAIN) {
+      // image size recovered from focal * tan * 2 with truncation, as
+      // P0/cr/backward.cu:607-608 does (it can come out one pixel short)
+      const int Wb = int(focal_x * vd.tanfovx * 2);
+      const int Hb = int(focal_y * vd.tanfovy * 2);
+      V3 T0, T1, T2, normal;
+      V3 L0, L1;
+      float4 P0c, P1c, P2c;
+      if (precomp) {
+        const float* tp = b.transmat_precomp + 9 * i;
+        T0 = v3(tp[0], tp[1], tp[2]);
+        T1 = v3(tp[3], tp[4], tp[5]);
+        T2 = v3(tp[6], tp[7], tp[8]);
+        normal = v3(0, 0, 0);
+      } else {
+        L0 = R.c[0] * sc.x;
+        L1 = R.c[1] * sc.y;
+        // P = world2ndc * ndc2pix (columns), with the recovered Wb, Hb
+        const float4 w0 = make_float4(pm[0], pm[4], pm[8], pm[12]);
+        const float4 w1 = make_float4(pm[1], pm[5], pm[9], pm[13]);
+        const float4 w3 = make_float4(pm[3], pm[7], pm[11], pm[15]);
+        const float wh = float(Wb) / 2.0f, wc = float(Wb - 1) / 2.0f;
+        const float hh = float(Hb) / 2.0f, hc = float(Hb - 1) / 2.0f;
+        P0c = make_float4(w0.x * wh + w3.x * wc, w0.y * wh + w3.y * wc, w0.z * wh + w3.z * wc, w0.w * wh + w3.w * wc);
+        P1c = make_float4(w1.x * hh + w3.x * hc, w1.y * hh + w3.y * hc, w1.z * hh + w3.z * hc, w1.w * hh + w3.w * hc);
+        P2c = w3;
+        auto row = [&](float4 Pc) {
+          return v3(L0.x * Pc.x + L0.y * Pc.y + L0.z * Pc.z, L1.x * Pc.x + L1.y * Pc.y + L1.z * Pc.z,
+                    p.x * Pc.x + p.y * Pc.y + p.z * Pc.z + Pc.w);
+        };
+        T0 = row(P0c);
+        T1 = row(P1c);
+        T2 = row(P2c);
+        normal = xform_vec43(R.c[2], vm);
+      }
+      V3 dT0 = v3(dT[0], dT[1], dT[2]), dT1 = v3(dT[3], dT[4], dT[5]), dT2 = v3(dT[6], dT[7], dT[8]);
+      if (dm2x != 0 || dm2y != 0) {
+        // adjoint of the screen-space centre (P0/cr/backward.cu:514-543)
+        const V3 tv = v3(9.0f, 9.0f, -1.0f);
+        const float d = dot3(tv, T2 * T2);
+        const V3 fv = tv * (1.0f / d);
+        const V3 a0 = dm2x * fv * T2;
+        const V3 a1 = dm2y * fv * T2;
+        V3 a3 = dm2x * fv * T0 + dm2y * fv * T1;
+        const V3 dL_df = dm2x * T0 * T2 + dm2y * T1 * T2;
+        const float dL_dd = (float)((double)dot3(dL_df, fv) * (-1.0 / (double)d));
+        a3 = a3 + dL_dd * (tv * T2 * 2.0f);
+        dT0 = dT0 + a0;
+        dT1 = dT1 + a1;
+        dT2 = dT2 + a3;
+        if (precomp) {
+          dT[0] = dT0.x; dT[1] = dT0.y; dT[2] = dT0.z;
+          dT[3] = dT1.x; dT[4] = dT1.y; dT[5] = dT1.z;
+          dT[6] = dT2.x; dT[7] = dT2.y; dT[8] = dT2.z;
+        }
+      }
+      if (!precomp) {
+        // dL/dM = P * dL/dT^T, columns (L0, L1, p)
+        auto dMcol = [&](int c) {
+          const float a = c == 0 ? dT0.x : (c == 1 ? dT0.y : dT0.z);
+          const float bb = c == 0 ? dT1.x : (c == 1 ? dT1.y : dT1.z);
+          const float cc = c == 0 ? dT2.x : (c == 1 ? dT2.y : dT2.z);
+          return v3(P0c.x * a + P1c.x * bb + P2c.x * cc, P0c.y * a + P1c.y * bb + P2c.y * cc,
+                    P0c.z * a + P1c.z * bb + P2c.z * cc);
+        };
+        const V3 dRS0 = dMcol(0), dRS1 = dMcol(1), dP = dMcol(2);
+        V3 dtn = xform_vec43_t(dn, vm);
+        const V3 pv = xform_point43(p, vm);
+        const float cosv = -sum3(pv * normal);
+        dtn = (cosv > 0 ? 1.f : -1.f) * dtn;
+        M3 dR;
+        dR.c[0] = dRS0 * sc.x;
+        dR.c[1] = dRS1 * sc.y;
+        dR.c[2] = dtn;
+        const float4 dq = quat_to_rot_vjp(q, dR);
+        drot = make_float4(drot.x + dq.x, drot.y + dq.y, drot.z + dq.z, drot.w + dq.w);
+        dsx += dot3(dRS0, R.c[0]);
+        dsy += dot3(dRS1, R.c[1]);
+        dmean = dmean + dP;
+      }
+      // densification proxy (P0/cr/backward.cu:626-629)
+      if (o2) {
+        o2[0] = (float)((double)(dT[2] * stored_depth) * 0.5 * (double)float(Wb));
+        o2[1] = (float)((double)(dT[5] * stored_depth) * 0.5 * (double)float(Hb));
+        o2[2] = 0.f;
+      }
+    } else {
+      // adjoint of the screen-space centre (P1/cr/backward.cu:621-671)
+      const V3 T0 = v3(rc0.x, rc0.y, rc0.z), T1 = v3(rc0.w, rc1.x, rc1.y), T3 = v3(rc1.z, rc1.w, rc2.x);
+      const V3 tv = v3(1.0f, 1.0f, -1.0f);
+      const float d = dot3(tv, T3 * T3);
+      const V3 fv = tv * (1.0f / d);
+      const V3 a0 = dm2x * fv * T3;
+      const V3 a1 = dm2y * fv * T3;
+      V3 a3 = dm2x * fv * T0 + dm2y * fv * T1;
+      const V3 dL_df = (dm2x * T0 * T3) + (dm2y * T1 * T3);
+      const float dL_dd = (float)((double)dot3(dL_df, fv) * (-1.0 / (double)d));
+      a3 = a3 + dL_dd * (tv * T3 * 2.0f);
+      dT[0] += a0.x; dT[1] += a0.y; dT[2] += a0.z;
+      dT[3] += a1.x; dT[4] += a1.y; dT[5] += a1.z;
+      dT[6] += a3.x; dT[7] += a3.y; dT[8] += a3.z;
+      if (o2) {
+        const float z = T3.z;
+        const float Wf = focal_x * vd.tanfovx, Hf = focal_y * vd.tanfovy;
+        o2[0] = dT[2] * z * Wf;
+        o2[1] = dT[5] * z * Hf;
+        o2[2] = 0.f;
+      }
+      if (!precomp) {
+        // computeTransMat adjoint (P1/cr/backward.cu:473-551)
+        const float cxb = focal_x * vd.tanfovx, cyb = focal_y * vd.tanfovy;
+        auto dMcol = [&](int c) {
+          return v3(focal_x * dT[c], focal_y * dT[3 + c], cxb * dT[c] + cyb * dT[3 + c] + dT[6 + c]);
+        };
+        const V3 dRS0 = xform_vec43_t(dMcol(0), vm);
+        const V3 dRS1 = xform_vec43_t(dMcol(1), vm);
+        const V3 dpw = xform_vec43_t(dMcol(2), vm);
+        V3 dtn = xform_vec43_t(dn, vm);
+        const V3 tn = xform_vec43(R.c[2], vm);
+        const V3 pv = xform_point43(p, vm);
+        const float cosv = dot3(v3(-tn.x, -tn.y, -tn.z), pv);
+        dtn = (cosv > 0 ? 1.f : -1.f) * dtn;
+        M3 dR;
+        dR.c[0] = dRS0 * sc.x;
+        dR.c[1] = dRS1 * sc.y;
+        dR.c[2] = dtn;
+        const float4 dq = quat_to_rot_vjp(q, dR);
+        drot = make_float4(drot.x + dq.x, drot.y + dq.y, drot.z + dq.z, drot.w + dq.w);
+        dsx += dot3(dRS0, R.c[0]);
+        dsy += dot3(dRS1, R.c[1]);
+        dmean = dmean + dpw;
+      }
+    }
+    if (oT)
+      for (int k = 0; k < 9; ++k) oT[k] = dT[k];
+    if (has_sh) {
+      const V3 cp = v3(b.campos[3 * v], b.campos[3 * v + 1], b.campos[3 * v + 2]);
+      sh_backward(b.sh_degree, sh, p - cp, __float_as_uint(rc4.w), dc, dsh, dmean);
+    }
+  }
+  if (out.dL_dmeans3D) {
+    out.dL_dmeans3D[3 * i] = dmean.x;
+    out.dL_dmeans3D[3 * i + 1] = dmean.y;
+    out.dL_dmeans3D[3 * i + 2] = dmean.z;
+  }
+  if (out.dL_dscales) {
+    out.dL_dscales[2 * i] = dsx;
+    out.dL_dscales[2 * i + 1] = dsy;
+  }
+  if (out.dL_drotations) reinterpret_cast<float4*>(out.dL_drotations)[i] = drot;
+  if (out.dL_dopacity) out.dL_dopacity[i] = dop;
+  if (out.dL_dcolors) {
+    out.dL_dcolors[3 * i] = dcol.x;
+    out.dL_dcolors[3 * i + 1] = dcol.y;
+    out.dL_dcolors[3 * i + 2] = dcol.z;
+  }
+  if (out.dL_dsh && M > 0) {
+    float* o = out.dL_dsh + (size_t)i * M * 3;
+    for (int k = 0; k < M * 3; ++k) o[k] = k < kMaxShCoeffs * 3 ? dsh[k] : 0.f;
+  }
+}
+
+void launch_render_bwd(const sgr_batch& b, const GeomView& g, const uint32_t* point_list, const sgr_bwd_inputs& in,
+                       float* grads, float* dL_dsemantics, cudaStream_t st) {
+  const unsigned blocks = (unsigned)(g.tiles_x * g.tiles_y) * (unsigned)b.num_views;
+  if (blocks == 0) return;
+  if (b.variant == SGR_VARIANT_PLAIN)
+    k_render_bwd<SGR_VARIANT_PLAIN><<<blocks, kBlock, 0, st>>>(b, g, point_list, in, grads, dL_dsemantics);
+  else
+    k_render_bwd<SGR_VARIANT_PART><<<blocks, kBlock, 0, st>>>(b, g, point_list, in, grads, dL_dsemantics);
+}
+
+void launch_preprocess_bwd(const sgr_batch& b, const GeomView& g, const float* grads, const sgr_bwd_outputs& out,
+                           cudaStream_t st) {
+  const int threads = 128;
+  const int blocks = (b.num_surfels + threads - 1) / threads;
+  if (blocks == 0) return;
+  if (b.variant == SGR_VARIANT_PLAIN) k_preprocess_bwd<SGR_VARIANT_PLAIN><<<blocks, threads, 0, st>>>(b, g, grads, out);
+  else k_preprocess_bwd<SGR_VARIANT_PART><<<blocks, threads, 0, st>>>(b, g, grads, out);
+}
+
+}  // namespace sgr

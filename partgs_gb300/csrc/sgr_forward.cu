@@ -1,0 +1,441 @@
+// Forward kernels of the GB300 surfel rasteriser: preprocess (both
+// variants), key duplication, tile ranges, blend, near-plane visibility.
+#include "sgr_kernels.cuh"
+
+namespace sgr {
+
+// ---------------------------------------------------------------------------
+// preprocess
+// ---------------------------------------------------------------------------
+// One thread per surfel; the surfel's attributes are read once and every view
+// of its scene is processed from registers (the reference reads them once per
+// view: P0/cr/forward.cu:148-251, P1/cr/forward.cu:166-260).
+template <int VARIANT>
+__global__ void __launch_bounds__(128) k_preprocess(const sgr_batch b, GeomView g) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= b.num_surfels) return;
+  const int s = find_scene(b.scenes, b.num_scenes, i);
+  const sgr_scene_desc sd = b.scenes[s];
+  const int local = i - sd.surfel_offset;
+  const int W = b.width, H = b.height;
+  const int gx = g.tiles_x, gy = g.tiles_y;
+
+  const V3 p = v3(b.means3D[3 * i + 0], b.means3D[3 * i + 1], b.means3D[3 * i + 2]);
+  const float opac = b.opacities[i];
+  const bool precomp = b.transmat_precomp != nullptr;
+  float2 sc = make_float2(0.f, 0.f);
+  float4 q = make_float4(1.f, 0.f, 0.f, 0.f);
+  if (!precomp) {
+    sc = make_float2(b.scales[2 * i + 0], b.scales[2 * i + 1]);
+    q = reinterpret_cast<const float4*>(b.rotations)[i];
+  }
+  // SH coefficients live in registers for all views of this surfel.
+  const int M = b.sh_coeffs;
+  float sh[kMaxShCoeffs * 3];
+  if (b.shs != nullptr) {
+#pragma unroll
+    for (int k = 0; k < kMaxShCoeffs * 3; ++k) sh[k] = (k < M * 3) ? b.shs[(size_t)i * M * 3 + k] : 0.f;
+  }
+  V3 cpre = v3(0.f, 0.f, 0.f);
+  if (b.colors_precomp != nullptr)
+    cpre = v3(b.colors_precomp[3 * i + 0], b.colors_precomp[3 * i + 1], b.colors_precomp[3 * i + 2]);
+
+  for (int vi = 0; vi < sd.view_count; ++vi) {
+    const int v = sd.view_begin + vi;
+    const sgr_view_desc vd = b.views[v];
+    const int r = vd.record_offset + local;
+    const float* vm = b.viewmatrix + 16 * v;
+    const float* pm = b.projmatrix + 16 * v;
+    g.radii[r] = 0;
+    g.tiles_touched[r] = 0;
+    g.depth_keys[r] = ((unsigned long long)v << 32) | 0xffffffffull;
+    g.depth_vals[r] = (uint32_t)r;
+
+    // near-plane test (in_frustum, P0/cr/auxiliary.h:185-210)
+    const V3 pv = xform_point43(p, vm);
+    if (pv.z <= 0.2f) {
+      if (b.prefiltered) atomicOr(&g.status->flags, SGR_FLAG_PREFILTERED);
+      continue;
+    }
+    const float focal_x = W / (2.0f * vd.tanfovx);
+    const float focal_y = H / (2.0f * vd.tanfovy);
+
+    V3 Tu, Tv, Tw, normal;
+    if (precomp) {
+      const float* t = b.transmat_precomp + 9 * i;
+      Tu = v3(t[0], t[1], t[2]);
+      Tv = v3(t[3], t[4], t[5]);
+      Tw = v3(t[6], t[7], t[8]);
+      normal = (VARIANT == SGR_VARIANT_PLAIN) ? v3(0.f, 0.f, 1.f) : v3(0.f, 0.f, 0.f);
+    } else if (VARIANT == SGR_VARIANT_PLAIN) {
+      // splat-to-pixel homography T = splat2world^T * world2ndc * ndc2pix
+      // (P0/cr/forward.cu:75-115)
+      const M3 R = quat_to_rot(q);
+      const float mod = b.scale_modifier;
+      const V3 L0 = R.c[0] * (mod * sc.x);
+      const V3 L1 = R.c[1] * (mod * sc.y);
+      // X[j] = (L0, L1, p-hom) . world2ndc column j
+      auto xcol = [&](int j) {
+        return v3(L0.x * pm[j] + L0.y * pm[4 + j] + L0.z * pm[8 + j],
+                  L1.x * pm[j] + L1.y * pm[4 + j] + L1.z * pm[8 + j],
+                  p.x * pm[j] + p.y * pm[4 + j] + p.z * pm[8 + j] + pm[12 + j]);
+      };
+      const V3 X0 = xcol(0), X1 = xcol(1), X3 = xcol(3);
+      const float wh = float(W) / 2.0f, wc = float(W - 1) / 2.0f;
+      const float hh = float(H) / 2.0f, hc = float(H - 1) / 2.0f;
+      Tu = X0 * wh + X3 * wc;
+      Tv = X1 * hh + X3 * hc;
+      Tw = X3;
+      normal = xform_vec43(R.c[2], vm);
+    } else {
+      // camera-space homography (P1/cr/forward.cu:75-128)
+      const M3 R = quat_to_rot(q);
+      const V3 m0 = xform_vec43(R.c[0] * sc.x, vm);
+      const V3 m1 = xform_vec43(R.c[1] * sc.y, vm);
+      V3 tn = xform_vec43(R.c[2], vm);
+      const float cosv = dot3(v3(-tn.x, -tn.y, -tn.z), pv);
+      if (cosv == 0.0f) continue;
+      tn = (cosv > 0 ? 1.f : -1.f) * tn;
+      const float cx = (float)(W / 2.0), cy = (float)(H / 2.0);
+      Tu = v3(focal_x * m0.x + cx * m0.z, focal_x * m1.x + cx * m1.z, focal_x * pv.x + cx * pv.z);
+      Tv = v3(focal_y * m0.y + cy * m0.z, focal_y * m1.y + cy * m1.z, focal_y * pv.y + cy * pv.z);
+      Tw = v3(m0.z, m1.z, pv.z);
+      normal = tn;
+    }
+    if (VARIANT == SGR_VARIANT_PLAIN) {
+      // dual visibility: orient the normal toward the camera (P0/cr/forward.cu:209-214)
+      const float cosv = -sum3(pv * normal);
+      if (cosv == 0.f) continue;
+      normal = (cosv > 0 ? 1.f : -1.f) * normal;
+    }
+
+    // screen-space centre and extent (P0/cr/forward.cu:119-145, P1/cr/forward.cu:133-163)
+    float cxp, cyp, radius;
+    {
+      const V3 tw2 = Tw * Tw;
+      if (VARIANT == SGR_VARIANT_PLAIN) {
+        const V3 t = v3(9.f, 9.f, -1.f);
+        const float d = dot3(t, tw2);
+        if (d == 0.0f) continue;
+        const V3 f = (1 / d) * t;
+        cxp = dot3(f, Tu * Tw);
+        cyp = dot3(f, Tv * Tw);
+        const float h0x = cxp * cxp - dot3(f, Tu * Tu);
+        const float h0y = cyp * cyp - dot3(f, Tv * Tv);
+        const float hx = sqrtf(fmaxf(1e-4f, h0x));
+        const float hy = sqrtf(fmaxf(1e-4f, h0y));
+        radius = ceilf(fmaxf(fmaxf(hx, hy), 3.0f * kFilterSizeP0));
+      } else {
+        const V3 t = v3(1.f, 1.f, -1.f);
+        const float d = dot3(t, tw2);
+        if (d == 0.0f) continue;
+        const V3 f = t * (1.0f / d);
+        cxp = dot3(f, Tu * Tw);
+        cyp = dot3(f, Tv * Tw);
+        const float h0x = cxp * cxp - dot3(f, Tu * Tu);
+        const float h0y = cyp * cyp - dot3(f, Tv * Tv);
+        const float hx = sqrtf(fmaxf(0.f, h0x));
+        const float hy = sqrtf(fmaxf(0.f, h0y));
+        radius = (float)ceil(3.0 * fmax((double)fmaxf(hx, hy), kFilterSizeP1));
+      }
+    }
+    int x0, y0, x1, y1;
+    tile_rect(cxp, cyp, (int)radius, gx, gy, x0, y0, x1, y1);
+    const int touched = (y1 - y0) * (x1 - x0);
+    if (touched == 0) continue;
+
+    // view-dependent colour (P0/cr/forward.cu:20-71)
+    V3 rgb = cpre;
+    uint32_t clamped = 0;
+    if (b.shs != nullptr) rgb = sh_to_rgb(b.sh_degree, sh, p, v3(b.campos[3 * v], b.campos[3 * v + 1], b.campos[3 * v + 2]), clamped);
+
+    float4* rec = g.records + (size_t)r * kRecF4;
+    rec[0] = make_float4(Tu.x, Tu.y, Tu.z, Tv.x);
+    rec[1] = make_float4(Tv.y, Tv.z, Tw.x, Tw.y);
+    rec[2] = make_float4(Tw.z, cxp, cyp, opac);
+    rec[3] = make_float4(normal.x, normal.y, normal.z, pv.z);
+    rec[4] = make_float4(rgb.x, rgb.y, rgb.z, __uint_as_float(clamped));
+    g.radii[r] = (int)radius;
+    g.tiles_touched[r] = (uint32_t)touched;
+    g.depth_keys[r] = ((unsigned long long)v << 32) | (unsigned long long)__float_as_uint(pv.z);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// key duplication: one key per (surfel, touched tile), emitted in depth order
+// so that a stable sort by tile alone reproduces the reference's
+// (tile, depth, surfel) order (P0/cr/rasterizer_impl.cu:70-111, 304-309)
+// ---------------------------------------------------------------------------
+__global__ void k_duplicate(const sgr_batch b, GeomView g, uint32_t* __restrict__ keys,
+                            uint32_t* __restrict__ vals, long long capacity) {
+  const long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= b.num_records) return;
+  const uint32_t r = g.depth_order[j];
+  const uint32_t n = g.tiles_touched[r];
+  if (n == 0) return;
+  const unsigned long long end = g.offsets[j];
+  const unsigned long long start = end - n;
+  // Past the capacity the keys are dropped and the overflow flag raised;
+  // every slot below the capacity still receives a valid key.
+  if ((long long)end > capacity) atomicOr(&g.status->flags, SGR_FLAG_KEY_OVERFLOW);
+  if ((long long)start >= capacity) return;
+  const int v = find_view(b.views, b.num_views, (int)r);
+  const float4 r2 = g.records[(size_t)r * kRecF4 + 2];
+  int x0, y0, x1, y1;
+  tile_rect(r2.y, r2.z, g.radii[r], g.tiles_x, g.tiles_y, x0, y0, x1, y1);
+  const uint32_t base = (uint32_t)v * (uint32_t)(g.tiles_x * g.tiles_y);
+  unsigned long long o = start;
+  for (int y = y0; y < y1; ++y)
+    for (int x = x0; x < x1; ++x) {
+      if ((long long)o < capacity) {
+        keys[o] = base + (uint32_t)(y * g.tiles_x + x);
+        vals[o] = r;
+      }
+      ++o;
+    }
+}
+
+// Pads the unused tail of a fixed-capacity key array with a key above every
+// tile so that a sort over the whole capacity leaves it at the end.
+__global__ void k_pad_keys(uint32_t* keys, long long capacity, const Status* st, uint32_t pad_key) {
+  const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= capacity) return;
+  if ((unsigned long long)k >= st->num_keys) keys[k] = pad_key;
+}
+
+__global__ void k_store_key_count(GeomView g, long long R) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) g.status->num_keys = R > 0 ? g.offsets[R - 1] : 0ull;
+}
+
+// Per-tile [start, end) of the sorted list (P0/cr/rasterizer_impl.cu:116-138).
+__global__ void k_tile_ranges(const uint32_t* __restrict__ keys, const Status* st, long long capacity,
+                              uint2* __restrict__ ranges) {
+  const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long K = (long long)min((unsigned long long)capacity, st->num_keys);
+  if (k >= K) return;
+  const uint32_t cur = keys[k];
+  if (k == 0) ranges[cur].x = 0;
+  else {
+    const uint32_t prev = keys[k - 1];
+    if (cur != prev) {
+      ranges[prev].y = (uint32_t)k;
+      ranges[cur].x = (uint32_t)k;
+    }
+  }
+  if (k == K - 1) ranges[cur].y = (uint32_t)K;
+}
+
+// ---------------------------------------------------------------------------
+// blend forward: one CTA per 16x16 tile, one pixel per thread, surfel records
+// staged 256 at a time in shared memory (P0/cr/forward.cu:256-441,
+// P1/cr/forward.cu:265-474)
+// ---------------------------------------------------------------------------
+template <int VARIANT>
+__global__ void __launch_bounds__(kBlock) k_render_fwd(const sgr_batch b, GeomView g,
+                                                       const uint32_t* __restrict__ point_list,
+                                                       sgr_fwd_outputs out) {
+  const int tiles_per_view = g.tiles_x * g.tiles_y;
+  const int tile = blockIdx.x;
+  const int v = tile / tiles_per_view;
+  const int t = tile - v * tiles_per_view;
+  const int ty = t / g.tiles_x, tx = t - ty * g.tiles_x;
+  const int W = b.width, H = b.height;
+  const int px = tx * kTile + (threadIdx.x & (kTile - 1));
+  const int py = ty * kTile + (threadIdx.x / kTile);
+  const bool inside = px < W && py < H;
+  const float pxf = (VARIANT == SGR_VARIANT_PLAIN) ? (float)px : (float)px + 0.5f;
+  const float pyf = (VARIANT == SGR_VARIANT_PLAIN) ? (float)py : (float)py + 0.5f;
+  const int S = (VARIANT == SGR_VARIANT_PART) ? b.semantic_channels : 0;
+  const sgr_view_desc vd = b.views[v];
+  const int sid_base = b.scenes[vd.scene].surfel_offset - vd.record_offset;
+
+  __shared__ float4 s_rec[kRecF4][kBlock];
+  __shared__ float s_sem[(VARIANT == SGR_VARIANT_PART) ? SGR_MAX_SEMANTICS : 1][kBlock];
+
+  const uint2 range = g.ranges[tile];
+  const int todo_all = (int)(range.y - range.x);
+  const int rounds = (todo_all + kBlock - 1) / kBlock;
+  int todo = todo_all;
+  bool done = !inside;
+
+  float T = 1.0f;
+  uint32_t contributor = 0, last_contributor = 0;
+  float C[3] = {0.f, 0.f, 0.f};
+  float N[3] = {0.f, 0.f, 0.f};
+  float D = 0.f, M1 = 0.f, M2 = 0.f, dist = 0.f, med_depth = 0.f, med_weight = 0.f;
+  int med_contrib = -1;
+  float Sem[SGR_MAX_SEMANTICS];
+#pragma unroll
+  for (int c = 0; c < SGR_MAX_SEMANTICS; ++c) Sem[c] = 0.f;
+
+  for (int i = 0; i < rounds; ++i, todo -= kBlock) {
+    if (__syncthreads_count(done) == kBlock) break;
+    const int progress = i * kBlock + threadIdx.x;
+    if ((int)range.x + progress < (int)range.y) {
+      const uint32_t r = point_list[range.x + progress];
+      const float4* rec = g.records + (size_t)r * kRecF4;
+#pragma unroll
+      for (int k = 0; k < kRecF4; ++k) s_rec[k][threadIdx.x] = rec[k];
+      if (VARIANT == SGR_VARIANT_PART) {
+        const float* sem = b.semantics + (size_t)(sid_base + (int)r) * S;
+        for (int c = 0; c < S; ++c) s_sem[c][threadIdx.x] = sem[c];
+      }
+    }
+    __syncthreads();
+    const int n = min(kBlock, todo);
+    for (int j = 0; !done && j < n; ++j) {
+      ++contributor;
+      const float4 r0 = s_rec[0][j], r1 = s_rec[1][j], r2 = s_rec[2][j];
+      const V3 Tu = v3(r0.x, r0.y, r0.z), Tv = v3(r0.w, r1.x, r1.y), Tw = v3(r1.z, r1.w, r2.x);
+      Frag fr;
+      intersect<VARIANT>(pxf, pyf, Tu, Tv, Tw, r2.y, r2.z, fr);
+      if (fr.p.z == 0.0f) continue;
+      if (fr.depth < kNearP0) continue;
+      const float power = -0.5f * fr.rho;
+      if (power > 0.0f) continue;
+      const float alpha = fminf(0.99f, r2.w * expf(power));
+      if (alpha < 1.0f / 255.0f) continue;
+      const float test_T = T * (1 - alpha);
+      if (test_T < 0.0001f) {
+        done = true;
+        continue;
+      }
+      const float4 r3 = s_rec[3][j], r4 = s_rec[4][j];
+      const float A = 1 - T;
+      if (VARIANT == SGR_VARIANT_PLAIN) {
+        const float w = alpha * T;
+        const float m = kFarP0 / (kFarP0 - kNearP0) * (1 - kNearP0 / fr.depth);
+        dist += (m * m * A + M2 - 2 * m * M1) * w;
+        D += fr.depth * w;
+        M1 += m * w;
+        M2 += m * m * w;
+        if (T > 0.5f) {
+          med_depth = fr.depth;
+          med_contrib = (int)contributor;
+        }
+        N[0] += r3.x * w;
+        N[1] += r3.y * w;
+        N[2] += r3.z * w;
+        C[0] += r4.x * w;
+        C[1] += r4.y * w;
+        C[2] += r4.z * w;
+      } else {
+        const float m = mapped_depth_p1(fr.depth);
+        const float err = m * m * A + M2 - 2 * m * M1;
+        dist += err * alpha * T;
+        if (T > 0.5f) {
+          med_depth = fr.depth;
+          med_weight = alpha * T;
+          med_contrib = (int)contributor;
+        }
+        N[0] += r3.x * alpha * T;
+        N[1] += r3.y * alpha * T;
+        N[2] += r3.z * alpha * T;
+        D += fr.depth * alpha * T;
+        M1 += m * alpha * T;
+        M2 += m * m * alpha * T;
+        C[0] += r4.x * alpha * T;
+        C[1] += r4.y * alpha * T;
+        C[2] += r4.z * alpha * T;
+        for (int c = 0; c < S; ++c) Sem[c] += s_sem[c][j] * alpha * T;
+      }
+      T = test_T;
+      last_contributor = contributor;
+    }
+  }
+
+  if (inside) {
+    const size_t HW = (size_t)H * W;
+    const size_t pix = (size_t)py * W + px;
+    float* fT = g.final_T + (size_t)v * 3 * HW;
+    uint32_t* nc = g.n_contrib + (size_t)v * 2 * HW;
+    fT[pix] = T;
+    fT[pix + HW] = M1;
+    fT[pix + 2 * HW] = M2;
+    nc[pix] = last_contributor;
+    nc[pix + HW] = med_contrib > 0 ? (uint32_t)med_contrib : 0u;
+    const float* bg = b.background;
+    float* col = out.color + (size_t)v * 3 * HW;
+    col[pix] = C[0] + T * bg[0];
+    col[pix + HW] = C[1] + T * bg[1];
+    col[pix + 2 * HW] = C[2] + T * bg[2];
+    const int NO = (VARIANT == SGR_VARIANT_PLAIN) ? 7 : 8;
+    float* oth = out.others + (size_t)v * NO * HW;
+    oth[pix] = D;
+    oth[pix + HW] = 1 - T;
+    oth[pix + 2 * HW] = N[0];
+    oth[pix + 3 * HW] = N[1];
+    oth[pix + 4 * HW] = N[2];
+    oth[pix + 5 * HW] = med_depth;
+    oth[pix + 6 * HW] = dist;
+    if (VARIANT == SGR_VARIANT_PART) {
+      oth[pix + 7 * HW] = med_weight;
+      float* sem = out.semantic + (size_t)v * S * HW;
+      for (int c = 0; c < S; ++c) sem[pix + c * HW] = Sem[c];
+    }
+  }
+}
+
+// Near-plane visibility (P0/cr/rasterizer_impl.cu:54-66).
+__global__ void k_mark_visible(int P, const float* __restrict__ means3D, const float* __restrict__ viewmatrix,
+                               uint8_t* __restrict__ present) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= P) return;
+  const V3 p = v3(means3D[3 * i], means3D[3 * i + 1], means3D[3 * i + 2]);
+  present[i] = xform_point43(p, viewmatrix).z > 0.2f ? 1 : 0;
+}
+
+// ---------------------------------------------------------------------------
+// launchers
+// ---------------------------------------------------------------------------
+void launch_preprocess(const sgr_batch& b, const GeomView& g, cudaStream_t st) {
+  const int threads = 128;
+  const int blocks = (b.num_surfels + threads - 1) / threads;
+  if (blocks == 0) return;
+  if (b.variant == SGR_VARIANT_PLAIN) k_preprocess<SGR_VARIANT_PLAIN><<<blocks, threads, 0, st>>>(b, g);
+  else k_preprocess<SGR_VARIANT_PART><<<blocks, threads, 0, st>>>(b, g);
+}
+
+void launch_store_key_count(const GeomView& g, long long R, cudaStream_t st) {
+  k_store_key_count<<<1, 32, 0, st>>>(g, R);
+}
+
+void launch_duplicate(const sgr_batch& b, const GeomView& g, uint32_t* keys, uint32_t* vals, long long capacity,
+                      cudaStream_t st) {
+  const int threads = 256;
+  const long long blocks = ((long long)b.num_records + threads - 1) / threads;
+  if (blocks == 0) return;
+  k_duplicate<<<(unsigned)blocks, threads, 0, st>>>(b, g, keys, vals, capacity);
+}
+
+void launch_pad_keys(uint32_t* keys, long long capacity, const Status* status, uint32_t pad_key, cudaStream_t st) {
+  const int threads = 256;
+  const long long blocks = (capacity + threads - 1) / threads;
+  if (blocks == 0) return;
+  k_pad_keys<<<(unsigned)blocks, threads, 0, st>>>(keys, capacity, status, pad_key);
+}
+
+void launch_tile_ranges(const uint32_t* keys, const Status* status, long long capacity, uint2* ranges,
+                        cudaStream_t st) {
+  const int threads = 256;
+  const long long blocks = (capacity + threads - 1) / threads;
+  if (blocks == 0) return;
+  k_tile_ranges<<<(unsigned)blocks, threads, 0, st>>>(keys, status, capacity, ranges);
+}
+
+void launch_render_fwd(const sgr_batch& b, const GeomView& g, const uint32_t* point_list,
+                       const sgr_fwd_outputs& out, cudaStream_t st) {
+  const unsigned blocks = (unsigned)(g.tiles_x * g.tiles_y) * (unsigned)b.num_views;
+  if (blocks == 0) return;
+  if (b.variant == SGR_VARIANT_PLAIN) k_render_fwd<SGR_VARIANT_PLAIN><<<blocks, kBlock, 0, st>>>(b, g, point_list, out);
+  else k_render_fwd<SGR_VARIANT_PART><<<blocks, kBlock, 0, st>>>(b, g, point_list, out);
+}
+
+void launch_mark_visible(int P, const float* means3D, const float* viewmatrix, uint8_t* present, cudaStream_t st) {
+  const int threads = 256;
+  const int blocks = (P + threads - 1) / threads;
+  if (blocks == 0) return;
+  k_mark_visible<<<blocks, threads, 0, st>>>(P, means3D, viewmatrix, present);
+}
+
+}  // namespace sgr

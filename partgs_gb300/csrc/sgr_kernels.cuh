@@ -1,0 +1,133 @@
+// Device functions shared by the forward and backward kernels, the views of
+// the workspaces the kernels receive, and the launcher declarations.
+#pragma once
+
+#include "sgr_common.cuh"
+
+namespace sgr {
+
+constexpr int kMaxShCoeffs = 16;
+
+// Pointers into the geometry workspace and the forward scratch.
+struct GeomView {
+  float4* records;                       // [R][5]
+  int* radii;                            // [R]
+  uint32_t* tiles_touched;               // [R]
+  unsigned long long* depth_keys;        // [R] (view << 32 | depth bits), forward scratch
+  uint32_t* depth_vals;                  // [R] record ids, forward scratch
+  unsigned long long* depth_keys_sorted; // [R] forward scratch
+  uint32_t* depth_order;                 // [R] record ids in (view, depth, id) order
+  unsigned long long* offsets;           // [R] inclusive scan of tiles_touched in that order
+  uint2* ranges;                         // [V*tiles]
+  float* final_T;                        // [V][3][H][W]
+  uint32_t* n_contrib;                   // [V][2][H][W]
+  Status* status;
+  int tiles_x, tiles_y;
+};
+
+// One pixel / surfel intersection (P0/cr/forward.cu:349-366).
+struct Frag {
+  V3 k, l, p;
+  float sx, sy, rho3d, rho2d, rho, depth, dx, dy;
+  bool use3d;
+};
+
+template <int VARIANT>
+__device__ __forceinline__ void intersect(float pxf, float pyf, V3 Tu, V3 Tv, V3 Tw, float cx, float cy, Frag& f) {
+  if (VARIANT == SGR_VARIANT_PLAIN) {
+    f.k = pxf * Tw - Tu;
+    f.l = pyf * Tw - Tv;
+  } else {
+    f.k = v3(-Tu.x + pxf * Tw.x, -Tu.y + pxf * Tw.y, -Tu.z + pxf * Tw.z);
+    f.l = v3(-Tv.x + pyf * Tw.x, -Tv.y + pyf * Tw.y, -Tv.z + pyf * Tw.z);
+  }
+  f.p = cross3(f.k, f.l);
+  f.sx = f.p.x / f.p.z;
+  f.sy = f.p.y / f.p.z;
+  f.rho3d = f.sx * f.sx + f.sy * f.sy;
+  f.dx = cx - pxf;
+  f.dy = cy - pyf;
+  // Both variants scale by 2: the part variant's double constant
+  // 1/(0.7071067811865476^2) times a float rounds to exactly 2x.
+  f.rho2d = kFilterInvSquareP0 * (f.dx * f.dx + f.dy * f.dy);
+  f.use3d = f.rho3d <= f.rho2d;
+  f.rho = fminf(f.rho3d, f.rho2d);
+  f.depth = f.use3d ? (f.sx * Tw.x + f.sy * Tw.y) + Tw.z : Tw.z;
+}
+
+// Mapped depth of the part variant, evaluated in double as its macros do
+// (P1/cr/forward.cu:415).
+__device__ __forceinline__ float mapped_depth_p1(float depth) {
+  return (float)((kFarP1 * depth - kFarP1 * kNearP1) / ((kFarP1 - kNearP1) * depth));
+}
+
+// View-dependent colour from degree <= 3 SH (P0/cr/forward.cu:20-71).
+__device__ __forceinline__ V3 sh_to_rgb(int deg, const float* sh, V3 pos, V3 campos, uint32_t& clamped) {
+  V3 dir = pos - campos;
+  const float len = sqrtf(dot3(dir, dir));
+  dir = v3(dir.x / len, dir.y / len, dir.z / len);
+  auto c = [&](int k) { return v3(sh[3 * k], sh[3 * k + 1], sh[3 * k + 2]); };
+  V3 res = kShC0 * c(0);
+  if (deg > 0) {
+    const float x = dir.x, y = dir.y, z = dir.z;
+    res = res - kShC1 * y * c(1) + kShC1 * z * c(2) - kShC1 * x * c(3);
+    if (deg > 1) {
+      const float xx = x * x, yy = y * y, zz = z * z;
+      const float xy = x * y, yz = y * z, xz = x * z;
+      res = res + kShC2[0] * xy * c(4) + kShC2[1] * yz * c(5) + kShC2[2] * (2.0f * zz - xx - yy) * c(6) +
+            kShC2[3] * xz * c(7) + kShC2[4] * (xx - yy) * c(8);
+      if (deg > 2) {
+        res = res + kShC3[0] * y * (3.0f * xx - yy) * c(9) + kShC3[1] * xy * z * c(10) +
+              kShC3[2] * y * (4.0f * zz - xx - yy) * c(11) + kShC3[3] * z * (2.0f * zz - 3.0f * xx - 3.0f * yy) * c(12) +
+              kShC3[4] * x * (4.0f * zz - xx - yy) * c(13) + kShC3[5] * z * (xx - yy) * c(14) +
+              kShC3[6] * x * (xx - 3.0f * yy) * c(15);
+      }
+    }
+  }
+  res = res + v3(0.5f, 0.5f, 0.5f);
+  clamped = (res.x < 0 ? 1u : 0u) | (res.y < 0 ? 2u : 0u) | (res.z < 0 ? 4u : 0u);
+  return v3(fmaxf(res.x, 0.0f), fmaxf(res.y, 0.0f), fmaxf(res.z, 0.0f));
+}
+
+__device__ __forceinline__ int find_view(const sgr_view_desc* views, int n, int record) {
+  int lo = 0, hi = n - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (views[mid].record_offset <= record) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+// Warp sum of 32 values per lane, transposed: afterwards lane l holds the
+// warp total of value l.  31 shuffles instead of 5 per value.
+__device__ __forceinline__ float warp_transpose_sum(float (&v)[32], int lane) {
+#pragma unroll
+  for (int o = 16; o >= 1; o >>= 1) {
+    const bool upper = (lane & o) != 0;
+#pragma unroll
+    for (int k = 0; k < o; ++k) {
+      const float send = upper ? v[k] : v[k + o];
+      const float keep = upper ? v[k + o] : v[k];
+      v[k] = keep + __shfl_xor_sync(0xffffffffu, send, o);
+    }
+  }
+  return v[0];
+}
+
+void launch_preprocess(const sgr_batch& b, const GeomView& g, cudaStream_t st);
+void launch_store_key_count(const GeomView& g, long long R, cudaStream_t st);
+void launch_duplicate(const sgr_batch& b, const GeomView& g, uint32_t* keys, uint32_t* vals, long long capacity,
+                      cudaStream_t st);
+void launch_pad_keys(uint32_t* keys, long long capacity, const Status* status, uint32_t pad_key, cudaStream_t st);
+void launch_tile_ranges(const uint32_t* keys, const Status* status, long long capacity, uint2* ranges,
+                        cudaStream_t st);
+void launch_render_fwd(const sgr_batch& b, const GeomView& g, const uint32_t* point_list,
+                       const sgr_fwd_outputs& out, cudaStream_t st);
+void launch_mark_visible(int P, const float* means3D, const float* viewmatrix, uint8_t* present, cudaStream_t st);
+
+void launch_render_bwd(const sgr_batch& b, const GeomView& g, const uint32_t* point_list, const sgr_bwd_inputs& in,
+                       float* grads, float* dL_dsemantics, cudaStream_t st);
+void launch_preprocess_bwd(const sgr_batch& b, const GeomView& g, const float* grads, const sgr_bwd_outputs& out,
+                           cudaStream_t st);
+
+}  // namespace sgr

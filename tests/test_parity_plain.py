@@ -1,0 +1,123 @@
+"""Parity of the plain rasteriser (libsgr.so on the GPU) against the CPU
+oracle on the 4,096-surfel, 128x128 workload: integer state bit-exact,
+images within 1e-5 relative (FP32), gradients within 1e-4 relative."""
+import numpy as np
+import pytest
+import torch
+
+from oracle import surfel_oracle as O
+from tests._util import grad_error, image_error, oracle_camera, oracle_surfels, settings
+
+pytestmark = pytest.mark.gpu
+
+IMG_TOL = 1e-5     # relative, per channel, FP32 vs the oracle
+GRAD_TOL = 1e-4    # relative to the tensor's largest magnitude
+
+
+@pytest.fixture(scope="module")
+def case(sgr_lib):
+    from partgs_gb300 import raster
+    from partgs_gb300.scenes import workload
+    from partgs_gb300 import _lib as L
+    scene, cams = workload("random4k_128")
+    cam = cams[0]
+    dev = torch.device("cuda")
+    sc = scene.to(dev)
+    rs = settings(__import__("partgs_gb300.diff_surfel_rasterization", fromlist=["x"]), cam, [0.0, 0.0, 0.0])
+    vs = raster.ViewSet(rs.viewmatrix.reshape(1, 16), rs.projmatrix.reshape(1, 16), rs.campos.reshape(1, 3),
+                        [(cam.tanfovx, cam.tanfovy)], cam.height, cam.width)
+    color, others, _, radii, state = raster.forward(L.SGR_VARIANT_PLAIN, sc.means3D, sc.opacities, sc.shs, None,
+                                                    sc.scales, sc.rotations, None, None, vs, rs.bg, 3)
+    dbg = raster.debug_state(state)
+    ocam = oracle_camera(cam)
+    osf = oracle_surfels(scene)
+    st64 = O.forward_view(osf, ocam, np.zeros(3), O.PLAIN, np.float64)
+    st32 = O.forward_view(osf, ocam, np.zeros(3), O.PLAIN, np.float32)
+    g = np.random.default_rng(1)
+    dcol = g.standard_normal((3, cam.height, cam.width)).astype(np.float32)
+    doth = g.standard_normal((7, cam.height, cam.width)).astype(np.float32)
+    amb = st64.amb_pixel | st32.amb_pixel
+    dcol[:, amb] = 0
+    doth[:, amb] = 0
+    grads = raster.backward(state, torch.from_numpy(dcol)[None].cuda(), torch.from_numpy(doth)[None].cuda())
+    ref_g = O.backward_view(st64, ocam, osf, np.zeros(3), dcol, doth, variant=O.PLAIN, dtype=np.float64)
+    torch.cuda.synchronize()
+    return dict(scene=scene, cam=cam, color=color[0].cpu().numpy(), others=others[0].cpu().numpy(),
+                radii=radii.cpu().numpy(), dbg={k: (v.cpu().numpy() if torch.is_tensor(v) else v) for k, v in dbg.items()},
+                st64=st64, st32=st32, amb=amb, grads={k: v.cpu().numpy() for k, v in grads.items()}, ref_g=ref_g,
+                state=state)
+
+
+def test_radii_and_tiles_bit_exact(case):
+    st, amb_s = case["st64"], case["st64"].amb_surfel | case["st32"].amb_surfel
+    assert amb_s.sum() <= 4, "too many surfels near a rounding boundary for a meaningful check"
+    np.testing.assert_array_equal(case["radii"][~amb_s], st.radii[~amb_s])
+    np.testing.assert_array_equal(case["dbg"]["tiles_touched"][~amb_s], st.tiles_touched[~amb_s])
+    assert (case["radii"] > 0).sum() == (st.radii > 0).sum()
+
+
+def test_tile_lists_bit_exact(case):
+    """Per tile, the sorted surfel list equals the reference's (tile, depth,
+    index) order: same keys, same order, same range lengths."""
+    st = case["st64"]
+    amb_t = st.extra["amb_tiles"] | case["st32"].extra["amb_tiles"]
+    ranges = case["dbg"]["ranges"]
+    pl = case["dbg"]["point_list"]
+    checked = 0
+    for t in range(ranges.shape[0]):
+        if amb_t[t]:
+            continue
+        mine = pl[ranges[t, 0]:ranges[t, 1]]
+        ref = st.point_list[st.ranges[t, 0]:st.ranges[t, 1]]
+        np.testing.assert_array_equal(mine, ref, err_msg=f"tile {t}")
+        checked += 1
+    assert checked >= ranges.shape[0] - 8
+    if not amb_t.any():
+        assert case["dbg"]["num_keys"] == len(st.point_list)
+        np.testing.assert_array_equal(ranges, st.ranges)
+
+
+def test_n_contrib_bit_exact(case):
+    st = case["st64"]
+    amb = case["amb"]
+    nc = case["dbg"]["n_contrib"][0]
+    np.testing.assert_array_equal(nc[0][~amb], st.n_contrib[0][~amb])
+    np.testing.assert_array_equal(nc[1][~amb], st.n_contrib[1][~amb])
+
+
+@pytest.mark.parametrize("which", ["st32", "st64"])
+def test_images(case, which):
+    st = case[which]
+    amb = case["amb"]
+    assert amb.mean() < 0.01
+    e_col = image_error(case["color"], st.color, amb)
+    e_oth = image_error(case["others"], st.others, amb)
+    assert max(e_col) <= IMG_TOL, e_col
+    assert max(e_oth) <= 10 * IMG_TOL if which == "st64" else max(e_oth) <= IMG_TOL, e_oth
+    ft = case["dbg"]["final_T"][0]
+    assert max(image_error(ft, st.final_T, amb)) <= IMG_TOL
+
+
+def test_gradients(case):
+    g, r = case["grads"], case["ref_g"]
+    names = ["dL_dcolors", "dL_dopacity", "dL_dmeans3D", "dL_dtransmat", "dL_dsh", "dL_dscales",
+             "dL_drotations", "dL_dmeans2D"]
+    errs = {k: grad_error(g[k], r[k]) for k in names}
+    bad = {k: v for k, v in errs.items() if v > GRAD_TOL}
+    assert not bad, errs
+
+
+def test_dropin_api_matches_core(case):
+    """The drop-in GaussianRasterizer returns the same tensors as the core."""
+    import partgs_gb300.diff_surfel_rasterization as dsr
+    scene = case["scene"].to("cuda")
+    rs = settings(dsr, case["cam"], [0.0, 0.0, 0.0])
+    means2D = torch.zeros_like(scene.means3D, requires_grad=True)
+    img, radii, allmap = dsr.GaussianRasterizer(rs)(means3D=scene.means3D, means2D=means2D, shs=scene.shs,
+                                                    colors_precomp=None, opacities=scene.opacities,
+                                                    scales=scene.scales, rotations=scene.rotations,
+                                                    cov3D_precomp=None)
+    assert img.shape == (3, 128, 128) and allmap.shape == (7, 128, 128) and radii.dtype == torch.int32
+    np.testing.assert_array_equal(img.detach().cpu().numpy(), case["color"])
+    np.testing.assert_array_equal(allmap.detach().cpu().numpy(), case["others"])
+    np.testing.assert_array_equal(radii.cpu().numpy(), case["radii"])
