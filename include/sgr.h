@@ -198,6 +198,25 @@ int sgr_backward(const sgr_batch* batch, const void* geom, const void* lists, in
                  void* bwd_scratch, size_t bwd_scratch_bytes, const sgr_bwd_inputs* in,
                  const sgr_bwd_outputs* out, void* stream);
 
+/* ---- phase timing ------------------------------------------------------ */
+
+/* Phases the entry points bracket with CUDA events while profiling is on. */
+#define SGR_PHASE_PREPROCESS 0      /* per-view preprocess */
+#define SGR_PHASE_DEPTH_ORDER 1     /* depth order and key offsets */
+#define SGR_PHASE_BINNING 2         /* (surfel, tile) list construction */
+#define SGR_PHASE_BLEND_FWD 3
+#define SGR_PHASE_BLEND_BWD 4
+#define SGR_PHASE_PREPROCESS_BWD 5
+#define SGR_NUM_PHASES 6
+
+/* Turns event recording on (1) or off (0) for calls made afterwards from
+ * any thread.  Events are recorded on the caller's stream. */
+int sgr_profile_enable(int enable);
+/* Waits for the recorded events, writes the summed milliseconds and the
+ * number of recordings of each phase since the last read (arrays of
+ * SGR_NUM_PHASES), and forgets them. */
+int sgr_profile_read(float* ms, int32_t* count);
+
 /* Near-plane visibility of P points in one view (present: uint8[P]). */
 int sgr_mark_visible(int32_t P, const float* means3D, const float* viewmatrix, const float* projmatrix,
                      uint8_t* present, void* stream);

@@ -452,18 +452,20 @@ def bin_tiles(pre: dict):
     xmin, ymin, xmax, ymax = pre["rect"]
     alive = pre["alive"]
     depth_bits = pre["depths"].astype(np.float32).view(np.uint32).astype(np.uint64)
-    tiles, ids = [], []
-    for i in np.nonzero(alive)[0]:
-        ys = np.arange(ymin[i], ymax[i])
-        xs = np.arange(xmin[i], xmax[i])
-        t = (ys[:, None] * gx + xs[None, :]).reshape(-1)
-        tiles.append(t)
-        ids.append(np.full(t.shape, i, dtype=np.int64))
     ntiles = gx * gy
-    if not tiles:
+    vis = np.nonzero(alive)[0]
+    w = (xmax - xmin)[vis]
+    n = ((ymax - ymin)[vis] * w).astype(np.int64)
+    if n.sum() == 0:
         return (np.zeros(0, np.int64), np.zeros((ntiles, 2), np.int64), np.zeros(0, np.uint64))
-    tiles = np.concatenate(tiles).astype(np.int64)
-    ids = np.concatenate(ids)
+    # one key per (surfel, tile), surfels in index order, tiles row-major
+    # inside each surfel's rectangle (P0/cr/rasterizer_impl.cu:98-109)
+    ids = np.repeat(vis, n)
+    starts = np.cumsum(n) - n
+    local = np.arange(int(n.sum()), dtype=np.int64) - np.repeat(starts, n)
+    wr = np.repeat(w, n)
+    tiles = (ymin[ids] + local // wr) * gx + (xmin[ids] + local % wr)
+    tiles = tiles.astype(np.int64)
     keys = (tiles.astype(np.uint64) << np.uint64(32)) | depth_bits[ids]
     # stable sort by the 64-bit key: equal keys keep emission (index) order
     order = np.argsort(keys, kind="stable")
@@ -477,9 +479,11 @@ def bin_tiles(pre: dict):
     return point_list, ranges, keys
 
 
-def _tile_pixels(gx, gy, W, H, variant, f):
-    """Per tile, per thread: pixel coordinates and the inside mask."""
-    ty, tx = np.divmod(np.arange(gx * gy), gx)
+def _tile_pixels(gx, gy, W, H, variant, f, tiles=None):
+    """Per tile, per thread: pixel coordinates and the inside mask (all
+    tiles, or the subset ``tiles``)."""
+    ids = np.arange(gx * gy) if tiles is None else np.asarray(tiles)
+    ty, tx = np.divmod(ids, gx)
     ly, lx = np.divmod(np.arange(BLOCK_SIZE), BLOCK_X)
     X = tx[:, None] * BLOCK_X + lx[None, :]
     Y = ty[:, None] * BLOCK_Y + ly[None, :]
@@ -488,7 +492,9 @@ def _tile_pixels(gx, gy, W, H, variant, f):
     return X, Y, X.astype(f) + f(off), Y.astype(f) + f(off), inside
 
 
-def _padded_lists(point_list, ranges):
+def _padded_lists(point_list, ranges, tiles=None):
+    if tiles is not None:
+        ranges = ranges[np.asarray(tiles)]
     lens = ranges[:, 1] - ranges[:, 0]
     L = int(lens.max()) if lens.size else 0
     lists = np.full((ranges.shape[0], max(L, 1)), -1, dtype=np.int64)
@@ -534,13 +540,13 @@ def _mapped_depth(variant, f, depth):
 
 
 def render_forward(pre, point_list, ranges, cam: Camera, s: Surfels, bg, variant=PLAIN, dtype=np.float64,
-                   amb_tol=2e-6):
+                   amb_tol=2e-6, tiles=None):
     f = _f(dtype)
     gx, gy = pre["grid"]
     W, H = cam.width, cam.height
-    X, Y, pxf, pyf, inside = _tile_pixels(gx, gy, W, H, variant, f)
-    lists, lens, L = _padded_lists(point_list, ranges)
-    nt = gx * gy
+    X, Y, pxf, pyf, inside = _tile_pixels(gx, gy, W, H, variant, f, tiles)
+    lists, lens, L = _padded_lists(point_list, ranges, tiles)
+    nt = lists.shape[0]
     Sn = 0 if s.semantics is None else s.semantics.shape[1]
     sem_all = None if s.semantics is None else s.semantics.astype(dtype)
     tm, xy2, no, rgb = pre["transmat"], pre["means2D"], pre["normal_opacity"], pre["rgb"]
@@ -564,6 +570,8 @@ def render_forward(pre, point_list, ranges, cam: Camera, s: Surfels, bg, variant
     amb = np.zeros(shape, bool)
     frags = 0
     for j in range(L):
+        if done.all():
+            break
         ids = lists[:, j]
         has = (ids >= 0)[:, None]
         act = has & ~done
@@ -669,10 +677,13 @@ def _gather_pixels(img, X, Y, inside):
 # --------------------------------------------------------------------------
 # full forward of one view
 # --------------------------------------------------------------------------
-def forward_view(s: Surfels, cam: Camera, bg, variant=PLAIN, dtype=np.float64, amb_tol=2e-6) -> ViewState:
+def forward_view(s: Surfels, cam: Camera, bg, variant=PLAIN, dtype=np.float64, amb_tol=2e-6,
+                 tiles=None) -> ViewState:
+    """Forward of one view; with ``tiles`` only those tiles are blended (the
+    other pixels stay zero)."""
     pre = preprocess(s, cam, variant, dtype, amb_tol)
     point_list, ranges, keys = bin_tiles(pre)
-    rf = render_forward(pre, point_list, ranges, cam, s, bg, variant, dtype, amb_tol)
+    rf = render_forward(pre, point_list, ranges, cam, s, bg, variant, dtype, amb_tol, tiles)
     st = ViewState(
         radii=pre["radii"], tiles_touched=pre["tiles_touched"], means2D=pre["means2D"],
         depths=pre["depths"], transmat=pre["transmat"], normal_opacity=pre["normal_opacity"],
@@ -712,7 +723,7 @@ def forward_view(s: Surfels, cam: Camera, bg, variant=PLAIN, dtype=np.float64, a
 # backward
 # --------------------------------------------------------------------------
 def render_backward(st: ViewState, cam: Camera, s: Surfels, bg, dL_dcolor, dL_dothers, dL_dsem=None,
-                    variant=PLAIN, dtype=np.float64):
+                    variant=PLAIN, dtype=np.float64, tiles=None):
     """Blend backward, P0/cr/backward.cu:143-440 / P1/cr/backward.cu:143-470.
     Returns per-surfel accumulators (dL_dtransmat, dL_dmean2D, dL_dnormal,
     dL_dopacity, dL_dcolor, dL_dsemantics)."""
@@ -721,9 +732,9 @@ def render_backward(st: ViewState, cam: Camera, s: Surfels, bg, dL_dcolor, dL_do
     gx, gy = pre["grid"]
     W, H = cam.width, cam.height
     P = s.P
-    X, Y, pxf, pyf, inside = _tile_pixels(gx, gy, W, H, variant, f)
-    lists, lens, L = _padded_lists(st.point_list, st.ranges)
-    nt = gx * gy
+    X, Y, pxf, pyf, inside = _tile_pixels(gx, gy, W, H, variant, f, tiles)
+    lists, lens, L = _padded_lists(st.point_list, st.ranges, tiles)
+    nt = lists.shape[0]
     tm, xy2, no, rgb = st.transmat, st.means2D, st.normal_opacity, st.rgb
     bg = np.asarray(bg, dtype=dtype)
     Sn = 0 if s.semantics is None else s.semantics.shape[1]
@@ -1011,7 +1022,7 @@ def preprocess_backward(st: ViewState, rb: dict, cam: Camera, s: Surfels, varian
         dL_dcolors=rb["dL_dcolor"],
         dL_dopacity=rb["dL_dopacity"][:, None],
         dL_dmeans3D=z3(dmean3D),
-        dL_dtransMat=gT,
+        dL_dtransmat=gT,
         dL_dsh=dsh,
         dL_dscales=z3(dscale),
         dL_drotations=z3(drot),
@@ -1021,8 +1032,9 @@ def preprocess_backward(st: ViewState, rb: dict, cam: Camera, s: Surfels, varian
     return out
 
 
-def backward_view(st, cam, s, bg, dL_dcolor, dL_dothers, dL_dsem=None, variant=PLAIN, dtype=np.float64):
-    rb = render_backward(st, cam, s, bg, dL_dcolor, dL_dothers, dL_dsem, variant, dtype)
+def backward_view(st, cam, s, bg, dL_dcolor, dL_dothers, dL_dsem=None, variant=PLAIN, dtype=np.float64,
+                  tiles=None):
+    rb = render_backward(st, cam, s, bg, dL_dcolor, dL_dothers, dL_dsem, variant, dtype, tiles)
     return preprocess_backward(st, rb, cam, s, variant, dtype)
 
 

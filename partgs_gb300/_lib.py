@@ -20,6 +20,7 @@ SGR_VARIANT_PLAIN = 0
 SGR_VARIANT_PART = 1
 SGR_MAX_SEMANTICS = 16
 SGR_TILE = 16
+PHASES = ("preprocess", "depth_order", "binning", "blend_fwd", "blend_bwd", "preprocess_bwd")
 
 _p = C.c_void_p
 _f = C.c_float
@@ -86,6 +87,8 @@ SIGNATURES = {
     "sgr_backward": (C.c_int, [C.POINTER(Batch), _p, _p, C.c_int64, _p, C.c_size_t, C.POINTER(BwdInputs),
                                C.POINTER(BwdOutputs), _p]),
     "sgr_mark_visible": (C.c_int, [_i, _p, _p, _p, _p, _p]),
+    "sgr_profile_enable": (C.c_int, [C.c_int]),
+    "sgr_profile_read": (C.c_int, [C.POINTER(C.c_float), C.POINTER(C.c_int32)]),
     "sgr_bind_forward": (C.c_int, [C.POINTER(BindArgs), _p, _p, _p, _p, _p]),
     "sgr_bind_scratch_bytes": (C.c_size_t, [C.POINTER(BindArgs)]),
     "sgr_bind_backward": (C.c_int, [C.POINTER(BindArgs), _p, _p, _p, _p, _p, _p, _p, _p, _p, _p, _p]),

@@ -1,0 +1,97 @@
+"""Many views (and many scenes) in one launch sequence.
+
+``MultiViewRasterizer`` rasterises every camera of a set in one call of the
+library: one preprocess over all (surfel, view) records, one depth order,
+one key list over all views' tiles and one blend launch over all tiles of
+all views; the backward sums each surfel's per-view gradients on the device.
+With ``key_capacity`` set, no call synchronises the host, so a whole
+training step built on it can be captured in a CUDA graph
+(``torch.cuda.graph``); the key count and overflow flag of the last forward
+are then read from ``status`` after the step.
+
+Scenes of different sizes are batched the same way: pass ``scene_sizes``
+(surfels per scene, surfels concatenated) and ``scene_views`` (cameras per
+scene, cameras grouped by scene).
+"""
+from __future__ import annotations
+
+import torch
+
+from . import _lib as L
+from . import raster as _r
+
+
+class _MultiViewFn(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, means3D, opacities, shs, scales, rotations, colors_precomp, semantics, cfg):
+        color, others, semantic, radii, state = _r.forward(
+            cfg.variant, means3D, opacities, shs, colors_precomp, scales, rotations, None, semantics, cfg.viewset,
+            cfg.bg, cfg.sh_degree, 1.0, False, key_capacity=cfg.key_capacity, tables=cfg.tables,
+            status_host=cfg.status)
+        ctx.state = state
+        ctx.cfg = cfg
+        ctx.op_shape = opacities.shape
+        ctx.has = (shs is not None, colors_precomp is not None, semantics is not None)
+        ctx.mark_non_differentiable(radii)
+        if semantic is None:
+            semantic = torch.empty(0, device=means3D.device)
+        return color, others, semantic, radii
+
+    @staticmethod
+    def backward(ctx, d_color, d_others, d_semantic, d_radii):
+        cfg = ctx.cfg
+        g = _r.backward(ctx.state, d_color, d_others, d_semantic if ctx.has[2] else None)
+        cfg.last_means2D_grad = g["dL_dmeans2D"]
+        return (g["dL_dmeans3D"], g["dL_dopacity"].reshape(ctx.op_shape),
+                g["dL_dsh"] if ctx.has[0] else None, g["dL_dscales"], g["dL_drotations"],
+                g["dL_dcolors"] if ctx.has[1] else None,
+                g["dL_dsemantics"] if ctx.has[2] else None, None)
+
+
+class MultiViewRasterizer:
+    """Rasterises a fixed set of cameras; tables and camera tensors are built
+    once, so calls make no host-to-device copies."""
+
+    def __init__(self, cameras, bg, sh_degree=3, variant=L.SGR_VARIANT_PLAIN, key_capacity=None,
+                 scene_sizes=None, scene_views=None, num_surfels=None, device="cuda"):
+        dev = torch.device(device)
+        self.cameras = list(cameras)
+        self.variant = variant
+        self.sh_degree = sh_degree
+        self.key_capacity = key_capacity
+        self.bg = torch.as_tensor(bg, dtype=torch.float32, device=dev)
+        vm = torch.stack([torch.as_tensor(c.world_view_transform, dtype=torch.float32) for c in cameras])
+        pm = torch.stack([torch.as_tensor(c.full_proj_transform, dtype=torch.float32) for c in cameras])
+        cp = torch.stack([torch.as_tensor(c.camera_center, dtype=torch.float32) for c in cameras])
+        H = {c.height for c in cameras}
+        W = {c.width for c in cameras}
+        if len(H) != 1 or len(W) != 1:
+            raise ValueError("all cameras of a batch share one image size")
+        self.viewset = _r.ViewSet(vm.reshape(-1, 16).to(dev), pm.reshape(-1, 16).to(dev), cp.to(dev),
+                                  [(c.tanfovx, c.tanfovy) for c in cameras], H.pop(), W.pop(),
+                                  scene_sizes, scene_views)
+        P = num_surfels if num_surfels is not None else (sum(scene_sizes) if scene_sizes else None)
+        self.tables = _r._tables(variant, P, self.viewset, dev) if P is not None else None
+        self.status = torch.zeros(16, dtype=torch.uint8).pin_memory()
+        self.last_means2D_grad = None
+
+    @property
+    def num_views(self):
+        return len(self.cameras)
+
+    def set_capacity(self, key_capacity):
+        self.key_capacity = key_capacity
+
+    def key_count(self):
+        """(key count, flags) of the last forward; valid once the stream has
+        passed that forward (capacity mode only)."""
+        return _r.read_status(self.status)
+
+    def __call__(self, means3D, opacities, shs=None, scales=None, rotations=None, colors_precomp=None,
+                 semantics=None):
+        if self.tables is None or self.tables[3] != int(means3D.shape[0]) * self.num_views and \
+                self.viewset.scene_sizes is None:
+            self.tables = _r._tables(self.variant, int(means3D.shape[0]), self.viewset, means3D.device)
+        color, others, semantic, radii = _MultiViewFn.apply(means3D, opacities, shs, scales, rotations,
+                                                            colors_precomp, semantics, self)
+        return color, others, (semantic if semantics is not None else None), radii

@@ -8,6 +8,7 @@
 #include <string>
 
 #include "sgr_kernels.cuh"
+#include "sgr_profile.cuh"
 
 namespace sgr {
 namespace {
@@ -224,8 +225,12 @@ int sgr_forward_geometry(const sgr_batch* batch, void* geom, void* fwd_scratch, 
   SGR_CUDA(cudaMemsetAsync(g.status, 0, sizeof(Status), st));
   const long long R = batch->num_records;
   if (R > 0) {
-    launch_preprocess(*batch, g, st);
+    {
+      PhaseScope ph(SGR_PHASE_PREPROCESS, st);
+      launch_preprocess(*batch, g, st);
+    }
     SGR_CUDA(cudaGetLastError());
+    PhaseScope ph(SGR_PHASE_DEPTH_ORDER, st);
     size_t tb = L.temp_a_bytes;
     char* sp = static_cast<char*>(fwd_scratch);
     SGR_CUDA(cub::DeviceRadixSort::SortPairs(sp + L.temp_a, tb, g.depth_keys, g.depth_keys_sorted, g.depth_vals,
@@ -276,6 +281,7 @@ int sgr_forward_raster(const sgr_batch* batch, void* geom, void* lists, int64_t 
   }
   SGR_CUDA(cudaMemsetAsync(g.ranges, 0, (size_t)batch->num_views * s.tiles_x * s.tiles_y * 8, st));
   if (key_capacity > 0) {
+    PhaseScope ph(SGR_PHASE_BINNING, st);
     launch_duplicate(*batch, g, keys, vals, key_capacity, st);
     SGR_CUDA(cudaGetLastError());
     const uint32_t pad = (s.tile_key_bits >= 32) ? 0xffffffffu : ((1u << s.tile_key_bits) - 1u);
@@ -287,7 +293,10 @@ int sgr_forward_raster(const sgr_batch* batch, void* geom, void* lists, int64_t 
     launch_tile_ranges(keys_sorted, g.status, key_capacity, g.ranges, st);
     SGR_CUDA(cudaGetLastError());
   }
-  launch_render_fwd(*batch, g, point_list, *out, st);
+  {
+    PhaseScope ph(SGR_PHASE_BLEND_FWD, st);
+    launch_render_fwd(*batch, g, point_list, *out, st);
+  }
   SGR_CUDA(cudaGetLastError());
   if (out->radii)
     SGR_CUDA(cudaMemcpyAsync(out->radii, g.radii, (size_t)batch->num_records * 4, cudaMemcpyDeviceToDevice, st));
@@ -311,15 +320,28 @@ int sgr_backward(const sgr_batch* batch, const void* geom, const void* lists, in
   const size_t P = (size_t)batch->num_surfels;
   if (out->dL_dsemantics && S > 0) SGR_CUDA(cudaMemsetAsync(out->dL_dsemantics, 0, P * S * 4, st));
   if (batch->num_records == 0) return SGR_OK;
-  SGR_CUDA(cudaMemsetAsync(grads, 0, (size_t)batch->num_records * kGradF * 4, st));
   float* dsem = (S > 0) ? out->dL_dsemantics : nullptr;
   if (S > 0 && !dsem) return SGR_ERR_INVALID_ARGUMENT;
-  launch_render_bwd(*batch, g, static_cast<const uint32_t*>(lists), *in, grads, dsem, st);
+  {
+    PhaseScope ph(SGR_PHASE_BLEND_BWD, st);
+    SGR_CUDA(cudaMemsetAsync(grads, 0, (size_t)batch->num_records * kGradF * 4, st));
+    launch_render_bwd(*batch, g, static_cast<const uint32_t*>(lists), *in, grads, dsem, st);
+  }
   SGR_CUDA(cudaGetLastError());
-  launch_preprocess_bwd(*batch, g, grads, *out, st);
+  {
+    PhaseScope ph(SGR_PHASE_PREPROCESS_BWD, st);
+    launch_preprocess_bwd(*batch, g, grads, *out, st);
+  }
   SGR_CUDA(cudaGetLastError());
   return SGR_OK;
 }
+
+int sgr_profile_enable(int enable) {
+  PhaseTimer::get().enable(enable != 0);
+  return SGR_OK;
+}
+
+int sgr_profile_read(float* ms, int32_t* count) { return PhaseTimer::get().read(ms, count); }
 
 int sgr_mark_visible(int32_t P, const float* means3D, const float* viewmatrix, const float* projmatrix,
                      uint8_t* present, void* stream) {

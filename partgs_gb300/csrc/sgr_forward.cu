@@ -198,9 +198,10 @@ __global__ void k_duplicate(const sgr_batch b, GeomView g, uint32_t* __restrict_
 // Pads the unused tail of a fixed-capacity key array with a key above every
 // tile so that a sort over the whole capacity leaves it at the end.
 __global__ void k_pad_keys(uint32_t* keys, long long capacity, const Status* st, uint32_t pad_key) {
-  const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= capacity) return;
-  if ((unsigned long long)k >= st->num_keys) keys[k] = pad_key;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long k = (long long)st->num_keys + (long long)blockIdx.x * blockDim.x + threadIdx.x; k < capacity;
+       k += stride)
+    keys[k] = pad_key;
 }
 
 __global__ void k_store_key_count(GeomView g, long long R) {
@@ -210,19 +211,20 @@ __global__ void k_store_key_count(GeomView g, long long R) {
 // Per-tile [start, end) of the sorted list (P0/cr/rasterizer_impl.cu:116-138).
 __global__ void k_tile_ranges(const uint32_t* __restrict__ keys, const Status* st, long long capacity,
                               uint2* __restrict__ ranges) {
-  const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const long long K = (long long)min((unsigned long long)capacity, st->num_keys);
-  if (k >= K) return;
-  const uint32_t cur = keys[k];
-  if (k == 0) ranges[cur].x = 0;
-  else {
-    const uint32_t prev = keys[k - 1];
-    if (cur != prev) {
-      ranges[prev].y = (uint32_t)k;
-      ranges[cur].x = (uint32_t)k;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < K; k += stride) {
+    const uint32_t cur = keys[k];
+    if (k == 0) ranges[cur].x = 0;
+    else {
+      const uint32_t prev = keys[k - 1];
+      if (cur != prev) {
+        ranges[prev].y = (uint32_t)k;
+        ranges[cur].x = (uint32_t)k;
+      }
     }
+    if (k == K - 1) ranges[cur].y = (uint32_t)K;
   }
-  if (k == K - 1) ranges[cur].y = (uint32_t)K;
 }
 
 // ---------------------------------------------------------------------------
@@ -408,19 +410,19 @@ void launch_duplicate(const sgr_batch& b, const GeomView& g, uint32_t* keys, uin
   k_duplicate<<<(unsigned)blocks, threads, 0, st>>>(b, g, keys, vals, capacity);
 }
 
+// Grid-stride kernels over the key list run on a fixed grid: 152 SMs x 8
+// resident CTAs of 256 threads.
+constexpr int kStrideBlocks = 152 * 8;
+
 void launch_pad_keys(uint32_t* keys, long long capacity, const Status* status, uint32_t pad_key, cudaStream_t st) {
-  const int threads = 256;
-  const long long blocks = (capacity + threads - 1) / threads;
-  if (blocks == 0) return;
-  k_pad_keys<<<(unsigned)blocks, threads, 0, st>>>(keys, capacity, status, pad_key);
+  if (capacity <= 0) return;
+  k_pad_keys<<<kStrideBlocks, 256, 0, st>>>(keys, capacity, status, pad_key);
 }
 
 void launch_tile_ranges(const uint32_t* keys, const Status* status, long long capacity, uint2* ranges,
                         cudaStream_t st) {
-  const int threads = 256;
-  const long long blocks = (capacity + threads - 1) / threads;
-  if (blocks == 0) return;
-  k_tile_ranges<<<(unsigned)blocks, threads, 0, st>>>(keys, status, capacity, ranges);
+  if (capacity <= 0) return;
+  k_tile_ranges<<<kStrideBlocks, 256, 0, st>>>(keys, status, capacity, ranges);
 }
 
 void launch_render_fwd(const sgr_batch& b, const GeomView& g, const uint32_t* point_list,

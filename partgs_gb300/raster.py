@@ -110,7 +110,7 @@ def _tables(variant, P, vs: ViewSet, device):
 
 
 def make_batch(variant, means3D, opacities, shs, colors_precomp, scales, rotations, transmat_precomp, semantics,
-               vs: ViewSet, bg, sh_degree, scale_modifier, prefiltered):
+               vs: ViewSet, bg, sh_degree, scale_modifier, prefiltered, tables=None):
     if means3D.dim() != 2 or means3D.shape[1] != 3:
         raise ValueError("means3D must have dimensions (num_points, 3)")
     device = means3D.device
@@ -140,7 +140,7 @@ def make_batch(variant, means3D, opacities, shs, colors_precomp, scales, rotatio
         if S > L.SGR_MAX_SEMANTICS:
             raise ValueError(f"at most {L.SGR_MAX_SEMANTICS} semantic channels are supported, got {S}")
     M = int(shs.shape[1]) if t["shs"] is not None else 0
-    sct, vwt, nscenes, R = _tables(variant, P, vs, device)
+    sct, vwt, nscenes, R = tables if tables is not None else _tables(variant, P, vs, device)
     keep += list(t.values()) + [sct, vwt]
     b = L.Batch()
     b.variant = variant
@@ -164,12 +164,20 @@ def make_batch(variant, means3D, opacities, shs, colors_precomp, scales, rotatio
 
 
 def forward(variant, means3D, opacities, shs, colors_precomp, scales, rotations, transmat_precomp, semantics,
-            vs: ViewSet, bg, sh_degree=0, scale_modifier=1.0, prefiltered=False):
+            vs: ViewSet, bg, sh_degree=0, scale_modifier=1.0, prefiltered=False, key_capacity=None, tables=None,
+            status_host=None):
     """Rasterises every view of ``vs``.  Returns (color [V,3,H,W], others
-    [V,7|8,H,W], semantic [V,S,H,W] or None, radii [R] int32, state)."""
+    [V,7|8,H,W], semantic [V,S,H,W] or None, radii [R] int32, state).
+
+    Without ``key_capacity`` the key count is read back (one host
+    synchronisation, as the reference does) and the list sized exactly.
+    With it nothing synchronises: the list holds ``key_capacity`` keys, and
+    the device status word (key count, overflow flag) is copied into the
+    pinned ``status_host`` tensor (16 bytes) for the caller to inspect once
+    the stream has reached it."""
     lib = L.load()
     b, keep, t = make_batch(variant, means3D, opacities, shs, colors_precomp, scales, rotations, transmat_precomp,
-                            semantics, vs, bg, sh_degree, scale_modifier, prefiltered)
+                            semantics, vs, bg, sh_degree, scale_modifier, prefiltered, tables)
     device = means3D.device
     s0 = L.Sizes()
     L.check(lib.sgr_query_sizes(C.byref(b), 0, C.byref(s0)), "sgr_query_sizes")
@@ -178,17 +186,22 @@ def forward(variant, means3D, opacities, shs, colors_precomp, scales, rotations,
     st = _stream()
     L.check(lib.sgr_forward_geometry(C.byref(b), geom.data_ptr(), scratch0.data_ptr(), s0.fwd_scratch_bytes, None, st),
             "sgr_forward_geometry")
-    # the key count sizes the list, as the reference's blocking copy of
-    # num_rendered does (cuda_rasterizer/rasterizer_impl.cu:282)
-    pin = _pinned(device)
-    pin.copy_(geom[s0.off_status:s0.off_status + 16], non_blocking=True)
-    ev = torch.cuda.Event()
-    ev.record()
-    ev.synchronize()
-    K = int(pin[:8].view(torch.int64)[0])
-    flags = int(pin[8:12].view(torch.int32)[0])
-    if flags & L.SGR_FLAG_PREFILTERED:
-        raise RuntimeError("Point is filtered although prefiltered is set. This shouldn't happen!")
+    if key_capacity is None:
+        # the key count sizes the list, as the reference's blocking copy of
+        # num_rendered does (cuda_rasterizer/rasterizer_impl.cu:282)
+        pin = _pinned(device)
+        pin.copy_(geom[s0.off_status:s0.off_status + 16], non_blocking=True)
+        ev = torch.cuda.Event()
+        ev.record()
+        ev.synchronize()
+        K = int(pin[:8].view(torch.int64)[0])
+        flags = int(pin[8:12].view(torch.int32)[0])
+        if flags & L.SGR_FLAG_PREFILTERED:
+            raise RuntimeError("Point is filtered although prefiltered is set. This shouldn't happen!")
+        if K >= 2 ** 31:
+            raise RuntimeError(f"{K} (surfel, tile) keys exceed the 2^31 - 1 list limit")
+    else:
+        K = int(key_capacity)
     del scratch0
     sK = L.Sizes()
     L.check(lib.sgr_query_sizes(C.byref(b), K, C.byref(sK)), "sgr_query_sizes")
@@ -205,9 +218,16 @@ def forward(variant, means3D, opacities, shs, colors_precomp, scales, rotations,
     out = L.FwdOutputs(color.data_ptr(), others.data_ptr(), _ptr(semantic), radii.data_ptr())
     L.check(lib.sgr_forward_raster(C.byref(b), geom.data_ptr(), lists.data_ptr(), K, scratch.data_ptr(),
                                    sK.fwd_scratch_bytes, C.byref(out), st), "sgr_forward_raster")
+    if status_host is not None:
+        status_host.copy_(geom[sK.off_status:sK.off_status + 16], non_blocking=True)
     state = RasterState(variant, b, keep, geom, lists, K, sK, b.num_surfels, b.num_records, V, b.sh_coeffs,
                         b.semantic_channels)
     return color, others, semantic, radii, state
+
+
+def read_status(status_host: torch.Tensor):
+    """(key count, flags) from a status copy made by ``forward``."""
+    return int(status_host[:8].view(torch.int64)[0]), int(status_host[8:12].view(torch.int32)[0])
 
 
 def backward(state: RasterState, dL_dcolor, dL_dothers, dL_dsemantic=None, need=None):

@@ -1,0 +1,162 @@
+"""Point-level surfel training step over a batch of views.
+
+The step is the reference's point-stage iteration (train.py:225-257) applied
+to every view of a batch at once: rasterise, L1 + D-SSIM photometric loss
+(utils/loss_utils.py:8-54), depth-distortion loss, and the normal-consistency
+loss between rendered normals and normals from the median depth map
+(renderer/gaussian_renderer/__init__.py:111-141, utils/point_utils.py:4-33),
+then an Adam update (scene/gaussian_model.py:266, eps 1e-15).  Parameters use
+the reference's activations: exp scales, normalised quaternions, sigmoid
+opacity, concatenated SH features (scene/gaussian_model.py:198-218).
+
+``SurfelTrainer.capture()`` records the whole step (forward, losses,
+backward, optimiser) in one CUDA graph; ``replay()`` runs it.
+"""
+from __future__ import annotations
+
+import math
+
+import torch
+import torch.nn.functional as F
+
+from .batched import MultiViewRasterizer
+
+
+def _gaussian_window(size=11, sigma=1.5, channels=3, device="cuda"):
+    g = torch.tensor([math.exp(-(x - size // 2) ** 2 / float(2 * sigma ** 2)) for x in range(size)])
+    g = g / g.sum()
+    w2 = (g[:, None] @ g[None, :]).float()
+    return w2.expand(channels, 1, size, size).contiguous().to(device)
+
+
+def ssim(img1, img2, window):
+    """Mean SSIM of [B,C,H,W] images, utils/loss_utils.py:24-54."""
+    C = img1.shape[-3]
+    pad = window.shape[-1] // 2
+    mu1 = F.conv2d(img1, window, padding=pad, groups=C)
+    mu2 = F.conv2d(img2, window, padding=pad, groups=C)
+    mu1_sq, mu2_sq, mu1_mu2 = mu1 * mu1, mu2 * mu2, mu1 * mu2
+    s1 = F.conv2d(img1 * img1, window, padding=pad, groups=C) - mu1_sq
+    s2 = F.conv2d(img2 * img2, window, padding=pad, groups=C) - mu2_sq
+    s12 = F.conv2d(img1 * img2, window, padding=pad, groups=C) - mu1_mu2
+    C1, C2 = 0.01 ** 2, 0.03 ** 2
+    m = ((2 * mu1_mu2 + C1) * (2 * s12 + C2)) / ((mu1_sq + mu2_sq + C1) * (s1 + s2 + C2))
+    return m.mean()
+
+
+class DepthNormals:
+    """Per-view ray directions for normals from depth maps
+    (utils/point_utils.py:4-33), precomputed once per camera set."""
+
+    def __init__(self, cameras, device="cuda"):
+        rays_d, rays_o, rot = [], [], []
+        for c in cameras:
+            wv = torch.as_tensor(c.world_view_transform, dtype=torch.float32)
+            full = torch.as_tensor(c.full_proj_transform, dtype=torch.float32)
+            W, H = c.width, c.height
+            c2w = wv.T.inverse()
+            ndc2pix = torch.tensor([[W / 2, 0, 0, W / 2], [0, H / 2, 0, H / 2], [0, 0, 0, 1]]).float().T
+            proj = c2w.T @ full
+            intr = (proj @ ndc2pix)[:3, :3].T
+            gx, gy = torch.meshgrid(torch.arange(W).float(), torch.arange(H).float(), indexing="xy")
+            pts = torch.stack([gx, gy, torch.ones_like(gx)], -1).reshape(-1, 3)
+            rays_d.append(pts @ intr.inverse().T @ c2w[:3, :3].T)
+            rays_o.append(c2w[:3, 3])
+            rot.append(wv[:3, :3].T)
+        self.H, self.W = cameras[0].height, cameras[0].width
+        self.rays_d = torch.stack(rays_d).to(device)          # [V,HW,3]
+        self.rays_o = torch.stack(rays_o).to(device)          # [V,3]
+        self.view_to_world = torch.stack(rot).to(device)      # [V,3,3]
+
+    def normals(self, depth):
+        """depth [V,1,H,W] -> normals [V,3,H,W] (zero border)."""
+        V = depth.shape[0]
+        pts = depth.reshape(V, -1, 1) * self.rays_d + self.rays_o[:, None, :]
+        pts = pts.reshape(V, self.H, self.W, 3)
+        dx = pts[:, 2:, 1:-1] - pts[:, :-2, 1:-1]
+        dy = pts[:, 1:-1, 2:] - pts[:, 1:-1, :-2]
+        n = F.normalize(torch.cross(dx, dy, dim=-1), dim=-1)
+        out = torch.zeros_like(pts)
+        out[:, 1:-1, 1:-1] = n
+        return out.permute(0, 3, 1, 2)
+
+
+class SurfelTrainer:
+    """Surfel parameters, the batched loss and Adam."""
+
+    def __init__(self, scene, cameras, key_capacity=None, lambda_dssim=0.2, lambda_dist=1000.0,
+                 lambda_normal=0.05, depth_ratio=1.0, bg=(0.0, 0.0, 0.0), device="cuda", extent=3.0):
+        dev = torch.device(device)
+        self.xyz = scene.means3D.detach().clone().to(dev).requires_grad_(True)
+        self.log_scaling = torch.log(scene.scales).detach().clone().to(dev).requires_grad_(True)
+        self.rotation = scene.rotations.detach().clone().to(dev).requires_grad_(True)
+        op = scene.opacities.clamp(1e-4, 1 - 1e-4)
+        self.opacity_logit = torch.log(op / (1 - op)).detach().clone().to(dev).requires_grad_(True)
+        self.features_dc = scene.shs[:, :1].detach().clone().to(dev).requires_grad_(True)
+        self.features_rest = scene.shs[:, 1:].detach().clone().to(dev).requires_grad_(True)
+        self.sh_degree = scene.sh_degree
+        self.raster = MultiViewRasterizer(cameras, bg, scene.sh_degree, key_capacity=key_capacity,
+                                          num_surfels=scene.P, device=dev)
+        self.normals = DepthNormals(cameras, dev)
+        self.window = _gaussian_window(device=dev)
+        self.lambda_dssim, self.lambda_dist, self.lambda_normal = lambda_dssim, lambda_dist, lambda_normal
+        self.depth_ratio = depth_ratio
+        groups = [
+            {"params": [self.xyz], "lr": 0.00016 * extent},
+            {"params": [self.features_dc], "lr": 0.0025},
+            {"params": [self.features_rest], "lr": 0.0025 / 20.0},
+            {"params": [self.opacity_logit], "lr": 0.05},
+            {"params": [self.log_scaling], "lr": 0.005},
+            {"params": [self.rotation], "lr": 0.001},
+        ]
+        self.opt = torch.optim.Adam(groups, lr=0.0, eps=1e-15, fused=True, capturable=True)
+        self.targets = None
+        self.graph = None
+        self.loss = None
+
+    def params(self):
+        return [self.xyz, self.features_dc, self.features_rest, self.opacity_logit, self.log_scaling, self.rotation]
+
+    def loss_fn(self, targets):
+        scales = torch.exp(self.log_scaling)
+        rots = F.normalize(self.rotation)
+        opac = torch.sigmoid(self.opacity_logit)
+        shs = torch.cat((self.features_dc, self.features_rest), dim=1)
+        color, allmap, _, _ = self.raster(self.xyz, opac, shs, scales, rots)
+        l1 = torch.abs(color - targets).mean()
+        loss = (1.0 - self.lambda_dssim) * l1 + self.lambda_dssim * (1.0 - ssim(color, targets, self.window))
+        alpha = allmap[:, 1:2]
+        rend_normal = torch.einsum("vchw,vcd->vdhw", allmap[:, 2:5], self.normals.view_to_world)
+        median = torch.nan_to_num(allmap[:, 5:6], 0, 0)
+        expected = torch.nan_to_num(allmap[:, 0:1] / alpha, 0, 0)
+        surf_depth = expected * (1 - self.depth_ratio) + self.depth_ratio * median
+        surf_normal = self.normals.normals(surf_depth) * alpha.detach()
+        normal_loss = self.lambda_normal * (1 - (rend_normal * surf_normal).sum(dim=1)).mean()
+        dist_loss = self.lambda_dist * allmap[:, 6:7].mean()
+        return loss + dist_loss + normal_loss
+
+    def step(self, targets):
+        """One eager step; returns the loss tensor."""
+        loss = self.loss_fn(targets)
+        loss.backward()
+        self.opt.step()
+        self.opt.zero_grad(set_to_none=False)
+        return loss
+
+    def capture(self, targets, warmup=3):
+        """Captures step() into a CUDA graph reading ``self.targets``."""
+        self.targets = targets.clone()
+        s = torch.cuda.Stream()
+        s.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(s):
+            for _ in range(warmup):
+                self.step(self.targets)
+        torch.cuda.current_stream().wait_stream(s)
+        self.graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(self.graph):
+            self.loss = self.step(self.targets)
+        return self.graph
+
+    def replay(self):
+        self.graph.replay()
+        return self.loss
