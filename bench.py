@@ -38,6 +38,18 @@ def _dist():
     return ws, rank, local
 
 
+def max_over_ranks(x: float, device=None) -> float:
+    """Largest value of ``x`` over the ranks of the default process group
+    (``x`` itself without one)."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return x
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def _workload_config(name):
     if name == "sq500k_16x800x600":
         return {"workload": name, "surfels": 500_000, "views": 16, "height": 600, "width": 800, "fovx_deg": 50,
@@ -187,9 +199,7 @@ def run_gpu(args):
     ms = e0.elapsed_time(e1)
     clk = clocks.stop() if clocks else None
     if ws > 1:
-        t = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+        ms = max_over_ranks(ms, dev)
         torch.distributed.barrier()
     keys, flags = tr.raster.key_count()
     if flags & L.SGR_FLAG_KEY_OVERFLOW:
@@ -206,10 +216,7 @@ def run_gpu(args):
         loss = tr.replay()
         float(loss.item())
     e2e_s = (time.perf_counter() - t0) / n_e2e
-    if ws > 1:
-        t = torch.tensor([e2e_s], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = max_over_ranks(e2e_s, dev)
 
     # ---- dominant kernel: per-phase CUDA events over eager steps of the same work ----
     import ctypes as C

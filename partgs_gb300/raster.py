@@ -113,6 +113,12 @@ def make_batch(variant, means3D, opacities, shs, colors_precomp, scales, rotatio
                vs: ViewSet, bg, sh_degree, scale_modifier, prefiltered, tables=None):
     if means3D.dim() != 2 or means3D.shape[1] != 3:
         raise ValueError("means3D must have dimensions (num_points, 3)")
+    if variant == L.SGR_VARIANT_PART and semantics is not None and semantics.dim() == 2 and \
+            int(semantics.shape[1]) > L.SGR_MAX_SEMANTICS:
+        raise ValueError(f"at most {L.SGR_MAX_SEMANTICS} semantic channels are supported, "
+                         f"got {int(semantics.shape[1])}")
+    if shs is not None and shs.numel() and (shs.dim() != 3 or shs.shape[2] != 3 or shs.shape[1] > 16):
+        raise ValueError("shs must have dimensions (num_points, M <= 16, 3)")
     device = means3D.device
     P = int(means3D.shape[0])
     keep = []
