@@ -112,4 +112,6 @@ def workload(name: str, seed: int = 0):
         return random_surfels(4096, seed), scene_cameras(1, 128, 128, 60.0, seed=seed)
     if name == "sq500k_16x800x600":
         return superquadric_surfels(500_000, 16, seed), scene_cameras(16, 600, 800, 50.0, seed=seed)
+    if name == "sq100k_4x800x600":      # a smaller case of the same distribution (profiling)
+        return superquadric_surfels(100_000, 16, seed), scene_cameras(4, 600, 800, 50.0, seed=seed)
     raise KeyError(name)
