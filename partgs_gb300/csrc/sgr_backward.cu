@@ -4,237 +4,6 @@
 namespace sgr {
 
 // ---------------------------------------------------------------------------
-// blend backward (P0/cr/backward.cu:143-440, P1/cr/backward.cu:143-470)
-//
-// Same per-pixel recurrences as the reference: back to front over the
-// surfels before each pixel's last contributor, transmittance recovered by
-// division from the stored final T.  Differences in how the work is laid out:
-//  * the CTA starts at the largest last-contributor of its tile instead of
-//    the end of the tile's list (positions past it are skipped by every
-//    pixel in the reference);
-//  * the 18 per-fragment gradients of a warp's 32 pixels are summed with a
-//    transposed shuffle reduction, then one lane per value issues a single
-//    atomic add into the per-view gradient record (the reference issues up to
-//    16 atomics per pixel and fragment).
-// ---------------------------------------------------------------------------
-template <int VARIANT>
-__global__ void __launch_bounds__(kBlock) k_render_bwd(const sgr_batch b, GeomView g,
-                                                       const uint32_t* __restrict__ point_list,
-                                                       const sgr_bwd_inputs in, float* __restrict__ grads,
-                                                       float* __restrict__ dL_dsemantics) {
-  const int tiles_per_view = g.tiles_x * g.tiles_y;
-  const int tile = blockIdx.x;
-  const int v = tile / tiles_per_view;
-  const int t = tile - v * tiles_per_view;
-  const int ty = t / g.tiles_x, tx = t - ty * g.tiles_x;
-  const int W = b.width, H = b.height;
-  const int px = tx * kTile + (threadIdx.x & (kTile - 1));
-  const int py = ty * kTile + (threadIdx.x / kTile);
-  const bool inside = px < W && py < H;
-  const float pxf = (VARIANT == SGR_VARIANT_PLAIN) ? (float)px : (float)px + 0.5f;
-  const float pyf = (VARIANT == SGR_VARIANT_PLAIN) ? (float)py : (float)py + 0.5f;
-  const int lane = threadIdx.x & 31;
-  const int S = (VARIANT == SGR_VARIANT_PART) ? b.semantic_channels : 0;
-  const sgr_view_desc vd = b.views[v];
-  const int sid_base = b.scenes[vd.scene].surfel_offset - vd.record_offset;
-
-  __shared__ float4 s_rec[kRecF4][kBlock];
-  __shared__ uint32_t s_id[kBlock];
-  __shared__ float s_sem[(VARIANT == SGR_VARIANT_PART) ? SGR_MAX_SEMANTICS : 1][kBlock];
-  __shared__ int s_max[kBlock / 32];
-
-  const uint2 range = g.ranges[tile];
-  const size_t HW = (size_t)H * W;
-  const size_t pix = inside ? (size_t)py * W + px : 0;
-  const float* fT = g.final_T + (size_t)v * 3 * HW;
-  const uint32_t* nc = g.n_contrib + (size_t)v * 2 * HW;
-  const int NO = (VARIANT == SGR_VARIANT_PLAIN) ? 7 : 8;
-  const float* dpix = in.dL_dcolor + (size_t)v * 3 * HW;
-  const float* doth = in.dL_dothers + (size_t)v * NO * HW;
-
-  const float T_final = inside ? fT[pix] : 0.f;
-  float T = T_final;
-  const int last_contributor = inside ? (int)nc[pix] : 0;
-  const int median_contributor = inside ? (int)nc[pix + HW] : 0;
-  float dL_dpixel[3] = {0.f, 0.f, 0.f};
-  float dL_ddepth = 0.f, dL_daccum = 0.f, dL_dreg = 0.f, dL_dmedian = 0.f, dL_dmaxw = 0.f;
-  float dL_dnormal2D[3] = {0.f, 0.f, 0.f};
-  float dsem_pix[SGR_MAX_SEMANTICS];
-#pragma unroll
-  for (int c = 0; c < SGR_MAX_SEMANTICS; ++c) dsem_pix[c] = 0.f;
-  float final_D = 0.f, final_D2 = 0.f;
-  if (inside) {
-    for (int c = 0; c < 3; ++c) dL_dpixel[c] = dpix[pix + c * HW];
-    dL_ddepth = doth[pix];
-    dL_daccum = doth[pix + HW];
-    for (int c = 0; c < 3; ++c) dL_dnormal2D[c] = doth[pix + (2 + c) * HW];
-    dL_dmedian = doth[pix + 5 * HW];
-    dL_dreg = doth[pix + 6 * HW];
-    if (VARIANT == SGR_VARIANT_PART) {
-      dL_dmaxw = doth[pix + 7 * HW];
-      const float* ds = in.dL_dsemantic + (size_t)v * S * HW;
-      for (int c = 0; c < S; ++c) dsem_pix[c] = ds[pix + c * HW];
-    }
-    final_D = fT[pix + HW];
-    final_D2 = fT[pix + 2 * HW];
-  }
-  const float final_A = 1 - T_final;
-  const float* bg = b.background;
-  const float bg_dot = bg[0] * dL_dpixel[0] + bg[1] * dL_dpixel[1] + bg[2] * dL_dpixel[2];
-
-  float accum_rec[3] = {0.f, 0.f, 0.f}, last_color[3] = {0.f, 0.f, 0.f};
-  float accum_sem[SGR_MAX_SEMANTICS], last_sem[SGR_MAX_SEMANTICS];
-#pragma unroll
-  for (int c = 0; c < SGR_MAX_SEMANTICS; ++c) accum_sem[c] = last_sem[c] = 0.f;
-  float last_alpha = 0.f, last_depth = 0.f, accum_depth = 0.f, accum_alpha = 0.f, last_dL_dT = 0.f;
-  float last_normal[3] = {0.f, 0.f, 0.f}, accum_normal[3] = {0.f, 0.f, 0.f};
-
-  // largest last contributor of the tile: list positions at or past it are
-  // skipped by every pixel
-  {
-    int m = last_contributor;
-#pragma unroll
-    for (int o = 16; o >= 1; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
-    if (lane == 0) s_max[threadIdx.x / 32] = m;
-    __syncthreads();
-    m = 0;
-#pragma unroll
-    for (int w = 0; w < kBlock / 32; ++w) m = max(m, s_max[w]);
-    // every thread computed the same m; the loop bounds below are uniform
-    int hi = min(m, (int)(range.y - range.x));
-    for (; hi > 0; hi -= kBlock) {
-      const int n = min(kBlock, hi);
-      __syncthreads();
-      if ((int)threadIdx.x < n) {
-        const uint32_t r = point_list[range.x + hi - 1 - threadIdx.x];
-        s_id[threadIdx.x] = r;
-        const float4* rec = g.records + (size_t)r * kRecF4;
-#pragma unroll
-        for (int k = 0; k < kRecF4; ++k) s_rec[k][threadIdx.x] = rec[k];
-        if (VARIANT == SGR_VARIANT_PART) {
-          const float* sem = b.semantics + (size_t)(sid_base + (int)r) * S;
-          for (int c = 0; c < S; ++c) s_sem[c][threadIdx.x] = sem[c];
-        }
-      }
-      __syncthreads();
-      for (int j = 0; j < n; ++j) {
-        const int pos = hi - 1 - j;
-        float gv[32];
-#pragma unroll
-        for (int k = 0; k < 32; ++k) gv[k] = 0.f;
-        float gsem[32];
-        bool ok = inside && pos < last_contributor;
-        if (ok) {
-          const float4 r0 = s_rec[0][j], r1 = s_rec[1][j], r2 = s_rec[2][j];
-          const V3 Tu = v3(r0.x, r0.y, r0.z), Tv = v3(r0.w, r1.x, r1.y), Tw = v3(r1.z, r1.w, r2.x);
-          Frag fr;
-          intersect<VARIANT>(pxf, pyf, Tu, Tv, Tw, r2.y, r2.z, fr);
-          ok = fr.p.z != 0.0f && !(fr.depth < kNearP0);
-          const float power = -0.5f * fr.rho;
-          ok = ok && !(power > 0.0f);
-          const float G = expf(power);
-          const float alpha = fminf(0.99f, r2.w * G);
-          ok = ok && !(alpha < 1.0f / 255.0f);
-          if (ok) {
-            const float4 r3 = s_rec[3][j], r4 = s_rec[4][j];
-            T = T / (1.f - alpha);
-            const float wgt = alpha * T;
-            float dL_dalpha = 0.0f;
-            const float col[3] = {r4.x, r4.y, r4.z};
-#pragma unroll
-            for (int ch = 0; ch < 3; ++ch) {
-              accum_rec[ch] = last_alpha * last_color[ch] + (1.f - last_alpha) * accum_rec[ch];
-              last_color[ch] = col[ch];
-              dL_dalpha += (col[ch] - accum_rec[ch]) * dL_dpixel[ch];
-              gv[14 + ch] = wgt * dL_dpixel[ch];
-            }
-            if (VARIANT == SGR_VARIANT_PART) {
-              for (int c = 0; c < S; ++c) {
-                accum_sem[c] = last_alpha * last_sem[c] + (1.f - last_alpha) * accum_sem[c];
-                last_sem[c] = s_sem[c][j];
-              }
-            }
-            float dL_dz = 0.0f, dL_dweight = 0.f;
-            float m_d, dmd_dd;
-            if (VARIANT == SGR_VARIANT_PLAIN) {
-              m_d = kFarP0 / (kFarP0 - kNearP0) * (1 - kNearP0 / fr.depth);
-              dmd_dd = (kFarP0 * kNearP0) / ((kFarP0 - kNearP0) * fr.depth * fr.depth);
-            } else {
-              m_d = mapped_depth_p1(fr.depth);
-              dmd_dd = (float)((kFarP1 * kNearP1) / ((kFarP1 - kNearP1) * fr.depth * fr.depth));
-            }
-            if (pos == median_contributor - 1) {
-              dL_dz += dL_dmedian;
-              if (VARIANT == SGR_VARIANT_PART) dL_dweight += dL_dmaxw;
-            }
-            dL_dweight += (final_D2 + m_d * m_d * final_A - 2 * m_d * final_D) * dL_dreg;
-            dL_dalpha += dL_dweight - last_dL_dT;
-            last_dL_dT = dL_dweight * alpha + (1 - alpha) * last_dL_dT;
-            const float dL_dmd = 2.0f * (T * alpha) * (m_d * final_A - final_D) * dL_dreg;
-            dL_dz += dL_dmd * dmd_dd;
-            accum_depth = last_alpha * last_depth + (1.f - last_alpha) * accum_depth;
-            last_depth = fr.depth;
-            dL_dalpha += (fr.depth - accum_depth) * dL_ddepth;
-            // the reference adds last_alpha * 1.0 in double: one rounding of
-            // an exact sum, i.e. a plain float add
-            accum_alpha = __fadd_rn(last_alpha, __fmul_rn(1.f - last_alpha, accum_alpha));
-            dL_dalpha += (1 - accum_alpha) * dL_daccum;
-            const float nrm[3] = {r3.x, r3.y, r3.z};
-#pragma unroll
-            for (int ch = 0; ch < 3; ++ch) {
-              accum_normal[ch] = last_alpha * last_normal[ch] + (1.f - last_alpha) * accum_normal[ch];
-              last_normal[ch] = nrm[ch];
-              dL_dalpha += (nrm[ch] - accum_normal[ch]) * dL_dnormal2D[ch];
-              gv[11 + ch] = alpha * T * dL_dnormal2D[ch];
-            }
-            dL_dalpha *= T;
-            last_alpha = alpha;
-            dL_dalpha += (-T_final / (1.f - alpha)) * bg_dot;
-            const float dL_dG = r2.w * dL_dalpha;
-            dL_dz += alpha * T * dL_ddepth;
-            if (fr.use3d) {
-              const float dsx = dL_dG * -G * fr.sx + dL_dz * Tw.x;
-              const float dsy = dL_dG * -G * fr.sy + dL_dz * Tw.y;
-              const float dsx_pz = dsx / fr.p.z;
-              const float dsy_pz = dsy / fr.p.z;
-              const V3 dL_dp = v3(dsx_pz, dsy_pz, -(dsx_pz * fr.sx + dsy_pz * fr.sy));
-              const V3 dL_dk = cross3(fr.l, dL_dp);
-              const V3 dL_dl = cross3(dL_dp, fr.k);
-              gv[0] = -dL_dk.x; gv[1] = -dL_dk.y; gv[2] = -dL_dk.z;
-              gv[3] = -dL_dl.x; gv[4] = -dL_dl.y; gv[5] = -dL_dl.z;
-              gv[6] = pxf * dL_dk.x + pyf * dL_dl.x + dL_dz * fr.sx;
-              gv[7] = pxf * dL_dk.y + pyf * dL_dl.y + dL_dz * fr.sy;
-              gv[8] = pxf * dL_dk.z + pyf * dL_dl.z + dL_dz * 1.0f;
-            } else {
-              const float dG_ddelx = -G * kFilterInvSquareP0 * fr.dx;
-              const float dG_ddely = -G * kFilterInvSquareP0 * fr.dy;
-              gv[9] = dL_dG * dG_ddelx;
-              gv[10] = dL_dG * dG_ddely;
-              gv[8] = dL_dz;
-            }
-            gv[17] = G * dL_dalpha;
-            if (VARIANT == SGR_VARIANT_PART) {
-              for (int c = 0; c < S; ++c) gsem[c] = wgt * dsem_pix[c];
-            }
-          }
-        }
-        if (__any_sync(0xffffffffu, ok)) {
-          const float total = warp_transpose_sum(gv, lane);
-          const uint32_t r = s_id[j];
-          if (lane < kGradUsed && total != 0.f) atomicAdd(grads + (size_t)r * kGradF + lane, total);
-          if (VARIANT == SGR_VARIANT_PART && S > 0) {
-#pragma unroll
-            for (int c = 0; c < 32; ++c) gsem[c] = (ok && c < S) ? gsem[c] : 0.f;
-            const float st = warp_transpose_sum(gsem, lane);
-            if (lane < S && st != 0.f) atomicAdd(dL_dsemantics + (size_t)(sid_base + (int)r) * S + lane, st);
-          }
-        }
-      }
-    }
-  }
-}
-
-// ---------------------------------------------------------------------------
 // preprocess backward: one thread per surfel, summing over its scene's views
 // (P0/cr/backward.cu:443-630; P1/cr/backward.cu:473-671)
 // ---------------------------------------------------------------------------
@@ -519,16 +288,6 @@ __global__ void __launch_bounds__(128) k_preprocess_bwd(const sgr_batch b, GeomV
     float* o = out.dL_dsh + (size_t)i * M * 3;
     for (int k = 0; k < M * 3; ++k) o[k] = k < kMaxShCoeffs * 3 ? dsh[k] : 0.f;
   }
-}
-
-void launch_render_bwd(const sgr_batch& b, const GeomView& g, const uint32_t* point_list, const sgr_bwd_inputs& in,
-                       float* grads, float* dL_dsemantics, cudaStream_t st) {
-  const unsigned blocks = (unsigned)(g.tiles_x * g.tiles_y) * (unsigned)b.num_views;
-  if (blocks == 0) return;
-  if (b.variant == SGR_VARIANT_PLAIN)
-    k_render_bwd<SGR_VARIANT_PLAIN><<<blocks, kBlock, 0, st>>>(b, g, point_list, in, grads, dL_dsemantics);
-  else
-    k_render_bwd<SGR_VARIANT_PART><<<blocks, kBlock, 0, st>>>(b, g, point_list, in, grads, dL_dsemantics);
 }
 
 void launch_preprocess_bwd(const sgr_batch& b, const GeomView& g, const float* grads, const sgr_bwd_outputs& out,

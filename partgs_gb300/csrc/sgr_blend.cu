@@ -1,0 +1,491 @@
+// Blend kernels: per-tile front-to-back compositing (forward) and its
+// back-to-front adjoint (backward), for both variants.
+//
+// Both follow the reference's per-pixel recurrences exactly
+// (P0/cr/forward.cu:256-441, P1/cr/forward.cu:265-474,
+//  P0/cr/backward.cu:143-440, P1/cr/backward.cu:143-470).  What differs is
+// which (surfel, pixel) pairs get evaluated.  A CTA owns one 16x16 tile and
+// stages 256 list entries at a time in shared memory; each entry's reach box
+// (sgr_common.cuh) is tested once against the tile's eight 16x2 pixel strips
+// (one strip per warp), and each warp then walks only the entries that can
+// reach its strip, in list order.  Entries that cannot reach a pixel are ones
+// the reference skips at its alpha test, so outputs, contributor counts and
+// median indices are unchanged; list positions are kept for the counts.
+// Per pixel, a fragment whose splat and filter distances both exceed the
+// reach threshold is rejected before the two divisions and the exponential.
+#include "sgr_kernels.cuh"
+
+namespace sgr {
+
+namespace {
+
+constexpr int kWarps = kBlock / 32;
+
+struct Strip {
+  float x0, x1;       // pixel-centre x range of the tile
+  float y0;           // pixel-centre y of the tile's first row
+};
+
+// Bit w set when the record's reach box meets strip w (rows 2w, 2w+1).
+__device__ __forceinline__ uint32_t strip_mask(const float4& box, const Strip& s) {
+  if (box.y < s.x0 || box.x > s.x1) return 0u;
+  uint32_t m = 0;
+#pragma unroll
+  for (int w = 0; w < kWarps; ++w) {
+    const float ya = s.y0 + 2.0f * w;
+    if (box.w >= ya && box.z <= ya + 1.0f) m |= 1u << w;
+  }
+  return m;
+}
+
+// Compacts this warp's surviving slots of a staged batch into `list`, in
+// slot order; returns their number.
+__device__ __forceinline__ int warp_survivors(const uint8_t* mask, int n, int warp, int lane, uint8_t* list) {
+  int cnt = 0;
+#pragma unroll
+  for (int k = 0; k < kWarps; ++k) {
+    const int j = k * 32 + lane;
+    const bool keep = j < n && ((mask[j] >> warp) & 1u);
+    const unsigned bal = __ballot_sync(0xffffffffu, keep);
+    if (keep) list[cnt + __popc(bal & ((1u << lane) - 1u))] = (uint8_t)j;
+    cnt += __popc(bal);
+  }
+  __syncwarp();
+  return cnt;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// forward
+// ---------------------------------------------------------------------------
+template <int VARIANT>
+__global__ void __launch_bounds__(kBlock) k_render_fwd(const sgr_batch b, GeomView g,
+                                                       const uint32_t* __restrict__ point_list,
+                                                       sgr_fwd_outputs out) {
+  const int tiles_per_view = g.tiles_x * g.tiles_y;
+  const int tile = blockIdx.x;
+  const int v = tile / tiles_per_view;
+  const int t = tile - v * tiles_per_view;
+  const int ty = t / g.tiles_x, tx = t - ty * g.tiles_x;
+  const int W = b.width, H = b.height;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int px = tx * kTile + (threadIdx.x & (kTile - 1));
+  const int py = ty * kTile + (threadIdx.x / kTile);
+  const bool inside = px < W && py < H;
+  const float off = (VARIANT == SGR_VARIANT_PLAIN) ? 0.0f : 0.5f;
+  const float pxf = (float)px + off, pyf = (float)py + off;
+  const Strip strip{(float)(tx * kTile) + off, (float)(tx * kTile) + off + (kTile - 1), (float)(ty * kTile) + off};
+  const int S = (VARIANT == SGR_VARIANT_PART) ? b.semantic_channels : 0;
+  const sgr_view_desc vd = b.views[v];
+  const int sid_base = b.scenes[vd.scene].surfel_offset - vd.record_offset;
+
+  __shared__ float4 s_rec[kRecF4 - 1][kBlock];
+  __shared__ uint8_t s_mask[kBlock];
+  __shared__ uint8_t s_list[kWarps][kBlock];
+  __shared__ float s_sem[(VARIANT == SGR_VARIANT_PART) ? SGR_MAX_SEMANTICS : 1][kBlock];
+
+  const uint2 range = g.ranges[tile];
+  const int todo_all = (int)(range.y - range.x);
+  const int rounds = (todo_all + kBlock - 1) / kBlock;
+  bool done = !inside;
+
+  float T = 1.0f;
+  uint32_t last_contributor = 0;
+  float C[3] = {0.f, 0.f, 0.f};
+  float N[3] = {0.f, 0.f, 0.f};
+  float D = 0.f, M1 = 0.f, M2 = 0.f, dist = 0.f, med_depth = 0.f, med_weight = 0.f;
+  int med_contrib = -1;
+  float Sem[SGR_MAX_SEMANTICS];
+#pragma unroll
+  for (int c = 0; c < SGR_MAX_SEMANTICS; ++c) Sem[c] = 0.f;
+
+  for (int i = 0; i < rounds; ++i) {
+    if (__syncthreads_count(done) == kBlock) break;
+    const int base = i * kBlock;
+    const int n = min(kBlock, todo_all - base);
+    if ((int)threadIdx.x < n) {
+      const uint32_t r = point_list[range.x + base + threadIdx.x];
+      const float4* rec = g.records + (size_t)r * kRecF4;
+#pragma unroll
+      for (int k = 0; k < kRecF4 - 1; ++k) s_rec[k][threadIdx.x] = rec[k];
+      s_mask[threadIdx.x] = (uint8_t)strip_mask(rec[5], strip);
+      if (VARIANT == SGR_VARIANT_PART) {
+        const float* sem = b.semantics + (size_t)(sid_base + (int)r) * S;
+        for (int c = 0; c < S; ++c) s_sem[c][threadIdx.x] = sem[c];
+      }
+    }
+    __syncthreads();
+    const int cnt = warp_survivors(s_mask, n, warp, lane, s_list[warp]);
+    for (int si = 0; !done && si < cnt; ++si) {
+      const int j = s_list[warp][si];
+      const uint32_t contributor = (uint32_t)(base + j + 1);
+      const float4 r0 = s_rec[0][j], r1 = s_rec[1][j], r2 = s_rec[2][j];
+      const V3 Tu = v3(r0.x, r0.y, r0.z), Tv = v3(r0.w, r1.x, r1.y), Tw = v3(r1.z, r1.w, r2.x);
+      V3 k, l;
+      if (VARIANT == SGR_VARIANT_PLAIN) {
+        k = pxf * Tw - Tu;
+        l = pyf * Tw - Tv;
+      } else {
+        k = v3(-Tu.x + pxf * Tw.x, -Tu.y + pxf * Tw.y, -Tu.z + pxf * Tw.z);
+        l = v3(-Tv.x + pyf * Tw.x, -Tv.y + pyf * Tw.y, -Tv.z + pyf * Tw.z);
+      }
+      const V3 p = cross3(k, l);
+      if (p.z == 0.0f) continue;
+      const float dx = r2.y - pxf, dy = r2.z - pyf;
+      const float rho2d = kFilterInvSquareP0 * (dx * dx + dy * dy);
+      const float reach = s_rec[3][j].w;
+      if (rho2d > reach && p.x * p.x + p.y * p.y > reach * (p.z * p.z)) continue;
+      const float sx = p.x / p.z, sy = p.y / p.z;
+      const float rho3d = sx * sx + sy * sy;
+      const float rho = fminf(rho3d, rho2d);
+      const float depth = (rho3d <= rho2d) ? (sx * Tw.x + sy * Tw.y) + Tw.z : Tw.z;
+      if (depth < kNearP0) continue;
+      const float power = -0.5f * rho;
+      if (power > 0.0f) continue;
+      const float alpha = fminf(0.99f, r2.w * expf(power));
+      if (alpha < 1.0f / 255.0f) continue;
+      const float test_T = T * (1 - alpha);
+      if (test_T < 0.0001f) {
+        done = true;
+        continue;
+      }
+      const float4 r3 = s_rec[3][j], r4 = s_rec[4][j];
+      const float A = 1 - T;
+      if (VARIANT == SGR_VARIANT_PLAIN) {
+        const float w = alpha * T;
+        const float m = kFarP0 / (kFarP0 - kNearP0) * (1 - kNearP0 / depth);
+        dist += (m * m * A + M2 - 2 * m * M1) * w;
+        D += depth * w;
+        M1 += m * w;
+        M2 += m * m * w;
+        if (T > 0.5f) {
+          med_depth = depth;
+          med_contrib = (int)contributor;
+        }
+        N[0] += r3.x * w;
+        N[1] += r3.y * w;
+        N[2] += r3.z * w;
+        C[0] += r4.x * w;
+        C[1] += r4.y * w;
+        C[2] += r4.z * w;
+      } else {
+        const float m = mapped_depth_p1(depth);
+        const float err = m * m * A + M2 - 2 * m * M1;
+        dist += err * alpha * T;
+        if (T > 0.5f) {
+          med_depth = depth;
+          med_weight = alpha * T;
+          med_contrib = (int)contributor;
+        }
+        N[0] += r3.x * alpha * T;
+        N[1] += r3.y * alpha * T;
+        N[2] += r3.z * alpha * T;
+        D += depth * alpha * T;
+        M1 += m * alpha * T;
+        M2 += m * m * alpha * T;
+        C[0] += r4.x * alpha * T;
+        C[1] += r4.y * alpha * T;
+        C[2] += r4.z * alpha * T;
+        for (int c = 0; c < S; ++c) Sem[c] += s_sem[c][j] * alpha * T;
+      }
+      T = test_T;
+      last_contributor = contributor;
+    }
+  }
+
+  if (inside) {
+    const size_t HW = (size_t)H * W;
+    const size_t pix = (size_t)py * W + px;
+    float* fT = g.final_T + (size_t)v * 3 * HW;
+    uint32_t* nc = g.n_contrib + (size_t)v * 2 * HW;
+    fT[pix] = T;
+    fT[pix + HW] = M1;
+    fT[pix + 2 * HW] = M2;
+    nc[pix] = last_contributor;
+    nc[pix + HW] = med_contrib > 0 ? (uint32_t)med_contrib : 0u;
+    const float* bg = b.background;
+    float* col = out.color + (size_t)v * 3 * HW;
+    col[pix] = C[0] + T * bg[0];
+    col[pix + HW] = C[1] + T * bg[1];
+    col[pix + 2 * HW] = C[2] + T * bg[2];
+    const int NO = (VARIANT == SGR_VARIANT_PLAIN) ? 7 : 8;
+    float* oth = out.others + (size_t)v * NO * HW;
+    oth[pix] = D;
+    oth[pix + HW] = 1 - T;
+    oth[pix + 2 * HW] = N[0];
+    oth[pix + 3 * HW] = N[1];
+    oth[pix + 4 * HW] = N[2];
+    oth[pix + 5 * HW] = med_depth;
+    oth[pix + 6 * HW] = dist;
+    if (VARIANT == SGR_VARIANT_PART) {
+      oth[pix + 7 * HW] = med_weight;
+      float* sem = out.semantic + (size_t)v * S * HW;
+      for (int c = 0; c < S; ++c) sem[pix + c * HW] = Sem[c];
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// backward
+//
+// Back to front over the positions before each pixel's last contributor,
+// transmittance recovered by division from the stored final T.  The CTA
+// starts at its tile's largest last contributor; each warp skips entries at
+// or past its own largest one.  The 18 per-fragment gradients of a warp's 32
+// pixels are summed with a transposed shuffle reduction and one lane per
+// value adds the total to the per-view gradient record (one atomic per value
+// and warp instead of one per value and pixel).
+// ---------------------------------------------------------------------------
+template <int VARIANT>
+__global__ void __launch_bounds__(kBlock) k_render_bwd(const sgr_batch b, GeomView g,
+                                                       const uint32_t* __restrict__ point_list,
+                                                       const sgr_bwd_inputs in, float* __restrict__ grads,
+                                                       float* __restrict__ dL_dsemantics) {
+  const int tiles_per_view = g.tiles_x * g.tiles_y;
+  const int tile = blockIdx.x;
+  const int v = tile / tiles_per_view;
+  const int t = tile - v * tiles_per_view;
+  const int ty = t / g.tiles_x, tx = t - ty * g.tiles_x;
+  const int W = b.width, H = b.height;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int px = tx * kTile + (threadIdx.x & (kTile - 1));
+  const int py = ty * kTile + (threadIdx.x / kTile);
+  const bool inside = px < W && py < H;
+  const float off = (VARIANT == SGR_VARIANT_PLAIN) ? 0.0f : 0.5f;
+  const float pxf = (float)px + off, pyf = (float)py + off;
+  const Strip strip{(float)(tx * kTile) + off, (float)(tx * kTile) + off + (kTile - 1), (float)(ty * kTile) + off};
+  const int S = (VARIANT == SGR_VARIANT_PART) ? b.semantic_channels : 0;
+  const sgr_view_desc vd = b.views[v];
+  const int sid_base = b.scenes[vd.scene].surfel_offset - vd.record_offset;
+
+  __shared__ float4 s_rec[kRecF4 - 1][kBlock];
+  __shared__ uint32_t s_id[kBlock];
+  __shared__ uint8_t s_mask[kBlock];
+  __shared__ uint8_t s_list[kWarps][kBlock];
+  __shared__ float s_sem[(VARIANT == SGR_VARIANT_PART) ? SGR_MAX_SEMANTICS : 1][kBlock];
+  __shared__ int s_max[kWarps];
+
+  const uint2 range = g.ranges[tile];
+  const size_t HW = (size_t)H * W;
+  const size_t pix = inside ? (size_t)py * W + px : 0;
+  const float* fT = g.final_T + (size_t)v * 3 * HW;
+  const uint32_t* nc = g.n_contrib + (size_t)v * 2 * HW;
+  const int NO = (VARIANT == SGR_VARIANT_PLAIN) ? 7 : 8;
+  const float* dpix = in.dL_dcolor + (size_t)v * 3 * HW;
+  const float* doth = in.dL_dothers + (size_t)v * NO * HW;
+
+  const float T_final = inside ? fT[pix] : 0.f;
+  float T = T_final;
+  const int last_contributor = inside ? (int)nc[pix] : 0;
+  const int median_contributor = inside ? (int)nc[pix + HW] : 0;
+  float dL_dpixel[3] = {0.f, 0.f, 0.f};
+  float dL_ddepth = 0.f, dL_daccum = 0.f, dL_dreg = 0.f, dL_dmedian = 0.f, dL_dmaxw = 0.f;
+  float dL_dnormal2D[3] = {0.f, 0.f, 0.f};
+  float dsem_pix[SGR_MAX_SEMANTICS];
+#pragma unroll
+  for (int c = 0; c < SGR_MAX_SEMANTICS; ++c) dsem_pix[c] = 0.f;
+  float final_D = 0.f, final_D2 = 0.f;
+  if (inside) {
+    for (int c = 0; c < 3; ++c) dL_dpixel[c] = dpix[pix + c * HW];
+    dL_ddepth = doth[pix];
+    dL_daccum = doth[pix + HW];
+    for (int c = 0; c < 3; ++c) dL_dnormal2D[c] = doth[pix + (2 + c) * HW];
+    dL_dmedian = doth[pix + 5 * HW];
+    dL_dreg = doth[pix + 6 * HW];
+    if (VARIANT == SGR_VARIANT_PART) {
+      dL_dmaxw = doth[pix + 7 * HW];
+      const float* ds = in.dL_dsemantic + (size_t)v * S * HW;
+      for (int c = 0; c < S; ++c) dsem_pix[c] = ds[pix + c * HW];
+    }
+    final_D = fT[pix + HW];
+    final_D2 = fT[pix + 2 * HW];
+  }
+  const float final_A = 1 - T_final;
+  const float* bg = b.background;
+  const float bg_dot = bg[0] * dL_dpixel[0] + bg[1] * dL_dpixel[1] + bg[2] * dL_dpixel[2];
+
+  float accum_rec[3] = {0.f, 0.f, 0.f}, last_color[3] = {0.f, 0.f, 0.f};
+  float accum_sem[SGR_MAX_SEMANTICS], last_sem[SGR_MAX_SEMANTICS];
+#pragma unroll
+  for (int c = 0; c < SGR_MAX_SEMANTICS; ++c) accum_sem[c] = last_sem[c] = 0.f;
+  float last_alpha = 0.f, last_depth = 0.f, accum_depth = 0.f, accum_alpha = 0.f, last_dL_dT = 0.f;
+  float last_normal[3] = {0.f, 0.f, 0.f}, accum_normal[3] = {0.f, 0.f, 0.f};
+
+  int warp_max = last_contributor;
+#pragma unroll
+  for (int o = 16; o >= 1; o >>= 1) warp_max = max(warp_max, __shfl_xor_sync(0xffffffffu, warp_max, o));
+  if (lane == 0) s_max[warp] = warp_max;
+  __syncthreads();
+  int block_max = 0;
+#pragma unroll
+  for (int w = 0; w < kWarps; ++w) block_max = max(block_max, s_max[w]);
+
+  for (int hi = min(block_max, (int)(range.y - range.x)); hi > 0; hi -= kBlock) {
+    const int n = min(kBlock, hi);
+    __syncthreads();
+    if ((int)threadIdx.x < n) {
+      const uint32_t r = point_list[range.x + hi - 1 - threadIdx.x];
+      s_id[threadIdx.x] = r;
+      const float4* rec = g.records + (size_t)r * kRecF4;
+#pragma unroll
+      for (int k = 0; k < kRecF4 - 1; ++k) s_rec[k][threadIdx.x] = rec[k];
+      s_mask[threadIdx.x] = (uint8_t)strip_mask(rec[5], strip);
+      if (VARIANT == SGR_VARIANT_PART) {
+        const float* sem = b.semantics + (size_t)(sid_base + (int)r) * S;
+        for (int c = 0; c < S; ++c) s_sem[c][threadIdx.x] = sem[c];
+      }
+    }
+    __syncthreads();
+    const int cnt = warp_survivors(s_mask, n, warp, lane, s_list[warp]);
+    for (int si = 0; si < cnt; ++si) {
+      const int j = s_list[warp][si];
+      const int pos = hi - 1 - j;
+      if (pos >= warp_max) continue;        // uniform: past every lane's last contributor
+      float gv[32];
+#pragma unroll
+      for (int q = 0; q < 32; ++q) gv[q] = 0.f;
+      float gsem[32];
+#pragma unroll
+      for (int q = 0; q < 32; ++q) gsem[q] = 0.f;
+      bool ok = inside && pos < last_contributor;
+      if (ok) {
+        const float4 r0 = s_rec[0][j], r1 = s_rec[1][j], r2 = s_rec[2][j];
+        const V3 Tu = v3(r0.x, r0.y, r0.z), Tv = v3(r0.w, r1.x, r1.y), Tw = v3(r1.z, r1.w, r2.x);
+        V3 k, l;
+        if (VARIANT == SGR_VARIANT_PLAIN) {
+          k = pxf * Tw - Tu;
+          l = pyf * Tw - Tv;
+        } else {
+          k = v3(-Tu.x + pxf * Tw.x, -Tu.y + pxf * Tw.y, -Tu.z + pxf * Tw.z);
+          l = v3(-Tv.x + pyf * Tw.x, -Tv.y + pyf * Tw.y, -Tv.z + pyf * Tw.z);
+        }
+        const V3 p = cross3(k, l);
+        const float dx = r2.y - pxf, dy = r2.z - pyf;
+        const float rho2d = kFilterInvSquareP0 * (dx * dx + dy * dy);
+        const float reach = s_rec[3][j].w;
+        ok = p.z != 0.0f && !(rho2d > reach && p.x * p.x + p.y * p.y > reach * (p.z * p.z));
+        if (ok) {
+          const float sx = p.x / p.z, sy = p.y / p.z;
+          const float rho3d = sx * sx + sy * sy;
+          const bool use3d = rho3d <= rho2d;
+          const float rho = fminf(rho3d, rho2d);
+          const float c_d = use3d ? (sx * Tw.x + sy * Tw.y) + Tw.z : Tw.z;
+          const float power = -0.5f * rho;
+          const float G = expf(power);
+          const float alpha = fminf(0.99f, r2.w * G);
+          ok = !(c_d < kNearP0) && !(power > 0.0f) && !(alpha < 1.0f / 255.0f);
+          if (ok) {
+            const float4 r3 = s_rec[3][j], r4 = s_rec[4][j];
+            T = T / (1.f - alpha);
+            const float wgt = alpha * T;
+            float dL_dalpha = 0.0f;
+            const float col[3] = {r4.x, r4.y, r4.z};
+#pragma unroll
+            for (int ch = 0; ch < 3; ++ch) {
+              accum_rec[ch] = last_alpha * last_color[ch] + (1.f - last_alpha) * accum_rec[ch];
+              last_color[ch] = col[ch];
+              dL_dalpha += (col[ch] - accum_rec[ch]) * dL_dpixel[ch];
+              gv[14 + ch] = wgt * dL_dpixel[ch];
+            }
+            if (VARIANT == SGR_VARIANT_PART) {
+              for (int c = 0; c < S; ++c) {
+                accum_sem[c] = last_alpha * last_sem[c] + (1.f - last_alpha) * accum_sem[c];
+                last_sem[c] = s_sem[c][j];
+              }
+            }
+            float dL_dz = 0.0f, dL_dweight = 0.f;
+            float m_d, dmd_dd;
+            if (VARIANT == SGR_VARIANT_PLAIN) {
+              m_d = kFarP0 / (kFarP0 - kNearP0) * (1 - kNearP0 / c_d);
+              dmd_dd = (kFarP0 * kNearP0) / ((kFarP0 - kNearP0) * c_d * c_d);
+            } else {
+              m_d = mapped_depth_p1(c_d);
+              dmd_dd = (float)((kFarP1 * kNearP1) / ((kFarP1 - kNearP1) * c_d * c_d));
+            }
+            if (pos == median_contributor - 1) {
+              dL_dz += dL_dmedian;
+              if (VARIANT == SGR_VARIANT_PART) dL_dweight += dL_dmaxw;
+            }
+            dL_dweight += (final_D2 + m_d * m_d * final_A - 2 * m_d * final_D) * dL_dreg;
+            dL_dalpha += dL_dweight - last_dL_dT;
+            last_dL_dT = dL_dweight * alpha + (1 - alpha) * last_dL_dT;
+            const float dL_dmd = 2.0f * (T * alpha) * (m_d * final_A - final_D) * dL_dreg;
+            dL_dz += dL_dmd * dmd_dd;
+            accum_depth = last_alpha * last_depth + (1.f - last_alpha) * accum_depth;
+            last_depth = c_d;
+            dL_dalpha += (c_d - accum_depth) * dL_ddepth;
+            // the reference adds last_alpha * 1.0 in double: one rounding of
+            // an exact sum, i.e. a plain float add
+            accum_alpha = __fadd_rn(last_alpha, __fmul_rn(1.f - last_alpha, accum_alpha));
+            dL_dalpha += (1 - accum_alpha) * dL_daccum;
+            const float nrm[3] = {r3.x, r3.y, r3.z};
+#pragma unroll
+            for (int ch = 0; ch < 3; ++ch) {
+              accum_normal[ch] = last_alpha * last_normal[ch] + (1.f - last_alpha) * accum_normal[ch];
+              last_normal[ch] = nrm[ch];
+              dL_dalpha += (nrm[ch] - accum_normal[ch]) * dL_dnormal2D[ch];
+              gv[11 + ch] = alpha * T * dL_dnormal2D[ch];
+            }
+            dL_dalpha *= T;
+            last_alpha = alpha;
+            dL_dalpha += (-T_final / (1.f - alpha)) * bg_dot;
+            const float dL_dG = r2.w * dL_dalpha;
+            dL_dz += alpha * T * dL_ddepth;
+            if (use3d) {
+              const float dsx = dL_dG * -G * sx + dL_dz * Tw.x;
+              const float dsy = dL_dG * -G * sy + dL_dz * Tw.y;
+              const float dsx_pz = dsx / p.z;
+              const float dsy_pz = dsy / p.z;
+              const V3 dL_dp = v3(dsx_pz, dsy_pz, -(dsx_pz * sx + dsy_pz * sy));
+              const V3 dL_dk = cross3(l, dL_dp);
+              const V3 dL_dl = cross3(dL_dp, k);
+              gv[0] = -dL_dk.x; gv[1] = -dL_dk.y; gv[2] = -dL_dk.z;
+              gv[3] = -dL_dl.x; gv[4] = -dL_dl.y; gv[5] = -dL_dl.z;
+              gv[6] = pxf * dL_dk.x + pyf * dL_dl.x + dL_dz * sx;
+              gv[7] = pxf * dL_dk.y + pyf * dL_dl.y + dL_dz * sy;
+              gv[8] = pxf * dL_dk.z + pyf * dL_dl.z + dL_dz * 1.0f;
+            } else {
+              gv[9] = dL_dG * (-G * kFilterInvSquareP0 * dx);
+              gv[10] = dL_dG * (-G * kFilterInvSquareP0 * dy);
+              gv[8] = dL_dz;
+            }
+            gv[17] = G * dL_dalpha;
+            if (VARIANT == SGR_VARIANT_PART) {
+              for (int c = 0; c < S; ++c) gsem[c] = wgt * dsem_pix[c];
+            }
+          }
+        }
+      }
+      if (__any_sync(0xffffffffu, ok)) {
+        const float total = warp_transpose_sum(gv, lane);
+        const uint32_t r = s_id[j];
+        if (lane < kGradUsed && total != 0.f) atomicAdd(grads + (size_t)r * kGradF + lane, total);
+        if (VARIANT == SGR_VARIANT_PART && S > 0) {
+          const float st = warp_transpose_sum(gsem, lane);
+          if (lane < S && st != 0.f) atomicAdd(dL_dsemantics + (size_t)(sid_base + (int)r) * S + lane, st);
+        }
+      }
+    }
+  }
+}
+
+void launch_render_fwd(const sgr_batch& b, const GeomView& g, const uint32_t* point_list,
+                       const sgr_fwd_outputs& out, cudaStream_t st) {
+  const unsigned blocks = (unsigned)(g.tiles_x * g.tiles_y) * (unsigned)b.num_views;
+  if (blocks == 0) return;
+  if (b.variant == SGR_VARIANT_PLAIN) k_render_fwd<SGR_VARIANT_PLAIN><<<blocks, kBlock, 0, st>>>(b, g, point_list, out);
+  else k_render_fwd<SGR_VARIANT_PART><<<blocks, kBlock, 0, st>>>(b, g, point_list, out);
+}
+
+void launch_render_bwd(const sgr_batch& b, const GeomView& g, const uint32_t* point_list, const sgr_bwd_inputs& in,
+                       float* grads, float* dL_dsemantics, cudaStream_t st) {
+  const unsigned blocks = (unsigned)(g.tiles_x * g.tiles_y) * (unsigned)b.num_views;
+  if (blocks == 0) return;
+  if (b.variant == SGR_VARIANT_PLAIN)
+    k_render_bwd<SGR_VARIANT_PLAIN><<<blocks, kBlock, 0, st>>>(b, g, point_list, in, grads, dL_dsemantics);
+  else
+    k_render_bwd<SGR_VARIANT_PART><<<blocks, kBlock, 0, st>>>(b, g, point_list, in, grads, dL_dsemantics);
+}
+
+}  // namespace sgr

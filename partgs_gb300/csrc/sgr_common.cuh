@@ -1,15 +1,23 @@
 // Shared device definitions of the GB300 surfel rasteriser.
 //
-// Per-view surfel record (80 B, five float4, 16-B aligned), written by the
+// Per-view surfel record (96 B, six float4, 16-B aligned), written by the
 // preprocess and gathered by both blends:
 //   r0 = (Tu.x, Tu.y, Tu.z, Tv.x)
 //   r1 = (Tv.y, Tv.z, Tw.x, Tw.y)
 //   r2 = (Tw.z, centre.x, centre.y, opacity)
-//   r3 = (normal.x, normal.y, normal.z, view depth)
+//   r3 = (normal.x, normal.y, normal.z, reach threshold c)
 //   r4 = (r, g, b, clamped bits as a float bit pattern)
+//   r5 = (x_min, x_max, y_min, y_max) pixel box the surfel can reach
 // Tu/Tv/Tw are the rows of the splat-to-pixel homography (the reference's
 // transMat, cuda_rasterizer/forward.cu:75-115), the centre and normal are
 // the reference's points_xy_image and normal_opacity.
+//
+// Reach: a fragment contributes only if opacity * exp(-rho/2) >= 1/255,
+// i.e. rho <= 2 ln(255 opacity).  c is that bound with a safety margin, and
+// r5 bounds every pixel centre whose rho (the smaller of the splat-space
+// distance rho3d and the screen-space filter distance rho2d) can be <= c.
+// Pixels outside the box, or with both distances above c, are skipped
+// without evaluating them: the reference would skip them at its alpha test.
 //
 // Per-view gradient record (80 B, 20 floats), accumulated by the blend
 // backward and reduced over views by the preprocess backward:
@@ -26,7 +34,7 @@ namespace sgr {
 
 constexpr int kTile = SGR_TILE;
 constexpr int kBlock = kTile * kTile;
-constexpr int kRecF4 = 5;          // float4 per record
+constexpr int kRecF4 = 6;          // float4 per record
 constexpr int kGradF = 20;         // floats per gradient record
 constexpr int kGradUsed = 18;
 

@@ -149,12 +149,16 @@ __global__ void __launch_bounds__(128) k_preprocess(const sgr_batch b, GeomView 
     uint32_t clamped = 0;
     if (b.shs != nullptr) rgb = sh_to_rgb(b.sh_degree, sh, p, v3(b.campos[3 * v], b.campos[3 * v + 1], b.campos[3 * v + 2]), clamped);
 
+    float reach_c;
+    float4 box;
+    reach_box(Tu, Tv, Tw, cxp, cyp, opac, reach_c, box);
     float4* rec = g.records + (size_t)r * kRecF4;
     rec[0] = make_float4(Tu.x, Tu.y, Tu.z, Tv.x);
     rec[1] = make_float4(Tv.y, Tv.z, Tw.x, Tw.y);
     rec[2] = make_float4(Tw.z, cxp, cyp, opac);
-    rec[3] = make_float4(normal.x, normal.y, normal.z, pv.z);
+    rec[3] = make_float4(normal.x, normal.y, normal.z, reach_c);
     rec[4] = make_float4(rgb.x, rgb.y, rgb.z, __uint_as_float(clamped));
+    rec[5] = box;
     g.radii[r] = (int)radius;
     g.tiles_touched[r] = (uint32_t)touched;
     g.depth_keys[r] = ((unsigned long long)v << 32) | (unsigned long long)__float_as_uint(pv.z);
@@ -227,157 +231,6 @@ __global__ void k_tile_ranges(const uint32_t* __restrict__ keys, const Status* s
   }
 }
 
-// ---------------------------------------------------------------------------
-// blend forward: one CTA per 16x16 tile, one pixel per thread, surfel records
-// staged 256 at a time in shared memory (P0/cr/forward.cu:256-441,
-// P1/cr/forward.cu:265-474)
-// ---------------------------------------------------------------------------
-template <int VARIANT>
-__global__ void __launch_bounds__(kBlock) k_render_fwd(const sgr_batch b, GeomView g,
-                                                       const uint32_t* __restrict__ point_list,
-                                                       sgr_fwd_outputs out) {
-  const int tiles_per_view = g.tiles_x * g.tiles_y;
-  const int tile = blockIdx.x;
-  const int v = tile / tiles_per_view;
-  const int t = tile - v * tiles_per_view;
-  const int ty = t / g.tiles_x, tx = t - ty * g.tiles_x;
-  const int W = b.width, H = b.height;
-  const int px = tx * kTile + (threadIdx.x & (kTile - 1));
-  const int py = ty * kTile + (threadIdx.x / kTile);
-  const bool inside = px < W && py < H;
-  const float pxf = (VARIANT == SGR_VARIANT_PLAIN) ? (float)px : (float)px + 0.5f;
-  const float pyf = (VARIANT == SGR_VARIANT_PLAIN) ? (float)py : (float)py + 0.5f;
-  const int S = (VARIANT == SGR_VARIANT_PART) ? b.semantic_channels : 0;
-  const sgr_view_desc vd = b.views[v];
-  const int sid_base = b.scenes[vd.scene].surfel_offset - vd.record_offset;
-
-  __shared__ float4 s_rec[kRecF4][kBlock];
-  __shared__ float s_sem[(VARIANT == SGR_VARIANT_PART) ? SGR_MAX_SEMANTICS : 1][kBlock];
-
-  const uint2 range = g.ranges[tile];
-  const int todo_all = (int)(range.y - range.x);
-  const int rounds = (todo_all + kBlock - 1) / kBlock;
-  int todo = todo_all;
-  bool done = !inside;
-
-  float T = 1.0f;
-  uint32_t contributor = 0, last_contributor = 0;
-  float C[3] = {0.f, 0.f, 0.f};
-  float N[3] = {0.f, 0.f, 0.f};
-  float D = 0.f, M1 = 0.f, M2 = 0.f, dist = 0.f, med_depth = 0.f, med_weight = 0.f;
-  int med_contrib = -1;
-  float Sem[SGR_MAX_SEMANTICS];
-#pragma unroll
-  for (int c = 0; c < SGR_MAX_SEMANTICS; ++c) Sem[c] = 0.f;
-
-  for (int i = 0; i < rounds; ++i, todo -= kBlock) {
-    if (__syncthreads_count(done) == kBlock) break;
-    const int progress = i * kBlock + threadIdx.x;
-    if ((int)range.x + progress < (int)range.y) {
-      const uint32_t r = point_list[range.x + progress];
-      const float4* rec = g.records + (size_t)r * kRecF4;
-#pragma unroll
-      for (int k = 0; k < kRecF4; ++k) s_rec[k][threadIdx.x] = rec[k];
-      if (VARIANT == SGR_VARIANT_PART) {
-        const float* sem = b.semantics + (size_t)(sid_base + (int)r) * S;
-        for (int c = 0; c < S; ++c) s_sem[c][threadIdx.x] = sem[c];
-      }
-    }
-    __syncthreads();
-    const int n = min(kBlock, todo);
-    for (int j = 0; !done && j < n; ++j) {
-      ++contributor;
-      const float4 r0 = s_rec[0][j], r1 = s_rec[1][j], r2 = s_rec[2][j];
-      const V3 Tu = v3(r0.x, r0.y, r0.z), Tv = v3(r0.w, r1.x, r1.y), Tw = v3(r1.z, r1.w, r2.x);
-      Frag fr;
-      intersect<VARIANT>(pxf, pyf, Tu, Tv, Tw, r2.y, r2.z, fr);
-      if (fr.p.z == 0.0f) continue;
-      if (fr.depth < kNearP0) continue;
-      const float power = -0.5f * fr.rho;
-      if (power > 0.0f) continue;
-      const float alpha = fminf(0.99f, r2.w * expf(power));
-      if (alpha < 1.0f / 255.0f) continue;
-      const float test_T = T * (1 - alpha);
-      if (test_T < 0.0001f) {
-        done = true;
-        continue;
-      }
-      const float4 r3 = s_rec[3][j], r4 = s_rec[4][j];
-      const float A = 1 - T;
-      if (VARIANT == SGR_VARIANT_PLAIN) {
-        const float w = alpha * T;
-        const float m = kFarP0 / (kFarP0 - kNearP0) * (1 - kNearP0 / fr.depth);
-        dist += (m * m * A + M2 - 2 * m * M1) * w;
-        D += fr.depth * w;
-        M1 += m * w;
-        M2 += m * m * w;
-        if (T > 0.5f) {
-          med_depth = fr.depth;
-          med_contrib = (int)contributor;
-        }
-        N[0] += r3.x * w;
-        N[1] += r3.y * w;
-        N[2] += r3.z * w;
-        C[0] += r4.x * w;
-        C[1] += r4.y * w;
-        C[2] += r4.z * w;
-      } else {
-        const float m = mapped_depth_p1(fr.depth);
-        const float err = m * m * A + M2 - 2 * m * M1;
-        dist += err * alpha * T;
-        if (T > 0.5f) {
-          med_depth = fr.depth;
-          med_weight = alpha * T;
-          med_contrib = (int)contributor;
-        }
-        N[0] += r3.x * alpha * T;
-        N[1] += r3.y * alpha * T;
-        N[2] += r3.z * alpha * T;
-        D += fr.depth * alpha * T;
-        M1 += m * alpha * T;
-        M2 += m * m * alpha * T;
-        C[0] += r4.x * alpha * T;
-        C[1] += r4.y * alpha * T;
-        C[2] += r4.z * alpha * T;
-        for (int c = 0; c < S; ++c) Sem[c] += s_sem[c][j] * alpha * T;
-      }
-      T = test_T;
-      last_contributor = contributor;
-    }
-  }
-
-  if (inside) {
-    const size_t HW = (size_t)H * W;
-    const size_t pix = (size_t)py * W + px;
-    float* fT = g.final_T + (size_t)v * 3 * HW;
-    uint32_t* nc = g.n_contrib + (size_t)v * 2 * HW;
-    fT[pix] = T;
-    fT[pix + HW] = M1;
-    fT[pix + 2 * HW] = M2;
-    nc[pix] = last_contributor;
-    nc[pix + HW] = med_contrib > 0 ? (uint32_t)med_contrib : 0u;
-    const float* bg = b.background;
-    float* col = out.color + (size_t)v * 3 * HW;
-    col[pix] = C[0] + T * bg[0];
-    col[pix + HW] = C[1] + T * bg[1];
-    col[pix + 2 * HW] = C[2] + T * bg[2];
-    const int NO = (VARIANT == SGR_VARIANT_PLAIN) ? 7 : 8;
-    float* oth = out.others + (size_t)v * NO * HW;
-    oth[pix] = D;
-    oth[pix + HW] = 1 - T;
-    oth[pix + 2 * HW] = N[0];
-    oth[pix + 3 * HW] = N[1];
-    oth[pix + 4 * HW] = N[2];
-    oth[pix + 5 * HW] = med_depth;
-    oth[pix + 6 * HW] = dist;
-    if (VARIANT == SGR_VARIANT_PART) {
-      oth[pix + 7 * HW] = med_weight;
-      float* sem = out.semantic + (size_t)v * S * HW;
-      for (int c = 0; c < S; ++c) sem[pix + c * HW] = Sem[c];
-    }
-  }
-}
-
 // Near-plane visibility (P0/cr/rasterizer_impl.cu:54-66).
 __global__ void k_mark_visible(int P, const float* __restrict__ means3D, const float* __restrict__ viewmatrix,
                                uint8_t* __restrict__ present) {
@@ -423,14 +276,6 @@ void launch_tile_ranges(const uint32_t* keys, const Status* status, long long ca
                         cudaStream_t st) {
   if (capacity <= 0) return;
   k_tile_ranges<<<kStrideBlocks, 256, 0, st>>>(keys, status, capacity, ranges);
-}
-
-void launch_render_fwd(const sgr_batch& b, const GeomView& g, const uint32_t* point_list,
-                       const sgr_fwd_outputs& out, cudaStream_t st) {
-  const unsigned blocks = (unsigned)(g.tiles_x * g.tiles_y) * (unsigned)b.num_views;
-  if (blocks == 0) return;
-  if (b.variant == SGR_VARIANT_PLAIN) k_render_fwd<SGR_VARIANT_PLAIN><<<blocks, kBlock, 0, st>>>(b, g, point_list, out);
-  else k_render_fwd<SGR_VARIANT_PART><<<blocks, kBlock, 0, st>>>(b, g, point_list, out);
 }
 
 void launch_mark_visible(int P, const float* means3D, const float* viewmatrix, uint8_t* present, cudaStream_t st) {

@@ -89,6 +89,54 @@ __device__ __forceinline__ V3 sh_to_rgb(int deg, const float* sh, V3 pos, V3 cam
   return v3(fmaxf(res.x, 0.0f), fmaxf(res.y, 0.0f), fmaxf(res.z, 0.0f));
 }
 
+// Reach of one record (see sgr_common.cuh): the threshold c and the box of
+// pixel centres where rho = min(rho3d, rho2d) <= c is possible.
+//  * rho2d <= c is the disk |pixel - centre| <= sqrt(c / 2).
+//  * rho3d <= c is the image of the splat-space disk u^2 + v^2 <= c under
+//    the homography x = Tu.S / Tw.S (S = (u, v, 1)).  A vertical line x = X
+//    pulls back to (Tu - X Tw).S = 0, which is tangent to the circle when
+//    (Tu.z - X Tw.z)^2 = c ((Tu.x - X Tw.x)^2 + (Tu.y - X Tw.y)^2); with
+//    d = c (Tw.x^2 + Tw.y^2) - Tw.z^2, p = c (Tu.x Tw.x + Tu.y Tw.y) - Tu.z Tw.z
+//    and q = c (Tu.x^2 + Tu.y^2) - Tu.z^2 the extreme X are p/d +- sqrt(p^2/d^2 - q/d).
+//    The image is a bounded ellipse only when d < 0 (Tw.S keeps its sign on
+//    the disk); otherwise the reach is unbounded and nothing is skipped.
+// Evaluated in double, widened by half a pixel.
+__device__ __forceinline__ void reach_box(V3 Tu, V3 Tv, V3 Tw, float cx, float cy, float opac, float& c_out,
+                                          float4& box) {
+  const float kBig = 3.0e38f;
+  if (!(opac >= 1.0f / 255.0f)) {   // alpha <= opacity < 1/255 everywhere
+    c_out = -1.0f;
+    box = make_float4(kBig, -kBig, kBig, -kBig);
+    return;
+  }
+  const double c = 2.0 * log(255.0 * (double)opac) * 1.001 + 0.01;
+  c_out = (float)c;
+  const double r2 = sqrt(c / 2.0);
+  double x0 = cx - r2, x1 = cx + r2, y0 = cy - r2, y1 = cy + r2;
+  const double twx = Tw.x, twy = Tw.y, twz = Tw.z;
+  const double d = c * (twx * twx + twy * twy) - twz * twz;
+  if (d < -1e-6 * twz * twz) {
+    auto extent = [&](V3 T, double& lo, double& hi) {
+      const double p = c * ((double)T.x * twx + (double)T.y * twy) - (double)T.z * twz;
+      const double q = c * ((double)T.x * T.x + (double)T.y * T.y) - (double)T.z * T.z;
+      const double e = p / d;
+      const double h = sqrt(fmax(0.0, e * e - q / d));
+      lo = e - h;
+      hi = e + h;
+    };
+    double ex0, ex1, ey0, ey1;
+    extent(Tu, ex0, ex1);
+    extent(Tv, ey0, ey1);
+    x0 = fmin(x0, ex0);
+    x1 = fmax(x1, ex1);
+    y0 = fmin(y0, ey0);
+    y1 = fmax(y1, ey1);
+    box = make_float4((float)(x0 - 0.5), (float)(x1 + 0.5), (float)(y0 - 0.5), (float)(y1 + 0.5));
+  } else {
+    box = make_float4(-kBig, kBig, -kBig, kBig);
+  }
+}
+
 __device__ __forceinline__ int find_view(const sgr_view_desc* views, int n, int record) {
   int lo = 0, hi = n - 1;
   while (lo < hi) {
