@@ -41,7 +41,7 @@ int bit_length(unsigned long long n) {
 // Byte layout of the forward scratch.
 struct ScratchLayout {
   size_t depth_keys, depth_vals, depth_keys_sorted, temp_a, temp_a_bytes;
-  size_t keys, vals, keys_sorted, temp_b, temp_b_bytes;
+  size_t bin;          // tile-list construction scratch (sgr_binning.cu)
   size_t end_a, end;
 };
 
@@ -100,18 +100,14 @@ int scratch_layout(const sgr_batch* b, long long cap, ScratchLayout& L) {
   L.temp_a_bytes = std::max(sort_a, scan_a);
   o = align_up(o + L.temp_a_bytes);
   L.end_a = o;
-  const size_t K = (size_t)std::max(0LL, cap);
-  L.keys = o; o = align_up(o + K * 4);
-  L.vals = o; o = align_up(o + K * 4);
-  L.keys_sorted = o; o = align_up(o + K * 4);
-  size_t sort_b = 0;
-  if (K > 0)
-    SGR_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, sort_b, (const uint32_t*)nullptr, (uint32_t*)nullptr,
-                                             (const uint32_t*)nullptr, (uint32_t*)nullptr, (int64_t)K, 0,
-                                             std::max(1, tile_key_bits(b))));
-  L.temp_b = o;
-  L.temp_b_bytes = sort_b;
-  o = align_up(o + sort_b);
+  (void)cap;
+  int gx, gy, chunk, warps;
+  tile_grid(b, gx, gy);
+  size_t oc, ot, otmp, tb;
+  const size_t bin = binning_scratch_bytes(b->num_records, b->num_views, gx, gy, &chunk, &warps, &oc, &ot, &otmp, &tb);
+  if (bin == 0) return SGR_ERR_UNSUPPORTED;   // tile grid too large for the per-warp counters
+  L.bin = o;
+  o = align_up(o + bin);
   L.end = o;
   return SGR_OK;
 }
@@ -264,9 +260,6 @@ int sgr_forward_raster(const sgr_batch* batch, void* geom, void* lists, int64_t 
   if (fwd_scratch_bytes < L.end || (!fwd_scratch && L.end > 0)) return SGR_ERR_WORKSPACE;
   GeomView g = geom_view(batch, s, geom, fwd_scratch, &L);
   char* sp = static_cast<char*>(fwd_scratch);
-  uint32_t* keys = reinterpret_cast<uint32_t*>(sp + L.keys);
-  uint32_t* vals = reinterpret_cast<uint32_t*>(sp + L.vals);
-  uint32_t* keys_sorted = reinterpret_cast<uint32_t*>(sp + L.keys_sorted);
   uint32_t* point_list = static_cast<uint32_t*>(lists);
   const int NO = batch->variant == SGR_VARIANT_PLAIN ? 7 : 8;
   const size_t HW = (size_t)batch->height * batch->width;
@@ -279,19 +272,11 @@ int sgr_forward_raster(const sgr_batch* batch, void* geom, void* lists, int64_t 
       SGR_CUDA(cudaMemsetAsync(out->semantic, 0, (size_t)batch->num_views * batch->semantic_channels * HW * 4, st));
     return SGR_OK;
   }
-  SGR_CUDA(cudaMemsetAsync(g.ranges, 0, (size_t)batch->num_views * s.tiles_x * s.tiles_y * 8, st));
-  if (key_capacity > 0) {
+  {
     PhaseScope ph(SGR_PHASE_BINNING, st);
-    launch_duplicate(*batch, g, keys, vals, key_capacity, st);
-    SGR_CUDA(cudaGetLastError());
-    const uint32_t pad = (s.tile_key_bits >= 32) ? 0xffffffffu : ((1u << s.tile_key_bits) - 1u);
-    launch_pad_keys(keys, key_capacity, g.status, pad, st);
-    SGR_CUDA(cudaGetLastError());
-    size_t tb = L.temp_b_bytes;
-    SGR_CUDA(cub::DeviceRadixSort::SortPairs(sp + L.temp_b, tb, keys, keys_sorted, vals, point_list,
-                                             (int64_t)key_capacity, 0, std::max(1, s.tile_key_bits), st));
-    launch_tile_ranges(keys_sorted, g.status, key_capacity, g.ranges, st);
-    SGR_CUDA(cudaGetLastError());
+    rc = launch_binning(*batch, g, point_list, key_capacity, sp + L.bin, st);
+    if (rc == SGR_ERR_CUDA) return cuda_fail(cudaGetLastError(), "tile-list construction");
+    if (rc) return rc;
   }
   {
     PhaseScope ph(SGR_PHASE_BLEND_FWD, st);

@@ -165,70 +165,8 @@ __global__ void __launch_bounds__(128) k_preprocess(const sgr_batch b, GeomView 
   }
 }
 
-// ---------------------------------------------------------------------------
-// key duplication: one key per (surfel, touched tile), emitted in depth order
-// so that a stable sort by tile alone reproduces the reference's
-// (tile, depth, surfel) order (P0/cr/rasterizer_impl.cu:70-111, 304-309)
-// ---------------------------------------------------------------------------
-__global__ void k_duplicate(const sgr_batch b, GeomView g, uint32_t* __restrict__ keys,
-                            uint32_t* __restrict__ vals, long long capacity) {
-  const long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= b.num_records) return;
-  const uint32_t r = g.depth_order[j];
-  const uint32_t n = g.tiles_touched[r];
-  if (n == 0) return;
-  const unsigned long long end = g.offsets[j];
-  const unsigned long long start = end - n;
-  // Past the capacity the keys are dropped and the overflow flag raised;
-  // every slot below the capacity still receives a valid key.
-  if ((long long)end > capacity) atomicOr(&g.status->flags, SGR_FLAG_KEY_OVERFLOW);
-  if ((long long)start >= capacity) return;
-  const int v = find_view(b.views, b.num_views, (int)r);
-  const float4 r2 = g.records[(size_t)r * kRecF4 + 2];
-  int x0, y0, x1, y1;
-  tile_rect(r2.y, r2.z, g.radii[r], g.tiles_x, g.tiles_y, x0, y0, x1, y1);
-  const uint32_t base = (uint32_t)v * (uint32_t)(g.tiles_x * g.tiles_y);
-  unsigned long long o = start;
-  for (int y = y0; y < y1; ++y)
-    for (int x = x0; x < x1; ++x) {
-      if ((long long)o < capacity) {
-        keys[o] = base + (uint32_t)(y * g.tiles_x + x);
-        vals[o] = r;
-      }
-      ++o;
-    }
-}
-
-// Pads the unused tail of a fixed-capacity key array with a key above every
-// tile so that a sort over the whole capacity leaves it at the end.
-__global__ void k_pad_keys(uint32_t* keys, long long capacity, const Status* st, uint32_t pad_key) {
-  const long long stride = (long long)gridDim.x * blockDim.x;
-  for (long long k = (long long)st->num_keys + (long long)blockIdx.x * blockDim.x + threadIdx.x; k < capacity;
-       k += stride)
-    keys[k] = pad_key;
-}
-
 __global__ void k_store_key_count(GeomView g, long long R) {
   if (threadIdx.x == 0 && blockIdx.x == 0) g.status->num_keys = R > 0 ? g.offsets[R - 1] : 0ull;
-}
-
-// Per-tile [start, end) of the sorted list (P0/cr/rasterizer_impl.cu:116-138).
-__global__ void k_tile_ranges(const uint32_t* __restrict__ keys, const Status* st, long long capacity,
-                              uint2* __restrict__ ranges) {
-  const long long K = (long long)min((unsigned long long)capacity, st->num_keys);
-  const long long stride = (long long)gridDim.x * blockDim.x;
-  for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < K; k += stride) {
-    const uint32_t cur = keys[k];
-    if (k == 0) ranges[cur].x = 0;
-    else {
-      const uint32_t prev = keys[k - 1];
-      if (cur != prev) {
-        ranges[prev].y = (uint32_t)k;
-        ranges[cur].x = (uint32_t)k;
-      }
-    }
-    if (k == K - 1) ranges[cur].y = (uint32_t)K;
-  }
 }
 
 // Near-plane visibility (P0/cr/rasterizer_impl.cu:54-66).
@@ -253,29 +191,6 @@ void launch_preprocess(const sgr_batch& b, const GeomView& g, cudaStream_t st) {
 
 void launch_store_key_count(const GeomView& g, long long R, cudaStream_t st) {
   k_store_key_count<<<1, 32, 0, st>>>(g, R);
-}
-
-void launch_duplicate(const sgr_batch& b, const GeomView& g, uint32_t* keys, uint32_t* vals, long long capacity,
-                      cudaStream_t st) {
-  const int threads = 256;
-  const long long blocks = ((long long)b.num_records + threads - 1) / threads;
-  if (blocks == 0) return;
-  k_duplicate<<<(unsigned)blocks, threads, 0, st>>>(b, g, keys, vals, capacity);
-}
-
-// Grid-stride kernels over the key list run on a fixed grid: 152 SMs x 8
-// resident CTAs of 256 threads.
-constexpr int kStrideBlocks = 152 * 8;
-
-void launch_pad_keys(uint32_t* keys, long long capacity, const Status* status, uint32_t pad_key, cudaStream_t st) {
-  if (capacity <= 0) return;
-  k_pad_keys<<<kStrideBlocks, 256, 0, st>>>(keys, capacity, status, pad_key);
-}
-
-void launch_tile_ranges(const uint32_t* keys, const Status* status, long long capacity, uint2* ranges,
-                        cudaStream_t st) {
-  if (capacity <= 0) return;
-  k_tile_ranges<<<kStrideBlocks, 256, 0, st>>>(keys, status, capacity, ranges);
 }
 
 void launch_mark_visible(int P, const float* means3D, const float* viewmatrix, uint8_t* present, cudaStream_t st) {

@@ -99,8 +99,14 @@ __device__ __forceinline__ V3 sh_to_rgb(int deg, const float* sh, V3 pos, V3 cam
 //    d = c (Tw.x^2 + Tw.y^2) - Tw.z^2, p = c (Tu.x Tw.x + Tu.y Tw.y) - Tu.z Tw.z
 //    and q = c (Tu.x^2 + Tu.y^2) - Tu.z^2 the extreme X are p/d +- sqrt(p^2/d^2 - q/d).
 //    The image is a bounded ellipse only when d < 0 (Tw.S keeps its sign on
-//    the disk); otherwise the reach is unbounded and nothing is skipped.
-// Evaluated in double, widened by half a pixel.
+//    the disk); near that limit (|d| under 1e-3 of its terms) or for a
+//    centre far outside any image the reach is treated as unbounded and
+//    nothing is skipped.
+// Evaluated in single precision in coordinates relative to the integer pixel
+// (X0, Y0) under the surfel's centre: Tu' = Tu - X0 Tw keeps p, q and e small,
+// so the cancellation in e^2 - q/d is relative to the offset from that pixel
+// (errors ~1e-4 px), not to the absolute pixel coordinate.  The box is
+// widened by half a pixel plus 1e-4 of its size.
 __device__ __forceinline__ void reach_box(V3 Tu, V3 Tv, V3 Tw, float cx, float cy, float opac, float& c_out,
                                           float4& box) {
   const float kBig = 3.0e38f;
@@ -109,32 +115,36 @@ __device__ __forceinline__ void reach_box(V3 Tu, V3 Tv, V3 Tw, float cx, float c
     box = make_float4(kBig, -kBig, kBig, -kBig);
     return;
   }
-  const double c = 2.0 * log(255.0 * (double)opac) * 1.001 + 0.01;
-  c_out = (float)c;
-  const double r2 = sqrt(c / 2.0);
-  double x0 = cx - r2, x1 = cx + r2, y0 = cy - r2, y1 = cy + r2;
-  const double twx = Tw.x, twy = Tw.y, twz = Tw.z;
-  const double d = c * (twx * twx + twy * twy) - twz * twz;
-  if (d < -1e-6 * twz * twz) {
-    auto extent = [&](V3 T, double& lo, double& hi) {
-      const double p = c * ((double)T.x * twx + (double)T.y * twy) - (double)T.z * twz;
-      const double q = c * ((double)T.x * T.x + (double)T.y * T.y) - (double)T.z * T.z;
-      const double e = p / d;
-      const double h = sqrt(fmax(0.0, e * e - q / d));
-      lo = e - h;
-      hi = e + h;
-    };
-    double ex0, ex1, ey0, ey1;
-    extent(Tu, ex0, ex1);
-    extent(Tv, ey0, ey1);
-    x0 = fmin(x0, ex0);
-    x1 = fmax(x1, ex1);
-    y0 = fmin(y0, ey0);
-    y1 = fmax(y1, ey1);
-    box = make_float4((float)(x0 - 0.5), (float)(x1 + 0.5), (float)(y0 - 0.5), (float)(y1 + 0.5));
-  } else {
+  const float c = 2.0f * logf(255.0f * opac) * 1.001f + 0.01f;
+  c_out = c;
+  const float r2 = sqrtf(0.5f * c) * 1.0001f + 1e-3f;
+  float x0 = cx - r2, x1 = cx + r2, y0 = cy - r2, y1 = cy + r2;
+  const float sxy = Tw.x * Tw.x + Tw.y * Tw.y;
+  const float d = c * sxy - Tw.z * Tw.z;
+  const bool bounded = d < -1e-3f * (c * sxy + Tw.z * Tw.z) && fabsf(cx) < 1e6f && fabsf(cy) < 1e6f;
+  if (!bounded) {
     box = make_float4(-kBig, kBig, -kBig, kBig);
+    return;
   }
+  const float inv = 1.0f / d;
+  auto extent = [&](V3 T, float O, float& lo, float& hi) {
+    const V3 Ts = v3(T.x - O * Tw.x, T.y - O * Tw.y, T.z - O * Tw.z);
+    const float p = c * (Ts.x * Tw.x + Ts.y * Tw.y) - Ts.z * Tw.z;
+    const float q = c * (Ts.x * Ts.x + Ts.y * Ts.y) - Ts.z * Ts.z;
+    const float e = p * inv;
+    const float h = sqrtf(fmaxf(0.0f, e * e - q * inv));
+    const float m = 1e-4f * (fabsf(e) + h);
+    lo = O + (e - h - m);
+    hi = O + (e + h + m);
+  };
+  float ex0, ex1, ey0, ey1;
+  extent(Tu, floorf(cx), ex0, ex1);
+  extent(Tv, floorf(cy), ey0, ey1);
+  x0 = fminf(x0, ex0);
+  x1 = fmaxf(x1, ex1);
+  y0 = fminf(y0, ey0);
+  y1 = fmaxf(y1, ey1);
+  box = make_float4(x0 - 0.5f, x1 + 0.5f, y0 - 0.5f, y1 + 0.5f);
 }
 
 __device__ __forceinline__ int find_view(const sgr_view_desc* views, int n, int record) {
@@ -164,11 +174,12 @@ __device__ __forceinline__ float warp_transpose_sum(float (&v)[32], int lane) {
 
 void launch_preprocess(const sgr_batch& b, const GeomView& g, cudaStream_t st);
 void launch_store_key_count(const GeomView& g, long long R, cudaStream_t st);
-void launch_duplicate(const sgr_batch& b, const GeomView& g, uint32_t* keys, uint32_t* vals, long long capacity,
-                      cudaStream_t st);
-void launch_pad_keys(uint32_t* keys, long long capacity, const Status* status, uint32_t pad_key, cudaStream_t st);
-void launch_tile_ranges(const uint32_t* keys, const Status* status, long long capacity, uint2* ranges,
-                        cudaStream_t st);
+// Tile-list construction (sgr_binning.cu).  binning_scratch_bytes returns 0
+// when the tile grid is too large for it.
+size_t binning_scratch_bytes(long long R, int V, int gx, int gy, int* chunk_out, int* warps_out,
+                             size_t* off_counts, size_t* off_tiles, size_t* off_temp, size_t* temp_bytes);
+int launch_binning(const sgr_batch& b, const GeomView& g, uint32_t* point_list, long long capacity, void* scratch,
+                   cudaStream_t st);
 void launch_render_fwd(const sgr_batch& b, const GeomView& g, const uint32_t* point_list,
                        const sgr_fwd_outputs& out, cudaStream_t st);
 void launch_mark_visible(int P, const float* means3D, const float* viewmatrix, uint8_t* present, cudaStream_t st);
