@@ -221,6 +221,35 @@ int sgr_profile_read(float* ms, int32_t* count);
 int sgr_mark_visible(int32_t P, const float* means3D, const float* viewmatrix, const float* projmatrix,
                      uint8_t* present, void* stream);
 
+/* ---- point-level training loss ------------------------------------------ */
+
+/* The per-view loss of the reference's point-stage step (train.py:229-250,
+ * utils/loss_utils.py:8-54, utils/point_utils.py:4-33), averaged over V views:
+ *   L = (1 - ls) mean|c - t| + ls (1 - mean SSIM11(c, t))
+ *     + ld mean(distortion) + ln mean(1 - n_render . n_surface)
+ * n_render is the rendered normal rotated to world space; n_surface is the
+ * normal of the surface depth (median depth weighted by depth_ratio, the
+ * expected depth by 1 - depth_ratio) times the detached alpha. */
+typedef struct sgr_loss_args {
+    int32_t V, H, W;
+    float lambda_dssim;
+    float lambda_dist;
+    float lambda_normal;
+    float depth_ratio;
+    const float* color;          /* [V,3,H,W] rendered */
+    const float* target;         /* [V,3,H,W] */
+    const float* others;         /* [V,7,H,W] rendered aux maps (plain layout) */
+    const float* view_to_world;  /* [V,3,3] rotation taking view normals to world: n_w[d] = sum_c n_v[c] R[c][d] */
+    const float* ray_basis;      /* [V,3,3] rows a0, a1, a2: ray(x, y) = x a0 + y a1 + a2 */
+    const float* ray_origin;     /* [V,3] */
+} sgr_loss_args;
+
+size_t sgr_loss_scratch_bytes(const sgr_loss_args* a);
+/* Loss value (device float) and its gradients w.r.t. color and others (every
+ * element written). */
+int sgr_loss_forward_backward(const sgr_loss_args* a, float* loss, float* dL_dcolor, float* dL_dothers, void* scratch,
+                              void* stream);
+
 /* ---- superquadric binding ---------------------------------------------- */
 
 /* Shapes of the binding: B superquadrics, each with V vertices on an

@@ -85,7 +85,8 @@ class SurfelTrainer:
     """Surfel parameters, the batched loss and Adam."""
 
     def __init__(self, scene, cameras, key_capacity=None, lambda_dssim=0.2, lambda_dist=1000.0,
-                 lambda_normal=0.05, depth_ratio=1.0, bg=(0.0, 0.0, 0.0), device="cuda", extent=3.0):
+                 lambda_normal=0.05, depth_ratio=1.0, bg=(0.0, 0.0, 0.0), device="cuda", extent=3.0,
+                 fused_loss=True):
         dev = torch.device(device)
         self.xyz = scene.means3D.detach().clone().to(dev).requires_grad_(True)
         self.log_scaling = torch.log(scene.scales).detach().clone().to(dev).requires_grad_(True)
@@ -101,6 +102,10 @@ class SurfelTrainer:
         self.window = _gaussian_window(device=dev)
         self.lambda_dssim, self.lambda_dist, self.lambda_normal = lambda_dssim, lambda_dist, lambda_normal
         self.depth_ratio = depth_ratio
+        self.point_loss = None
+        if fused_loss:
+            from .losses import PointLoss
+            self.point_loss = PointLoss(cameras, lambda_dssim, lambda_dist, lambda_normal, depth_ratio, dev)
         groups = [
             {"params": [self.xyz], "lr": 0.00016 * extent},
             {"params": [self.features_dc], "lr": 0.0025},
@@ -123,6 +128,13 @@ class SurfelTrainer:
         opac = torch.sigmoid(self.opacity_logit)
         shs = torch.cat((self.features_dc, self.features_rest), dim=1)
         color, allmap, _, _ = self.raster(self.xyz, opac, shs, scales, rots)
+        if self.point_loss is not None:
+            return self.point_loss(color, allmap, targets)
+        return self.reference_loss(color, allmap, targets)
+
+    def reference_loss(self, color, allmap, targets):
+        """The loss in PyTorch operations (the statement the fused kernels
+        follow)."""
         l1 = torch.abs(color - targets).mean()
         loss = (1.0 - self.lambda_dssim) * l1 + self.lambda_dssim * (1.0 - ssim(color, targets, self.window))
         alpha = allmap[:, 1:2]

@@ -1,0 +1,71 @@
+"""The fused point-level loss kernels against the same loss in PyTorch
+operations (autograd, float64): value and gradients w.r.t. the rendered
+colour and aux maps."""
+import types
+
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+
+def _inputs(V=3, H=60, W=80, seed=0):
+    g = torch.Generator().manual_seed(seed)
+    color = torch.rand(V, 3, H, W, generator=g)
+    target = torch.rand(V, 3, H, W, generator=g)
+    yy, xx = torch.meshgrid(torch.linspace(-1, 1, H), torch.linspace(-1, 1, W), indexing="ij")
+    alpha = (0.2 + 0.8 * torch.rand(V, 1, H, W, generator=g)).clamp(max=1.0)
+    median = 2.5 + 0.3 * torch.sin(3 * xx + 1) * torch.cos(2 * yy) + 0.01 * torch.rand(V, 1, H, W, generator=g)
+    expected = median * alpha * (1 + 0.05 * torch.rand(V, 1, H, W, generator=g))
+    normal = torch.nn.functional.normalize(torch.randn(V, 3, H, W, generator=g), dim=1) * alpha
+    dist = 1e-3 * torch.rand(V, 1, H, W, generator=g)
+    others = torch.cat([expected, alpha, normal, median, dist], 1)
+    alpha0 = others[:, 1].clone()
+    others[:, 1][:, :3, :3] = 0.0             # a few empty pixels: expected depth 0/0
+    others[:, 0][:, :3, :3] = 0.0
+    del alpha0
+    return color, others, target
+
+
+@pytest.mark.parametrize("depth_ratio", [1.0, 0.4])
+def test_fused_loss_matches_pytorch(sgr_lib, depth_ratio):
+    from partgs_gb300.cameras import orbit_cameras
+    from partgs_gb300.losses import PointLoss
+    from partgs_gb300.surfel_step import DepthNormals, SurfelTrainer, _gaussian_window
+    cams = orbit_cameras(3, 3.0, 60, 80, 55.0, seed=2)
+    color, others, target = _inputs()
+    loss_fn = PointLoss(cams, 0.2, 1000.0, 0.05, depth_ratio)
+    c = color.cuda().requires_grad_(True)
+    o = others.cuda().requires_grad_(True)
+    L = loss_fn(c, o, target.cuda())
+    L.backward()
+
+    ref = types.SimpleNamespace(window=_gaussian_window(device="cuda").double(), lambda_dssim=0.2,
+                                lambda_dist=1000.0, lambda_normal=0.05, depth_ratio=depth_ratio,
+                                normals=DepthNormals(cams, "cuda"))
+    ref.normals.rays_d = ref.normals.rays_d.double()
+    ref.normals.rays_o = ref.normals.rays_o.double()
+    ref.normals.view_to_world = ref.normals.view_to_world.double()
+    c64 = color.double().cuda().requires_grad_(True)
+    o64 = others.double().cuda().requires_grad_(True)
+    L64 = SurfelTrainer.reference_loss(ref, c64, o64, target.double().cuda())
+    L64.backward()
+    assert abs(float(L.detach()) - float(L64.detach())) <= 1e-5 * abs(float(L64.detach()))
+    # At empty pixels (alpha = 0) the PyTorch statement divides 0 by 0 for the
+    # expected depth; nan_to_num zeroes the value but autograd's division
+    # backward still yields NaN there.  The kernels write 0; compare elsewhere.
+    assert torch.isfinite(c.grad).all() and torch.isfinite(o.grad).all()
+    for mine, theirs, name in ((c.grad, c64.grad, "color"), (o.grad, o64.grad, "others")):
+        fin = torch.isfinite(theirs)
+        err = float((mine.double() - theirs)[fin].abs().max() / theirs[fin].abs().max())
+        assert err < 1e-4, (name, err)
+    # per-channel check of the aux-map gradient (each term has its own scale)
+    for ch in range(7):
+        t = o64.grad[:, ch]
+        fin = torch.isfinite(t)
+        if float(t[fin].abs().max()) == 0:
+            assert float(o.grad[:, ch][fin].abs().max()) == 0, ch
+            continue
+        err = float((o.grad[:, ch].double() - t)[fin].abs().max() / t[fin].abs().max())
+        assert err < 1e-4, (ch, err)
