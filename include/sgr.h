@@ -28,12 +28,18 @@
  *
  * The reference forward sizes its scratch buffers from the number of
  * (surfel, tile) keys, which it learns with a blocking device-to-host copy
- * (cuda_rasterizer/rasterizer_impl.cu:282).  Here the forward is split in
- * two calls instead: sgr_forward_geometry computes the key count on the
- * device (and, if asked, copies it to pinned host memory); the caller sizes
- * the key list from it, or passes a capacity it chose earlier, to
- * sgr_forward_raster.  A key count above the capacity is reported through
- * the device status word (SGR_FLAG_KEY_OVERFLOW), never by faulting.
+ * (cuda_rasterizer/rasterizer_impl.cu:282), and writes and sorts every key.
+ * Here the records are put in depth order once and binned into cells of
+ * 8x8 tiles; each tile's list is streamed out of its cell's list by the
+ * blend kernels, so no per-tile list is written.  The forward is split in
+ * two calls: sgr_forward_geometry counts, on the device, the keys (the
+ * reference's num_rendered) and the (record, cell) entries the cell lists
+ * need (and, if asked, copies the status word to pinned host memory); the
+ * caller sizes the cell-list buffer from that count, or passes a capacity
+ * it chose earlier, to sgr_forward_raster.  A count above the capacity is
+ * reported through the device status word (SGR_FLAG_BIN_OVERFLOW), never by
+ * faulting.  The reference's exact per-tile lists and ranges can still be
+ * written out with sgr_tile_lists, for inspection.
  */
 #ifndef SGR_H_INCLUDED
 #define SGR_H_INCLUDED
@@ -45,7 +51,7 @@
 extern "C" {
 #endif
 
-#define SGR_ABI_VERSION 1
+#define SGR_ABI_VERSION 2
 
 /* status codes returned by every entry point */
 #define SGR_OK 0
@@ -57,9 +63,10 @@ extern "C" {
 #define SGR_ERR_CUDA 6               /* a CUDA runtime call failed; see sgr_last_error_message */
 
 /* bits of the device status word (sgr_sizes.off_status), set by kernels */
-#define SGR_FLAG_KEY_OVERFLOW 1u     /* more (surfel, tile) keys than the key capacity */
+#define SGR_FLAG_KEY_OVERFLOW 1u     /* sgr_tile_lists: more (surfel, tile) keys than its capacity */
 #define SGR_FLAG_PREFILTERED 2u      /* prefiltered was set but a surfel failed the near test
                                         (the reference traps here, cuda_rasterizer/auxiliary.h:200-206) */
+#define SGR_FLAG_BIN_OVERFLOW 4u     /* more (record, cell) entries than the cell-list capacity */
 
 #define SGR_VARIANT_PLAIN 0
 #define SGR_VARIANT_PART 1
@@ -119,21 +126,27 @@ typedef struct sgr_batch {
 /* Workspace sizes and the layout of the geometry workspace. */
 typedef struct sgr_sizes {
     size_t geom_bytes;           /* kept from the forward to the backward */
-    size_t list_bytes;           /* kept: the sorted (surfel, tile) list, key_capacity entries */
+    size_t list_bytes;           /* kept: the cell lists, bin_capacity entries */
     size_t fwd_scratch_bytes;    /* forward only */
     size_t bwd_scratch_bytes;    /* backward only */
+    size_t tile_list_scratch_bytes;  /* sgr_tile_lists only */
     /* byte offsets inside the geometry workspace */
-    size_t off_records;          /* float4[R][5] per-view surfel records */
+    size_t off_records;          /* float4[R][6] per-view surfel records */
     size_t off_radii;            /* int32[R] */
     size_t off_tiles_touched;    /* uint32[R] */
     size_t off_depth_order;      /* uint32[R] record ids in (view, depth, id) order */
     size_t off_offsets;          /* uint64[R] inclusive scan of tiles_touched in that order */
-    size_t off_ranges;           /* uint32[V*tiles][2] per-tile [start, end) of the list */
+    size_t off_ranges;           /* uint32[V*tiles][2] per-tile [start, end), written by sgr_tile_lists */
     size_t off_final_T;          /* float[V][3][H][W]: T, M1, M2 */
     size_t off_n_contrib;        /* uint32[V][2][H][W]: last contributor, median contributor */
-    size_t off_status;           /* uint64 key count, uint32 status flags */
+    size_t off_status;           /* uint64 key count, uint32 flags, uint32 pad, uint64 cell-list entries, pad */
+    size_t off_rects;            /* uint32[R][2] tile rectangle of each record in depth order */
+    size_t off_bin_start;        /* uint32[V*cells] start of each cell list */
+    size_t off_bin_count;        /* uint32[V*cells] length of each cell list */
+    size_t off_tile_resume;      /* uint32[V*tiles][2] cell-list entries the forward scanned, tile entries found */
     int32_t tiles_x, tiles_y;
     int32_t tile_key_bits;
+    int32_t cell_tiles;          /* cell edge in tiles */
 } sgr_sizes;
 
 /* Per-view outputs of the forward.  color [V,3,H,W], others [V,7,H,W]
@@ -175,35 +188,44 @@ const char* sgr_status_string(int status);
 /* Message of the last failing CUDA call on this host thread ("" if none). */
 const char* sgr_last_error_message(void);
 
-/* Workspace sizes for a batch and a key capacity (0 when only the geometry
- * phase will run).  Replaces the sizing in required<GeometryState> /
- * required<ImageState> / required<BinningState>,
+/* Workspace sizes for a batch and a cell-list capacity in entries (0 when
+ * only the geometry phase will run).  Replaces the sizing in
+ * required<GeometryState> / required<ImageState> / required<BinningState>,
  * cuda_rasterizer/rasterizer_impl.cu:155-194. */
-int sgr_query_sizes(const sgr_batch* batch, int64_t key_capacity, sgr_sizes* out);
+int sgr_query_sizes(const sgr_batch* batch, int64_t bin_capacity, sgr_sizes* out);
 
 /* Phase 1 of the forward: per-view preprocess (transform, screen bounds,
- * SH colour), depth order, key offsets and the key count.  If
- * num_keys_host is not NULL it must be pinned host memory; the key count
- * is copied there asynchronously on the stream.  fwd_scratch must hold
- * sizes.fwd_scratch_bytes for key_capacity 0 or more. */
+ * SH colour), depth order, the key count and the cell-list entry count.  If
+ * status_host is not NULL it must be pinned host memory of 32 bytes; the
+ * status word is copied there asynchronously on the stream. */
 int sgr_forward_geometry(const sgr_batch* batch, void* geom, void* fwd_scratch, size_t fwd_scratch_bytes,
-                         int64_t* num_keys_host, void* stream);
+                         void* status_host, void* stream);
 
-/* Phase 2: key duplication, stable tile sort, tile ranges and the blend. */
-int sgr_forward_raster(const sgr_batch* batch, void* geom, void* lists, int64_t key_capacity,
+/* Phase 2: the cell lists (bin_capacity entries in `bins`) and the blend
+ * (replaces duplicateWithKeys, the tile sort, identifyTileRanges and
+ * renderCUDA, cuda_rasterizer/rasterizer_impl.cu:288-342). */
+int sgr_forward_raster(const sgr_batch* batch, void* geom, void* bins, int64_t bin_capacity,
                        void* fwd_scratch, size_t fwd_scratch_bytes, const sgr_fwd_outputs* out, void* stream);
 
-/* Backward of both phases. */
-int sgr_backward(const sgr_batch* batch, const void* geom, const void* lists, int64_t key_capacity,
+/* Backward of both phases, from the geometry workspace and the cell lists
+ * of the forward. */
+int sgr_backward(const sgr_batch* batch, const void* geom, const void* bins, int64_t bin_capacity,
                  void* bwd_scratch, size_t bwd_scratch_bytes, const sgr_bwd_inputs* in,
                  const sgr_bwd_outputs* out, void* stream);
+
+/* Writes out, after a forward, the reference's per-tile lists (record ids,
+ * at most key_capacity of them, in the binning buffer's layout) and their
+ * [start, end) ranges at sizes.off_ranges of the geometry workspace.  For
+ * inspection; the blend never reads them. */
+int sgr_tile_lists(const sgr_batch* batch, void* geom, int32_t* lists, int64_t key_capacity, void* scratch,
+                   size_t scratch_bytes, void* stream);
 
 /* ---- phase timing ------------------------------------------------------ */
 
 /* Phases the entry points bracket with CUDA events while profiling is on. */
 #define SGR_PHASE_PREPROCESS 0      /* per-view preprocess */
 #define SGR_PHASE_DEPTH_ORDER 1     /* depth order and key offsets */
-#define SGR_PHASE_BINNING 2         /* (surfel, tile) list construction */
+#define SGR_PHASE_BINNING 2         /* per-(chunk, tile) list index and ranges */
 #define SGR_PHASE_BLEND_FWD 3
 #define SGR_PHASE_BLEND_BWD 4
 #define SGR_PHASE_PREPROCESS_BWD 5
@@ -216,6 +238,10 @@ int sgr_profile_enable(int enable);
  * number of recordings of each phase since the last read (arrays of
  * SGR_NUM_PHASES), and forgets them. */
 int sgr_profile_read(float* ms, int32_t* count);
+/* Number of kernels this library has launched (or recorded into a stream
+ * capture) since it was loaded, over all threads.  Instrumentation with no
+ * counterpart in the reference. */
+uint64_t sgr_kernel_launches(void);
 
 /* Near-plane visibility of P points in one view (present: uint8[P]). */
 int sgr_mark_visible(int32_t P, const float* means3D, const float* viewmatrix, const float* projmatrix,

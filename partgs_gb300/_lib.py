@@ -14,8 +14,11 @@ LIB_PATH = _HERE / "_lib" / "libsgr.so"
 
 SGR_OK = 0
 SGR_ERR_CUDA = 6
+ABI_VERSION = 2
 SGR_FLAG_KEY_OVERFLOW = 1
 SGR_FLAG_PREFILTERED = 2
+SGR_FLAG_BIN_OVERFLOW = 4
+STATUS_BYTES = 32
 SGR_VARIANT_PLAIN = 0
 SGR_VARIANT_PART = 1
 SGR_MAX_SEMANTICS = 16
@@ -49,10 +52,12 @@ class Batch(C.Structure):
 class Sizes(C.Structure):
     _fields_ = [
         ("geom_bytes", C.c_size_t), ("list_bytes", C.c_size_t), ("fwd_scratch_bytes", C.c_size_t),
-        ("bwd_scratch_bytes", C.c_size_t), ("off_records", C.c_size_t), ("off_radii", C.c_size_t),
-        ("off_tiles_touched", C.c_size_t), ("off_depth_order", C.c_size_t), ("off_offsets", C.c_size_t),
-        ("off_ranges", C.c_size_t), ("off_final_T", C.c_size_t), ("off_n_contrib", C.c_size_t),
-        ("off_status", C.c_size_t), ("tiles_x", _i), ("tiles_y", _i), ("tile_key_bits", _i),
+        ("bwd_scratch_bytes", C.c_size_t), ("tile_list_scratch_bytes", C.c_size_t), ("off_records", C.c_size_t),
+        ("off_radii", C.c_size_t), ("off_tiles_touched", C.c_size_t), ("off_depth_order", C.c_size_t),
+        ("off_offsets", C.c_size_t), ("off_ranges", C.c_size_t), ("off_final_T", C.c_size_t),
+        ("off_n_contrib", C.c_size_t), ("off_status", C.c_size_t), ("off_rects", C.c_size_t),
+        ("off_bin_start", C.c_size_t), ("off_bin_count", C.c_size_t), ("off_tile_resume", C.c_size_t),
+        ("tiles_x", _i), ("tiles_y", _i), ("tile_key_bits", _i), ("cell_tiles", _i),
     ]
 
 
@@ -79,6 +84,7 @@ class BindArgs(C.Structure):
 # (name, restype, argtypes) of every exported entry point
 SIGNATURES = {
     "sgr_abi_version": (C.c_int, []),
+    "sgr_kernel_launches": (C.c_uint64, []),
     "sgr_status_string": (C.c_char_p, [C.c_int]),
     "sgr_last_error_message": (C.c_char_p, []),
     "sgr_query_sizes": (C.c_int, [C.POINTER(Batch), C.c_int64, C.POINTER(Sizes)]),
@@ -86,6 +92,7 @@ SIGNATURES = {
     "sgr_forward_raster": (C.c_int, [C.POINTER(Batch), _p, _p, C.c_int64, _p, C.c_size_t, C.POINTER(FwdOutputs), _p]),
     "sgr_backward": (C.c_int, [C.POINTER(Batch), _p, _p, C.c_int64, _p, C.c_size_t, C.POINTER(BwdInputs),
                                C.POINTER(BwdOutputs), _p]),
+    "sgr_tile_lists": (C.c_int, [C.POINTER(Batch), _p, _p, C.c_int64, _p, C.c_size_t, _p]),
     "sgr_mark_visible": (C.c_int, [_i, _p, _p, _p, _p, _p]),
     "sgr_profile_enable": (C.c_int, [C.c_int]),
     "sgr_profile_read": (C.c_int, [C.POINTER(C.c_float), C.POINTER(C.c_int32)]),
@@ -115,7 +122,7 @@ def load(path: str | os.PathLike | None = None):
         fn = getattr(lib, name)
         fn.restype = res
         fn.argtypes = args
-    if lib.sgr_abi_version() != 1:
+    if lib.sgr_abi_version() != ABI_VERSION:
         raise ImportError("libsgr.so ABI version mismatch")
     _lib = lib
     return lib

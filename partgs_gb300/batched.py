@@ -2,11 +2,11 @@
 
 ``MultiViewRasterizer`` rasterises every camera of a set in one call of the
 library: one preprocess over all (surfel, view) records, one depth order,
-one key list over all views' tiles and one blend launch over all tiles of
-all views; the backward sums each surfel's per-view gradients on the device.
-With ``key_capacity`` set, no call synchronises the host, so a whole
-training step built on it can be captured in a CUDA graph
-(``torch.cuda.graph``); the key count and overflow flag of the last forward
+one set of cell lists over all views and one blend launch over all tiles
+of all views; the backward sums each surfel's per-view gradients on the
+device.  With ``bin_capacity`` set, no call synchronises the host, so a
+whole training step built on it can be captured in a CUDA graph
+(``torch.cuda.graph``); the counts and overflow flag of the last forward
 are then read from ``status`` after the step.
 
 Scenes of different sizes are batched the same way: pass ``scene_sizes``
@@ -26,7 +26,7 @@ class _MultiViewFn(torch.autograd.Function):
     def forward(ctx, means3D, opacities, shs, scales, rotations, colors_precomp, semantics, cfg):
         color, others, semantic, radii, state = _r.forward(
             cfg.variant, means3D, opacities, shs, colors_precomp, scales, rotations, None, semantics, cfg.viewset,
-            cfg.bg, cfg.sh_degree, 1.0, False, key_capacity=cfg.key_capacity, tables=cfg.tables,
+            cfg.bg, cfg.sh_degree, 1.0, False, bin_capacity=cfg.bin_capacity, tables=cfg.tables,
             status_host=cfg.status)
         ctx.state = state
         ctx.cfg = cfg
@@ -52,13 +52,13 @@ class MultiViewRasterizer:
     """Rasterises a fixed set of cameras; tables and camera tensors are built
     once, so calls make no host-to-device copies."""
 
-    def __init__(self, cameras, bg, sh_degree=3, variant=L.SGR_VARIANT_PLAIN, key_capacity=None,
+    def __init__(self, cameras, bg, sh_degree=3, variant=L.SGR_VARIANT_PLAIN, bin_capacity=None,
                  scene_sizes=None, scene_views=None, num_surfels=None, device="cuda"):
         dev = torch.device(device)
         self.cameras = list(cameras)
         self.variant = variant
         self.sh_degree = sh_degree
-        self.key_capacity = key_capacity
+        self.bin_capacity = bin_capacity
         self.bg = torch.as_tensor(bg, dtype=torch.float32, device=dev)
         vm = torch.stack([torch.as_tensor(c.world_view_transform, dtype=torch.float32) for c in cameras])
         pm = torch.stack([torch.as_tensor(c.full_proj_transform, dtype=torch.float32) for c in cameras])
@@ -72,19 +72,19 @@ class MultiViewRasterizer:
                                   scene_sizes, scene_views)
         P = num_surfels if num_surfels is not None else (sum(scene_sizes) if scene_sizes else None)
         self.tables = _r._tables(variant, P, self.viewset, dev) if P is not None else None
-        self.status = torch.zeros(16, dtype=torch.uint8).pin_memory()
+        self.status = torch.zeros(L.STATUS_BYTES, dtype=torch.uint8).pin_memory()
         self.last_means2D_grad = None
 
     @property
     def num_views(self):
         return len(self.cameras)
 
-    def set_capacity(self, key_capacity):
-        self.key_capacity = key_capacity
+    def set_capacity(self, bin_capacity):
+        self.bin_capacity = bin_capacity
 
-    def key_count(self):
-        """(key count, flags) of the last forward; valid once the stream has
-        passed that forward (capacity mode only)."""
+    def counts(self):
+        """(key count, flags, cell-list entry count) of the last forward;
+        valid once the stream has passed that forward."""
         return _r.read_status(self.status)
 
     def __call__(self, means3D, opacities, shs=None, scales=None, rotations=None, colors_precomp=None,

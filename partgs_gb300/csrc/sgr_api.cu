@@ -3,6 +3,7 @@
 #include <cub/device/device_radix_sort.cuh>
 #include <cub/device/device_scan.cuh>
 
+#include <atomic>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -14,6 +15,7 @@ namespace sgr {
 namespace {
 
 thread_local std::string g_last_error;
+std::atomic<unsigned long long> g_launches{0};
 
 int cuda_fail(cudaError_t e, const char* what) {
   g_last_error = std::string(what) + ": " + cudaGetErrorString(e);
@@ -41,7 +43,7 @@ int bit_length(unsigned long long n) {
 // Byte layout of the forward scratch.
 struct ScratchLayout {
   size_t depth_keys, depth_vals, depth_keys_sorted, temp_a, temp_a_bytes;
-  size_t bin;          // tile-list construction scratch (sgr_binning.cu)
+  size_t bin;          // list-index scratch (sgr_binning.cu)
   size_t end_a, end;
 };
 
@@ -101,11 +103,10 @@ int scratch_layout(const sgr_batch* b, long long cap, ScratchLayout& L) {
   o = align_up(o + L.temp_a_bytes);
   L.end_a = o;
   (void)cap;
-  int gx, gy, chunk, warps;
+  int gx, gy;
   tile_grid(b, gx, gy);
-  size_t oc, ot, otmp, tb;
-  const size_t bin = binning_scratch_bytes(b->num_records, b->num_views, gx, gy, &chunk, &warps, &oc, &ot, &otmp, &tb);
-  if (bin == 0) return SGR_ERR_UNSUPPORTED;   // tile grid too large for the per-warp counters
+  if (!binning_supported(gx, gy)) return SGR_ERR_UNSUPPORTED;   // tile grid too large for the cell lists
+  const size_t bin = bin_scratch_bytes((long long)R, b->num_views, gx, gy);
   L.bin = o;
   o = align_up(o + bin);
   L.end = o;
@@ -128,6 +129,12 @@ int sizes_impl(const sgr_batch* b, long long cap, sgr_sizes* s) {
   s->off_final_T = o; o = align_up(o + V * 3 * HW * 4);
   s->off_n_contrib = o; o = align_up(o + V * 2 * HW * 4);
   s->off_status = o; o = align_up(o + sizeof(Status));
+  s->off_rects = o; o = align_up(o + R * 8);
+  const size_t cells = V * (size_t)bin_cells_x(gx) * bin_cells_y(gy);
+  s->off_bin_start = o; o = align_up(o + cells * 4);
+  s->off_bin_count = o; o = align_up(o + cells * 4);
+  s->off_tile_resume = o; o = align_up(o + V * gx * gy * 8);
+  s->cell_tiles = kBinTiles;
   s->geom_bytes = o;
   s->list_bytes = align_up((size_t)std::max(0LL, cap) * 4);
   ScratchLayout L;
@@ -135,6 +142,7 @@ int sizes_impl(const sgr_batch* b, long long cap, sgr_sizes* s) {
   if (rc) return rc;
   s->fwd_scratch_bytes = L.end;
   s->bwd_scratch_bytes = align_up(R * kGradF * 4);
+  s->tile_list_scratch_bytes = tile_list_scratch_bytes((long long)R, (int)V, gx, gy);
   s->tiles_x = gx;
   s->tiles_y = gy;
   s->tile_key_bits = tile_key_bits(b);
@@ -154,6 +162,12 @@ GeomView geom_view(const sgr_batch* b, const sgr_sizes& s, void* geom, void* scr
   g.final_T = reinterpret_cast<float*>(gp + s.off_final_T);
   g.n_contrib = reinterpret_cast<uint32_t*>(gp + s.off_n_contrib);
   g.status = reinterpret_cast<Status*>(gp + s.off_status);
+  g.rects = reinterpret_cast<uint2*>(gp + s.off_rects);
+  g.bin_start = reinterpret_cast<uint32_t*>(gp + s.off_bin_start);
+  g.bin_count = reinterpret_cast<uint32_t*>(gp + s.off_bin_count);
+  g.tile_resume = reinterpret_cast<uint2*>(gp + s.off_tile_resume);
+  g.bins = nullptr;
+  g.bin_capacity = 0;
   g.depth_keys = (sp && L) ? reinterpret_cast<unsigned long long*>(sp + L->depth_keys) : nullptr;
   g.depth_vals = (sp && L) ? reinterpret_cast<uint32_t*>(sp + L->depth_vals) : nullptr;
   g.depth_keys_sorted = (sp && L) ? reinterpret_cast<unsigned long long*>(sp + L->depth_keys_sorted) : nullptr;
@@ -162,18 +176,15 @@ GeomView geom_view(const sgr_batch* b, const sgr_sizes& s, void* geom, void* scr
   return g;
 }
 
-__global__ void k_gather_counts(const uint32_t* __restrict__ order, const uint32_t* __restrict__ touched,
-                                unsigned long long* __restrict__ out, long long R) {
-  const long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (j < R) out[j] = touched[order[j]];
-}
-
 int check_cap(long long cap) {
   if (cap < 0 || cap > 0x7fffffffLL) return SGR_ERR_KEY_CAPACITY;
   return SGR_OK;
 }
 
 }  // namespace
+
+void count_launches(int n) { g_launches.fetch_add((unsigned long long)n, std::memory_order_relaxed); }
+
 }  // namespace sgr
 
 using namespace sgr;
@@ -207,7 +218,7 @@ int sgr_query_sizes(const sgr_batch* batch, int64_t key_capacity, sgr_sizes* out
 }
 
 int sgr_forward_geometry(const sgr_batch* batch, void* geom, void* fwd_scratch, size_t fwd_scratch_bytes,
-                         int64_t* num_keys_host, void* stream) {
+                         void* status_host, void* stream) {
   int rc = check_batch(batch);
   if (rc) return rc;
   if (!geom) return SGR_ERR_INVALID_ARGUMENT;
@@ -231,36 +242,36 @@ int sgr_forward_geometry(const sgr_batch* batch, void* geom, void* fwd_scratch, 
     char* sp = static_cast<char*>(fwd_scratch);
     SGR_CUDA(cub::DeviceRadixSort::SortPairs(sp + L.temp_a, tb, g.depth_keys, g.depth_keys_sorted, g.depth_vals,
                                              g.depth_order, (int64_t)R, 0, depth_key_bits(batch), st));
-    k_gather_counts<<<(unsigned)((R + 255) / 256), 256, 0, st>>>(g.depth_order, g.tiles_touched, g.offsets, R);
+    launch_gather_rects(g, R, st);
     SGR_CUDA(cudaGetLastError());
     tb = L.temp_a_bytes;
     SGR_CUDA(cub::DeviceScan::InclusiveSum(sp + L.temp_a, tb, g.offsets, g.offsets, (int64_t)R, st));
     launch_store_key_count(g, R, st);
     SGR_CUDA(cudaGetLastError());
   }
-  if (num_keys_host)
-    SGR_CUDA(cudaMemcpyAsync(num_keys_host, &g.status->num_keys, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+  if (status_host) SGR_CUDA(cudaMemcpyAsync(status_host, g.status, sizeof(Status), cudaMemcpyDeviceToHost, st));
   return SGR_OK;
 }
 
-int sgr_forward_raster(const sgr_batch* batch, void* geom, void* lists, int64_t key_capacity, void* fwd_scratch,
+int sgr_forward_raster(const sgr_batch* batch, void* geom, void* bins, int64_t bin_capacity, void* fwd_scratch,
                        size_t fwd_scratch_bytes, const sgr_fwd_outputs* out, void* stream) {
   int rc = check_batch(batch);
   if (rc) return rc;
-  if ((rc = check_cap(key_capacity))) return rc;
+  if ((rc = check_cap(bin_capacity))) return rc;
   if (!geom || !out || !out->color || !out->others) return SGR_ERR_INVALID_ARGUMENT;
   if (batch->variant == SGR_VARIANT_PART && batch->semantic_channels > 0 && !out->semantic)
     return SGR_ERR_INVALID_ARGUMENT;
-  if (key_capacity > 0 && !lists) return SGR_ERR_INVALID_ARGUMENT;
+  if (bin_capacity > 0 && !bins) return SGR_ERR_INVALID_ARGUMENT;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   sgr_sizes s;
-  if ((rc = sizes_impl(batch, key_capacity, &s))) return rc;
+  if ((rc = sizes_impl(batch, bin_capacity, &s))) return rc;
   ScratchLayout L;
-  if ((rc = scratch_layout(batch, key_capacity, L))) return rc;
+  if ((rc = scratch_layout(batch, bin_capacity, L))) return rc;
   if (fwd_scratch_bytes < L.end || (!fwd_scratch && L.end > 0)) return SGR_ERR_WORKSPACE;
   GeomView g = geom_view(batch, s, geom, fwd_scratch, &L);
+  g.bins = static_cast<const uint32_t*>(bins);
+  g.bin_capacity = bin_capacity;
   char* sp = static_cast<char*>(fwd_scratch);
-  uint32_t* point_list = static_cast<uint32_t*>(lists);
   const int NO = batch->variant == SGR_VARIANT_PLAIN ? 7 : 8;
   const size_t HW = (size_t)batch->height * batch->width;
   if (batch->num_surfels == 0) {
@@ -274,13 +285,13 @@ int sgr_forward_raster(const sgr_batch* batch, void* geom, void* lists, int64_t 
   }
   {
     PhaseScope ph(SGR_PHASE_BINNING, st);
-    rc = launch_binning(*batch, g, point_list, key_capacity, sp + L.bin, st);
-    if (rc == SGR_ERR_CUDA) return cuda_fail(cudaGetLastError(), "tile-list construction");
+    rc = launch_binning(*batch, g, sp + L.bin, st);
+    if (rc == SGR_ERR_CUDA) return cuda_fail(cudaGetLastError(), "cell lists");
     if (rc) return rc;
   }
   {
     PhaseScope ph(SGR_PHASE_BLEND_FWD, st);
-    launch_render_fwd(*batch, g, point_list, *out, st);
+    launch_render_fwd(*batch, g, *out, st);
   }
   SGR_CUDA(cudaGetLastError());
   if (out->radii)
@@ -288,19 +299,22 @@ int sgr_forward_raster(const sgr_batch* batch, void* geom, void* lists, int64_t 
   return SGR_OK;
 }
 
-int sgr_backward(const sgr_batch* batch, const void* geom, const void* lists, int64_t key_capacity, void* bwd_scratch,
+int sgr_backward(const sgr_batch* batch, const void* geom, const void* bins, int64_t bin_capacity, void* bwd_scratch,
                  size_t bwd_scratch_bytes, const sgr_bwd_inputs* in, const sgr_bwd_outputs* out, void* stream) {
   int rc = check_batch(batch);
   if (rc) return rc;
-  if ((rc = check_cap(key_capacity))) return rc;
+  if ((rc = check_cap(bin_capacity))) return rc;
+  if (bin_capacity > 0 && !bins) return SGR_ERR_INVALID_ARGUMENT;
   if (!geom || !in || !out || !in->dL_dcolor || !in->dL_dothers) return SGR_ERR_INVALID_ARGUMENT;
   const int S = batch->variant == SGR_VARIANT_PART ? batch->semantic_channels : 0;
   if (S > 0 && !in->dL_dsemantic) return SGR_ERR_INVALID_ARGUMENT;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   sgr_sizes s;
-  if ((rc = sizes_impl(batch, key_capacity, &s))) return rc;
+  if ((rc = sizes_impl(batch, 0, &s))) return rc;
   if (bwd_scratch_bytes < s.bwd_scratch_bytes || (!bwd_scratch && s.bwd_scratch_bytes > 0)) return SGR_ERR_WORKSPACE;
   GeomView g = geom_view(batch, s, const_cast<void*>(geom), nullptr, nullptr);
+  g.bins = static_cast<const uint32_t*>(bins);
+  g.bin_capacity = bin_capacity;
   float* grads = static_cast<float*>(bwd_scratch);
   const size_t P = (size_t)batch->num_surfels;
   if (out->dL_dsemantics && S > 0) SGR_CUDA(cudaMemsetAsync(out->dL_dsemantics, 0, P * S * 4, st));
@@ -310,7 +324,7 @@ int sgr_backward(const sgr_batch* batch, const void* geom, const void* lists, in
   {
     PhaseScope ph(SGR_PHASE_BLEND_BWD, st);
     SGR_CUDA(cudaMemsetAsync(grads, 0, (size_t)batch->num_records * kGradF * 4, st));
-    launch_render_bwd(*batch, g, static_cast<const uint32_t*>(lists), *in, grads, dsem, st);
+    launch_render_bwd(*batch, g, *in, grads, dsem, st);
   }
   SGR_CUDA(cudaGetLastError());
   {
@@ -320,6 +334,25 @@ int sgr_backward(const sgr_batch* batch, const void* geom, const void* lists, in
   SGR_CUDA(cudaGetLastError());
   return SGR_OK;
 }
+
+int sgr_tile_lists(const sgr_batch* batch, void* geom, int32_t* lists, int64_t key_capacity, void* scratch,
+                   size_t scratch_bytes, void* stream) {
+  int rc = check_batch(batch);
+  if (rc) return rc;
+  if ((rc = check_cap(key_capacity))) return rc;
+  if (!geom || (key_capacity > 0 && !lists)) return SGR_ERR_INVALID_ARGUMENT;
+  sgr_sizes s;
+  if ((rc = sizes_impl(batch, 0, &s))) return rc;
+  if (scratch_bytes < s.tile_list_scratch_bytes || !scratch) return SGR_ERR_WORKSPACE;
+  if (batch->num_records == 0) return SGR_OK;
+  GeomView g = geom_view(batch, s, geom, nullptr, nullptr);
+  rc = launch_tile_lists(*batch, g, reinterpret_cast<uint32_t*>(lists), key_capacity, scratch,
+                         static_cast<cudaStream_t>(stream));
+  if (rc == SGR_ERR_CUDA) return cuda_fail(cudaGetLastError(), "tile lists");
+  return rc;
+}
+
+uint64_t sgr_kernel_launches(void) { return g_launches.load(std::memory_order_relaxed); }
 
 int sgr_profile_enable(int enable) {
   PhaseTimer::get().enable(enable != 0);

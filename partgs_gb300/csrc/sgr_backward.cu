@@ -297,6 +297,7 @@ void launch_preprocess_bwd(const sgr_batch& b, const GeomView& g, const float* g
   if (blocks == 0) return;
   if (b.variant == SGR_VARIANT_PLAIN) k_preprocess_bwd<SGR_VARIANT_PLAIN><<<blocks, threads, 0, st>>>(b, g, grads, out);
   else k_preprocess_bwd<SGR_VARIANT_PART><<<blocks, threads, 0, st>>>(b, g, grads, out);
+  count_launches();
 }
 
 }  // namespace sgr

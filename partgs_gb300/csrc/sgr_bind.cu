@@ -19,6 +19,10 @@
 
 #include "../../include/sgr.h"
 
+namespace sgr {
+void count_launches(int n);   // sgr_api.cu
+}  // namespace sgr
+
 namespace sgrbind {
 
 constexpr float kEps = 1e-8f;
@@ -412,6 +416,7 @@ int sgr_bind_forward(const sgr_bind_args* a, float* xyz, float* log_scaling, flo
   if (n == 0 || a->N == 0) return SGR_OK;
   k_bind_forward<<<(n + 127) / 128, 128, 0, static_cast<cudaStream_t>(stream)>>>(*a, xyz, log_scaling, rotation,
                                                                                   opacity);
+  sgr::count_launches(1);
   return cudaGetLastError() == cudaSuccess ? SGR_OK : SGR_ERR_CUDA;
 }
 
@@ -434,10 +439,13 @@ int sgr_bind_backward(const sgr_bind_args* a, const float* d_xyz, const float* d
   float* dop_face = reinterpret_cast<float*>(static_cast<char*>(scratch) + dv);
   if (cudaMemsetAsync(scratch, 0, sgr_bind_scratch_bytes(a), st) != cudaSuccess) return SGR_ERR_CUDA;
   const int n = a->B * a->F;
-  if (n > 0 && a->N > 0)
+  if (n > 0 && a->N > 0) {
     k_bind_backward_faces<<<(n + 127) / 128, 128, 0, st>>>(*a, d_xyz, d_log_scaling, d_rotation, d_opacity, dvert,
                                                             dop_face);
+    sgr::count_launches(1);
+  }
   k_bind_backward_sq<<<a->B, 256, 0, st>>>(*a, dvert, dop_face, d_sq_s, d_sq_r, d_sq_t, d_sq_eps, d_sq_occ);
+  sgr::count_launches(1);
   return cudaGetLastError() == cudaSuccess ? SGR_OK : SGR_ERR_CUDA;
 }
 

@@ -1,27 +1,40 @@
-// Per-tile surfel lists by a stable counting sort over tiles.
+// Cell lists: the records of each view binned into square cells of
+// kBinTiles x kBinTiles tiles, each cell's list in depth order.
 //
 // The reference emits one 64-bit key (tile << 32 | depth bits) per (surfel,
 // tile) pair in surfel order and radix-sorts them (cuda_rasterizer/
 // rasterizer_impl.cu:70-111, 288-318); a tile's list is then its surfels by
 // (depth bits, index).  Here the records are already in (view, depth bits,
-// index) order (the depth order of the geometry phase), so the same lists
-// come from a stable distribution of that sequence into tiles, with no key
-// array and no sort:
+// index) order after the geometry phase, so a tile's list is the
+// subsequence of that order whose tile rectangle holds the tile, and any
+// depth-ordered superset of it can stand in for it: a blend CTA streams its
+// cell's list and keeps the entries whose rectangle holds its tile
+// (sgr_blend.cu).  A record touches ~4 cells instead of ~60 tiles, so the
+// lists are a small fraction of the reference's keys, and front-to-back
+// termination means a tile reads only a short prefix of its cell's list.
 //
-//  1. the depth-ordered records are cut into chunks of C (inside a view);
-//     each chunk's per-tile counts come from a 2-D difference array of its
-//     records' tile rectangles in shared memory (four updates per record);
-//  2. per tile, an exclusive scan over the chunks gives each chunk's first
-//     slot inside the tile's list, and the per-tile totals are scanned into
-//     the tile ranges;
-//  3. each chunk writes its records: every warp first counts its own slice
-//     of the chunk per tile, the block turns the counts into per-warp bases,
-//     then each warp walks its slice record by record (the lanes cover the
-//     record's tiles, which are distinct) and places the record id at its
-//     tile's next slot.
+// Construction, a stable counting sort over cells with no sort and no keys:
+//  0. (geometry phase) each record's tile rectangle is gathered into depth
+//     order, 8 bytes per record, and the (record, cell) pairs are counted
+//     (k_gather_rects);
+//  1. the depth-ordered records of a view are cut into chunks of kChunk;
+//     each chunk's per-cell counts come from a 2-D difference array of its
+//     records' cell rectangles in shared memory (four updates per record);
+//  2. per cell, an exclusive scan over the view's chunks gives each chunk's
+//     first position in the cell's list and the cell's total; the totals are
+//     scanned into each cell's start in one concatenated array;
+//  3. per chunk, every warp counts its own slice of records per cell, the
+//     block turns the counts into per-warp bases, then each warp walks its
+//     slice record by record (the lanes cover the record's cells, which are
+//     distinct) and writes the entry at its cell's next slot.  Within a
+//     cell, entries come in chunk order, then warp order, then record order:
+//     depth order.
+// Cell-list entries are depth-order positions (the blend reads the
+// rectangle and the record id from them).
 //
-// The result is bit-identical to the sort: within a tile, records appear in
-// chunk order, then warp order, then record order, i.e. depth order.
+// With one-tile cells and record ids as entries, the same kernels write the
+// reference's exact per-tile lists and [start, end) ranges; that form is
+// kept for inspection and tests (sgr_tile_lists).
 #include <cub/device/device_scan.cuh>
 
 #include "sgr_kernels.cuh"
@@ -30,33 +43,33 @@ namespace sgr {
 
 namespace {
 
-constexpr int kRecsPerWarp = 256;
-
-struct BinArgs {
+struct CellArgs {
   const uint32_t* depth_order;       // [R]
-  const uint32_t* tiles_touched;     // [R]
-  const int* radii;                  // [R]
-  const float4* records;             // [R][kRecF4]
+  const uint2* rects;                // [R] packed tile rectangles, depth order
   const sgr_view_desc* views;        // [V]
   const sgr_scene_desc* scenes;
   uint32_t* chunk_offset;            // [V+1] first chunk of each view
-  uint32_t* chunk_counts;            // [chunks][tpv] counts, then bases
-  uint32_t* tile_count;              // [V*tpv]
-  uint32_t* tile_start;              // [V*tpv]
-  uint32_t* point_list;
-  uint2* ranges;
+  uint32_t* chunk_base;              // [chunks][cells per view] counts, then list positions
+  uint32_t* cell_count;              // [V*cells]
+  uint32_t* cell_start;              // [V*cells] exclusive scan of cell_count
+  uint32_t* out;                     // the lists
+  uint2* ranges;                     // [V*cells] [start, end) clamped to the capacity, or null
   Status* status;
-  long long capacity;
-  int V, gx, gy, chunk;              // chunk = records per chunk
-  int warps;                         // warps per chunk-writing CTA (chunk / kRecsPerWarp)
+  long long capacity;                // entries `out` holds
+  unsigned int overflow_flag;        // status flag raised when the lists exceed the capacity
+  int V;
+  int B;                             // cell edge in tiles
+  int cx, cy;                        // cells per view along x and y
+  int warps;                         // warps of the list-writing CTA
+  bool ids;                          // write record ids (else depth-order positions)
 };
 
-__device__ __forceinline__ int view_count(const BinArgs& a, int v) {
+__device__ __forceinline__ int view_count(const CellArgs& a, int v) {
   return a.scenes[a.views[v].scene].surfel_count;
 }
 
-// (view, first record position, end position) of a global chunk; false past the last.
-__device__ __forceinline__ bool chunk_span(const BinArgs& a, int c, int& v, int& p0, int& p1) {
+// (view, first depth-order position, end position) of a global chunk; false past the last.
+__device__ __forceinline__ bool chunk_span(const CellArgs& a, int c, int& v, int& p0, int& p1) {
   if ((uint32_t)c >= a.chunk_offset[a.V]) return false;
   int lo = 0, hi = a.V - 1;
   while (lo < hi) {
@@ -65,36 +78,85 @@ __device__ __forceinline__ bool chunk_span(const BinArgs& a, int c, int& v, int&
   }
   v = lo;
   const int base = a.views[v].record_offset;
-  const int cv = c - (int)a.chunk_offset[v];
-  p0 = base + cv * a.chunk;
-  p1 = min(base + view_count(a, v), p0 + a.chunk);
+  p0 = base + (c - (int)a.chunk_offset[v]) * kChunk;
+  p1 = min(base + view_count(a, v), p0 + kChunk);
   return true;
 }
 
-__global__ void k_chunk_table(BinArgs a) {
+// Cell rectangle [x0, x1) x [y0, y1) of a packed tile rectangle; empty for an empty one.
+__device__ __forceinline__ void cell_rect(uint2 r, int B, int& x0, int& y0, int& x1, int& y1) {
+  unpack_rect(r, x0, y0, x1, y1);
+  if (x0 >= x1 || y0 >= y1) {
+    x0 = y0 = x1 = y1 = 0;
+    return;
+  }
+  x0 /= B;
+  y0 /= B;
+  x1 = (x1 + B - 1) / B;
+  y1 = (y1 + B - 1) / B;
+}
+
+// 0. tile rectangles and key counts in depth order; (record, cell) pair count
+__global__ void __launch_bounds__(256) k_gather_rects(const uint32_t* __restrict__ order,
+                                                      const uint32_t* __restrict__ touched,
+                                                      const float4* __restrict__ records,
+                                                      const int* __restrict__ radii,
+                                                      unsigned long long* __restrict__ counts,
+                                                      uint2* __restrict__ rects, Status* status, long long R,
+                                                      int gx, int gy) {
+  __shared__ unsigned long long s_sum[8];
+  const long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  unsigned int cells = 0;
+  if (j < R) {
+    const uint32_t r = order[j];
+    const uint32_t n = touched[r];
+    counts[j] = n;
+    uint2 out = make_uint2(0u, 0u);
+    if (n != 0) {
+      const float4 r2 = records[(size_t)r * kRecF4 + 2];
+      int x0, y0, x1, y1;
+      tile_rect(r2.y, r2.z, radii[r], gx, gy, x0, y0, x1, y1);
+      out = pack_rect(x0, y0, x1, y1);
+      int cx0, cy0, cx1, cy1;
+      cell_rect(out, kBinTiles, cx0, cy0, cx1, cy1);
+      cells = (unsigned int)((cx1 - cx0) * (cy1 - cy0));
+    }
+    rects[j] = out;
+  }
+  unsigned long long sum = cells;
+#pragma unroll
+  for (int o = 16; o >= 1; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+  if ((threadIdx.x & 31) == 0) s_sum[threadIdx.x >> 5] = sum;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned long long t = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += s_sum[w];
+    if (t) atomicAdd(&status->num_bin_entries, t);
+  }
+}
+
+__global__ void k_chunk_table(CellArgs a) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
   uint32_t acc = 0;
   for (int v = 0; v < a.V; ++v) {
     a.chunk_offset[v] = acc;
-    acc += (uint32_t)((view_count(a, v) + a.chunk - 1) / a.chunk);
+    acc += (uint32_t)((view_count(a, v) + kChunk - 1) / kChunk);
   }
   a.chunk_offset[a.V] = acc;
 }
 
-// 1. per-chunk tile histogram via a 2-D difference array
-__global__ void __launch_bounds__(256) k_chunk_hist(BinArgs a) {
-  extern __shared__ int s_diff[];                  // [(gy + 1) * (gx + 1)]
+// 1. per-chunk cell histogram via a 2-D difference array
+__global__ void __launch_bounds__(256) k_cell_hist(CellArgs a) {
+  extern __shared__ int s_diff[];                  // [(cy + 1) * (cx + 1)]
   int v, p0, p1;
   if (!chunk_span(a, blockIdx.x, v, p0, p1)) return;
-  const int W1 = a.gx + 1, H1 = a.gy + 1;
+  const int W1 = a.cx + 1, H1 = a.cy + 1;
   for (int i = threadIdx.x; i < W1 * H1; i += blockDim.x) s_diff[i] = 0;
   __syncthreads();
   for (int p = p0 + threadIdx.x; p < p1; p += blockDim.x) {
-    const uint32_t r = a.depth_order[p];
-    if (a.tiles_touched[r] == 0) continue;
-    const float4 r2 = a.records[(size_t)r * kRecF4 + 2];
     int x0, y0, x1, y1;
-    tile_rect(r2.y, r2.z, a.radii[r], a.gx, a.gy, x0, y0, x1, y1);
+    cell_rect(a.rects[p], a.B, x0, y0, x1, y1);
+    if (x0 >= x1) continue;
     atomicAdd(&s_diff[y0 * W1 + x0], 1);
     atomicAdd(&s_diff[y0 * W1 + x1], -1);
     atomicAdd(&s_diff[y1 * W1 + x0], -1);
@@ -117,81 +179,84 @@ __global__ void __launch_bounds__(256) k_chunk_hist(BinArgs a) {
     }
   }
   __syncthreads();
-  const int tpv = a.gx * a.gy;
-  uint32_t* out = a.chunk_counts + (size_t)blockIdx.x * tpv;
-  for (int t = threadIdx.x; t < tpv; t += blockDim.x) {
-    const int ty = t / a.gx, tx = t - ty * a.gx;
+  const int ncell = a.cx * a.cy;
+  uint32_t* out = a.chunk_base + (size_t)blockIdx.x * ncell;
+  for (int t = threadIdx.x; t < ncell; t += blockDim.x) {
+    const int ty = t / a.cx, tx = t - ty * a.cx;
     out[t] = (uint32_t)s_diff[ty * W1 + tx];
   }
 }
 
-// 2a. per (view, tile): exclusive scan of the counts over the view's chunks
-__global__ void k_chunk_scan(BinArgs a) {
-  const int tpv = a.gx * a.gy;
+// 2a. per (view, cell): exclusive scan of the counts over the view's chunks
+__global__ void k_cell_scan(CellArgs a) {
+  const int ncell = a.cx * a.cy;
   const long long gt = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (gt >= (long long)a.V * tpv) return;
-  const int v = (int)(gt / tpv), t = (int)(gt - (long long)v * tpv);
+  if (gt >= (long long)a.V * ncell) return;
+  const int v = (int)(gt / ncell), t = (int)(gt - (long long)v * ncell);
   const uint32_t c0 = a.chunk_offset[v], c1 = a.chunk_offset[v + 1];
   uint32_t run = 0;
-  for (uint32_t c = c0; c < c1; ++c) {
-    uint32_t* cell = a.chunk_counts + (size_t)c * tpv + t;
-    const uint32_t n = *cell;
-    *cell = run;
-    run += n;
+  constexpr int kStep = 8;                         // loads in flight per thread
+  for (uint32_t c = c0; c < c1; c += kStep) {
+    uint32_t n[kStep];
+#pragma unroll
+    for (int k = 0; k < kStep; ++k) n[k] = (c + k < c1) ? a.chunk_base[(size_t)(c + k) * ncell + t] : 0u;
+#pragma unroll
+    for (int k = 0; k < kStep; ++k) {
+      if (c + k < c1) a.chunk_base[(size_t)(c + k) * ncell + t] = run;
+      run += n[k];
+    }
   }
-  a.tile_count[gt] = run;
+  a.cell_count[gt] = run;
 }
 
-// 2b. tile ranges from the scanned starts (clamped to the list capacity)
-__global__ void k_tile_ranges_from_counts(BinArgs a) {
-  const long long n = (long long)a.V * a.gx * a.gy;
+// 2b. ranges (when asked for) and the capacity check
+__global__ void k_cell_ranges(CellArgs a) {
+  const long long n = (long long)a.V * a.cx * a.cy;
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n) return;
-  const unsigned long long s = a.tile_start[t], e = s + a.tile_count[t];
+  const unsigned long long s = a.cell_start[t], e = s + a.cell_count[t];
   const unsigned long long cap = (unsigned long long)a.capacity;
-  a.ranges[t] = make_uint2((uint32_t)min(s, cap), (uint32_t)min(e, cap));
-  if (t == n - 1 && e > cap) atomicOr(&a.status->flags, SGR_FLAG_KEY_OVERFLOW);
+  if (a.ranges) a.ranges[t] = make_uint2((uint32_t)min(s, cap), (uint32_t)min(e, cap));
+  if (t == n - 1 && e > cap) atomicOr(&a.status->flags, a.overflow_flag);
 }
 
-// 3. stable scatter of each chunk's records into the tile lists
-__global__ void __launch_bounds__(256) k_chunk_write(BinArgs a) {
-  extern __shared__ uint32_t s_cnt[];              // [warps][tpv]
+// 3. stable scatter of each chunk's records into the cell lists
+__global__ void __launch_bounds__(256) k_cell_write(CellArgs a) {
+  extern __shared__ uint32_t s_cnt[];              // [warps][cells per view]
   int v, p0, p1;
   if (!chunk_span(a, blockIdx.x, v, p0, p1)) return;
-  const int tpv = a.gx * a.gy;
+  const int ncell = a.cx * a.cy;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  uint32_t* cnt = s_cnt + (size_t)warp * tpv;
-  for (int i = threadIdx.x; i < a.warps * tpv; i += blockDim.x) s_cnt[i] = 0;
+  uint32_t* cnt = s_cnt + (size_t)warp * ncell;
+  for (int i = threadIdx.x; i < a.warps * ncell; i += blockDim.x) s_cnt[i] = 0;
   __syncthreads();
-  const int w0 = p0 + warp * kRecsPerWarp, w1 = min(p1, w0 + kRecsPerWarp);
+  const int per_warp = kChunk / a.warps;
+  const int w0 = p0 + warp * per_warp, w1 = min(p1, w0 + per_warp);
 
-  // walks this warp's records in order; for each, the lanes cover its tiles
+  // walks this warp's records in order; for each, the lanes cover its cells
   auto walk = [&](bool place) {
     for (int g = w0; g < w1; g += 32) {
       const int p = g + lane;
-      uint32_t r = 0xffffffffu;
       int x0 = 0, y0 = 0, x1 = 0, y1 = 0;
+      uint32_t e = 0;
       if (p < w1) {
-        r = a.depth_order[p];
-        if (a.tiles_touched[r] != 0) {
-          const float4 r2 = a.records[(size_t)r * kRecF4 + 2];
-          tile_rect(r2.y, r2.z, a.radii[r], a.gx, a.gy, x0, y0, x1, y1);
-        }
+        cell_rect(a.rects[p], a.B, x0, y0, x1, y1);
+        if (place) e = a.ids ? a.depth_order[p] : (uint32_t)p;
       }
       const int m = min(32, w1 - g);
       for (int k = 0; k < m; ++k) {
-        const uint32_t rk = __shfl_sync(0xffffffffu, r, k);
+        const uint32_t ek = __shfl_sync(0xffffffffu, e, k);
         const int ax = __shfl_sync(0xffffffffu, x0, k), ay = __shfl_sync(0xffffffffu, y0, k);
         const int bx = __shfl_sync(0xffffffffu, x1, k), by = __shfl_sync(0xffffffffu, y1, k);
         const int w = bx - ax, n = w * (by - ay);
         for (int q = lane; q < n; q += 32) {
           const int ty = ay + q / w, tx = ax + q - (q / w) * w;
-          const int t = ty * a.gx + tx;
+          const int t = ty * a.cx + tx;
           if (!place) {
             cnt[t] += 1;
           } else {
             const uint32_t pos = cnt[t]++;
-            if ((long long)pos < a.capacity) a.point_list[pos] = rk;
+            if ((long long)pos < a.capacity) a.out[pos] = ek;
           }
         }
         __syncwarp();
@@ -200,13 +265,13 @@ __global__ void __launch_bounds__(256) k_chunk_write(BinArgs a) {
   };
   walk(false);
   __syncthreads();
-  const uint32_t* cbase = a.chunk_counts + (size_t)blockIdx.x * tpv;
-  const uint32_t* tstart = a.tile_start + (size_t)v * tpv;
-  for (int t = threadIdx.x; t < tpv; t += blockDim.x) {
-    uint32_t run = tstart[t] + cbase[t];
+  const uint32_t* cbase = a.chunk_base + (size_t)blockIdx.x * ncell;
+  const uint32_t* cstart = a.cell_start + (size_t)v * ncell;
+  for (int t = threadIdx.x; t < ncell; t += blockDim.x) {
+    uint32_t run = cstart[t] + cbase[t];
     for (int w = 0; w < a.warps; ++w) {
-      const uint32_t n = s_cnt[(size_t)w * tpv + t];
-      s_cnt[(size_t)w * tpv + t] = run;
+      const uint32_t n = s_cnt[(size_t)w * ncell + t];
+      s_cnt[(size_t)w * ncell + t] = run;
       run += n;
     }
   }
@@ -214,83 +279,127 @@ __global__ void __launch_bounds__(256) k_chunk_write(BinArgs a) {
   walk(true);
 }
 
-}  // namespace
+constexpr size_t kMaxDynSmem = 220 * 1024;
+constexpr size_t kAlignB = 256;
+size_t al(size_t x) { return (x + kAlignB - 1) & ~(kAlignB - 1); }
 
-// Layout of the binning scratch for R records, V views and a tpv-tile grid.
-size_t binning_scratch_bytes(long long R, int V, int gx, int gy, int* chunk_out, int* warps_out,
-                             size_t* off_counts, size_t* off_tiles, size_t* off_temp, size_t* temp_bytes) {
-  const int tpv = gx * gy;
-  // per-warp counters of the chunk-writing CTA must fit in shared memory
-  int warps = (int)std::min<long long>(8, (200 * 1024) / (4LL * std::max(1, tpv)));
-  if (warps < 1) return 0;
-  const int chunk = warps * kRecsPerWarp;
-  const long long chunks = (R + chunk - 1) / chunk + V;
-  auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
-  size_t o = 0;
-  const size_t off_table = o;
-  (void)off_table;
-  o = al(o + (size_t)(V + 1) * 4);
-  *off_counts = o;
-  o = al(o + (size_t)chunks * tpv * 4);
-  *off_tiles = o;                       // tile_count then tile_start
-  o = al(o + (size_t)2 * V * tpv * 4);
-  size_t tb = 0;
-  cub::DeviceScan::ExclusiveSum(nullptr, tb, (uint32_t*)nullptr, (uint32_t*)nullptr, (int64_t)V * tpv);
-  *off_temp = o;
-  *temp_bytes = tb;
-  o = al(o + tb);
-  *chunk_out = chunk;
-  *warps_out = warps;
-  return o;
+int writer_warps(int ncell) {
+  const long long fit = (long long)(200 * 1024) / (4LL * std::max(1, ncell));
+  return fit >= 8 ? 8 : fit >= 4 ? 4 : fit >= 2 ? 2 : fit >= 1 ? 1 : 0;
 }
 
-int launch_binning(const sgr_batch& b, const GeomView& g, uint32_t* point_list, long long capacity, void* scratch,
-                   cudaStream_t st) {
-  int chunk, warps;
-  size_t off_counts, off_tiles, off_temp, temp_bytes;
-  const size_t need = binning_scratch_bytes(b.num_records, b.num_views, g.tiles_x, g.tiles_y, &chunk, &warps,
-                                            &off_counts, &off_tiles, &off_temp, &temp_bytes);
-  if (need == 0) return SGR_ERR_UNSUPPORTED;
+// Scratch of one cell-list construction: chunk table, per-chunk bases, and
+// (when the counts and starts are not given) counts, starts, and the scan's
+// temporary storage.
+struct CellScratch {
+  size_t chunk_offset, chunk_base, count, start, temp, temp_bytes, end;
+};
+
+CellScratch cell_scratch(long long R, int V, int ncell, bool own_counts) {
+  CellScratch s;
+  const long long chunks = (R + kChunk - 1) / kChunk + V;
+  const size_t cells = (size_t)V * ncell;
+  size_t o = 0;
+  s.chunk_offset = o; o = al(o + (size_t)(V + 1) * 4);
+  s.chunk_base = o; o = al(o + (size_t)chunks * ncell * 4);
+  s.count = s.start = 0;
+  if (own_counts) {
+    s.count = o; o = al(o + cells * 4);
+    s.start = o; o = al(o + cells * 4);
+  }
+  size_t tb = 0;
+  cub::DeviceScan::ExclusiveSum(nullptr, tb, (uint32_t*)nullptr, (uint32_t*)nullptr, (int64_t)cells);
+  s.temp = o;
+  s.temp_bytes = tb;
+  o = al(o + tb);
+  s.end = o;
+  return s;
+}
+
+int run_cells(const sgr_batch& b, const GeomView& g, int B, bool ids, uint32_t* out, long long capacity,
+              unsigned int overflow_flag, uint32_t* count, uint32_t* start, uint2* ranges, void* scratch,
+              cudaStream_t st) {
+  const int cx = (g.tiles_x + B - 1) / B, cy = (g.tiles_y + B - 1) / B;
+  const int ncell = cx * cy;
+  const size_t hist_smem = (size_t)(cx + 1) * (cy + 1) * 4;
+  const int warps = writer_warps(ncell);
+  if (hist_smem > kMaxDynSmem || warps == 0) return SGR_ERR_UNSUPPORTED;
+  const CellScratch L = cell_scratch(b.num_records, b.num_views, ncell, count == nullptr);
   char* sp = static_cast<char*>(scratch);
-  const int tpv = g.tiles_x * g.tiles_y;
-  BinArgs a;
+  CellArgs a;
   a.depth_order = g.depth_order;
-  a.tiles_touched = g.tiles_touched;
-  a.radii = g.radii;
-  a.records = g.records;
+  a.rects = g.rects;
   a.views = b.views;
   a.scenes = b.scenes;
-  a.chunk_offset = reinterpret_cast<uint32_t*>(sp);
-  a.chunk_counts = reinterpret_cast<uint32_t*>(sp + off_counts);
-  a.tile_count = reinterpret_cast<uint32_t*>(sp + off_tiles);
-  a.tile_start = a.tile_count + (size_t)b.num_views * tpv;
-  a.point_list = point_list;
-  a.ranges = g.ranges;
+  a.chunk_offset = reinterpret_cast<uint32_t*>(sp + L.chunk_offset);
+  a.chunk_base = reinterpret_cast<uint32_t*>(sp + L.chunk_base);
+  a.cell_count = count ? count : reinterpret_cast<uint32_t*>(sp + L.count);
+  a.cell_start = start ? start : reinterpret_cast<uint32_t*>(sp + L.start);
+  a.out = out;
+  a.ranges = ranges;
   a.status = g.status;
   a.capacity = capacity;
+  a.overflow_flag = overflow_flag;
   a.V = b.num_views;
-  a.gx = g.tiles_x;
-  a.gy = g.tiles_y;
-  a.chunk = chunk;
+  a.B = B;
+  a.cx = cx;
+  a.cy = cy;
   a.warps = warps;
-  const long long max_chunks = ((long long)b.num_records + chunk - 1) / chunk + b.num_views;
+  a.ids = ids;
+  const long long chunks = (b.num_records + kChunk - 1) / kChunk + b.num_views;
+  const long long ncells = (long long)b.num_views * ncell;
   k_chunk_table<<<1, 32, 0, st>>>(a);
-  const size_t hist_smem = (size_t)(g.tiles_x + 1) * (g.tiles_y + 1) * 4;
-  const size_t write_smem = (size_t)warps * tpv * 4;
-  if (hist_smem > 220 * 1024) return SGR_ERR_UNSUPPORTED;
+  count_launches();
   // per-function attributes apply to the current device; set them every call
-  if (cudaFuncSetAttribute(k_chunk_hist, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024) != cudaSuccess ||
-      cudaFuncSetAttribute(k_chunk_write, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024) != cudaSuccess)
+  if (cudaFuncSetAttribute(k_cell_hist, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxDynSmem) != cudaSuccess ||
+      cudaFuncSetAttribute(k_cell_write, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxDynSmem) != cudaSuccess)
     return SGR_ERR_CUDA;
-  k_chunk_hist<<<(unsigned)max_chunks, 256, hist_smem, st>>>(a);
-  const long long ntiles = (long long)b.num_views * tpv;
-  k_chunk_scan<<<(unsigned)((ntiles + 255) / 256), 256, 0, st>>>(a);
-  size_t tb = temp_bytes;
-  if (cub::DeviceScan::ExclusiveSum(sp + off_temp, tb, a.tile_count, a.tile_start, (int64_t)ntiles, st) != cudaSuccess)
+  k_cell_hist<<<(unsigned)chunks, 256, hist_smem, st>>>(a);
+  count_launches();
+  k_cell_scan<<<(unsigned)((ncells + 255) / 256), 256, 0, st>>>(a);
+  count_launches();
+  size_t tb = L.temp_bytes;
+  if (cub::DeviceScan::ExclusiveSum(sp + L.temp, tb, a.cell_count, a.cell_start, (int64_t)ncells, st) != cudaSuccess)
     return SGR_ERR_CUDA;
-  k_tile_ranges_from_counts<<<(unsigned)((ntiles + 255) / 256), 256, 0, st>>>(a);
-  k_chunk_write<<<(unsigned)max_chunks, warps * 32, write_smem, st>>>(a);
+  k_cell_ranges<<<(unsigned)((ncells + 255) / 256), 256, 0, st>>>(a);
+  count_launches();
+  k_cell_write<<<(unsigned)chunks, warps * 32, (size_t)warps * ncell * 4, st>>>(a);
+  count_launches();
   return cudaGetLastError() == cudaSuccess ? SGR_OK : SGR_ERR_CUDA;
+}
+
+}  // namespace
+
+int bin_cells_x(int gx) { return (gx + kBinTiles - 1) / kBinTiles; }
+int bin_cells_y(int gy) { return (gy + kBinTiles - 1) / kBinTiles; }
+
+bool binning_supported(int gx, int gy) {
+  const int cx = bin_cells_x(gx), cy = bin_cells_y(gy);
+  return gx < 65536 && gy < 65536 && (size_t)(cx + 1) * (cy + 1) * 4 <= kMaxDynSmem && writer_warps(cx * cy) > 0;
+}
+
+size_t bin_scratch_bytes(long long R, int V, int gx, int gy) {
+  return cell_scratch(R, V, bin_cells_x(gx) * bin_cells_y(gy), false).end;
+}
+
+size_t tile_list_scratch_bytes(long long R, int V, int gx, int gy) {
+  return cell_scratch(R, V, gx * gy, true).end;
+}
+
+void launch_gather_rects(const GeomView& g, long long R, cudaStream_t st) {
+  k_gather_rects<<<(unsigned)((R + 255) / 256), 256, 0, st>>>(g.depth_order, g.tiles_touched, g.records, g.radii,
+                                                               g.offsets, g.rects, g.status, R, g.tiles_x, g.tiles_y);
+  count_launches();
+}
+
+int launch_binning(const sgr_batch& b, const GeomView& g, void* scratch, cudaStream_t st) {
+  return run_cells(b, g, kBinTiles, false, const_cast<uint32_t*>(g.bins), g.bin_capacity, SGR_FLAG_BIN_OVERFLOW,
+                   g.bin_count, g.bin_start, nullptr, scratch, st);
+}
+
+int launch_tile_lists(const sgr_batch& b, const GeomView& g, uint32_t* lists, long long capacity, void* scratch,
+                      cudaStream_t st) {
+  return run_cells(b, g, 1, true, lists, capacity, SGR_FLAG_KEY_OVERFLOW, nullptr, nullptr, g.ranges, scratch, st);
 }
 
 }  // namespace sgr

@@ -4,15 +4,22 @@
 // Both follow the reference's per-pixel recurrences exactly
 // (P0/cr/forward.cu:256-441, P1/cr/forward.cu:265-474,
 //  P0/cr/backward.cu:143-440, P1/cr/backward.cu:143-470).  What differs is
-// which (surfel, pixel) pairs get evaluated.  A CTA owns one 16x16 tile and
-// stages 256 list entries at a time in shared memory; each entry's reach box
-// (sgr_common.cuh) is tested once against the tile's eight 16x2 pixel strips
-// (one strip per warp), and each warp then walks only the entries that can
-// reach its strip, in list order.  Entries that cannot reach a pixel are ones
-// the reference skips at its alpha test, so outputs, contributor counts and
-// median indices are unchanged; list positions are kept for the counts.
-// Per pixel, a fragment whose splat and filter distances both exceed the
-// reach threshold is rejected before the two divisions and the exponential.
+// where the tile's list comes from and which (surfel, pixel) pairs get
+// evaluated.
+//
+// A CTA owns one 16x16 tile.  Its list is streamed from the depth-ordered
+// list of the cell that holds the tile (sgr_binning.cu), 1024 entries at a
+// time: the entries whose tile rectangle holds the tile go, in order, into a
+// ring of record ids in shared memory; their count gives list positions.
+// The forward records how far it scanned; the backward streams the same
+// span back to front.  256 ring entries at a time are staged; each entry's
+// reach box (sgr_common.cuh) is tested once against the tile's eight 16x2
+// pixel strips (one strip per warp), and each warp then walks only the
+// entries that can reach its strip, in list order.  Entries that cannot
+// reach a pixel are ones the reference skips at its alpha test, so outputs,
+// contributor counts and median indices are unchanged.  Per pixel, a
+// fragment whose splat and filter distances both exceed the reach threshold
+// is rejected before the two divisions and the exponential.
 #include "sgr_kernels.cuh"
 
 namespace sgr {
@@ -20,6 +27,9 @@ namespace sgr {
 namespace {
 
 constexpr int kWarps = kBlock / 32;
+constexpr int kRing = 2048;            // ring of streamed list entries: >= kBlock + kChunk, a power of two
+static_assert(kRing >= kBlock + kChunk && (kRing & (kRing - 1)) == 0, "ring size");
+static_assert(kChunk == 4 * kBlock && kWarps * 4 == 32, "one scan lane per (record slot, warp)");
 
 struct Strip {
   float x0, x1;       // pixel-centre x range of the tile
@@ -54,15 +64,77 @@ __device__ __forceinline__ int warp_survivors(const uint8_t* mask, int n, int wa
   return cnt;
 }
 
+// One window [i0, i1) (at most kChunk entries) of a cell list: the entries
+// whose tile rectangle holds tile (tx, ty), `found` of them, in list order.
+// They are written to the ring from slot `tail` on as record ids: all of
+// them in list order, or, when REVERSE, in reverse list order only those
+// whose tile-list position is below `top`, given that the window's entries
+// end at position `pos_end`.  Returns how many were written (the same value
+// in every thread).  Every thread of the CTA calls it; it synchronises the
+// CTA.
+template <bool REVERSE>
+__device__ int stream_window(const GeomView& g, const uint32_t* __restrict__ list, int i0, int i1, uint32_t tx,
+                             uint32_t ty, int pos_end, int top, uint32_t* ring, int tail, int* s_count, int& found) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  bool hit[4];
+  uint32_t pos[4], bal[4];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const int i = i0 + k * kBlock + (int)threadIdx.x;
+    pos[k] = i < i1 ? list[i] : 0u;
+    hit[k] = i < i1 && rect_holds(g.rects[pos[k]], tx, ty);
+    bal[k] = __ballot_sync(0xffffffffu, hit[k]);
+  }
+  if (lane == 0) {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) s_count[k * kWarps + warp] = __popc(bal[k]);
+  }
+  __syncthreads();
+  // exclusive scan over the 32 (slot, warp) groups, which are in list order
+  const int own = s_count[lane];
+  int incl = own;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += y;
+  }
+  const int total = __shfl_sync(0xffffffffu, incl, 31);
+  const int m = REVERSE ? max(0, min(total, top - (pos_end - total))) : total;
+  const uint32_t below = (1u << lane) - 1u;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const int base = __shfl_sync(0xffffffffu, incl - own, k * kWarps + warp);
+    if (hit[k]) {
+      const int rank = base + __popc(bal[k] & below);
+      if (rank < m) {
+        const int slot = REVERSE ? tail + (m - 1 - rank) : tail + rank;
+        ring[slot & (kRing - 1)] = g.depth_order[pos[k]];
+      }
+    }
+  }
+  __syncthreads();
+  found = total;
+  return m;
+}
+
+// The cell list of tile (tx, ty) of view v: its start in g.bins and its
+// length, clipped to the entries the buffer holds.
+__device__ __forceinline__ void cell_list(const GeomView& g, int v, int tx, int ty, const uint32_t*& list, int& len) {
+  const int cx = (g.tiles_x + kBinTiles - 1) / kBinTiles, cy = (g.tiles_y + kBinTiles - 1) / kBinTiles;
+  const size_t cell = (size_t)v * cx * cy + (size_t)(ty / kBinTiles) * cx + (tx / kBinTiles);
+  const long long s = g.bin_start[cell];
+  const long long n = g.bin_count[cell];
+  list = g.bins + s;
+  len = (int)max(0LL, min(n, g.bin_capacity - s));
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------------------
 // forward
 // ---------------------------------------------------------------------------
 template <int VARIANT>
-__global__ void __launch_bounds__(kBlock) k_render_fwd(const sgr_batch b, GeomView g,
-                                                       const uint32_t* __restrict__ point_list,
-                                                       sgr_fwd_outputs out) {
+__global__ void __launch_bounds__(kBlock) k_render_fwd(const sgr_batch b, GeomView g, sgr_fwd_outputs out) {
   const int tiles_per_view = g.tiles_x * g.tiles_y;
   const int tile = blockIdx.x;
   const int v = tile / tiles_per_view;
@@ -84,10 +156,13 @@ __global__ void __launch_bounds__(kBlock) k_render_fwd(const sgr_batch b, GeomVi
   __shared__ uint8_t s_mask[kBlock];
   __shared__ uint8_t s_list[kWarps][kBlock];
   __shared__ float s_sem[(VARIANT == SGR_VARIANT_PART) ? SGR_MAX_SEMANTICS : 1][kBlock];
+  __shared__ uint32_t s_ring[kRing];
+  __shared__ int s_count[32];
 
-  const uint2 range = g.ranges[tile];
-  const int todo_all = (int)(range.y - range.x);
-  const int rounds = (todo_all + kBlock - 1) / kBlock;
+  const uint32_t* list;
+  int len;
+  cell_list(g, v, tx, ty, list, len);
+  int head = 0, tail = 0, scanned = 0, base = 0;
   bool done = !inside;
 
   float T = 1.0f;
@@ -100,12 +175,18 @@ __global__ void __launch_bounds__(kBlock) k_render_fwd(const sgr_batch b, GeomVi
 #pragma unroll
   for (int c = 0; c < SGR_MAX_SEMANTICS; ++c) Sem[c] = 0.f;
 
-  for (int i = 0; i < rounds; ++i) {
+  for (;; base += kBlock, head += kBlock) {
     if (__syncthreads_count(done) == kBlock) break;
-    const int base = i * kBlock;
-    const int n = min(kBlock, todo_all - base);
+    while (tail - head < kBlock && scanned < len) {   // refill the ring (CTA-uniform)
+      int found;
+      tail += stream_window<false>(g, list, scanned, min(scanned + kChunk, len), (uint32_t)tx, (uint32_t)ty, 0, 0,
+                                   s_ring, tail, s_count, found);
+      scanned = min(scanned + kChunk, len);
+    }
+    const int n = min(kBlock, tail - head);
+    if (n <= 0) break;
     if ((int)threadIdx.x < n) {
-      const uint32_t r = point_list[range.x + base + threadIdx.x];
+      const uint32_t r = s_ring[(head + threadIdx.x) & (kRing - 1)];
       const float4* rec = g.records + (size_t)r * kRecF4;
 #pragma unroll
       for (int k = 0; k < kRecF4 - 1; ++k) s_rec[k][threadIdx.x] = rec[k];
@@ -194,6 +275,7 @@ __global__ void __launch_bounds__(kBlock) k_render_fwd(const sgr_batch b, GeomVi
     }
   }
 
+  if (threadIdx.x == 0) g.tile_resume[tile] = make_uint2((uint32_t)scanned, (uint32_t)tail);
   if (inside) {
     const size_t HW = (size_t)H * W;
     const size_t pix = (size_t)py * W + px;
@@ -238,10 +320,8 @@ __global__ void __launch_bounds__(kBlock) k_render_fwd(const sgr_batch b, GeomVi
 // and warp instead of one per value and pixel).
 // ---------------------------------------------------------------------------
 template <int VARIANT>
-__global__ void __launch_bounds__(kBlock) k_render_bwd(const sgr_batch b, GeomView g,
-                                                       const uint32_t* __restrict__ point_list,
-                                                       const sgr_bwd_inputs in, float* __restrict__ grads,
-                                                       float* __restrict__ dL_dsemantics) {
+__global__ void __launch_bounds__(kBlock) k_render_bwd(const sgr_batch b, GeomView g, const sgr_bwd_inputs in,
+                                                       float* __restrict__ grads, float* __restrict__ dL_dsemantics) {
   const int tiles_per_view = g.tiles_x * g.tiles_y;
   const int tile = blockIdx.x;
   const int v = tile / tiles_per_view;
@@ -265,8 +345,9 @@ __global__ void __launch_bounds__(kBlock) k_render_bwd(const sgr_batch b, GeomVi
   __shared__ uint8_t s_list[kWarps][kBlock];
   __shared__ float s_sem[(VARIANT == SGR_VARIANT_PART) ? SGR_MAX_SEMANTICS : 1][kBlock];
   __shared__ int s_max[kWarps];
+  __shared__ uint32_t s_ring[kRing];
+  __shared__ int s_count[32];
 
-  const uint2 range = g.ranges[tile];
   const size_t HW = (size_t)H * W;
   const size_t pix = inside ? (size_t)py * W + px : 0;
   const float* fT = g.final_T + (size_t)v * 3 * HW;
@@ -321,11 +402,30 @@ __global__ void __launch_bounds__(kBlock) k_render_bwd(const sgr_batch b, GeomVi
 #pragma unroll
   for (int w = 0; w < kWarps; ++w) block_max = max(block_max, s_max[w]);
 
-  for (int hi = min(block_max, (int)(range.y - range.x)); hi > 0; hi -= kBlock) {
+  // positions [0, block_max) of the list, streamed back to front over the
+  // span of the cell list the forward scanned
+  const uint2 resume = g.tile_resume[tile];
+  const uint32_t* list;
+  int len;
+  cell_list(g, v, tx, ty, list, len);
+  int scan_end = min((int)resume.x, len);          // cell-list entries left to stream
+  int pos_end = (int)resume.y;                     // tile-list position after them
+  const int top = min(block_max, pos_end);
+  int head = 0, tail = 0;
+  for (int hi = top; hi > 0; hi -= kBlock, head += kBlock) {
+    while (tail - head < kBlock && scan_end > 0) {   // refill the ring (CTA-uniform)
+      const int i0 = max(0, scan_end - kChunk);
+      int found;
+      tail += stream_window<true>(g, list, i0, scan_end, (uint32_t)tx, (uint32_t)ty, pos_end, top, s_ring, tail,
+                                  s_count, found);
+      pos_end -= found;
+      scan_end = i0;
+    }
     const int n = min(kBlock, hi);
+    if (tail - head < n) break;                    // index inconsistent with the rectangles: stop
     __syncthreads();
     if ((int)threadIdx.x < n) {
-      const uint32_t r = point_list[range.x + hi - 1 - threadIdx.x];
+      const uint32_t r = s_ring[(head + threadIdx.x) & (kRing - 1)];
       s_id[threadIdx.x] = r;
       const float4* rec = g.records + (size_t)r * kRecF4;
 #pragma unroll
@@ -470,22 +570,23 @@ __global__ void __launch_bounds__(kBlock) k_render_bwd(const sgr_batch b, GeomVi
   }
 }
 
-void launch_render_fwd(const sgr_batch& b, const GeomView& g, const uint32_t* point_list,
-                       const sgr_fwd_outputs& out, cudaStream_t st) {
+void launch_render_fwd(const sgr_batch& b, const GeomView& g, const sgr_fwd_outputs& out, cudaStream_t st) {
   const unsigned blocks = (unsigned)(g.tiles_x * g.tiles_y) * (unsigned)b.num_views;
   if (blocks == 0) return;
-  if (b.variant == SGR_VARIANT_PLAIN) k_render_fwd<SGR_VARIANT_PLAIN><<<blocks, kBlock, 0, st>>>(b, g, point_list, out);
-  else k_render_fwd<SGR_VARIANT_PART><<<blocks, kBlock, 0, st>>>(b, g, point_list, out);
+  if (b.variant == SGR_VARIANT_PLAIN) k_render_fwd<SGR_VARIANT_PLAIN><<<blocks, kBlock, 0, st>>>(b, g, out);
+  else k_render_fwd<SGR_VARIANT_PART><<<blocks, kBlock, 0, st>>>(b, g, out);
+  count_launches();
 }
 
-void launch_render_bwd(const sgr_batch& b, const GeomView& g, const uint32_t* point_list, const sgr_bwd_inputs& in,
-                       float* grads, float* dL_dsemantics, cudaStream_t st) {
+void launch_render_bwd(const sgr_batch& b, const GeomView& g, const sgr_bwd_inputs& in, float* grads,
+                       float* dL_dsemantics, cudaStream_t st) {
   const unsigned blocks = (unsigned)(g.tiles_x * g.tiles_y) * (unsigned)b.num_views;
   if (blocks == 0) return;
   if (b.variant == SGR_VARIANT_PLAIN)
-    k_render_bwd<SGR_VARIANT_PLAIN><<<blocks, kBlock, 0, st>>>(b, g, point_list, in, grads, dL_dsemantics);
+    k_render_bwd<SGR_VARIANT_PLAIN><<<blocks, kBlock, 0, st>>>(b, g, in, grads, dL_dsemantics);
   else
-    k_render_bwd<SGR_VARIANT_PART><<<blocks, kBlock, 0, st>>>(b, g, point_list, in, grads, dL_dsemantics);
+    k_render_bwd<SGR_VARIANT_PART><<<blocks, kBlock, 0, st>>>(b, g, in, grads, dL_dsemantics);
+  count_launches();
 }
 
 }  // namespace sgr

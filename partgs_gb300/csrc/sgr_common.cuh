@@ -37,6 +37,14 @@ constexpr int kBlock = kTile * kTile;
 constexpr int kRecF4 = 6;          // float4 per record
 constexpr int kGradF = 20;         // floats per gradient record
 constexpr int kGradUsed = 18;
+// Records per chunk of the depth order, and list entries per streaming window
+// of a blend CTA (four per thread), sgr_binning.cu / sgr_blend.cu.
+constexpr int kChunk = 4 * kBlock;
+// Edge, in tiles, of the square cells records are binned into (sgr_binning.cu).
+constexpr int kBinTiles = 8;
+
+// Host-side count of this library's kernel launches (sgr_kernel_launches).
+void count_launches(int n = 1);
 
 // P0/cr/auxiliary.h:37-40 (float) and P1/cr/auxiliary.h:20-36 (double macros)
 constexpr float kNearP0 = 0.2f;
@@ -145,6 +153,23 @@ __device__ __forceinline__ void tile_rect(float px, float py, int radius, int gx
   y1 = min(gy, max(0, (int)((py + radius + kTile - 1) / kTile)));
 }
 
+// A tile rectangle [x0, x1) x [y0, y1) in 8 bytes: (x0 | y0 << 16, x1 | y1 << 16).
+__device__ __forceinline__ uint2 pack_rect(int x0, int y0, int x1, int y1) {
+  return make_uint2((uint32_t)x0 | ((uint32_t)y0 << 16), (uint32_t)x1 | ((uint32_t)y1 << 16));
+}
+
+__device__ __forceinline__ void unpack_rect(uint2 r, int& x0, int& y0, int& x1, int& y1) {
+  x0 = (int)(r.x & 0xffffu);
+  y0 = (int)(r.x >> 16);
+  x1 = (int)(r.y & 0xffffu);
+  y1 = (int)(r.y >> 16);
+}
+
+// True when packed rectangle r holds tile (tx, ty).
+__device__ __forceinline__ bool rect_holds(uint2 r, uint32_t tx, uint32_t ty) {
+  return tx - (r.x & 0xffffu) < (r.y & 0xffffu) - (r.x & 0xffffu) && ty - (r.x >> 16) < (r.y >> 16) - (r.x >> 16);
+}
+
 // Scene of a surfel / view of a record: binary search over the tables.
 __device__ __forceinline__ int find_scene(const sgr_scene_desc* scenes, int n, int surfel) {
   int lo = 0, hi = n - 1;
@@ -155,10 +180,13 @@ __device__ __forceinline__ int find_scene(const sgr_scene_desc* scenes, int n, i
   return lo;
 }
 
+// Device status word (sgr_sizes.off_status).
 struct Status {
-  unsigned long long num_keys;
-  unsigned int flags;
+  unsigned long long num_keys;          // (surfel, tile) pairs, the reference's num_rendered
+  unsigned int flags;                   // SGR_FLAG_*
   unsigned int pad;
+  unsigned long long num_bin_entries;   // (record, cell) pairs: the entries of the cell lists
+  unsigned long long pad2;
 };
 
 }  // namespace sgr

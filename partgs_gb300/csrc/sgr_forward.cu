@@ -187,10 +187,12 @@ void launch_preprocess(const sgr_batch& b, const GeomView& g, cudaStream_t st) {
   if (blocks == 0) return;
   if (b.variant == SGR_VARIANT_PLAIN) k_preprocess<SGR_VARIANT_PLAIN><<<blocks, threads, 0, st>>>(b, g);
   else k_preprocess<SGR_VARIANT_PART><<<blocks, threads, 0, st>>>(b, g);
+  count_launches();
 }
 
 void launch_store_key_count(const GeomView& g, long long R, cudaStream_t st) {
   k_store_key_count<<<1, 32, 0, st>>>(g, R);
+  count_launches();
 }
 
 void launch_mark_visible(int P, const float* means3D, const float* viewmatrix, uint8_t* present, cudaStream_t st) {
@@ -198,6 +200,7 @@ void launch_mark_visible(int P, const float* means3D, const float* viewmatrix, u
   const int blocks = (P + threads - 1) / threads;
   if (blocks == 0) return;
   k_mark_visible<<<blocks, threads, 0, st>>>(P, means3D, viewmatrix, present);
+  count_launches();
 }
 
 }  // namespace sgr

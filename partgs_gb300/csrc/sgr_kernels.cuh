@@ -18,7 +18,13 @@ struct GeomView {
   unsigned long long* depth_keys_sorted; // [R] forward scratch
   uint32_t* depth_order;                 // [R] record ids in (view, depth, id) order
   unsigned long long* offsets;           // [R] inclusive scan of tiles_touched in that order
-  uint2* ranges;                         // [V*tiles]
+  uint2* ranges;                         // [V*tiles] [start, end) of the written-out tile lists
+  uint2* rects;                          // [R] packed tile rectangles in depth order
+  uint32_t* bin_start;                   // [V*cells] start of each cell list in `bins`
+  uint32_t* bin_count;                   // [V*cells] length of each cell list
+  uint2* tile_resume;                    // [V*tiles] (cell-list entries the forward scanned, tile entries found)
+  const uint32_t* bins;                  // cell lists: depth-order positions
+  long long bin_capacity;                // entries `bins` holds
   float* final_T;                        // [V][3][H][W]
   uint32_t* n_contrib;                   // [V][2][H][W]
   Status* status;
@@ -174,18 +180,22 @@ __device__ __forceinline__ float warp_transpose_sum(float (&v)[32], int lane) {
 
 void launch_preprocess(const sgr_batch& b, const GeomView& g, cudaStream_t st);
 void launch_store_key_count(const GeomView& g, long long R, cudaStream_t st);
-// Tile-list construction (sgr_binning.cu).  binning_scratch_bytes returns 0
-// when the tile grid is too large for it.
-size_t binning_scratch_bytes(long long R, int V, int gx, int gy, int* chunk_out, int* warps_out,
-                             size_t* off_counts, size_t* off_tiles, size_t* off_temp, size_t* temp_bytes);
-int launch_binning(const sgr_batch& b, const GeomView& g, uint32_t* point_list, long long capacity, void* scratch,
-                   cudaStream_t st);
-void launch_render_fwd(const sgr_batch& b, const GeomView& g, const uint32_t* point_list,
-                       const sgr_fwd_outputs& out, cudaStream_t st);
+// Cell lists (sgr_binning.cu).  binning_supported is false for tile grids
+// whose cell difference array does not fit in shared memory.
+int bin_cells_x(int gx);
+int bin_cells_y(int gy);
+bool binning_supported(int gx, int gy);
+size_t bin_scratch_bytes(long long R, int V, int gx, int gy);
+size_t tile_list_scratch_bytes(long long R, int V, int gx, int gy);
+void launch_gather_rects(const GeomView& g, long long R, cudaStream_t st);
+int launch_binning(const sgr_batch& b, const GeomView& g, void* scratch, cudaStream_t st);
+int launch_tile_lists(const sgr_batch& b, const GeomView& g, uint32_t* lists, long long capacity, void* scratch,
+                      cudaStream_t st);
+void launch_render_fwd(const sgr_batch& b, const GeomView& g, const sgr_fwd_outputs& out, cudaStream_t st);
 void launch_mark_visible(int P, const float* means3D, const float* viewmatrix, uint8_t* present, cudaStream_t st);
 
-void launch_render_bwd(const sgr_batch& b, const GeomView& g, const uint32_t* point_list, const sgr_bwd_inputs& in,
-                       float* grads, float* dL_dsemantics, cudaStream_t st);
+void launch_render_bwd(const sgr_batch& b, const GeomView& g, const sgr_bwd_inputs& in, float* grads,
+                       float* dL_dsemantics, cudaStream_t st);
 void launch_preprocess_bwd(const sgr_batch& b, const GeomView& g, const float* grads, const sgr_bwd_outputs& out,
                            cudaStream_t st);
 

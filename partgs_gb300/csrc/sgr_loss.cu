@@ -22,6 +22,10 @@
 
 #include "../../include/sgr.h"
 
+namespace sgr {
+void count_launches(int n);   // sgr_api.cu
+}  // namespace sgr
+
 namespace sgrloss {
 
 constexpr int kR = 5;                 // window radius
@@ -384,6 +388,7 @@ int sgr_loss_forward_backward(const sgr_loss_args* a, float* loss, float* dL_dco
   const dim3 grid_g((a->W + kGX - 1) / kGX, (a->H + kGY - 1) / kGY, a->V);
   k_geom<<<grid_g, 256, 0, st>>>(*a, (float)(a->lambda_normal / n1), (float)(a->lambda_dist / n1), dL_dothers, acc);
   k_finalize<<<1, 1, 0, st>>>(*a, acc, loss);
+  sgr::count_launches(4);
   return cudaGetLastError() == cudaSuccess ? SGR_OK : SGR_ERR_CUDA;
 }
 

@@ -61,7 +61,6 @@ class _RasterizeGaussians(torch.autograd.Function):
             raise
         ctx.raster_settings = rs
         ctx.state = state
-        ctx.num_rendered = state.key_capacity
         ctx.shapes = (means3D.shape[0], None if sh is None else tuple(sh.shape))
         ctx.save_for_backward(colors_precomp, means3D, scales, rotations, cov3Ds_precomp, radii, sh)
         return color[0], radii, others[0]

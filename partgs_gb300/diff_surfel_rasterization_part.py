@@ -52,7 +52,6 @@ class _RasterizeGaussians(torch.autograd.Function):
             raise
         ctx.raster_settings = rs
         ctx.state = state
-        ctx.num_rendered = state.key_capacity
         ctx.P = means3D.shape[0]
         ctx.save_for_backward(colors_precomp, semantics, means3D, scales, rotations, cov3Ds_precomp, radii, sh)
         return color[0], semantic[0], radii, others[0]

@@ -44,7 +44,7 @@ def _f32(t: torch.Tensor | None, align16: bool = False) -> torch.Tensor | None:
     return t
 
 
-def _pinned(device, nbytes=16):
+def _pinned(device, nbytes=L.STATUS_BYTES):
     key = (device, nbytes)
     buf = _PINNED.get(key)
     if buf is None:
@@ -73,8 +73,8 @@ class RasterState:
     batch: L.Batch
     keep: list
     geom: torch.Tensor
-    lists: torch.Tensor
-    key_capacity: int
+    bins: torch.Tensor            # cell lists
+    bin_capacity: int             # entries they hold
     sizes: L.Sizes
     num_surfels: int
     num_records: int
@@ -170,17 +170,18 @@ def make_batch(variant, means3D, opacities, shs, colors_precomp, scales, rotatio
 
 
 def forward(variant, means3D, opacities, shs, colors_precomp, scales, rotations, transmat_precomp, semantics,
-            vs: ViewSet, bg, sh_degree=0, scale_modifier=1.0, prefiltered=False, key_capacity=None, tables=None,
+            vs: ViewSet, bg, sh_degree=0, scale_modifier=1.0, prefiltered=False, bin_capacity=None, tables=None,
             status_host=None):
     """Rasterises every view of ``vs``.  Returns (color [V,3,H,W], others
     [V,7|8,H,W], semantic [V,S,H,W] or None, radii [R] int32, state).
 
-    Without ``key_capacity`` the key count is read back (one host
-    synchronisation, as the reference does) and the list sized exactly.
-    With it nothing synchronises: the list holds ``key_capacity`` keys, and
-    the device status word (key count, overflow flag) is copied into the
-    pinned ``status_host`` tensor (16 bytes) for the caller to inspect once
-    the stream has reached it."""
+    Without ``bin_capacity`` the cell-list entry count is read back (one
+    host synchronisation, where the reference reads its key count back,
+    cuda_rasterizer/rasterizer_impl.cu:282) and the cell lists are sized
+    exactly.  With it nothing synchronises: the lists hold ``bin_capacity``
+    entries, and the device status word (key count, flags, entry count) is
+    copied into the pinned ``status_host`` tensor (32 bytes) for the caller
+    to inspect once the stream has reached it."""
     lib = L.load()
     b, keep, t = make_batch(variant, means3D, opacities, shs, colors_precomp, scales, rotations, transmat_precomp,
                             semantics, vs, bg, sh_degree, scale_modifier, prefiltered, tables)
@@ -188,31 +189,25 @@ def forward(variant, means3D, opacities, shs, colors_precomp, scales, rotations,
     s0 = L.Sizes()
     L.check(lib.sgr_query_sizes(C.byref(b), 0, C.byref(s0)), "sgr_query_sizes")
     geom = torch.empty(max(1, s0.geom_bytes), dtype=torch.uint8, device=device)
-    scratch0 = torch.empty(max(1, s0.fwd_scratch_bytes), dtype=torch.uint8, device=device)
+    scratch = torch.empty(max(1, s0.fwd_scratch_bytes), dtype=torch.uint8, device=device)
     st = _stream()
-    L.check(lib.sgr_forward_geometry(C.byref(b), geom.data_ptr(), scratch0.data_ptr(), s0.fwd_scratch_bytes, None, st),
-            "sgr_forward_geometry")
-    if key_capacity is None:
-        # the key count sizes the list, as the reference's blocking copy of
-        # num_rendered does (cuda_rasterizer/rasterizer_impl.cu:282)
+    L.check(lib.sgr_forward_geometry(C.byref(b), geom.data_ptr(), scratch.data_ptr(), s0.fwd_scratch_bytes, None,
+                                     st), "sgr_forward_geometry")
+    if bin_capacity is None:
         pin = _pinned(device)
-        pin.copy_(geom[s0.off_status:s0.off_status + 16], non_blocking=True)
+        pin.copy_(geom[s0.off_status:s0.off_status + L.STATUS_BYTES], non_blocking=True)
         ev = torch.cuda.Event()
         ev.record()
         ev.synchronize()
-        K = int(pin[:8].view(torch.int64)[0])
-        flags = int(pin[8:12].view(torch.int32)[0])
+        _, flags, nbins = read_status(pin)
         if flags & L.SGR_FLAG_PREFILTERED:
             raise RuntimeError("Point is filtered although prefiltered is set. This shouldn't happen!")
-        if K >= 2 ** 31:
-            raise RuntimeError(f"{K} (surfel, tile) keys exceed the 2^31 - 1 list limit")
+        if nbins >= 2 ** 31:
+            raise RuntimeError(f"{nbins} (surfel, cell) entries exceed the 2^31 - 1 list limit")
+        cap = nbins
     else:
-        K = int(key_capacity)
-    del scratch0
-    sK = L.Sizes()
-    L.check(lib.sgr_query_sizes(C.byref(b), K, C.byref(sK)), "sgr_query_sizes")
-    lists = torch.empty(max(1, K), dtype=torch.int32, device=device)
-    scratch = torch.empty(max(1, sK.fwd_scratch_bytes), dtype=torch.uint8, device=device)
+        cap = int(bin_capacity)
+    bins = torch.empty(max(1, cap), dtype=torch.int32, device=device)
     V, H, W = b.num_views, b.height, b.width
     NO = 7 if variant == L.SGR_VARIANT_PLAIN else 8
     color = torch.empty((V, 3, H, W), dtype=torch.float32, device=device)
@@ -222,18 +217,19 @@ def forward(variant, means3D, opacities, shs, colors_precomp, scales, rotations,
         semantic = torch.empty((V, b.semantic_channels, H, W), dtype=torch.float32, device=device)
     radii = torch.zeros(b.num_records, dtype=torch.int32, device=device)
     out = L.FwdOutputs(color.data_ptr(), others.data_ptr(), _ptr(semantic), radii.data_ptr())
-    L.check(lib.sgr_forward_raster(C.byref(b), geom.data_ptr(), lists.data_ptr(), K, scratch.data_ptr(),
-                                   sK.fwd_scratch_bytes, C.byref(out), st), "sgr_forward_raster")
+    L.check(lib.sgr_forward_raster(C.byref(b), geom.data_ptr(), bins.data_ptr(), cap, scratch.data_ptr(),
+                                   s0.fwd_scratch_bytes, C.byref(out), st), "sgr_forward_raster")
     if status_host is not None:
-        status_host.copy_(geom[sK.off_status:sK.off_status + 16], non_blocking=True)
-    state = RasterState(variant, b, keep, geom, lists, K, sK, b.num_surfels, b.num_records, V, b.sh_coeffs,
+        status_host.copy_(geom[s0.off_status:s0.off_status + L.STATUS_BYTES], non_blocking=True)
+    state = RasterState(variant, b, keep, geom, bins, cap, s0, b.num_surfels, b.num_records, V, b.sh_coeffs,
                         b.semantic_channels)
     return color, others, semantic, radii, state
 
 
 def read_status(status_host: torch.Tensor):
-    """(key count, flags) from a status copy made by ``forward``."""
-    return int(status_host[:8].view(torch.int64)[0]), int(status_host[8:12].view(torch.int32)[0])
+    """(key count, flags, cell-list entry count) from a status copy."""
+    w = status_host[:L.STATUS_BYTES].view(torch.int64)
+    return int(w[0]), int(status_host[8:12].view(torch.int32)[0]), int(w[2])
 
 
 def backward(state: RasterState, dL_dcolor, dL_dothers, dL_dsemantic=None, need=None):
@@ -257,7 +253,7 @@ def backward(state: RasterState, dL_dcolor, dL_dothers, dL_dsemantic=None, need=
     out = L.BwdOutputs(*(_ptr(g[k]) for k in ("dL_dmeans2D", "dL_dcolors", "dL_dopacity", "dL_dmeans3D",
                                                "dL_dtransmat", "dL_dsh", "dL_dscales", "dL_drotations",
                                                "dL_dsemantics")))
-    L.check(lib.sgr_backward(C.byref(b), state.geom.data_ptr(), state.lists.data_ptr(), state.key_capacity,
+    L.check(lib.sgr_backward(C.byref(b), state.geom.data_ptr(), state.bins.data_ptr(), state.bin_capacity,
                              scratch.data_ptr(), state.sizes.bwd_scratch_bytes, C.byref(inp), C.byref(out), st),
             "sgr_backward")
     return g
@@ -277,26 +273,46 @@ def mark_visible(positions: torch.Tensor, viewmatrix: torch.Tensor, projmatrix: 
     return present
 
 
+def tile_lists(state: RasterState):
+    """The reference's per-tile lists of the last forward, written out from
+    the depth order: (ranges [V*tiles, 2], point_list [K] record ids, K).
+    Synchronises the host (the key count sizes the list)."""
+    lib = L.load()
+    s = state.sizes
+    device = state.geom.device
+    pin = _pinned(device)
+    pin.copy_(state.geom[s.off_status:s.off_status + L.STATUS_BYTES], non_blocking=True)
+    torch.cuda.current_stream().synchronize()
+    K = read_status(pin)[0]
+    lists = torch.empty(max(1, K), dtype=torch.int32, device=device)
+    scratch = torch.empty(max(1, s.tile_list_scratch_bytes), dtype=torch.uint8, device=device)
+    L.check(lib.sgr_tile_lists(C.byref(state.batch), state.geom.data_ptr(), lists.data_ptr(), K, scratch.data_ptr(),
+                               s.tile_list_scratch_bytes, _stream()), "sgr_tile_lists")
+    ntiles = state.num_views * s.tiles_x * s.tiles_y
+    ranges = state.geom[s.off_ranges:s.off_ranges + ntiles * 8].view(torch.int32).reshape(ntiles, 2).clone()
+    return ranges, lists[:K].clone(), K
+
+
 def debug_state(state: RasterState) -> dict:
     """Copies of the internal per-view state (for tests and inspection)."""
     s = state.sizes
     g = state.geom
     R, V = state.num_records, state.num_views
     H, W = state.batch.height, state.batch.width
-    ntiles = V * s.tiles_x * s.tiles_y
 
     def sl(off, n, dtype):
         nbytes = n * torch.tensor([], dtype=dtype).element_size()
         return g[off:off + nbytes].view(dtype).clone()
 
+    ranges, point_list, K = tile_lists(state)
     return dict(
-        records=sl(s.off_records, R * 20, torch.float32).reshape(R, 20),
+        records=sl(s.off_records, R * 24, torch.float32).reshape(R, 24),
         radii=sl(s.off_radii, R, torch.int32),
         tiles_touched=sl(s.off_tiles_touched, R, torch.int32),
         depth_order=sl(s.off_depth_order, R, torch.int32),
-        ranges=sl(s.off_ranges, ntiles * 2, torch.int32).reshape(ntiles, 2),
+        ranges=ranges,
+        point_list=point_list,
+        num_keys=K,
         final_T=sl(s.off_final_T, V * 3 * H * W, torch.float32).reshape(V, 3, H, W),
         n_contrib=sl(s.off_n_contrib, V * 2 * H * W, torch.int32).reshape(V, 2, H, W),
-        point_list=state.lists[:state.key_capacity].clone(),
-        num_keys=state.key_capacity,
     )

@@ -19,6 +19,7 @@ import math
 import torch
 import torch.nn.functional as F
 
+from . import _lib
 from .batched import MultiViewRasterizer
 
 
@@ -84,7 +85,7 @@ class DepthNormals:
 class SurfelTrainer:
     """Surfel parameters, the batched loss and Adam."""
 
-    def __init__(self, scene, cameras, key_capacity=None, lambda_dssim=0.2, lambda_dist=1000.0,
+    def __init__(self, scene, cameras, bin_capacity=None, lambda_dssim=0.2, lambda_dist=1000.0,
                  lambda_normal=0.05, depth_ratio=1.0, bg=(0.0, 0.0, 0.0), device="cuda", extent=3.0,
                  fused_loss=True):
         dev = torch.device(device)
@@ -96,7 +97,7 @@ class SurfelTrainer:
         self.features_dc = scene.shs[:, :1].detach().clone().to(dev).requires_grad_(True)
         self.features_rest = scene.shs[:, 1:].detach().clone().to(dev).requires_grad_(True)
         self.sh_degree = scene.sh_degree
-        self.raster = MultiViewRasterizer(cameras, bg, scene.sh_degree, key_capacity=key_capacity,
+        self.raster = MultiViewRasterizer(cameras, bg, scene.sh_degree, bin_capacity=bin_capacity,
                                           num_surfels=scene.P, device=dev)
         self.normals = DepthNormals(cameras, dev)
         self.window = _gaussian_window(device=dev)
@@ -155,20 +156,54 @@ class SurfelTrainer:
         self.opt.zero_grad(set_to_none=False)
         return loss
 
-    def capture(self, targets, warmup=3):
-        """Captures step() into a CUDA graph reading ``self.targets``."""
+    def capture(self, targets, warmup=3, headroom=1.25):
+        """Captures step() into a CUDA graph reading ``self.targets``.
+
+        Without a cell-list capacity, the eager warm-up steps size it
+        (``headroom`` times the largest entry count they saw); after replays,
+        ``self.raster.counts()`` reports the flags (SGR_FLAG_BIN_OVERFLOW
+        when the parameters have drifted past the capacity)."""
         self.targets = targets.clone()
         s = torch.cuda.Stream()
         s.wait_stream(torch.cuda.current_stream())
+        most = 0
         with torch.cuda.stream(s):
-            for _ in range(warmup):
+            for _ in range(max(1, warmup)):
                 self.step(self.targets)
+                s.synchronize()
+                most = max(most, self.raster.counts()[2])
         torch.cuda.current_stream().wait_stream(s)
+        if self.raster.bin_capacity is None:
+            self.raster.set_capacity(int(most * headroom) + 4096)
         self.graph = torch.cuda.CUDAGraph()
+        lib = _lib.load()
+        n0 = lib.sgr_kernel_launches()
         with torch.cuda.graph(self.graph):
             self.loss = self.step(self.targets)
+        self.launches_per_step = int(lib.sgr_kernel_launches() - n0)   # libsgr kernels in one replay
         return self.graph
 
     def replay(self):
         self.graph.replay()
         return self.loss
+
+    def snapshot(self):
+        """Copies of the parameters and the optimiser state."""
+        state = [p.detach().clone() for p in self.params()]
+        for p in self.params():
+            st = self.opt.state.get(p, {})
+            state += [v.detach().clone() for _, v in sorted(st.items()) if torch.is_tensor(v)]
+        return state
+
+    def restore(self, state):
+        """Writes a snapshot back in place (captured graphs keep their
+        addresses)."""
+        dst = [p.detach() for p in self.params()]
+        for p in self.params():
+            st = self.opt.state.get(p, {})
+            dst += [v for _, v in sorted(st.items()) if torch.is_tensor(v)]
+        if len(dst) != len(state):
+            raise ValueError("snapshot does not match the optimiser state")
+        with torch.no_grad():
+            for d, s in zip(dst, state):
+                d.copy_(s)

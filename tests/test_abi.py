@@ -33,7 +33,8 @@ def test_library_exports_every_declared_symbol(sgr_lib):
 
 
 def test_status_strings_and_version(sgr_lib):
-    assert sgr_lib.sgr_abi_version() == 1
+    from partgs_gb300 import _lib as L
+    assert sgr_lib.sgr_abi_version() == L.ABI_VERSION
     assert sgr_lib.sgr_status_string(0) == b"ok"
     assert b"16" in sgr_lib.sgr_status_string(3)
 

@@ -97,7 +97,7 @@ def test_transmat_precomp_forward_and_gradient(base):
     assert grad_error(Td.grad.cpu().numpy(), ref["dL_dtransmat"]) <= 3e-4
 
 
-def test_key_overflow_is_flagged_not_faulted(base):
+def test_cell_list_overflow_is_flagged_not_faulted(base):
     from partgs_gb300 import _lib as L
     from partgs_gb300 import raster
     scene, cam = base
@@ -105,13 +105,19 @@ def test_key_overflow_is_flagged_not_faulted(base):
     rs = settings(__import__("partgs_gb300.diff_surfel_rasterization", fromlist=["x"]), cam, [0, 0, 0])
     vs = raster.ViewSet(rs.viewmatrix.reshape(1, 16), rs.projmatrix.reshape(1, 16), rs.campos.reshape(1, 3),
                         [(cam.tanfovx, cam.tanfovy)], cam.height, cam.width)
-    status = torch.zeros(16, dtype=torch.uint8).pin_memory()
-    color, others, _, radii, st = raster.forward(0, sc.means3D, sc.opacities, sc.shs, None, sc.scales, sc.rotations,
-                                                 None, None, vs, rs.bg, 3, key_capacity=100, status_host=status)
+    status = torch.zeros(L.STATUS_BYTES, dtype=torch.uint8).pin_memory()
+    args = (0, sc.means3D, sc.opacities, sc.shs, None, sc.scales, sc.rotations, None, None, vs, rs.bg, 3)
+    color, others, _, radii, st = raster.forward(*args, bin_capacity=100, status_host=status)
     torch.cuda.synchronize()
-    K, flags = raster.read_status(status)
-    assert K > 100 and flags & L.SGR_FLAG_KEY_OVERFLOW
-    assert torch.isfinite(color).all()
+    K, flags, nbins = raster.read_status(status)
+    assert nbins > 100 and flags & L.SGR_FLAG_BIN_OVERFLOW
+    assert torch.isfinite(color).all() and torch.isfinite(others).all()
+    # with room for every entry the same call is exact and raises no flag
+    color2, _, _, _, _ = raster.forward(*args, bin_capacity=nbins, status_host=status)
+    torch.cuda.synchronize()
+    assert raster.read_status(status)[1] == 0
+    color3, _, _, _, _ = raster.forward(*args)
+    assert torch.equal(color2, color3)
 
 
 def test_mark_visible(base):

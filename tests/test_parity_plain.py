@@ -62,8 +62,9 @@ def test_radii_and_tiles_bit_exact(case):
 
 
 def test_tile_lists_bit_exact(case):
-    """Per tile, the sorted surfel list equals the reference's (tile, depth,
-    index) order: same keys, same order, same range lengths."""
+    """Per tile, the surfel list (written out from the depth order the blend
+    streams its cell lists from) equals the reference's (tile, depth, index)
+    order: same keys, same order, same range lengths."""
     st = case["st64"]
     amb_t = st.extra["amb_tiles"] | case["st32"].extra["amb_tiles"]
     ranges = case["dbg"]["ranges"]
