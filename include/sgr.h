@@ -312,6 +312,18 @@ int sgr_bind_backward(const sgr_bind_args* a, const float* d_xyz, const float* d
                       const float* d_rotation, const float* d_opacity, float* d_sq_s, float* d_sq_r,
                       float* d_sq_t, float* d_sq_eps, float* d_sq_occ, void* scratch, void* stream);
 
+/* sgr_bind_backward without a scratch argument: the scratch is a fixed
+ * 4 MiB device array inside the library, so the call allocates nothing.
+ * No counterpart in the reference.  For callers that cannot allocate device
+ * memory at the call (no device allocator of their own, or a loop that must
+ * not enter cudaMalloc).  Shapes needing more than 4 MiB of scratch
+ * (sgr_bind_scratch_bytes) return SGR_ERR_WORKSPACE; calls that overlap on
+ * one device race on the array; the first call on a device sets it up and
+ * should come before any stream capture. */
+int sgr_bind_backward_static(const sgr_bind_args* a, const float* d_xyz, const float* d_log_scaling,
+                             const float* d_rotation, const float* d_opacity, float* d_sq_s, float* d_sq_r,
+                             float* d_sq_t, float* d_sq_eps, float* d_sq_occ, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

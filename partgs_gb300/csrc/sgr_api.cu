@@ -185,6 +185,8 @@ int check_cap(long long cap) {
 
 void count_launches(int n) { g_launches.fetch_add((unsigned long long)n, std::memory_order_relaxed); }
 
+void set_last_error(const std::string& message) { g_last_error = message; }
+
 }  // namespace sgr
 
 using namespace sgr;

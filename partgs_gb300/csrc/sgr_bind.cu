@@ -15,12 +15,14 @@
 // contributions without atomics.
 #include <cuda_runtime.h>
 
+#include <mutex>
 #include <string>
 
 #include "../../include/sgr.h"
 
 namespace sgr {
-void count_launches(int n);   // sgr_api.cu
+void count_launches(int n);                      // sgr_api.cu
+void set_last_error(const std::string& message); // sgr_api.cu
 }  // namespace sgr
 
 namespace sgrbind {
@@ -402,6 +404,47 @@ int check_args(const sgr_bind_args* a) {
   return SGR_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Scratch of the allocation-free backward (sgr_bind_backward_static): one
+// file-scope device array, so calling it allocates nothing.  Its bytes are
+// per-vertex gradient sums and per-triangle opacity sums, accumulated with
+// atomics, so each call clears the bytes it uses before its kernels run.
+// ---------------------------------------------------------------------------
+constexpr size_t kBindStaticScratchBytes = size_t(4) << 20;   // 4 MiB
+constexpr int kMaxDevices = 64;
+
+static __device__ __align__(256) unsigned char g_bind_static_scratch[kBindStaticScratchBytes];
+
+std::mutex g_static_mu;
+void* g_static_ptr[kMaxDevices] = {};
+
+// Device address of the array on the current device, looked up once per
+// device with that device current.
+int static_scratch(void** out) {
+  int dev = -1;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) {
+    sgr::set_last_error(std::string("cudaGetDevice: ") + cudaGetErrorString(e));
+    return SGR_ERR_CUDA;
+  }
+  if (dev < 0 || dev >= kMaxDevices) {
+    sgr::set_last_error("sgr_bind_backward_static: device ordinal beyond the supported 64");
+    return SGR_ERR_UNSUPPORTED;
+  }
+  std::lock_guard<std::mutex> lock(g_static_mu);
+  if (!g_static_ptr[dev]) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_bind_static_scratch);
+    if (e != cudaSuccess || !p) {
+      sgr::set_last_error(std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+      return SGR_ERR_CUDA;
+    }
+    g_static_ptr[dev] = p;
+  }
+  *out = g_static_ptr[dev];
+  return SGR_OK;
+}
+
 }  // namespace sgrbind
 
 using namespace sgrbind;
@@ -447,6 +490,40 @@ int sgr_bind_backward(const sgr_bind_args* a, const float* d_xyz, const float* d
   k_bind_backward_sq<<<a->B, 256, 0, st>>>(*a, dvert, dop_face, d_sq_s, d_sq_r, d_sq_t, d_sq_eps, d_sq_occ);
   sgr::count_launches(1);
   return cudaGetLastError() == cudaSuccess ? SGR_OK : SGR_ERR_CUDA;
+}
+
+// sgr_bind_backward with its scratch in this library's fixed device array
+// instead of a caller buffer; the same kernels, the same results.  For
+// callers that cannot allocate device memory where they call the backward:
+// a host that binds the C ABI without a device allocator of its own (it
+// holds only the buffers it was handed), or a loop that must not enter
+// cudaMalloc, which synchronises the device.
+//   * Limit: sgr_bind_scratch_bytes(a) <= 4 MiB; larger shapes return
+//     SGR_ERR_WORKSPACE and say so in sgr_last_error_message.
+//   * One array per device: calls that overlap on a device (other streams,
+//     other host threads) race on it; the caller serialises them.
+//   * The first call on a device looks the array up (cudaGetSymbolAddress)
+//     with that device current; make that first call before any stream
+//     capture.
+//   * The array must start each call at zero; the call clears the bytes it
+//     uses with cudaMemsetAsync on `stream` before its kernels.
+int sgr_bind_backward_static(const sgr_bind_args* a, const float* d_xyz, const float* d_log_scaling,
+                             const float* d_rotation, const float* d_opacity, float* d_sq_s, float* d_sq_r,
+                             float* d_sq_t, float* d_sq_eps, float* d_sq_occ, void* stream) {
+  int rc = check_args(a);
+  if (rc) return rc;
+  if (a->B == 0) return SGR_OK;
+  const size_t need = sgr_bind_scratch_bytes(a);
+  if (need > kBindStaticScratchBytes) {
+    sgr::set_last_error("sgr_bind_backward_static: the shape needs " + std::to_string(need) +
+                        " bytes of scratch, above the fixed " + std::to_string(kBindStaticScratchBytes) +
+                        "; use sgr_bind_backward with a caller buffer");
+    return SGR_ERR_WORKSPACE;
+  }
+  void* scratch = nullptr;
+  if ((rc = static_scratch(&scratch))) return rc;
+  return sgr_bind_backward(a, d_xyz, d_log_scaling, d_rotation, d_opacity, d_sq_s, d_sq_r, d_sq_t, d_sq_eps,
+                           d_sq_occ, scratch, stream);
 }
 
 }  // extern "C"
