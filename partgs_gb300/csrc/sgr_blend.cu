@@ -29,21 +29,22 @@ namespace {
 constexpr int kWarps = kBlock / 32;
 constexpr int kRing = 2048;            // ring of streamed list entries: >= kBlock + kChunk, a power of two
 static_assert(kRing >= kBlock + kChunk && (kRing & (kRing - 1)) == 0, "ring size");
-static_assert(kChunk == 4 * kBlock && kWarps * 4 == 32, "one scan lane per (record slot, warp)");
 
 struct Strip {
   float x0, x1;       // pixel-centre x range of the tile
   float y0;           // pixel-centre y of the tile's first row
 };
 
-// Bit w set when the record's reach box meets strip w (rows 2w, 2w+1).
+// Bit w set when the record's reach box meets strip w: rows
+// [ROWS*w, ROWS*w + ROWS) of the tile, one strip per warp.
+template <int ROWS, int NWARPS>
 __device__ __forceinline__ uint32_t strip_mask(const float4& box, const Strip& s) {
   if (box.y < s.x0 || box.x > s.x1) return 0u;
   uint32_t m = 0;
 #pragma unroll
-  for (int w = 0; w < kWarps; ++w) {
-    const float ya = s.y0 + 2.0f * w;
-    if (box.w >= ya && box.z <= ya + 1.0f) m |= 1u << w;
+  for (int w = 0; w < NWARPS; ++w) {
+    const float ya = s.y0 + (float)(ROWS * w);
+    if (box.w >= ya && box.z <= ya + (float)(ROWS - 1)) m |= 1u << w;
   }
   return m;
 }
@@ -72,22 +73,25 @@ __device__ __forceinline__ int warp_survivors(const uint8_t* mask, int n, int wa
 // end at position `pos_end`.  Returns how many were written (the same value
 // in every thread).  Every thread of the CTA calls it; it synchronises the
 // CTA.
-template <bool REVERSE>
+template <bool REVERSE, int NT>
 __device__ int stream_window(const GeomView& g, const uint32_t* __restrict__ list, int i0, int i1, uint32_t tx,
                              uint32_t ty, int pos_end, int top, uint32_t* ring, int tail, int* s_count, int& found) {
+  constexpr int RPT = kChunk / NT;                 // entries per thread
+  constexpr int NW = NT / 32;
+  static_assert(RPT * NW == 32, "one scan lane per (entry slot, warp)");
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  bool hit[4];
-  uint32_t pos[4], bal[4];
+  bool hit[RPT];
+  uint32_t pos[RPT], bal[RPT];
 #pragma unroll
-  for (int k = 0; k < 4; ++k) {
-    const int i = i0 + k * kBlock + (int)threadIdx.x;
+  for (int k = 0; k < RPT; ++k) {
+    const int i = i0 + k * NT + (int)threadIdx.x;
     pos[k] = i < i1 ? list[i] : 0u;
     hit[k] = i < i1 && rect_holds(g.rects[pos[k]], tx, ty);
     bal[k] = __ballot_sync(0xffffffffu, hit[k]);
   }
   if (lane == 0) {
 #pragma unroll
-    for (int k = 0; k < 4; ++k) s_count[k * kWarps + warp] = __popc(bal[k]);
+    for (int k = 0; k < RPT; ++k) s_count[k * NW + warp] = __popc(bal[k]);
   }
   __syncthreads();
   // exclusive scan over the 32 (slot, warp) groups, which are in list order
@@ -102,8 +106,8 @@ __device__ int stream_window(const GeomView& g, const uint32_t* __restrict__ lis
   const int m = REVERSE ? max(0, min(total, top - (pos_end - total))) : total;
   const uint32_t below = (1u << lane) - 1u;
 #pragma unroll
-  for (int k = 0; k < 4; ++k) {
-    const int base = __shfl_sync(0xffffffffu, incl - own, k * kWarps + warp);
+  for (int k = 0; k < RPT; ++k) {
+    const int base = __shfl_sync(0xffffffffu, incl - own, k * NW + warp);
     if (hit[k]) {
       const int rank = base + __popc(bal[k] & below);
       if (rank < m) {
@@ -179,7 +183,7 @@ __global__ void __launch_bounds__(kBlock) k_render_fwd(const sgr_batch b, GeomVi
     if (__syncthreads_count(done) == kBlock) break;
     while (tail - head < kBlock && scanned < len) {   // refill the ring (CTA-uniform)
       int found;
-      tail += stream_window<false>(g, list, scanned, min(scanned + kChunk, len), (uint32_t)tx, (uint32_t)ty, 0, 0,
+      tail += stream_window<false, kBlock>(g, list, scanned, min(scanned + kChunk, len), (uint32_t)tx, (uint32_t)ty, 0, 0,
                                    s_ring, tail, s_count, found);
       scanned = min(scanned + kChunk, len);
     }
@@ -190,7 +194,7 @@ __global__ void __launch_bounds__(kBlock) k_render_fwd(const sgr_batch b, GeomVi
       const float4* rec = g.records + (size_t)r * kRecF4;
 #pragma unroll
       for (int k = 0; k < kRecF4 - 1; ++k) s_rec[k][threadIdx.x] = rec[k];
-      s_mask[threadIdx.x] = (uint8_t)strip_mask(rec[5], strip);
+      s_mask[threadIdx.x] = (uint8_t)strip_mask<2, kWarps>(rec[5], strip);
       if (VARIANT == SGR_VARIANT_PART) {
         const float* sem = b.semantics + (size_t)(sid_base + (int)r) * S;
         for (int c = 0; c < S; ++c) s_sem[c][threadIdx.x] = sem[c];
@@ -314,14 +318,163 @@ __global__ void __launch_bounds__(kBlock) k_render_fwd(const sgr_batch b, GeomVi
 // Back to front over the positions before each pixel's last contributor,
 // transmittance recovered by division from the stored final T.  The CTA
 // starts at its tile's largest last contributor; each warp skips entries at
-// or past its own largest one.  The 18 per-fragment gradients of a warp's 32
-// pixels are summed with a transposed shuffle reduction and one lane per
-// value adds the total to the per-view gradient record (one atomic per value
-// and warp instead of one per value and pixel).
+// or past its own largest one.
+//
+// Plain variant: each thread owns two pixels of one column, two rows apart,
+// so a warp covers a 16x4 strip and a CTA of 128 threads the tile.  The part
+// variant keeps one pixel per thread (its 48 floats of per-pixel semantic
+// state would not fit twice).  The 18 per-fragment gradients of a warp's
+// pixels are summed in registers over the thread's pixels, then over the
+// warp with a transposed shuffle reduction, and one lane per value adds the
+// total to the per-view gradient record (one atomic per value and warp
+// instead of one per value and pixel).
 // ---------------------------------------------------------------------------
 template <int VARIANT>
-__global__ void __launch_bounds__(kBlock) k_render_bwd(const sgr_batch b, GeomView g, const sgr_bwd_inputs in,
-                                                       float* __restrict__ grads, float* __restrict__ dL_dsemantics) {
+struct BwdShape {
+  static constexpr int PX = (VARIANT == SGR_VARIANT_PLAIN) ? 2 : 1;   // pixels per thread
+  static constexpr int NT = kBlock / PX;                              // threads per CTA
+  static constexpr int NW = NT / 32;                                  // warps, one strip each
+  static constexpr int ROWS = kTile / NW;                             // strip height
+  static constexpr int NS = (VARIANT == SGR_VARIANT_PART) ? SGR_MAX_SEMANTICS : 1;
+};
+
+// Per-pixel state of the backward recurrences (P0/cr/backward.cu:160-260).
+template <int VARIANT>
+struct BwdPixel {
+  static constexpr int NS = BwdShape<VARIANT>::NS;
+  float pxf, pyf;
+  float T, T_final, final_A, final_D, final_D2, bg_dot;
+  int last_contributor, median_contributor;
+  float dL_dpixel[3], dL_dnormal2D[3];
+  float dL_ddepth, dL_daccum, dL_dreg, dL_dmedian, dL_dmaxw;
+  float accum_rec[3], last_color[3], last_normal[3], accum_normal[3];
+  float last_alpha, last_depth, accum_depth, accum_alpha, last_dL_dT;
+  float dsem_pix[NS], accum_sem[NS], last_sem[NS];
+};
+
+// One fragment of the backward for one pixel: entry j of the staged batch at
+// list position pos.  Adds this pixel's share of the entry's 18 gradient
+// values to gv (and of its semantic gradients to gsem); false when the
+// fragment contributes nothing.
+template <int VARIANT>
+__device__ __forceinline__ bool bwd_fragment(BwdPixel<VARIANT>& q, const float4 (*s_rec)[kBlock], const float* s_sem,
+                                             int j, int pos, int S, float (&gv)[32], float (&gsem)[32]) {
+  if (pos >= q.last_contributor) return false;
+  const float4 r0 = s_rec[0][j], r1 = s_rec[1][j], r2 = s_rec[2][j];
+  const V3 Tu = v3(r0.x, r0.y, r0.z), Tv = v3(r0.w, r1.x, r1.y), Tw = v3(r1.z, r1.w, r2.x);
+  V3 k, l;
+  if (VARIANT == SGR_VARIANT_PLAIN) {
+    k = q.pxf * Tw - Tu;
+    l = q.pyf * Tw - Tv;
+  } else {
+    k = v3(-Tu.x + q.pxf * Tw.x, -Tu.y + q.pxf * Tw.y, -Tu.z + q.pxf * Tw.z);
+    l = v3(-Tv.x + q.pyf * Tw.x, -Tv.y + q.pyf * Tw.y, -Tv.z + q.pyf * Tw.z);
+  }
+  const V3 p = cross3(k, l);
+  const float dx = r2.y - q.pxf, dy = r2.z - q.pyf;
+  const float rho2d = kFilterInvSquareP0 * (dx * dx + dy * dy);
+  const float reach = s_rec[3][j].w;
+  if (p.z == 0.0f || (rho2d > reach && p.x * p.x + p.y * p.y > reach * (p.z * p.z))) return false;
+  // the same divisions as the forward, so alpha and the tests agree bit for bit
+  const float sx = p.x / p.z, sy = p.y / p.z;
+  const float rho3d = sx * sx + sy * sy;
+  const bool use3d = rho3d <= rho2d;
+  const float rho = fminf(rho3d, rho2d);
+  const float c_d = use3d ? (sx * Tw.x + sy * Tw.y) + Tw.z : Tw.z;
+  const float power = -0.5f * rho;
+  const float G = expf(power);
+  const float alpha = fminf(0.99f, r2.w * G);
+  if (c_d < kNearP0 || power > 0.0f || alpha < 1.0f / 255.0f) return false;
+
+  const float4 r3 = s_rec[3][j], r4 = s_rec[4][j];
+  const float inv_1ma = __frcp_rn(1.f - alpha);
+  q.T = q.T * inv_1ma;
+  const float wgt = alpha * q.T;
+  float dL_dalpha = 0.0f;
+  const float col[3] = {r4.x, r4.y, r4.z};
+#pragma unroll
+  for (int ch = 0; ch < 3; ++ch) {
+    q.accum_rec[ch] = q.last_alpha * q.last_color[ch] + (1.f - q.last_alpha) * q.accum_rec[ch];
+    q.last_color[ch] = col[ch];
+    dL_dalpha += (col[ch] - q.accum_rec[ch]) * q.dL_dpixel[ch];
+    gv[14 + ch] += wgt * q.dL_dpixel[ch];
+  }
+  if (VARIANT == SGR_VARIANT_PART) {
+    for (int c = 0; c < S; ++c) {
+      q.accum_sem[c] = q.last_alpha * q.last_sem[c] + (1.f - q.last_alpha) * q.accum_sem[c];
+      q.last_sem[c] = s_sem[c * kBlock + j];
+    }
+  }
+  float dL_dz = 0.0f, dL_dweight = 0.f;
+  float m_d, dmd_dd;
+  if (VARIANT == SGR_VARIANT_PLAIN) {
+    const float inv_d = __frcp_rn(c_d);
+    m_d = kFarP0 / (kFarP0 - kNearP0) * (1 - kNearP0 * inv_d);
+    dmd_dd = (kFarP0 * kNearP0) / (kFarP0 - kNearP0) * (inv_d * inv_d);
+  } else {
+    m_d = mapped_depth_p1(c_d);
+    dmd_dd = (float)((kFarP1 * kNearP1) / ((kFarP1 - kNearP1) * c_d * c_d));
+  }
+  if (pos == q.median_contributor - 1) {
+    dL_dz += q.dL_dmedian;
+    if (VARIANT == SGR_VARIANT_PART) dL_dweight += q.dL_dmaxw;
+  }
+  dL_dweight += (q.final_D2 + m_d * m_d * q.final_A - 2 * m_d * q.final_D) * q.dL_dreg;
+  dL_dalpha += dL_dweight - q.last_dL_dT;
+  q.last_dL_dT = dL_dweight * alpha + (1 - alpha) * q.last_dL_dT;
+  const float dL_dmd = 2.0f * (q.T * alpha) * (m_d * q.final_A - q.final_D) * q.dL_dreg;
+  dL_dz += dL_dmd * dmd_dd;
+  q.accum_depth = q.last_alpha * q.last_depth + (1.f - q.last_alpha) * q.accum_depth;
+  q.last_depth = c_d;
+  dL_dalpha += (c_d - q.accum_depth) * q.dL_ddepth;
+  // the reference adds last_alpha * 1.0 in double: one rounding of an exact
+  // sum, i.e. a plain float add
+  q.accum_alpha = __fadd_rn(q.last_alpha, __fmul_rn(1.f - q.last_alpha, q.accum_alpha));
+  dL_dalpha += (1 - q.accum_alpha) * q.dL_daccum;
+  const float nrm[3] = {r3.x, r3.y, r3.z};
+#pragma unroll
+  for (int ch = 0; ch < 3; ++ch) {
+    q.accum_normal[ch] = q.last_alpha * q.last_normal[ch] + (1.f - q.last_alpha) * q.accum_normal[ch];
+    q.last_normal[ch] = nrm[ch];
+    dL_dalpha += (nrm[ch] - q.accum_normal[ch]) * q.dL_dnormal2D[ch];
+    gv[11 + ch] += alpha * q.T * q.dL_dnormal2D[ch];
+  }
+  dL_dalpha *= q.T;
+  q.last_alpha = alpha;
+  dL_dalpha += (-q.T_final * inv_1ma) * q.bg_dot;
+  const float dL_dG = r2.w * dL_dalpha;
+  dL_dz += alpha * q.T * q.dL_ddepth;
+  if (use3d) {
+    const float inv_pz = __frcp_rn(p.z);
+    const float dsx_pz = (dL_dG * -G * sx + dL_dz * Tw.x) * inv_pz;
+    const float dsy_pz = (dL_dG * -G * sy + dL_dz * Tw.y) * inv_pz;
+    const V3 dL_dp = v3(dsx_pz, dsy_pz, -(dsx_pz * sx + dsy_pz * sy));
+    const V3 dL_dk = cross3(l, dL_dp);
+    const V3 dL_dl = cross3(dL_dp, k);
+    gv[0] -= dL_dk.x; gv[1] -= dL_dk.y; gv[2] -= dL_dk.z;
+    gv[3] -= dL_dl.x; gv[4] -= dL_dl.y; gv[5] -= dL_dl.z;
+    gv[6] += q.pxf * dL_dk.x + q.pyf * dL_dl.x + dL_dz * sx;
+    gv[7] += q.pxf * dL_dk.y + q.pyf * dL_dl.y + dL_dz * sy;
+    gv[8] += q.pxf * dL_dk.z + q.pyf * dL_dl.z + dL_dz * 1.0f;
+  } else {
+    gv[9] += dL_dG * (-G * kFilterInvSquareP0 * dx);
+    gv[10] += dL_dG * (-G * kFilterInvSquareP0 * dy);
+    gv[8] += dL_dz;
+  }
+  gv[17] += G * dL_dalpha;
+  if (VARIANT == SGR_VARIANT_PART) {
+    for (int c = 0; c < S; ++c) gsem[c] += wgt * q.dsem_pix[c];
+  }
+  return true;
+}
+
+template <int VARIANT>
+__global__ void __launch_bounds__(BwdShape<VARIANT>::NT) k_render_bwd(const sgr_batch b, GeomView g,
+                                                                      const sgr_bwd_inputs in,
+                                                                      float* __restrict__ grads,
+                                                                      float* __restrict__ dL_dsemantics) {
+  using Shape = BwdShape<VARIANT>;
+  constexpr int PX = Shape::PX, NT = Shape::NT, NW = Shape::NW, ROWS = Shape::ROWS, NS = Shape::NS;
   const int tiles_per_view = g.tiles_x * g.tiles_y;
   const int tile = blockIdx.x;
   const int v = tile / tiles_per_view;
@@ -329,11 +482,7 @@ __global__ void __launch_bounds__(kBlock) k_render_bwd(const sgr_batch b, GeomVi
   const int ty = t / g.tiles_x, tx = t - ty * g.tiles_x;
   const int W = b.width, H = b.height;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int px = tx * kTile + (threadIdx.x & (kTile - 1));
-  const int py = ty * kTile + (threadIdx.x / kTile);
-  const bool inside = px < W && py < H;
   const float off = (VARIANT == SGR_VARIANT_PLAIN) ? 0.0f : 0.5f;
-  const float pxf = (float)px + off, pyf = (float)py + off;
   const Strip strip{(float)(tx * kTile) + off, (float)(tx * kTile) + off + (kTile - 1), (float)(ty * kTile) + off};
   const int S = (VARIANT == SGR_VARIANT_PART) ? b.semantic_channels : 0;
   const sgr_view_desc vd = b.views[v];
@@ -342,65 +491,69 @@ __global__ void __launch_bounds__(kBlock) k_render_bwd(const sgr_batch b, GeomVi
   __shared__ float4 s_rec[kRecF4 - 1][kBlock];
   __shared__ uint32_t s_id[kBlock];
   __shared__ uint8_t s_mask[kBlock];
-  __shared__ uint8_t s_list[kWarps][kBlock];
-  __shared__ float s_sem[(VARIANT == SGR_VARIANT_PART) ? SGR_MAX_SEMANTICS : 1][kBlock];
-  __shared__ int s_max[kWarps];
+  __shared__ uint8_t s_list[NW][kBlock];
+  __shared__ float s_sem[NS * kBlock];
+  __shared__ int s_max[NW];
   __shared__ uint32_t s_ring[kRing];
   __shared__ int s_count[32];
 
   const size_t HW = (size_t)H * W;
-  const size_t pix = inside ? (size_t)py * W + px : 0;
   const float* fT = g.final_T + (size_t)v * 3 * HW;
   const uint32_t* nc = g.n_contrib + (size_t)v * 2 * HW;
   const int NO = (VARIANT == SGR_VARIANT_PLAIN) ? 7 : 8;
   const float* dpix = in.dL_dcolor + (size_t)v * 3 * HW;
   const float* doth = in.dL_dothers + (size_t)v * NO * HW;
-
-  const float T_final = inside ? fT[pix] : 0.f;
-  float T = T_final;
-  const int last_contributor = inside ? (int)nc[pix] : 0;
-  const int median_contributor = inside ? (int)nc[pix + HW] : 0;
-  float dL_dpixel[3] = {0.f, 0.f, 0.f};
-  float dL_ddepth = 0.f, dL_daccum = 0.f, dL_dreg = 0.f, dL_dmedian = 0.f, dL_dmaxw = 0.f;
-  float dL_dnormal2D[3] = {0.f, 0.f, 0.f};
-  float dsem_pix[SGR_MAX_SEMANTICS];
-#pragma unroll
-  for (int c = 0; c < SGR_MAX_SEMANTICS; ++c) dsem_pix[c] = 0.f;
-  float final_D = 0.f, final_D2 = 0.f;
-  if (inside) {
-    for (int c = 0; c < 3; ++c) dL_dpixel[c] = dpix[pix + c * HW];
-    dL_ddepth = doth[pix];
-    dL_daccum = doth[pix + HW];
-    for (int c = 0; c < 3; ++c) dL_dnormal2D[c] = doth[pix + (2 + c) * HW];
-    dL_dmedian = doth[pix + 5 * HW];
-    dL_dreg = doth[pix + 6 * HW];
-    if (VARIANT == SGR_VARIANT_PART) {
-      dL_dmaxw = doth[pix + 7 * HW];
-      const float* ds = in.dL_dsemantic + (size_t)v * S * HW;
-      for (int c = 0; c < S; ++c) dsem_pix[c] = ds[pix + c * HW];
-    }
-    final_D = fT[pix + HW];
-    final_D2 = fT[pix + 2 * HW];
-  }
-  const float final_A = 1 - T_final;
   const float* bg = b.background;
-  const float bg_dot = bg[0] * dL_dpixel[0] + bg[1] * dL_dpixel[1] + bg[2] * dL_dpixel[2];
 
-  float accum_rec[3] = {0.f, 0.f, 0.f}, last_color[3] = {0.f, 0.f, 0.f};
-  float accum_sem[SGR_MAX_SEMANTICS], last_sem[SGR_MAX_SEMANTICS];
+  // pixel i of this thread: column lane % 16, row ROWS * warp + lane / 16 + 2 i
+  BwdPixel<VARIANT> q[PX];
+  int thread_max = 0;
 #pragma unroll
-  for (int c = 0; c < SGR_MAX_SEMANTICS; ++c) accum_sem[c] = last_sem[c] = 0.f;
-  float last_alpha = 0.f, last_depth = 0.f, accum_depth = 0.f, accum_alpha = 0.f, last_dL_dT = 0.f;
-  float last_normal[3] = {0.f, 0.f, 0.f}, accum_normal[3] = {0.f, 0.f, 0.f};
+  for (int i = 0; i < PX; ++i) {
+    BwdPixel<VARIANT>& Q = q[i];
+    const int px = tx * kTile + (lane & (kTile - 1));
+    const int py = ty * kTile + ROWS * warp + (lane >> 4) + 2 * i;
+    const bool inside = px < W && py < H;
+    const size_t pix = inside ? (size_t)py * W + px : 0;
+    Q.pxf = (float)px + off;
+    Q.pyf = (float)py + off;
+    Q.T_final = inside ? fT[pix] : 0.f;
+    Q.T = Q.T_final;
+    Q.last_contributor = inside ? (int)nc[pix] : 0;
+    Q.median_contributor = inside ? (int)nc[pix + HW] : 0;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      Q.dL_dpixel[c] = inside ? dpix[pix + c * HW] : 0.f;
+      Q.dL_dnormal2D[c] = inside ? doth[pix + (2 + c) * HW] : 0.f;
+      Q.accum_rec[c] = Q.last_color[c] = Q.last_normal[c] = Q.accum_normal[c] = 0.f;
+    }
+    Q.dL_ddepth = inside ? doth[pix] : 0.f;
+    Q.dL_daccum = inside ? doth[pix + HW] : 0.f;
+    Q.dL_dmedian = inside ? doth[pix + 5 * HW] : 0.f;
+    Q.dL_dreg = inside ? doth[pix + 6 * HW] : 0.f;
+    Q.dL_dmaxw = (VARIANT == SGR_VARIANT_PART && inside) ? doth[pix + 7 * HW] : 0.f;
+#pragma unroll
+    for (int c = 0; c < NS; ++c) Q.dsem_pix[c] = Q.accum_sem[c] = Q.last_sem[c] = 0.f;
+    if (VARIANT == SGR_VARIANT_PART && inside) {
+      const float* ds = in.dL_dsemantic + (size_t)v * S * HW;
+      for (int c = 0; c < S; ++c) Q.dsem_pix[c] = ds[pix + c * HW];
+    }
+    Q.final_D = inside ? fT[pix + HW] : 0.f;
+    Q.final_D2 = inside ? fT[pix + 2 * HW] : 0.f;
+    Q.final_A = 1 - Q.T_final;
+    Q.bg_dot = bg[0] * Q.dL_dpixel[0] + bg[1] * Q.dL_dpixel[1] + bg[2] * Q.dL_dpixel[2];
+    Q.last_alpha = Q.last_depth = Q.accum_depth = Q.accum_alpha = Q.last_dL_dT = 0.f;
+    thread_max = max(thread_max, Q.last_contributor);
+  }
 
-  int warp_max = last_contributor;
+  int warp_max = thread_max;
 #pragma unroll
   for (int o = 16; o >= 1; o >>= 1) warp_max = max(warp_max, __shfl_xor_sync(0xffffffffu, warp_max, o));
   if (lane == 0) s_max[warp] = warp_max;
   __syncthreads();
   int block_max = 0;
 #pragma unroll
-  for (int w = 0; w < kWarps; ++w) block_max = max(block_max, s_max[w]);
+  for (int w = 0; w < NW; ++w) block_max = max(block_max, s_max[w]);
 
   // positions [0, block_max) of the list, streamed back to front over the
   // span of the cell list the forward scanned
@@ -416,24 +569,24 @@ __global__ void __launch_bounds__(kBlock) k_render_bwd(const sgr_batch b, GeomVi
     while (tail - head < kBlock && scan_end > 0) {   // refill the ring (CTA-uniform)
       const int i0 = max(0, scan_end - kChunk);
       int found;
-      tail += stream_window<true>(g, list, i0, scan_end, (uint32_t)tx, (uint32_t)ty, pos_end, top, s_ring, tail,
-                                  s_count, found);
+      tail += stream_window<true, NT>(g, list, i0, scan_end, (uint32_t)tx, (uint32_t)ty, pos_end, top, s_ring,
+                                      tail, s_count, found);
       pos_end -= found;
       scan_end = i0;
     }
     const int n = min(kBlock, hi);
     if (tail - head < n) break;                    // index inconsistent with the rectangles: stop
     __syncthreads();
-    if ((int)threadIdx.x < n) {
-      const uint32_t r = s_ring[(head + threadIdx.x) & (kRing - 1)];
-      s_id[threadIdx.x] = r;
+    for (int e = threadIdx.x; e < n; e += NT) {
+      const uint32_t r = s_ring[(head + e) & (kRing - 1)];
+      s_id[e] = r;
       const float4* rec = g.records + (size_t)r * kRecF4;
 #pragma unroll
-      for (int k = 0; k < kRecF4 - 1; ++k) s_rec[k][threadIdx.x] = rec[k];
-      s_mask[threadIdx.x] = (uint8_t)strip_mask(rec[5], strip);
+      for (int k = 0; k < kRecF4 - 1; ++k) s_rec[k][e] = rec[k];
+      s_mask[e] = (uint8_t)strip_mask<ROWS, NW>(rec[5], strip);
       if (VARIANT == SGR_VARIANT_PART) {
         const float* sem = b.semantics + (size_t)(sid_base + (int)r) * S;
-        for (int c = 0; c < S; ++c) s_sem[c][threadIdx.x] = sem[c];
+        for (int c = 0; c < S; ++c) s_sem[c * kBlock + e] = sem[c];
       }
     }
     __syncthreads();
@@ -444,119 +597,13 @@ __global__ void __launch_bounds__(kBlock) k_render_bwd(const sgr_batch b, GeomVi
       if (pos >= warp_max) continue;        // uniform: past every lane's last contributor
       float gv[32];
 #pragma unroll
-      for (int q = 0; q < 32; ++q) gv[q] = 0.f;
+      for (int u = 0; u < 32; ++u) gv[u] = 0.f;
       float gsem[32];
 #pragma unroll
-      for (int q = 0; q < 32; ++q) gsem[q] = 0.f;
-      bool ok = inside && pos < last_contributor;
-      if (ok) {
-        const float4 r0 = s_rec[0][j], r1 = s_rec[1][j], r2 = s_rec[2][j];
-        const V3 Tu = v3(r0.x, r0.y, r0.z), Tv = v3(r0.w, r1.x, r1.y), Tw = v3(r1.z, r1.w, r2.x);
-        V3 k, l;
-        if (VARIANT == SGR_VARIANT_PLAIN) {
-          k = pxf * Tw - Tu;
-          l = pyf * Tw - Tv;
-        } else {
-          k = v3(-Tu.x + pxf * Tw.x, -Tu.y + pxf * Tw.y, -Tu.z + pxf * Tw.z);
-          l = v3(-Tv.x + pyf * Tw.x, -Tv.y + pyf * Tw.y, -Tv.z + pyf * Tw.z);
-        }
-        const V3 p = cross3(k, l);
-        const float dx = r2.y - pxf, dy = r2.z - pyf;
-        const float rho2d = kFilterInvSquareP0 * (dx * dx + dy * dy);
-        const float reach = s_rec[3][j].w;
-        ok = p.z != 0.0f && !(rho2d > reach && p.x * p.x + p.y * p.y > reach * (p.z * p.z));
-        if (ok) {
-          const float sx = p.x / p.z, sy = p.y / p.z;
-          const float rho3d = sx * sx + sy * sy;
-          const bool use3d = rho3d <= rho2d;
-          const float rho = fminf(rho3d, rho2d);
-          const float c_d = use3d ? (sx * Tw.x + sy * Tw.y) + Tw.z : Tw.z;
-          const float power = -0.5f * rho;
-          const float G = expf(power);
-          const float alpha = fminf(0.99f, r2.w * G);
-          ok = !(c_d < kNearP0) && !(power > 0.0f) && !(alpha < 1.0f / 255.0f);
-          if (ok) {
-            const float4 r3 = s_rec[3][j], r4 = s_rec[4][j];
-            T = T / (1.f - alpha);
-            const float wgt = alpha * T;
-            float dL_dalpha = 0.0f;
-            const float col[3] = {r4.x, r4.y, r4.z};
+      for (int u = 0; u < 32; ++u) gsem[u] = 0.f;
+      bool ok = false;
 #pragma unroll
-            for (int ch = 0; ch < 3; ++ch) {
-              accum_rec[ch] = last_alpha * last_color[ch] + (1.f - last_alpha) * accum_rec[ch];
-              last_color[ch] = col[ch];
-              dL_dalpha += (col[ch] - accum_rec[ch]) * dL_dpixel[ch];
-              gv[14 + ch] = wgt * dL_dpixel[ch];
-            }
-            if (VARIANT == SGR_VARIANT_PART) {
-              for (int c = 0; c < S; ++c) {
-                accum_sem[c] = last_alpha * last_sem[c] + (1.f - last_alpha) * accum_sem[c];
-                last_sem[c] = s_sem[c][j];
-              }
-            }
-            float dL_dz = 0.0f, dL_dweight = 0.f;
-            float m_d, dmd_dd;
-            if (VARIANT == SGR_VARIANT_PLAIN) {
-              m_d = kFarP0 / (kFarP0 - kNearP0) * (1 - kNearP0 / c_d);
-              dmd_dd = (kFarP0 * kNearP0) / ((kFarP0 - kNearP0) * c_d * c_d);
-            } else {
-              m_d = mapped_depth_p1(c_d);
-              dmd_dd = (float)((kFarP1 * kNearP1) / ((kFarP1 - kNearP1) * c_d * c_d));
-            }
-            if (pos == median_contributor - 1) {
-              dL_dz += dL_dmedian;
-              if (VARIANT == SGR_VARIANT_PART) dL_dweight += dL_dmaxw;
-            }
-            dL_dweight += (final_D2 + m_d * m_d * final_A - 2 * m_d * final_D) * dL_dreg;
-            dL_dalpha += dL_dweight - last_dL_dT;
-            last_dL_dT = dL_dweight * alpha + (1 - alpha) * last_dL_dT;
-            const float dL_dmd = 2.0f * (T * alpha) * (m_d * final_A - final_D) * dL_dreg;
-            dL_dz += dL_dmd * dmd_dd;
-            accum_depth = last_alpha * last_depth + (1.f - last_alpha) * accum_depth;
-            last_depth = c_d;
-            dL_dalpha += (c_d - accum_depth) * dL_ddepth;
-            // the reference adds last_alpha * 1.0 in double: one rounding of
-            // an exact sum, i.e. a plain float add
-            accum_alpha = __fadd_rn(last_alpha, __fmul_rn(1.f - last_alpha, accum_alpha));
-            dL_dalpha += (1 - accum_alpha) * dL_daccum;
-            const float nrm[3] = {r3.x, r3.y, r3.z};
-#pragma unroll
-            for (int ch = 0; ch < 3; ++ch) {
-              accum_normal[ch] = last_alpha * last_normal[ch] + (1.f - last_alpha) * accum_normal[ch];
-              last_normal[ch] = nrm[ch];
-              dL_dalpha += (nrm[ch] - accum_normal[ch]) * dL_dnormal2D[ch];
-              gv[11 + ch] = alpha * T * dL_dnormal2D[ch];
-            }
-            dL_dalpha *= T;
-            last_alpha = alpha;
-            dL_dalpha += (-T_final / (1.f - alpha)) * bg_dot;
-            const float dL_dG = r2.w * dL_dalpha;
-            dL_dz += alpha * T * dL_ddepth;
-            if (use3d) {
-              const float dsx = dL_dG * -G * sx + dL_dz * Tw.x;
-              const float dsy = dL_dG * -G * sy + dL_dz * Tw.y;
-              const float dsx_pz = dsx / p.z;
-              const float dsy_pz = dsy / p.z;
-              const V3 dL_dp = v3(dsx_pz, dsy_pz, -(dsx_pz * sx + dsy_pz * sy));
-              const V3 dL_dk = cross3(l, dL_dp);
-              const V3 dL_dl = cross3(dL_dp, k);
-              gv[0] = -dL_dk.x; gv[1] = -dL_dk.y; gv[2] = -dL_dk.z;
-              gv[3] = -dL_dl.x; gv[4] = -dL_dl.y; gv[5] = -dL_dl.z;
-              gv[6] = pxf * dL_dk.x + pyf * dL_dl.x + dL_dz * sx;
-              gv[7] = pxf * dL_dk.y + pyf * dL_dl.y + dL_dz * sy;
-              gv[8] = pxf * dL_dk.z + pyf * dL_dl.z + dL_dz * 1.0f;
-            } else {
-              gv[9] = dL_dG * (-G * kFilterInvSquareP0 * dx);
-              gv[10] = dL_dG * (-G * kFilterInvSquareP0 * dy);
-              gv[8] = dL_dz;
-            }
-            gv[17] = G * dL_dalpha;
-            if (VARIANT == SGR_VARIANT_PART) {
-              for (int c = 0; c < S; ++c) gsem[c] = wgt * dsem_pix[c];
-            }
-          }
-        }
-      }
+      for (int i = 0; i < PX; ++i) ok |= bwd_fragment<VARIANT>(q[i], s_rec, s_sem, j, pos, S, gv, gsem);
       if (__any_sync(0xffffffffu, ok)) {
         const float total = warp_transpose_sum(gv, lane);
         const uint32_t r = s_id[j];
@@ -583,9 +630,10 @@ void launch_render_bwd(const sgr_batch& b, const GeomView& g, const sgr_bwd_inpu
   const unsigned blocks = (unsigned)(g.tiles_x * g.tiles_y) * (unsigned)b.num_views;
   if (blocks == 0) return;
   if (b.variant == SGR_VARIANT_PLAIN)
-    k_render_bwd<SGR_VARIANT_PLAIN><<<blocks, kBlock, 0, st>>>(b, g, in, grads, dL_dsemantics);
+    k_render_bwd<SGR_VARIANT_PLAIN>
+        <<<blocks, BwdShape<SGR_VARIANT_PLAIN>::NT, 0, st>>>(b, g, in, grads, dL_dsemantics);
   else
-    k_render_bwd<SGR_VARIANT_PART><<<blocks, kBlock, 0, st>>>(b, g, in, grads, dL_dsemantics);
+    k_render_bwd<SGR_VARIANT_PART><<<blocks, BwdShape<SGR_VARIANT_PART>::NT, 0, st>>>(b, g, in, grads, dL_dsemantics);
   count_launches();
 }
 
