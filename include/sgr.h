@@ -324,6 +324,33 @@ int sgr_bind_backward_static(const sgr_bind_args* a, const float* d_xyz, const f
                              const float* d_rotation, const float* d_opacity, float* d_sq_s, float* d_sq_r,
                              float* d_sq_t, float* d_sq_eps, float* d_sq_occ, void* stream);
 
+/* ---- optimiser ---------------------------------------------------------- */
+
+/* One parameter tensor of an Adam step: numel floats each of param, grad and
+ * the two moment buffers (device pointers), and its learning rate. */
+#define SGR_ADAM_MAX_TENSORS 8
+typedef struct sgr_adam_tensor {
+    float* param;
+    float* grad;
+    float* exp_avg;
+    float* exp_avg_sq;
+    int64_t numel;
+    float lr;
+} sgr_adam_tensor;
+
+typedef struct sgr_adam_args {
+    sgr_adam_tensor tensors[SGR_ADAM_MAX_TENSORS];
+    int32_t count;
+    float beta1, beta2, eps;
+    int32_t zero_grad;           /* 1: clear each gradient after its update */
+} sgr_adam_args;
+
+/* Adam update of up to SGR_ADAM_MAX_TENSORS tensors in one launch, the
+ * surfel optimiser of scene/gaussian_model.py:266 (torch.optim.Adam, one
+ * learning rate per group, eps 1e-15).  `step` is a device float holding the
+ * step count; the call increments it first.  Never synchronises. */
+int sgr_adam_step(const sgr_adam_args* args, float* step, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -135,10 +135,133 @@ __device__ __forceinline__ void cell_list(const GeomView& g, int v, int tx, int 
 }  // namespace
 
 // ---------------------------------------------------------------------------
+// CTA shapes.  A thread owns PX pixels of one column, two rows apart, so a
+// warp covers a 16 x (2 PX) strip and a CTA of 256 / PX threads the tile.
+// The backward of the plain variant uses PX = 2: per-entry work (shared-
+// memory loads, the loop, the warp reduction of the gradients) is shared by
+// two pixels.  The forward keeps PX = 1: its pixels terminate independently
+// and it has no reduction to share; so does the part variant's backward,
+// whose 48 floats of per-pixel semantic state would not fit twice.
+// ---------------------------------------------------------------------------
+template <int PX_>
+struct BlendShape {
+  static constexpr int PX = PX_;                                      // pixels per thread
+  static constexpr int NT = kBlock / PX;                              // threads per CTA
+  static constexpr int NW = NT / 32;                                  // warps, one strip each
+  static constexpr int ROWS = kTile / NW;                             // strip height
+};
+using FwdShape = BlendShape<1>;
+template <int VARIANT>
+using BwdShape = BlendShape<(VARIANT == SGR_VARIANT_PLAIN) ? 2 : 1>;
+template <int VARIANT>
+constexpr int kSemSlots = (VARIANT == SGR_VARIANT_PART) ? SGR_MAX_SEMANTICS : 1;
+
+// Pixel i of a thread: column lane % 16, row ROWS * warp + lane / 16 + 2 i.
+template <class Shape>
+__device__ __forceinline__ void pixel_of(int tx, int ty, int lane, int warp, int i, int& px, int& py) {
+  px = tx * kTile + (lane & (kTile - 1));
+  py = ty * kTile + Shape::ROWS * warp + (lane >> 4) + 2 * i;
+}
+
+// ---------------------------------------------------------------------------
 // forward
 // ---------------------------------------------------------------------------
+// Per-pixel state of the forward recurrences (P0/cr/forward.cu:300-330).
 template <int VARIANT>
-__global__ void __launch_bounds__(kBlock) k_render_fwd(const sgr_batch b, GeomView g, sgr_fwd_outputs out) {
+struct FwdPixel {
+  float pxf, pyf;
+  bool done;
+  float T;
+  uint32_t last_contributor;
+  float C[3], N[3];
+  float D, M1, M2, dist, med_depth, med_weight;
+  int med_contrib;
+  float Sem[kSemSlots<VARIANT>];
+};
+
+// One fragment of the forward for one pixel: entry j of the staged batch,
+// list position contributor - 1 (P0/cr/forward.cu:349-430).
+template <int VARIANT>
+__device__ __forceinline__ void fwd_fragment(FwdPixel<VARIANT>& q, const float4 (*s_rec)[kBlock], const float* s_sem,
+                                             int j, uint32_t contributor, int S) {
+  if (q.done) return;
+  const float4 r0 = s_rec[0][j], r1 = s_rec[1][j], r2 = s_rec[2][j];
+  const V3 Tu = v3(r0.x, r0.y, r0.z), Tv = v3(r0.w, r1.x, r1.y), Tw = v3(r1.z, r1.w, r2.x);
+  V3 k, l;
+  if (VARIANT == SGR_VARIANT_PLAIN) {
+    k = q.pxf * Tw - Tu;
+    l = q.pyf * Tw - Tv;
+  } else {
+    k = v3(-Tu.x + q.pxf * Tw.x, -Tu.y + q.pxf * Tw.y, -Tu.z + q.pxf * Tw.z);
+    l = v3(-Tv.x + q.pyf * Tw.x, -Tv.y + q.pyf * Tw.y, -Tv.z + q.pyf * Tw.z);
+  }
+  const V3 p = cross3(k, l);
+  if (p.z == 0.0f) return;
+  const float dx = r2.y - q.pxf, dy = r2.z - q.pyf;
+  const float rho2d = kFilterInvSquareP0 * (dx * dx + dy * dy);
+  const float reach = s_rec[3][j].w;
+  if (rho2d > reach && p.x * p.x + p.y * p.y > reach * (p.z * p.z)) return;
+  const float sx = p.x / p.z, sy = p.y / p.z;
+  const float rho3d = sx * sx + sy * sy;
+  const float rho = fminf(rho3d, rho2d);
+  const float depth = (rho3d <= rho2d) ? (sx * Tw.x + sy * Tw.y) + Tw.z : Tw.z;
+  if (depth < kNearP0) return;
+  const float power = -0.5f * rho;
+  if (power > 0.0f) return;
+  const float alpha = fminf(0.99f, r2.w * expf(power));
+  if (alpha < 1.0f / 255.0f) return;
+  const float test_T = q.T * (1 - alpha);
+  if (test_T < 0.0001f) {
+    q.done = true;
+    return;
+  }
+  const float4 r3 = s_rec[3][j], r4 = s_rec[4][j];
+  const float A = 1 - q.T;
+  if (VARIANT == SGR_VARIANT_PLAIN) {
+    const float w = alpha * q.T;
+    const float m = kFarP0 / (kFarP0 - kNearP0) * (1 - kNearP0 / depth);
+    q.dist += (m * m * A + q.M2 - 2 * m * q.M1) * w;
+    q.D += depth * w;
+    q.M1 += m * w;
+    q.M2 += m * m * w;
+    if (q.T > 0.5f) {
+      q.med_depth = depth;
+      q.med_contrib = (int)contributor;
+    }
+    q.N[0] += r3.x * w;
+    q.N[1] += r3.y * w;
+    q.N[2] += r3.z * w;
+    q.C[0] += r4.x * w;
+    q.C[1] += r4.y * w;
+    q.C[2] += r4.z * w;
+  } else {
+    const float m = mapped_depth_p1(depth);
+    const float err = m * m * A + q.M2 - 2 * m * q.M1;
+    q.dist += err * alpha * q.T;
+    if (q.T > 0.5f) {
+      q.med_depth = depth;
+      q.med_weight = alpha * q.T;
+      q.med_contrib = (int)contributor;
+    }
+    q.N[0] += r3.x * alpha * q.T;
+    q.N[1] += r3.y * alpha * q.T;
+    q.N[2] += r3.z * alpha * q.T;
+    q.D += depth * alpha * q.T;
+    q.M1 += m * alpha * q.T;
+    q.M2 += m * m * alpha * q.T;
+    q.C[0] += r4.x * alpha * q.T;
+    q.C[1] += r4.y * alpha * q.T;
+    q.C[2] += r4.z * alpha * q.T;
+    for (int c = 0; c < S; ++c) q.Sem[c] += s_sem[c * kBlock + j] * alpha * q.T;
+  }
+  q.T = test_T;
+  q.last_contributor = contributor;
+}
+
+template <int VARIANT>
+__global__ void __launch_bounds__(FwdShape::NT) k_render_fwd(const sgr_batch b, GeomView g, sgr_fwd_outputs out) {
+  using Shape = FwdShape;
+  constexpr int PX = Shape::PX, NT = Shape::NT, NW = Shape::NW, ROWS = Shape::ROWS, NS = kSemSlots<VARIANT>;
   const int tiles_per_view = g.tiles_x * g.tiles_y;
   const int tile = blockIdx.x;
   const int v = tile / tiles_per_view;
@@ -146,11 +269,7 @@ __global__ void __launch_bounds__(kBlock) k_render_fwd(const sgr_batch b, GeomVi
   const int ty = t / g.tiles_x, tx = t - ty * g.tiles_x;
   const int W = b.width, H = b.height;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int px = tx * kTile + (threadIdx.x & (kTile - 1));
-  const int py = ty * kTile + (threadIdx.x / kTile);
-  const bool inside = px < W && py < H;
   const float off = (VARIANT == SGR_VARIANT_PLAIN) ? 0.0f : 0.5f;
-  const float pxf = (float)px + off, pyf = (float)py + off;
   const Strip strip{(float)(tx * kTile) + off, (float)(tx * kTile) + off + (kTile - 1), (float)(ty * kTile) + off};
   const int S = (VARIANT == SGR_VARIANT_PART) ? b.semantic_channels : 0;
   const sgr_view_desc vd = b.views[v];
@@ -158,8 +277,8 @@ __global__ void __launch_bounds__(kBlock) k_render_fwd(const sgr_batch b, GeomVi
 
   __shared__ float4 s_rec[kRecF4 - 1][kBlock];
   __shared__ uint8_t s_mask[kBlock];
-  __shared__ uint8_t s_list[kWarps][kBlock];
-  __shared__ float s_sem[(VARIANT == SGR_VARIANT_PART) ? SGR_MAX_SEMANTICS : 1][kBlock];
+  __shared__ uint8_t s_list[NW][kBlock];
+  __shared__ float s_sem[NS * kBlock];
   __shared__ uint32_t s_ring[kRing];
   __shared__ int s_count[32];
 
@@ -167,37 +286,47 @@ __global__ void __launch_bounds__(kBlock) k_render_fwd(const sgr_batch b, GeomVi
   int len;
   cell_list(g, v, tx, ty, list, len);
   int head = 0, tail = 0, scanned = 0, base = 0;
-  bool done = !inside;
 
-  float T = 1.0f;
-  uint32_t last_contributor = 0;
-  float C[3] = {0.f, 0.f, 0.f};
-  float N[3] = {0.f, 0.f, 0.f};
-  float D = 0.f, M1 = 0.f, M2 = 0.f, dist = 0.f, med_depth = 0.f, med_weight = 0.f;
-  int med_contrib = -1;
-  float Sem[SGR_MAX_SEMANTICS];
+  FwdPixel<VARIANT> q[PX];
+  bool done = true;                                // every pixel of this thread
 #pragma unroll
-  for (int c = 0; c < SGR_MAX_SEMANTICS; ++c) Sem[c] = 0.f;
+  for (int i = 0; i < PX; ++i) {
+    int px, py;
+    pixel_of<Shape>(tx, ty, lane, warp, i, px, py);
+    FwdPixel<VARIANT>& Q = q[i];
+    Q.pxf = (float)px + off;
+    Q.pyf = (float)py + off;
+    Q.done = !(px < W && py < H);
+    Q.T = 1.0f;
+    Q.last_contributor = 0;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) Q.C[c] = Q.N[c] = 0.f;
+    Q.D = Q.M1 = Q.M2 = Q.dist = Q.med_depth = Q.med_weight = 0.f;
+    Q.med_contrib = -1;
+#pragma unroll
+    for (int c = 0; c < NS; ++c) Q.Sem[c] = 0.f;
+    done = done && Q.done;
+  }
 
   for (;; base += kBlock, head += kBlock) {
-    if (__syncthreads_count(done) == kBlock) break;
+    if (__syncthreads_count(done) == NT) break;
     while (tail - head < kBlock && scanned < len) {   // refill the ring (CTA-uniform)
       int found;
-      tail += stream_window<false, kBlock>(g, list, scanned, min(scanned + kChunk, len), (uint32_t)tx, (uint32_t)ty, 0, 0,
-                                   s_ring, tail, s_count, found);
+      tail += stream_window<false, NT>(g, list, scanned, min(scanned + kChunk, len), (uint32_t)tx, (uint32_t)ty, 0,
+                                       0, s_ring, tail, s_count, found);
       scanned = min(scanned + kChunk, len);
     }
     const int n = min(kBlock, tail - head);
     if (n <= 0) break;
-    if ((int)threadIdx.x < n) {
-      const uint32_t r = s_ring[(head + threadIdx.x) & (kRing - 1)];
+    for (int e = threadIdx.x; e < n; e += NT) {
+      const uint32_t r = s_ring[(head + e) & (kRing - 1)];
       const float4* rec = g.records + (size_t)r * kRecF4;
 #pragma unroll
-      for (int k = 0; k < kRecF4 - 1; ++k) s_rec[k][threadIdx.x] = rec[k];
-      s_mask[threadIdx.x] = (uint8_t)strip_mask<2, kWarps>(rec[5], strip);
+      for (int k = 0; k < kRecF4 - 1; ++k) s_rec[k][e] = rec[k];
+      s_mask[e] = (uint8_t)strip_mask<ROWS, NW>(rec[5], strip);
       if (VARIANT == SGR_VARIANT_PART) {
         const float* sem = b.semantics + (size_t)(sid_base + (int)r) * S;
-        for (int c = 0; c < S; ++c) s_sem[c][threadIdx.x] = sem[c];
+        for (int c = 0; c < S; ++c) s_sem[c * kBlock + e] = sem[c];
       }
     }
     __syncthreads();
@@ -205,109 +334,49 @@ __global__ void __launch_bounds__(kBlock) k_render_fwd(const sgr_batch b, GeomVi
     for (int si = 0; !done && si < cnt; ++si) {
       const int j = s_list[warp][si];
       const uint32_t contributor = (uint32_t)(base + j + 1);
-      const float4 r0 = s_rec[0][j], r1 = s_rec[1][j], r2 = s_rec[2][j];
-      const V3 Tu = v3(r0.x, r0.y, r0.z), Tv = v3(r0.w, r1.x, r1.y), Tw = v3(r1.z, r1.w, r2.x);
-      V3 k, l;
-      if (VARIANT == SGR_VARIANT_PLAIN) {
-        k = pxf * Tw - Tu;
-        l = pyf * Tw - Tv;
-      } else {
-        k = v3(-Tu.x + pxf * Tw.x, -Tu.y + pxf * Tw.y, -Tu.z + pxf * Tw.z);
-        l = v3(-Tv.x + pyf * Tw.x, -Tv.y + pyf * Tw.y, -Tv.z + pyf * Tw.z);
+      done = true;
+#pragma unroll
+      for (int i = 0; i < PX; ++i) {
+        fwd_fragment<VARIANT>(q[i], s_rec, s_sem, j, contributor, S);
+        done = done && q[i].done;
       }
-      const V3 p = cross3(k, l);
-      if (p.z == 0.0f) continue;
-      const float dx = r2.y - pxf, dy = r2.z - pyf;
-      const float rho2d = kFilterInvSquareP0 * (dx * dx + dy * dy);
-      const float reach = s_rec[3][j].w;
-      if (rho2d > reach && p.x * p.x + p.y * p.y > reach * (p.z * p.z)) continue;
-      const float sx = p.x / p.z, sy = p.y / p.z;
-      const float rho3d = sx * sx + sy * sy;
-      const float rho = fminf(rho3d, rho2d);
-      const float depth = (rho3d <= rho2d) ? (sx * Tw.x + sy * Tw.y) + Tw.z : Tw.z;
-      if (depth < kNearP0) continue;
-      const float power = -0.5f * rho;
-      if (power > 0.0f) continue;
-      const float alpha = fminf(0.99f, r2.w * expf(power));
-      if (alpha < 1.0f / 255.0f) continue;
-      const float test_T = T * (1 - alpha);
-      if (test_T < 0.0001f) {
-        done = true;
-        continue;
-      }
-      const float4 r3 = s_rec[3][j], r4 = s_rec[4][j];
-      const float A = 1 - T;
-      if (VARIANT == SGR_VARIANT_PLAIN) {
-        const float w = alpha * T;
-        const float m = kFarP0 / (kFarP0 - kNearP0) * (1 - kNearP0 / depth);
-        dist += (m * m * A + M2 - 2 * m * M1) * w;
-        D += depth * w;
-        M1 += m * w;
-        M2 += m * m * w;
-        if (T > 0.5f) {
-          med_depth = depth;
-          med_contrib = (int)contributor;
-        }
-        N[0] += r3.x * w;
-        N[1] += r3.y * w;
-        N[2] += r3.z * w;
-        C[0] += r4.x * w;
-        C[1] += r4.y * w;
-        C[2] += r4.z * w;
-      } else {
-        const float m = mapped_depth_p1(depth);
-        const float err = m * m * A + M2 - 2 * m * M1;
-        dist += err * alpha * T;
-        if (T > 0.5f) {
-          med_depth = depth;
-          med_weight = alpha * T;
-          med_contrib = (int)contributor;
-        }
-        N[0] += r3.x * alpha * T;
-        N[1] += r3.y * alpha * T;
-        N[2] += r3.z * alpha * T;
-        D += depth * alpha * T;
-        M1 += m * alpha * T;
-        M2 += m * m * alpha * T;
-        C[0] += r4.x * alpha * T;
-        C[1] += r4.y * alpha * T;
-        C[2] += r4.z * alpha * T;
-        for (int c = 0; c < S; ++c) Sem[c] += s_sem[c][j] * alpha * T;
-      }
-      T = test_T;
-      last_contributor = contributor;
     }
   }
 
   if (threadIdx.x == 0) g.tile_resume[tile] = make_uint2((uint32_t)scanned, (uint32_t)tail);
-  if (inside) {
-    const size_t HW = (size_t)H * W;
+  const size_t HW = (size_t)H * W;
+  const float* bg = b.background;
+  const int NO = (VARIANT == SGR_VARIANT_PLAIN) ? 7 : 8;
+#pragma unroll
+  for (int i = 0; i < PX; ++i) {
+    int px, py;
+    pixel_of<Shape>(tx, ty, lane, warp, i, px, py);
+    if (!(px < W && py < H)) continue;
+    const FwdPixel<VARIANT>& Q = q[i];
     const size_t pix = (size_t)py * W + px;
     float* fT = g.final_T + (size_t)v * 3 * HW;
     uint32_t* nc = g.n_contrib + (size_t)v * 2 * HW;
-    fT[pix] = T;
-    fT[pix + HW] = M1;
-    fT[pix + 2 * HW] = M2;
-    nc[pix] = last_contributor;
-    nc[pix + HW] = med_contrib > 0 ? (uint32_t)med_contrib : 0u;
-    const float* bg = b.background;
+    fT[pix] = Q.T;
+    fT[pix + HW] = Q.M1;
+    fT[pix + 2 * HW] = Q.M2;
+    nc[pix] = Q.last_contributor;
+    nc[pix + HW] = Q.med_contrib > 0 ? (uint32_t)Q.med_contrib : 0u;
     float* col = out.color + (size_t)v * 3 * HW;
-    col[pix] = C[0] + T * bg[0];
-    col[pix + HW] = C[1] + T * bg[1];
-    col[pix + 2 * HW] = C[2] + T * bg[2];
-    const int NO = (VARIANT == SGR_VARIANT_PLAIN) ? 7 : 8;
+    col[pix] = Q.C[0] + Q.T * bg[0];
+    col[pix + HW] = Q.C[1] + Q.T * bg[1];
+    col[pix + 2 * HW] = Q.C[2] + Q.T * bg[2];
     float* oth = out.others + (size_t)v * NO * HW;
-    oth[pix] = D;
-    oth[pix + HW] = 1 - T;
-    oth[pix + 2 * HW] = N[0];
-    oth[pix + 3 * HW] = N[1];
-    oth[pix + 4 * HW] = N[2];
-    oth[pix + 5 * HW] = med_depth;
-    oth[pix + 6 * HW] = dist;
+    oth[pix] = Q.D;
+    oth[pix + HW] = 1 - Q.T;
+    oth[pix + 2 * HW] = Q.N[0];
+    oth[pix + 3 * HW] = Q.N[1];
+    oth[pix + 4 * HW] = Q.N[2];
+    oth[pix + 5 * HW] = Q.med_depth;
+    oth[pix + 6 * HW] = Q.dist;
     if (VARIANT == SGR_VARIANT_PART) {
-      oth[pix + 7 * HW] = med_weight;
+      oth[pix + 7 * HW] = Q.med_weight;
       float* sem = out.semantic + (size_t)v * S * HW;
-      for (int c = 0; c < S; ++c) sem[pix + c * HW] = Sem[c];
+      for (int c = 0; c < S; ++c) sem[pix + c * HW] = Q.Sem[c];
     }
   }
 }
@@ -329,19 +398,12 @@ __global__ void __launch_bounds__(kBlock) k_render_fwd(const sgr_batch b, GeomVi
 // total to the per-view gradient record (one atomic per value and warp
 // instead of one per value and pixel).
 // ---------------------------------------------------------------------------
-template <int VARIANT>
-struct BwdShape {
-  static constexpr int PX = (VARIANT == SGR_VARIANT_PLAIN) ? 2 : 1;   // pixels per thread
-  static constexpr int NT = kBlock / PX;                              // threads per CTA
-  static constexpr int NW = NT / 32;                                  // warps, one strip each
-  static constexpr int ROWS = kTile / NW;                             // strip height
-  static constexpr int NS = (VARIANT == SGR_VARIANT_PART) ? SGR_MAX_SEMANTICS : 1;
-};
+static_assert(kGradUsed == 18, "warp_sum18 reduces the 18 gradient values of a fragment");
 
 // Per-pixel state of the backward recurrences (P0/cr/backward.cu:160-260).
 template <int VARIANT>
 struct BwdPixel {
-  static constexpr int NS = BwdShape<VARIANT>::NS;
+  static constexpr int NS = kSemSlots<VARIANT>;
   float pxf, pyf;
   float T, T_final, final_A, final_D, final_D2, bg_dot;
   int last_contributor, median_contributor;
@@ -474,7 +536,7 @@ __global__ void __launch_bounds__(BwdShape<VARIANT>::NT) k_render_bwd(const sgr_
                                                                       float* __restrict__ grads,
                                                                       float* __restrict__ dL_dsemantics) {
   using Shape = BwdShape<VARIANT>;
-  constexpr int PX = Shape::PX, NT = Shape::NT, NW = Shape::NW, ROWS = Shape::ROWS, NS = Shape::NS;
+  constexpr int PX = Shape::PX, NT = Shape::NT, NW = Shape::NW, ROWS = Shape::ROWS, NS = kSemSlots<VARIANT>;
   const int tiles_per_view = g.tiles_x * g.tiles_y;
   const int tile = blockIdx.x;
   const int v = tile / tiles_per_view;
@@ -505,14 +567,13 @@ __global__ void __launch_bounds__(BwdShape<VARIANT>::NT) k_render_bwd(const sgr_
   const float* doth = in.dL_dothers + (size_t)v * NO * HW;
   const float* bg = b.background;
 
-  // pixel i of this thread: column lane % 16, row ROWS * warp + lane / 16 + 2 i
   BwdPixel<VARIANT> q[PX];
   int thread_max = 0;
 #pragma unroll
   for (int i = 0; i < PX; ++i) {
     BwdPixel<VARIANT>& Q = q[i];
-    const int px = tx * kTile + (lane & (kTile - 1));
-    const int py = ty * kTile + ROWS * warp + (lane >> 4) + 2 * i;
+    int px, py;
+    pixel_of<Shape>(tx, ty, lane, warp, i, px, py);
     const bool inside = px < W && py < H;
     const size_t pix = inside ? (size_t)py * W + px : 0;
     Q.pxf = (float)px + off;
@@ -605,9 +666,10 @@ __global__ void __launch_bounds__(BwdShape<VARIANT>::NT) k_render_bwd(const sgr_
 #pragma unroll
       for (int i = 0; i < PX; ++i) ok |= bwd_fragment<VARIANT>(q[i], s_rec, s_sem, j, pos, S, gv, gsem);
       if (__any_sync(0xffffffffu, ok)) {
-        const float total = warp_transpose_sum(gv, lane);
+        int which;
+        const float total = warp_sum18(gv, lane, which);
         const uint32_t r = s_id[j];
-        if (lane < kGradUsed && total != 0.f) atomicAdd(grads + (size_t)r * kGradF + lane, total);
+        if (which >= 0 && total != 0.f) atomicAdd(grads + (size_t)r * kGradF + which, total);
         if (VARIANT == SGR_VARIANT_PART && S > 0) {
           const float st = warp_transpose_sum(gsem, lane);
           if (lane < S && st != 0.f) atomicAdd(dL_dsemantics + (size_t)(sid_base + (int)r) * S + lane, st);
@@ -620,8 +682,10 @@ __global__ void __launch_bounds__(BwdShape<VARIANT>::NT) k_render_bwd(const sgr_
 void launch_render_fwd(const sgr_batch& b, const GeomView& g, const sgr_fwd_outputs& out, cudaStream_t st) {
   const unsigned blocks = (unsigned)(g.tiles_x * g.tiles_y) * (unsigned)b.num_views;
   if (blocks == 0) return;
-  if (b.variant == SGR_VARIANT_PLAIN) k_render_fwd<SGR_VARIANT_PLAIN><<<blocks, kBlock, 0, st>>>(b, g, out);
-  else k_render_fwd<SGR_VARIANT_PART><<<blocks, kBlock, 0, st>>>(b, g, out);
+  if (b.variant == SGR_VARIANT_PLAIN)
+    k_render_fwd<SGR_VARIANT_PLAIN><<<blocks, FwdShape::NT, 0, st>>>(b, g, out);
+  else
+    k_render_fwd<SGR_VARIANT_PART><<<blocks, FwdShape::NT, 0, st>>>(b, g, out);
   count_launches();
 }
 

@@ -178,6 +178,48 @@ __device__ __forceinline__ float warp_transpose_sum(float (&v)[32], int lane) {
   return v[0];
 }
 
+// One halving step of a warp reduction of N values per lane over lane bit
+// o: with h = ceil(N / 2), lanes with the bit clear keep values [0, h) and
+// lanes with it set keep values [h, N) (renumbered from 0, plus a zero when
+// N is odd), each adding its partner's copy.  h shuffles.
+template <int N>
+__device__ __forceinline__ void fold_half(float (&v)[32], bool upper, int o) {
+  constexpr int h = (N + 1) / 2;
+#pragma unroll
+  for (int k = 0; k < h; ++k) {
+    const float a = v[k];
+    const float b = (k + h < N) ? v[k + h] : 0.0f;
+    const float send = upper ? a : b;
+    const float keep = upper ? b : a;
+    v[k] = keep + __shfl_xor_sync(0xffffffffu, send, o);
+  }
+}
+
+// Warp sum of values 0..17 of every lane with uneven halvings (18, 9, 5, 3,
+// 2 values: 20 shuffles instead of the 31 of a full transpose).  Afterwards
+// 18 lanes each hold one total; `index` is the value a lane holds, -1 for
+// the other 14.
+__device__ __forceinline__ float warp_sum18(float (&v)[32], int lane, int& index) {
+  fold_half<18>(v, (lane & 16) != 0, 16);
+  fold_half<9>(v, (lane & 8) != 0, 8);
+  fold_half<5>(v, (lane & 4) != 0, 4);
+  fold_half<3>(v, (lane & 2) != 0, 2);
+  fold_half<2>(v, (lane & 1) != 0, 1);
+  // each halving maps a kept slot s to value s + h when the lane bit is set
+  int i = lane & 1;
+  bool ok = true;
+  i += 2 * ((lane >> 1) & 1);
+  ok &= i < 3;
+  i += 3 * ((lane >> 2) & 1);
+  ok &= i < 5;
+  i += 5 * ((lane >> 3) & 1);
+  ok &= i < 9;
+  i += 9 * ((lane >> 4) & 1);
+  ok &= i < 18;
+  index = ok ? i : -1;
+  return v[0];
+}
+
 void launch_preprocess(const sgr_batch& b, const GeomView& g, cudaStream_t st);
 void launch_store_key_count(const GeomView& g, long long R, cudaStream_t st);
 // Cell lists (sgr_binning.cu).  binning_supported is false for tile grids

@@ -5,7 +5,8 @@ to every view of a batch at once: rasterise, L1 + D-SSIM photometric loss
 (utils/loss_utils.py:8-54), depth-distortion loss, and the normal-consistency
 loss between rendered normals and normals from the median depth map
 (renderer/gaussian_renderer/__init__.py:111-141, utils/point_utils.py:4-33),
-then an Adam update (scene/gaussian_model.py:266, eps 1e-15).  Parameters use
+then an Adam update (scene/gaussian_model.py:266, eps 1e-15; one launch,
+optim.py).  Parameters use
 the reference's activations: exp scales, normalised quaternions, sigmoid
 opacity, concatenated SH features (scene/gaussian_model.py:198-218).
 
@@ -21,6 +22,7 @@ import torch.nn.functional as F
 
 from . import _lib
 from .batched import MultiViewRasterizer
+from .optim import SurfelAdam
 
 
 def _gaussian_window(size=11, sigma=1.5, channels=3, device="cuda"):
@@ -115,7 +117,7 @@ class SurfelTrainer:
             {"params": [self.log_scaling], "lr": 0.005},
             {"params": [self.rotation], "lr": 0.001},
         ]
-        self.opt = torch.optim.Adam(groups, lr=0.0, eps=1e-15, fused=True, capturable=True)
+        self.opt = SurfelAdam(groups, eps=1e-15)
         self.targets = None
         self.graph = None
         self.loss = None
@@ -149,11 +151,11 @@ class SurfelTrainer:
         return loss + dist_loss + normal_loss
 
     def step(self, targets):
-        """One eager step; returns the loss tensor."""
+        """One eager step; returns the loss tensor.  The optimiser clears the
+        gradients it consumes."""
         loss = self.loss_fn(targets)
         loss.backward()
         self.opt.step()
-        self.opt.zero_grad(set_to_none=False)
         return loss
 
     def capture(self, targets, warmup=3, headroom=1.25):
@@ -187,21 +189,17 @@ class SurfelTrainer:
         self.graph.replay()
         return self.loss
 
+    def _state(self):
+        return [p.detach() for p in self.params()] + self.opt.state_tensors()
+
     def snapshot(self):
         """Copies of the parameters and the optimiser state."""
-        state = [p.detach().clone() for p in self.params()]
-        for p in self.params():
-            st = self.opt.state.get(p, {})
-            state += [v.detach().clone() for _, v in sorted(st.items()) if torch.is_tensor(v)]
-        return state
+        return [t.clone() for t in self._state()]
 
     def restore(self, state):
         """Writes a snapshot back in place (captured graphs keep their
         addresses)."""
-        dst = [p.detach() for p in self.params()]
-        for p in self.params():
-            st = self.opt.state.get(p, {})
-            dst += [v for _, v in sorted(st.items()) if torch.is_tensor(v)]
+        dst = self._state()
         if len(dst) != len(state):
             raise ValueError("snapshot does not match the optimiser state")
         with torch.no_grad():
