@@ -414,41 +414,63 @@ struct BwdPixel {
   float dsem_pix[NS], accum_sem[NS], last_sem[NS];
 };
 
-// One fragment of the backward for one pixel: entry j of the staged batch at
-// list position pos.  Adds this pixel's share of the entry's 18 gradient
-// values to gv (and of its semantic gradients to gsem); false when the
+// Geometry of one backward fragment (P0/cr/backward.cu:290-330): the
+// ray-splat intersection, alpha and the tests, computed without branches so
+// that the two pixels of a thread interleave.  `live` is false when the
 // fragment contributes nothing.
-template <int VARIANT>
-__device__ __forceinline__ bool bwd_fragment(BwdPixel<VARIANT>& q, const float4 (*s_rec)[kBlock], const float* s_sem,
-                                             int j, int pos, int S, float (&gv)[32], float (&gsem)[32]) {
-  if (pos >= q.last_contributor) return false;
-  const float4 r0 = s_rec[0][j], r1 = s_rec[1][j], r2 = s_rec[2][j];
-  const V3 Tu = v3(r0.x, r0.y, r0.z), Tv = v3(r0.w, r1.x, r1.y), Tw = v3(r1.z, r1.w, r2.x);
-  V3 k, l;
-  if (VARIANT == SGR_VARIANT_PLAIN) {
-    k = q.pxf * Tw - Tu;
-    l = q.pyf * Tw - Tv;
-  } else {
-    k = v3(-Tu.x + q.pxf * Tw.x, -Tu.y + q.pxf * Tw.y, -Tu.z + q.pxf * Tw.z);
-    l = v3(-Tv.x + q.pyf * Tw.x, -Tv.y + q.pyf * Tw.y, -Tv.z + q.pyf * Tw.z);
-  }
-  const V3 p = cross3(k, l);
-  const float dx = r2.y - q.pxf, dy = r2.z - q.pyf;
-  const float rho2d = kFilterInvSquareP0 * (dx * dx + dy * dy);
-  const float reach = s_rec[3][j].w;
-  if (p.z == 0.0f || (rho2d > reach && p.x * p.x + p.y * p.y > reach * (p.z * p.z))) return false;
-  // the same divisions as the forward, so alpha and the tests agree bit for bit
-  const float sx = p.x / p.z, sy = p.y / p.z;
-  const float rho3d = sx * sx + sy * sy;
-  const bool use3d = rho3d <= rho2d;
-  const float rho = fminf(rho3d, rho2d);
-  const float c_d = use3d ? (sx * Tw.x + sy * Tw.y) + Tw.z : Tw.z;
-  const float power = -0.5f * rho;
-  const float G = expf(power);
-  const float alpha = fminf(0.99f, r2.w * G);
-  if (c_d < kNearP0 || power > 0.0f || alpha < 1.0f / 255.0f) return false;
+struct BwdGeom {
+  V3 k, l, p;
+  float sx, sy, dx, dy, G, alpha, c_d;
+  bool use3d, live;
+};
 
-  const float4 r3 = s_rec[3][j], r4 = s_rec[4][j];
+// Stage 1: the reach test; true when the fragment may contribute.
+template <int VARIANT>
+__device__ __forceinline__ bool bwd_reach(const BwdPixel<VARIANT>& q, const float4& r0, const float4& r1,
+                                          const float4& r2, float reach, int pos, BwdGeom& f) {
+  const V3 Tu = v3(r0.x, r0.y, r0.z), Tv = v3(r0.w, r1.x, r1.y), Tw = v3(r1.z, r1.w, r2.x);
+  if (VARIANT == SGR_VARIANT_PLAIN) {
+    f.k = q.pxf * Tw - Tu;
+    f.l = q.pyf * Tw - Tv;
+  } else {
+    f.k = v3(-Tu.x + q.pxf * Tw.x, -Tu.y + q.pxf * Tw.y, -Tu.z + q.pxf * Tw.z);
+    f.l = v3(-Tv.x + q.pyf * Tw.x, -Tv.y + q.pyf * Tw.y, -Tv.z + q.pyf * Tw.z);
+  }
+  f.p = cross3(f.k, f.l);
+  f.dx = r2.y - q.pxf;
+  f.dy = r2.z - q.pyf;
+  const float rho2d = kFilterInvSquareP0 * (f.dx * f.dx + f.dy * f.dy);
+  f.live = pos < q.last_contributor && f.p.z != 0.0f &&
+           !(rho2d > reach && f.p.x * f.p.x + f.p.y * f.p.y > reach * (f.p.z * f.p.z));
+  return f.live;
+}
+
+// Stage 2: alpha and the remaining tests, with the forward's divisions so
+// that alpha and the tests agree with it bit for bit.
+__device__ __forceinline__ void bwd_alpha(const float4& r1, const float4& r2, BwdGeom& f) {
+  const float Twx = r1.z, Twy = r1.w, Twz = r2.x;
+  const float pz = f.live ? f.p.z : 1.0f;
+  f.sx = f.p.x / pz;
+  f.sy = f.p.y / pz;
+  const float rho3d = f.sx * f.sx + f.sy * f.sy;
+  const float rho2d = kFilterInvSquareP0 * (f.dx * f.dx + f.dy * f.dy);
+  f.use3d = rho3d <= rho2d;
+  const float rho = fminf(rho3d, rho2d);
+  f.c_d = f.use3d ? (f.sx * Twx + f.sy * Twy) + Twz : Twz;
+  const float power = -0.5f * rho;
+  f.G = expf(power);
+  f.alpha = fminf(0.99f, r2.w * f.G);
+  f.live = f.live && !(f.c_d < kNearP0) && !(power > 0.0f) && !(f.alpha < 1.0f / 255.0f);
+}
+
+// Stage 3: the pixel's recurrences and its share of the entry's 18 gradient
+// values (gv) and semantic gradients (gsem), for a live fragment.
+template <int VARIANT>
+__device__ __forceinline__ void bwd_update(BwdPixel<VARIANT>& q, const BwdGeom& f, const float4& r1, const float4& r2,
+                                           const float4& r3, const float4& r4, const float* s_sem, int j, int pos,
+                                           int S, float (&gv)[32], float (&gsem)[32]) {
+  const float Twx = r1.z, Twy = r1.w;
+  const float alpha = f.alpha, G = f.G, c_d = f.c_d;
   const float inv_1ma = __frcp_rn(1.f - alpha);
   q.T = q.T * inv_1ma;
   const float wgt = alpha * q.T;
@@ -506,32 +528,38 @@ __device__ __forceinline__ bool bwd_fragment(BwdPixel<VARIANT>& q, const float4 
   dL_dalpha += (-q.T_final * inv_1ma) * q.bg_dot;
   const float dL_dG = r2.w * dL_dalpha;
   dL_dz += alpha * q.T * q.dL_ddepth;
-  if (use3d) {
-    const float inv_pz = __frcp_rn(p.z);
-    const float dsx_pz = (dL_dG * -G * sx + dL_dz * Tw.x) * inv_pz;
-    const float dsy_pz = (dL_dG * -G * sy + dL_dz * Tw.y) * inv_pz;
-    const V3 dL_dp = v3(dsx_pz, dsy_pz, -(dsx_pz * sx + dsy_pz * sy));
-    const V3 dL_dk = cross3(l, dL_dp);
-    const V3 dL_dl = cross3(dL_dp, k);
+  if (f.use3d) {
+    const float inv_pz = __frcp_rn(f.p.z);
+    const float dsx_pz = (dL_dG * -G * f.sx + dL_dz * Twx) * inv_pz;
+    const float dsy_pz = (dL_dG * -G * f.sy + dL_dz * Twy) * inv_pz;
+    const V3 dL_dp = v3(dsx_pz, dsy_pz, -(dsx_pz * f.sx + dsy_pz * f.sy));
+    const V3 dL_dk = cross3(f.l, dL_dp);
+    const V3 dL_dl = cross3(dL_dp, f.k);
     gv[0] -= dL_dk.x; gv[1] -= dL_dk.y; gv[2] -= dL_dk.z;
     gv[3] -= dL_dl.x; gv[4] -= dL_dl.y; gv[5] -= dL_dl.z;
-    gv[6] += q.pxf * dL_dk.x + q.pyf * dL_dl.x + dL_dz * sx;
-    gv[7] += q.pxf * dL_dk.y + q.pyf * dL_dl.y + dL_dz * sy;
+    gv[6] += q.pxf * dL_dk.x + q.pyf * dL_dl.x + dL_dz * f.sx;
+    gv[7] += q.pxf * dL_dk.y + q.pyf * dL_dl.y + dL_dz * f.sy;
     gv[8] += q.pxf * dL_dk.z + q.pyf * dL_dl.z + dL_dz * 1.0f;
   } else {
-    gv[9] += dL_dG * (-G * kFilterInvSquareP0 * dx);
-    gv[10] += dL_dG * (-G * kFilterInvSquareP0 * dy);
+    gv[9] += dL_dG * (-G * kFilterInvSquareP0 * f.dx);
+    gv[10] += dL_dG * (-G * kFilterInvSquareP0 * f.dy);
     gv[8] += dL_dz;
   }
   gv[17] += G * dL_dalpha;
   if (VARIANT == SGR_VARIANT_PART) {
     for (int c = 0; c < S; ++c) gsem[c] += wgt * q.dsem_pix[c];
   }
-  return true;
 }
 
+// Resident CTAs per SM the plain backward is compiled for (registers per
+// thread = 65536 / (128 threads x this)).
+#ifndef SGR_BWD_MIN_CTAS
+#define SGR_BWD_MIN_CTAS 4
+#endif
+
 template <int VARIANT>
-__global__ void __launch_bounds__(BwdShape<VARIANT>::NT) k_render_bwd(const sgr_batch b, GeomView g,
+__global__ void __launch_bounds__(BwdShape<VARIANT>::NT, (VARIANT == SGR_VARIANT_PLAIN) ? SGR_BWD_MIN_CTAS : 1)
+    k_render_bwd(const sgr_batch b, GeomView g,
                                                                       const sgr_bwd_inputs in,
                                                                       float* __restrict__ grads,
                                                                       float* __restrict__ dL_dsemantics) {
@@ -662,10 +690,25 @@ __global__ void __launch_bounds__(BwdShape<VARIANT>::NT) k_render_bwd(const sgr_
       float gsem[32];
 #pragma unroll
       for (int u = 0; u < 32; ++u) gsem[u] = 0.f;
+      const float4 r0 = s_rec[0][j], r1 = s_rec[1][j], r2 = s_rec[2][j];
+      const float reach = s_rec[3][j].w;
+      BwdGeom f[PX];
+      bool may = false;
+#pragma unroll
+      for (int i = 0; i < PX; ++i) may |= bwd_reach<VARIANT>(q[i], r0, r1, r2, reach, pos, f[i]);
+      if (!__any_sync(0xffffffffu, may)) continue;  // uniform: no pixel of the warp within reach
       bool ok = false;
 #pragma unroll
-      for (int i = 0; i < PX; ++i) ok |= bwd_fragment<VARIANT>(q[i], s_rec, s_sem, j, pos, S, gv, gsem);
-      if (__any_sync(0xffffffffu, ok)) {
+      for (int i = 0; i < PX; ++i) {
+        bwd_alpha(r1, r2, f[i]);
+        ok |= f[i].live;
+      }
+      if (!__any_sync(0xffffffffu, ok)) continue;
+      const float4 r3 = s_rec[3][j], r4 = s_rec[4][j];
+#pragma unroll
+      for (int i = 0; i < PX; ++i)
+        if (f[i].live) bwd_update<VARIANT>(q[i], f[i], r1, r2, r3, r4, s_sem, j, pos, S, gv, gsem);
+      {
         int which;
         const float total = warp_sum18(gv, lane, which);
         const uint32_t r = s_id[j];
