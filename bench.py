@@ -55,7 +55,7 @@ def _workload_config(name):
         return {"workload": name, "surfels": 500_000, "views": 16, "height": 600, "width": 800, "fovx_deg": 50,
                 "sh_degree": 3, "loss": "0.8 L1 + 0.2 D-SSIM + 1000 distortion + 0.05 normal consistency",
                 "optimizer": "Adam (fused, capturable)", "cuda_graph": True,
-                "l2": "per-step working set (key lists, per-view records) far larger than the 129 MB L2"}
+                "l2": "per-step working set (per-view records, cell lists, images, gradients) far larger than the 129 MB L2"}
     return {"workload": name}
 
 
