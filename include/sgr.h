@@ -351,6 +351,42 @@ typedef struct sgr_adam_args {
  * step count; the call increments it first.  Never synchronises. */
 int sgr_adam_step(const sgr_adam_args* args, float* step, void* stream);
 
+/* ---- proposal network: BF16 tensor-core GEMM --------------------------- */
+
+/* Epilogues of sgr_mlp_gemm (x = accumulator + bias) */
+#define SGR_GEMM_STORE_F32 0   /* out[m,n] = x (fp32) */
+#define SGR_GEMM_ADD_F32 1     /* out[m,n] += x (fp32, atomic; with split_k) */
+#define SGR_GEMM_RELU_BF16 2   /* out[m,n] = bf16(max(x, 0)) */
+#define SGR_GEMM_MASK_BF16 3   /* out[m,n] = bf16(mask[m,n] > 0 ? x : 0): a ReLU's backward */
+#define SGR_MLP_TIMEOUT 1u     /* status bit: a wait for the tensor cores ran out */
+
+/* C[M,N] = A[M,K] . B[N,K]^T with bf16 operands, fp32 accumulation.  A is
+ * row-major with K contiguous (lda elements per row) or, with a_trans, its
+ * transpose (K rows of M contiguous values); likewise B (a_trans and b_trans
+ * must agree).  Strides are multiples of 8 and bases 16-byte aligned. */
+typedef struct sgr_gemm_args {
+    int64_t M, N, K;
+    const void* A;               /* bf16 */
+    int64_t lda;
+    int32_t a_trans;
+    const void* B;               /* bf16 */
+    int64_t ldb;
+    int32_t b_trans;
+    const float* bias;           /* [N] or NULL */
+    int32_t epilogue;            /* SGR_GEMM_* */
+    void* out;
+    int64_t ldo;
+    const void* mask;            /* bf16 [M, ldmask], SGR_GEMM_MASK_BF16 only */
+    int64_t ldmask;
+    int64_t split_k;             /* 0, or K per CTA (a multiple of 64; SGR_GEMM_ADD_F32) */
+    uint32_t* status;            /* device word, OR-ed with SGR_MLP_TIMEOUT */
+} sgr_gemm_args;
+
+/* The GEMM of the point-set proposal network's layers and their backward
+ * (no counterpart in the reference: the network is new).  tcgen05 MMA with
+ * tensor-memory accumulators; never synchronises. */
+int sgr_mlp_gemm(const sgr_gemm_args* args, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,289 @@
+// BF16 tensor-core GEMM for the superquadric proposal network (tcgen05, FP32
+// accumulation in tensor memory), with the epilogues its forward and
+// backward need.
+//
+//   C[M, N] = A[M, K] . B[N, K]^T        (A, B bf16; C accumulated in fp32)
+//
+// A is given K-major (row m holds K contiguous values) or, with a_trans,
+// transposed (row k holds M contiguous values); likewise B.  The transposed
+// forms serve the weight gradient dW = X^T dZ, whose reduction runs over the
+// point rows.
+//
+// One CTA of 128 threads computes a 128 x NT tile (NT = 64, 128 or 256).
+// Per K chunk of 64, all threads stage the A and B chunks in shared memory
+// in the no-swizzle K-major core-matrix layout (8 rows x 16 bytes per core
+// matrix; core matrices adjacent in K 128 bytes apart, 8-row groups 1024
+// bytes apart), one thread issues four tcgen05.mma (K = 16 each) into the
+// tensor-memory accumulator (lane = row, column = output column) and commits
+// them to an mbarrier, which every thread waits on before the stage is
+// reused.  The epilogue reads the accumulator with tcgen05.ld, 32 lanes per
+// warp, 16 columns at a time.  With split_k > 0 each CTA reduces one slice of
+// K and adds its partial tile atomically (fp32).
+//
+// Every wait is bounded: on timeout the kernel raises SGR_MLP_TIMEOUT in the
+// status word, waits once more (bounded) for its own MMAs, frees its tensor
+// memory and returns.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "../../include/sgr.h"
+
+namespace sgr {
+void count_launches(int n);   // sgr_api.cu
+}  // namespace sgr
+
+namespace sgrmlp {
+
+constexpr int kTM = 128;        // rows per CTA tile (= tensor-memory lanes)
+constexpr int kKC = 64;         // K per shared-memory chunk
+constexpr int kThreads = 128;
+constexpr unsigned kWaitLimit = 1u << 26;
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+// Shared-memory matrix descriptor: no swizzle, K-major, start address and
+// the two core-matrix strides (bytes, multiples of 16), descriptor version 1.
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+  return (uint64_t)((addr & 0x3FFFFu) >> 4) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+         ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+
+// Instruction descriptor of kind::f16: fp32 accumulator, bf16 A and B, both
+// K-major, M = 128, N = n.
+__host__ __device__ constexpr uint32_t instr_desc(int n) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(kTM >> 4) << 24);
+}
+
+__device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+  for (unsigned it = 0; it < kWaitLimit; ++it)
+    if (mbar_try(bar, parity)) return true;
+  return false;
+}
+
+// Offset of element (row r, k) of a chunk in the core-matrix layout.
+__device__ __forceinline__ uint32_t cm_offset(int r, int k) {
+  return (uint32_t)(((r >> 3) * (kKC / 8) + (k >> 3)) * 128 + (r & 7) * 16 + (k & 7) * 2);
+}
+
+// Stages rows [r0, r0 + rows) x K [k0, k0 + kKC) of an operand (zero outside
+// [0, R) x [0, K)) in shared memory.  Row-major source: ld elements per row,
+// K contiguous; transposed source: row k holds R contiguous values.
+template <bool TRANS>
+__device__ __forceinline__ void stage(uint8_t* dst, const __nv_bfloat16* __restrict__ src, long long ld, int r0,
+                                      int rows, long long R, long long k0, long long K) {
+  if (!TRANS) {
+    // 16-byte chunks: 8 consecutive k of one row
+    const int chunks = rows * (kKC / 8);
+    for (int c = threadIdx.x; c < chunks; c += kThreads) {
+      const int r = c / (kKC / 8), kk = (c % (kKC / 8)) * 8;
+      const long long gr = r0 + r, gk = k0 + kk;
+      uint4 v = make_uint4(0u, 0u, 0u, 0u);
+      if (gr < R && gk + 8 <= K) {
+        v = *reinterpret_cast<const uint4*>(src + gr * ld + gk);
+      } else if (gr < R && gk < K) {
+        __nv_bfloat16 t[8];
+#pragma unroll
+        for (int e = 0; e < 8; ++e) t[e] = (gk + e < K) ? src[gr * ld + gk + e] : __float2bfloat16(0.f);
+        v = *reinterpret_cast<const uint4*>(t);
+      }
+      *reinterpret_cast<uint4*>(dst + cm_offset(r, kk)) = v;
+    }
+  } else {
+    // 16-byte chunks: 8 consecutive rows at one k, scattered into 8 core-matrix rows
+    const int chunks = (rows / 8) * kKC;
+    for (int c = threadIdx.x; c < chunks; c += kThreads) {
+      const int kk = c / (rows / 8), r = (c % (rows / 8)) * 8;
+      const long long gr = r0 + r, gk = k0 + kk;
+      __nv_bfloat16 t[8];
+      if (gk < K && gr + 8 <= R) {
+        *reinterpret_cast<uint4*>(t) = *reinterpret_cast<const uint4*>(src + gk * ld + gr);
+      } else {
+#pragma unroll
+        for (int e = 0; e < 8; ++e) t[e] = (gk < K && gr + e < R) ? src[gk * ld + gr + e] : __float2bfloat16(0.f);
+      }
+#pragma unroll
+      for (int e = 0; e < 8; ++e) *reinterpret_cast<__nv_bfloat16*>(dst + cm_offset(r + e, kk)) = t[e];
+    }
+  }
+}
+
+template <int NT, bool A_T, bool B_T>
+__global__ void __launch_bounds__(kThreads) k_gemm_tc(const sgr_gemm_args a) {
+  extern __shared__ __align__(1024) uint8_t smem[];
+  uint8_t* sA = smem;                                  // kTM x kKC bf16: 16 KB
+  uint8_t* sB = smem + kTM * kKC * 2;                  // NT x kKC bf16
+  __shared__ __align__(8) uint64_t s_bar;
+  __shared__ uint32_t s_tmem;
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int m0 = blockIdx.x * kTM, n0 = blockIdx.y * NT;
+  long long k_begin = 0, k_end = a.K;
+  if (a.split_k > 0) {
+    k_begin = (long long)blockIdx.z * a.split_k;
+    k_end = k_begin + a.split_k < a.K ? k_begin + a.split_k : a.K;
+  }
+  if (k_begin >= k_end) return;                        // CTA-uniform
+
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_addr(&s_tmem)),
+                 "r"(NT)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+  }
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_addr(&s_bar)) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+  const uint32_t tmem = s_tmem;
+  const uint32_t bar = smem_addr(&s_bar);
+  const uint32_t idesc = instr_desc(NT);
+  uint32_t phase = 0;
+  bool ok = true;
+
+  for (long long k0 = k_begin; k0 < k_end; k0 += kKC) {
+    stage<A_T>(sA, static_cast<const __nv_bfloat16*>(a.A), a.lda, m0, kTM, a.M, k0, k_end);
+    stage<B_T>(sB, static_cast<const __nv_bfloat16*>(a.B), a.ldb, n0, NT, a.N, k0, k_end);
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+      const uint32_t a0 = smem_addr(sA), b0 = smem_addr(sB);
+#pragma unroll
+      for (int s = 0; s < kKC / 16; ++s) {
+        const uint64_t da = smem_desc(a0 + 256u * s, 128u, 1024u);
+        const uint64_t db = smem_desc(b0 + 256u * s, 128u, 1024u);
+        const uint32_t acc = (k0 > k_begin || s > 0) ? 1u : 0u;
+        asm volatile(
+            "{\n .reg .pred p;\n setp.ne.u32 p, %4, 0;\n"
+            " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+            "l"(da), "l"(db), "r"(idesc), "r"(acc)
+            : "memory");
+      }
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(bar)
+                   : "memory");
+    }
+    ok = mbar_wait(bar, phase);
+    phase ^= 1u;
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    if (!__syncthreads_and(ok)) break;
+  }
+
+  if (__syncthreads_or(!ok)) {
+    if (threadIdx.x == 0) {
+      atomicOr(a.status, (unsigned)SGR_MLP_TIMEOUT);
+      mbar_wait(bar, phase ^ 1u);                       // once more for the MMAs in flight
+    }
+  } else {
+    // epilogue: warp w owns rows m0 + 32 w + lane (tensor-memory lanes 32 w ..)
+    const long long row = (long long)m0 + 32 * warp + lane;
+#pragma unroll 1
+    for (int c0 = 0; c0 < NT; c0 += 16) {
+      uint32_t v[16];
+      const uint32_t taddr = tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)c0;
+      asm volatile(
+          "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+          : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+            "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
+          : "r"(taddr)
+          : "memory");
+      asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+      if (row >= a.M) continue;
+#pragma unroll
+      for (int e = 0; e < 16; ++e) {
+        const long long col = (long long)n0 + c0 + e;
+        if (col >= a.N) break;
+        float x = __uint_as_float(v[e]);
+        if (a.bias) x += a.bias[col];
+        switch (a.epilogue) {
+          case SGR_GEMM_STORE_F32:
+            static_cast<float*>(a.out)[row * a.ldo + col] = x;
+            break;
+          case SGR_GEMM_ADD_F32:
+            atomicAdd(static_cast<float*>(a.out) + row * a.ldo + col, x);
+            break;
+          case SGR_GEMM_RELU_BF16:
+            static_cast<__nv_bfloat16*>(a.out)[row * a.ldo + col] = __float2bfloat16(fmaxf(x, 0.0f));
+            break;
+          case SGR_GEMM_MASK_BF16: {
+            const float h = __bfloat162float(static_cast<const __nv_bfloat16*>(a.mask)[row * a.ldmask + col]);
+            static_cast<__nv_bfloat16*>(a.out)[row * a.ldo + col] = __float2bfloat16(h > 0.0f ? x : 0.0f);
+            break;
+          }
+          default:
+            break;
+        }
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(NT) : "memory");
+  }
+}
+
+template <int NT, bool A_T, bool B_T>
+int launch(const sgr_gemm_args& a, cudaStream_t st) {
+  const size_t smem = (size_t)(kTM + NT) * kKC * 2;
+  if (cudaFuncSetAttribute(k_gemm_tc<NT, A_T, B_T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+      cudaSuccess)
+    return SGR_ERR_CUDA;
+  const unsigned gz = a.split_k > 0 ? (unsigned)((a.K + a.split_k - 1) / a.split_k) : 1u;
+  dim3 grid((unsigned)((a.M + kTM - 1) / kTM), (unsigned)((a.N + NT - 1) / NT), gz);
+  k_gemm_tc<NT, A_T, B_T><<<grid, kThreads, smem, st>>>(a);
+  sgr::count_launches(1);
+  return cudaGetLastError() == cudaSuccess ? SGR_OK : SGR_ERR_CUDA;
+}
+
+template <int NT>
+int launch_nt(const sgr_gemm_args& a, cudaStream_t st) {
+  if (!a.a_trans && !a.b_trans) return launch<NT, false, false>(a, st);
+  if (a.a_trans && a.b_trans) return launch<NT, true, true>(a, st);
+  return SGR_ERR_UNSUPPORTED;
+}
+
+}  // namespace sgrmlp
+
+using namespace sgrmlp;
+
+extern "C" {
+
+int sgr_mlp_gemm(const sgr_gemm_args* a, void* stream) {
+  if (!a || a->M < 0 || a->N < 0 || a->K < 0 || !a->status) return SGR_ERR_INVALID_ARGUMENT;
+  if (a->M == 0 || a->N == 0) return SGR_OK;
+  if (!a->A || !a->B || !a->out || a->K == 0) return SGR_ERR_INVALID_ARGUMENT;
+  if (a->epilogue < SGR_GEMM_STORE_F32 || a->epilogue > SGR_GEMM_MASK_BF16) return SGR_ERR_INVALID_ARGUMENT;
+  if (a->epilogue == SGR_GEMM_MASK_BF16 && !a->mask) return SGR_ERR_INVALID_ARGUMENT;
+  if (a->split_k < 0 || (a->split_k > 0 && a->split_k % kKC != 0)) return SGR_ERR_INVALID_ARGUMENT;
+  if (a->split_k > 0 && a->epilogue != SGR_GEMM_ADD_F32) return SGR_ERR_UNSUPPORTED;
+  // 16-byte vector loads: row strides and base addresses in multiples of 8 bf16
+  if (a->lda % 8 || a->ldb % 8 || (reinterpret_cast<uintptr_t>(a->A) & 15) || (reinterpret_cast<uintptr_t>(a->B) & 15))
+    return SGR_ERR_INVALID_ARGUMENT;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const int n = a->N <= 64 ? 64 : a->N <= 128 ? 128 : 256;
+  switch (n) {
+    case 64: return launch_nt<64>(*a, st);
+    case 128: return launch_nt<128>(*a, st);
+    default: return launch_nt<256>(*a, st);
+  }
+}
+
+}  // extern "C"

@@ -1,0 +1,66 @@
+"""Host side of the proposal network's BF16 tensor-core GEMM (libsgr.so
+``sgr_mlp_gemm``): C[M, N] = A[M, K] . B[N, K]^T with a fused epilogue."""
+from __future__ import annotations
+
+import ctypes as C
+
+import torch
+
+from . import _lib as L
+
+STORE_F32, ADD_F32, RELU_BF16, MASK_BF16 = 0, 1, 2, 3
+TIMEOUT = 1
+_p = C.c_void_p
+
+
+class GemmArgs(C.Structure):
+    _fields_ = [("M", C.c_int64), ("N", C.c_int64), ("K", C.c_int64), ("A", _p), ("lda", C.c_int64),
+                ("a_trans", C.c_int32), ("B", _p), ("ldb", C.c_int64), ("b_trans", C.c_int32), ("bias", _p),
+                ("epilogue", C.c_int32), ("out", _p), ("ldo", C.c_int64), ("mask", _p), ("ldmask", C.c_int64),
+                ("split_k", C.c_int64), ("status", _p)]
+
+
+_STATUS: dict = {}
+
+
+def _lib():
+    lib = L.load()
+    fn = lib.sgr_mlp_gemm
+    fn.restype, fn.argtypes = C.c_int, [C.POINTER(GemmArgs), _p]
+    return lib
+
+
+def status_word(device) -> torch.Tensor:
+    """The device status word every GEMM on ``device`` ORs its flags into."""
+    key = torch.device(device)
+    if key not in _STATUS:
+        _STATUS[key] = torch.zeros(1, dtype=torch.int32, device=key)
+    return _STATUS[key]
+
+
+def gemm(a, b, out, epilogue, bias=None, mask=None, trans=False, split_k=0):
+    """out (+)= epilogue(a . b^T + bias).  Without ``trans``: a [M, K], b
+    [N, K] (bf16, K contiguous).  With it: a [K, M], b [K, N] (the reduction
+    runs over their rows).  ``out`` is [M, N] (fp32, or bf16 for the ReLU
+    epilogues)."""
+    if a.dtype != torch.bfloat16 or b.dtype != torch.bfloat16:
+        raise TypeError("gemm operands are bf16")
+    if not (a.is_contiguous() and b.is_contiguous() and out.is_contiguous()):
+        raise ValueError("gemm operands must be contiguous")
+    if trans:
+        K, M = a.shape
+        K2, N = b.shape
+    else:
+        M, K = a.shape
+        N, K2 = b.shape
+    if K != K2 or tuple(out.shape) != (M, N):
+        raise ValueError("gemm shapes do not agree")
+    want = torch.float32 if epilogue in (STORE_F32, ADD_F32) else torch.bfloat16
+    if out.dtype != want:
+        raise TypeError(f"epilogue {epilogue} writes {want}")
+    args = GemmArgs(M, N, K, a.data_ptr(), a.shape[1], int(trans), b.data_ptr(), b.shape[1], int(trans),
+                    bias.data_ptr() if bias is not None else None, epilogue, out.data_ptr(), N,
+                    mask.data_ptr() if mask is not None else None, mask.shape[1] if mask is not None else 0,
+                    split_k, status_word(out.device).data_ptr())
+    L.check(_lib().sgr_mlp_gemm(C.byref(args), torch.cuda.current_stream().cuda_stream), "sgr_mlp_gemm")
+    return out

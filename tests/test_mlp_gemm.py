@@ -1,0 +1,71 @@
+"""The proposal network's tcgen05 BF16 GEMM against a PyTorch fp32 matmul of
+the same bf16 operands: every epilogue, each output-tile width (64, 128,
+256), ragged M, N and K, the transposed (weight-gradient) form with split K."""
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+# fp32 accumulation of exact bf16 products, in a different order than the
+# reference matmul: relative to the largest |C|
+TOL = 2e-5
+
+
+def _bf(shape, g, scale=1.0):
+    return (torch.randn(shape, generator=g) * scale).to(torch.bfloat16).cuda()
+
+
+def _ref(a, b, bias=None, trans=False):
+    a32, b32 = a.float(), b.float()
+    c = a32.t() @ b32 if trans else a32 @ b32.t()
+    if bias is not None:
+        c = c + bias
+    return c
+
+
+@pytest.mark.parametrize("M,N,K", [(128, 64, 64), (300, 64, 16), (257, 128, 200), (520, 256, 128), (64, 104, 256)])
+def test_gemm_store_and_bias(sgr_lib, M, N, K):
+    from partgs_gb300 import proposal_gemm as G
+    g = torch.Generator().manual_seed(M + N + K)
+    a, b = _bf((M, K), g), _bf((N, K), g)
+    bias = torch.randn(N, generator=g).cuda()
+    out = torch.full((M, N), float("nan"), device="cuda")
+    G.gemm(a, b, out, G.STORE_F32, bias=bias)
+    torch.cuda.synchronize()
+    ref = _ref(a, b, bias)
+    assert int(G.status_word("cuda").item()) == 0
+    assert float((out - ref).abs().max()) <= TOL * float(ref.abs().max())
+
+
+def test_gemm_relu_and_mask_epilogues(sgr_lib):
+    from partgs_gb300 import proposal_gemm as G
+    g = torch.Generator().manual_seed(5)
+    M, N, K = 384, 128, 64
+    a, b = _bf((M, K), g), _bf((N, K), g)
+    bias = torch.randn(N, generator=g).cuda()
+    out = torch.empty((M, N), dtype=torch.bfloat16, device="cuda")
+    G.gemm(a, b, out, G.RELU_BF16, bias=bias)
+    ref = torch.relu(_ref(a, b, bias))
+    assert float((out.float() - ref).abs().max()) <= 1e-2 * float(ref.abs().max())      # bf16 output
+    mask = _bf((M, N), g)
+    out2 = torch.empty((M, N), dtype=torch.bfloat16, device="cuda")
+    G.gemm(a, b, out2, G.MASK_BF16, mask=mask)
+    ref2 = _ref(a, b) * (mask.float() > 0)
+    assert float((out2.float() - ref2).abs().max()) <= 1e-2 * float(ref2.abs().max())
+    assert bool(((mask.float() <= 0) <= (out2.float() == 0)).all())
+    torch.cuda.synchronize()
+    assert int(G.status_word("cuda").item()) == 0
+
+
+@pytest.mark.parametrize("Kin,N,rows", [(64, 128, 4096), (128, 256, 3000), (16, 64, 2048)])
+def test_gemm_transposed_split_k(sgr_lib, Kin, N, rows):
+    """dW[Kin, N] = X^T dZ over `rows` point rows, split over CTAs."""
+    from partgs_gb300 import proposal_gemm as G
+    g = torch.Generator().manual_seed(Kin + N)
+    x, dz = _bf((rows, Kin), g), _bf((rows, N), g)
+    out = torch.zeros((Kin, N), device="cuda")
+    G.gemm(x, dz, out, G.ADD_F32, trans=True, split_k=512)
+    torch.cuda.synchronize()
+    ref = _ref(x, dz, trans=True)
+    assert int(G.status_word("cuda").item()) == 0
+    assert float((out - ref).abs().max()) <= TOL * float(ref.abs().max()) * 4
