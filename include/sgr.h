@@ -328,7 +328,7 @@ int sgr_bind_backward_static(const sgr_bind_args* a, const float* d_xyz, const f
 
 /* One parameter tensor of an Adam step: numel floats each of param, grad and
  * the two moment buffers (device pointers), and its learning rate. */
-#define SGR_ADAM_MAX_TENSORS 8
+#define SGR_ADAM_MAX_TENSORS 16
 typedef struct sgr_adam_tensor {
     float* param;
     float* grad;
@@ -386,6 +386,16 @@ typedef struct sgr_gemm_args {
  * (no counterpart in the reference: the network is new).  tcgen05 MMA with
  * tensor-memory accumulators; never synchronises. */
 int sgr_mlp_gemm(const sgr_gemm_args* args, void* stream);
+
+/* Max-pool of a bf16 [sets*P, C] activation over each set's P rows: g
+ * [sets, C] fp32 (and bf16 into g_bf16 unless NULL) and arg [sets, C], the
+ * row of each maximum. */
+int sgr_mlp_maxpool(const void* h, int32_t sets, int32_t P, int32_t C, float* g, void* g_bf16, int32_t* arg,
+                    void* stream);
+/* Its backward through the ReLU below it: dh (bf16 [sets*P, C], cleared
+ * here) gets dg[s, c] at row arg[s, c] where g[s, c] > 0. */
+int sgr_mlp_maxpool_backward(const float* dg, const float* g, const int32_t* arg, int32_t sets, int32_t P,
+                             int32_t C, void* dh, void* stream);
 
 #ifdef __cplusplus
 }

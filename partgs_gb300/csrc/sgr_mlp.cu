@@ -260,6 +260,40 @@ int launch_nt(const sgr_gemm_args& a, cudaStream_t st) {
   return SGR_ERR_UNSUPPORTED;
 }
 
+// Max over each set's P rows of a [S*P, C] activation: g[s, c] (fp32 and
+// bf16 copies) and the row that holds it (first on ties).  One CTA per set,
+// threads over channels, rows read coalesced.
+__global__ void k_maxpool(const __nv_bfloat16* __restrict__ h, int P, int C, float* __restrict__ g,
+                          __nv_bfloat16* __restrict__ g_bf16, int* __restrict__ arg) {
+  const int set = blockIdx.x;
+  for (int c = threadIdx.x; c < C; c += blockDim.x) {
+    const __nv_bfloat16* col = h + (size_t)set * P * C + c;
+    float best = __bfloat162float(col[0]);
+    int at = 0;
+    for (int p = 1; p < P; ++p) {
+      const float v = __bfloat162float(col[(size_t)p * C]);
+      if (v > best) {
+        best = v;
+        at = p;
+      }
+    }
+    g[(size_t)set * C + c] = best;
+    if (g_bf16) g_bf16[(size_t)set * C + c] = __float2bfloat16(best);
+    arg[(size_t)set * C + c] = set * P + at;
+  }
+}
+
+// Backward of the max-pool and of the ReLU below it: dh[arg[s, c], c] =
+// dg[s, c] where g[s, c] > 0; every other entry of dh is zero (cleared by
+// the caller's launch sequence).
+__global__ void k_maxpool_bwd(const float* __restrict__ dg, const float* __restrict__ g, const int* __restrict__ arg,
+                              long long n, int C, __nv_bfloat16* __restrict__ dh) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int c = (int)(i % C);
+  dh[(size_t)arg[i] * C + c] = __float2bfloat16(g[i] > 0.0f ? dg[i] : 0.0f);
+}
+
 }  // namespace sgrmlp
 
 using namespace sgrmlp;
@@ -284,6 +318,28 @@ int sgr_mlp_gemm(const sgr_gemm_args* a, void* stream) {
     case 128: return launch_nt<128>(*a, st);
     default: return launch_nt<256>(*a, st);
   }
+}
+
+int sgr_mlp_maxpool(const void* h, int32_t sets, int32_t P, int32_t C, float* g, void* g_bf16, int32_t* arg,
+                    void* stream) {
+  if (sets < 0 || P < 1 || C < 1 || (sets > 0 && (!h || !g || !arg))) return SGR_ERR_INVALID_ARGUMENT;
+  if (sets == 0) return SGR_OK;
+  k_maxpool<<<sets, 256, 0, static_cast<cudaStream_t>(stream)>>>(static_cast<const __nv_bfloat16*>(h), P, C, g,
+                                                                  static_cast<__nv_bfloat16*>(g_bf16), arg);
+  sgr::count_launches(1);
+  return cudaGetLastError() == cudaSuccess ? SGR_OK : SGR_ERR_CUDA;
+}
+
+int sgr_mlp_maxpool_backward(const float* dg, const float* g, const int32_t* arg, int32_t sets, int32_t P,
+                             int32_t C, void* dh, void* stream) {
+  if (sets < 0 || P < 1 || C < 1 || (sets > 0 && (!dg || !g || !arg || !dh))) return SGR_ERR_INVALID_ARGUMENT;
+  if (sets == 0) return SGR_OK;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (cudaMemsetAsync(dh, 0, (size_t)sets * P * C * 2, st) != cudaSuccess) return SGR_ERR_CUDA;
+  const long long n = (long long)sets * C;
+  k_maxpool_bwd<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(dg, g, arg, n, C, static_cast<__nv_bfloat16*>(dh));
+  sgr::count_launches(1);
+  return cudaGetLastError() == cudaSuccess ? SGR_OK : SGR_ERR_CUDA;
 }
 
 }  // extern "C"

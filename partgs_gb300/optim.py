@@ -2,7 +2,7 @@
 
 ``SurfelAdam`` is the reference's surfel optimiser (torch.optim.Adam with one
 learning rate per parameter group and eps 1e-15, scene/gaussian_model.py:266)
-for up to eight parameter tensors.  The step count lives on the device and
+for up to sixteen parameter tensors.  The step count lives on the device and
 each gradient is cleared by the update itself, so a step neither
 synchronises nor needs a separate ``zero_grad`` launch, and it can be
 captured in a CUDA graph.  Gradients are created (zero) up front so that
@@ -24,7 +24,7 @@ class AdamTensor(C.Structure):
                 ("lr", C.c_float)]
 
 
-MAX_TENSORS = 8
+MAX_TENSORS = 16
 
 
 class AdamArgs(C.Structure):
