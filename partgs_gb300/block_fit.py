@@ -1,0 +1,141 @@
+"""Block-level superquadric fit and the time-to-Chamfer comparison of its two
+initialisations.
+
+The fit optimises each superquadric's log semi-axes, exponent logits,
+rotation and centre (the block model's sq_s, sq_eps, sq_r, sq_t with the
+reference's learning rates 5e-3 / 1e-3 / 5e-3 / 5e-3 and Adam eps 1e-15,
+games/block_mesh_splatting/scene/block_gaussian_model.py:430-442) through
+the CUDA binding and rasteriser, so that the union's silhouettes and median
+depth maps match those of the target scene from V orbit cameras.  (The
+reference fits RGB images with photometric losses; the synthetic scenes
+here carry geometry only, so the geometric maps stand in for them.)
+
+``time_to_chamfer`` runs the fit from the reference's initialisation
+(k-means blocks, ``proposal.plain_init``) and from the proposal network's,
+and reports how long each takes to reach the Chamfer distance the plain fit
+ends at.
+"""
+from __future__ import annotations
+
+import time
+
+import torch
+
+from .batched import MultiViewRasterizer
+from .binding import SuperquadricBinding
+from .cameras import orbit_cameras
+from .optim import SurfelAdam
+from .proposal import chamfer
+from .sq_data import RATIO, SMIN, grid_topology, surface_samples, to_binding_params
+
+LR = {"sq_s": 5e-3, "sq_eps": 1e-3, "sq_r": 5e-3, "sq_t": 5e-3}
+
+
+class BlockFit:
+    def __init__(self, target, views: int = 8, res: int = 96, n_eta: int = 30, n_omega: int = 30, seed: int = 0,
+                 device="cuda"):
+        """target: (semi [K,3], eps [K,2], quat [K,4], trans [K,3])."""
+        self.dev = torch.device(device)
+        self.cams = orbit_cameras(views, 3.0, res, res, 50.0, seed=seed)
+        eta, omega, faces = grid_topology(n_eta, n_omega)
+        self.eta = torch.tensor(eta, dtype=torch.float32, device=self.dev)
+        self.omega = torch.tensor(omega, dtype=torch.float32, device=self.dev)
+        self.faces = torch.tensor(faces, dtype=torch.int32, device=self.dev)
+        self.F = faces.shape[0]
+        self.seed = seed
+        self._rasters, self._bindings = {}, {}
+        g = torch.Generator().manual_seed(seed)
+        self.target = [t.float() for t in target]
+        self.target_pts = surface_samples(*self.target, 256, g).reshape(-1, 3)
+        with torch.no_grad():
+            others = self.render(*(t.to(self.dev) for t in to_binding_params(*self.target)))
+        self.alpha_t = others[:, 1].detach()
+        self.depth_t = others[:, 5].detach()
+        self.mask_t = (self.alpha_t > 0.5).float()
+
+    def _parts(self, K):
+        """The binding topology and the rasteriser of K superquadrics (built once)."""
+        if K not in self._bindings:
+            g = torch.Generator().manual_seed(self.seed + 7)
+            alpha = torch.rand(K * self.F, 1, 3, generator=g).to(self.dev)
+            self._bindings[K] = SuperquadricBinding(self.eta.expand(K, -1), self.omega.expand(K, -1),
+                                                    self.faces.expand(K, -1, -1).contiguous(), alpha,
+                                                    torch.ones(K, self.F, 1, device=self.dev), RATIO, SMIN)
+            self._rasters[K] = MultiViewRasterizer(self.cams, [0.0, 0.0, 0.0], 0, num_surfels=K * self.F,
+                                                   device=self.dev)
+        return self._bindings[K], self._rasters[K]
+
+    def render(self, sq_s, sq_eps, sq_r, sq_t):
+        K = sq_s.shape[0]
+        bind, raster = self._parts(K)
+        occ = torch.full((K, 1), 4.6, device=self.dev)
+        xyz, log_s, rot, op = bind(sq_s, sq_r, sq_t, sq_eps, occ)
+        _, others, _, _ = raster(xyz, op, None, torch.exp(log_s), rot, colors_precomp=torch.ones_like(xyz))
+        return others
+
+    def fit(self, init, iters: int = 300, eval_every: int = 10):
+        """Runs the fit from init (semi, eps, quat, trans); returns
+        [(fit seconds so far, Chamfer distance to the target)]."""
+        raw = [t.detach().float().to(self.dev).clone().contiguous() for t in to_binding_params(*init)]
+        sq_s, sq_eps, sq_r, sq_t = (t.requires_grad_(True) for t in raw)
+        opt = SurfelAdam([{"params": [sq_s], "lr": LR["sq_s"]}, {"params": [sq_eps], "lr": LR["sq_eps"]},
+                          {"params": [sq_r], "lr": LR["sq_r"]}, {"params": [sq_t], "lr": LR["sq_t"]}], eps=1e-15)
+        hist = [(0.0, self.chamfer_of(sq_s, sq_eps, sq_r, sq_t))]
+        elapsed = 0.0
+        for it0 in range(0, iters, eval_every):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            for _ in range(min(eval_every, iters - it0)):
+                others = self.render(sq_s, sq_eps, sq_r, sq_t)
+                loss = (others[:, 1] - self.alpha_t).abs().mean() + \
+                    (self.mask_t * (others[:, 5] - self.depth_t).abs()).mean()
+                loss.backward()
+                opt.step()
+            torch.cuda.synchronize()
+            elapsed += time.perf_counter() - t0
+            hist.append((elapsed, self.chamfer_of(sq_s, sq_eps, sq_r, sq_t)))
+        return hist
+
+    def chamfer_of(self, sq_s, sq_eps, sq_r, sq_t):
+        with torch.no_grad():
+            semi = RATIO * (torch.exp(sq_s) + SMIN)
+            eps = torch.sigmoid(sq_eps) * 1.8 + 0.1
+            quat = torch.nn.functional.normalize(sq_r, dim=-1)
+            g = torch.Generator().manual_seed(self.seed + 11)
+            pts = surface_samples(semi.cpu(), eps.cpu(), quat.cpu(), sq_t.detach().cpu(), 256, g).reshape(-1, 3)
+        return chamfer(pts, self.target_pts)
+
+
+def time_to_reach(hist, level):
+    """Fit seconds until the Chamfer distance first reaches ``level`` (None if never)."""
+    for t, c in hist:
+        if c <= level:
+            return t
+    return None
+
+
+def time_to_chamfer(net, batch, points, iters: int = 300, views: int = 8, res: int = 96):
+    """Per scene of ``batch`` (an SQBatch with its ``points`` [S, 2048, 3]):
+    plain-init and proposal-init fits; the plain fit's final Chamfer is the
+    level both are timed to.  The proposal's time includes its network
+    forward.  Returns a list of dicts."""
+    from .proposal import plain_init, predict
+    out = []
+    for s in range(points.shape[0]):
+        k = int(batch.counts[s])
+        target = (batch.semi[s, :k], batch.eps[s, :k], batch.quat[s, :k], batch.trans[s, :k])
+        fit = BlockFit(target, views=views, res=res, seed=s)
+        plain = plain_init(points[s].float(), k, g=torch.Generator().manual_seed(s))
+        h_plain = fit.fit(plain, iters)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        prop = predict(net, points[s:s + 1].contiguous())[0]
+        torch.cuda.synchronize()
+        t_net = time.perf_counter() - t0
+        h_prop = fit.fit(prop, iters)
+        level = h_plain[-1][1]
+        t_prop = time_to_reach(h_prop, level)
+        out.append(dict(k=k, k_proposed=int(prop[0].shape[0]), plain_final=level, plain_time=h_plain[-1][0],
+                        proposal_start=h_prop[0][1], plain_start=h_plain[0][1], proposal_final=h_prop[-1][1],
+                        proposal_time=None if t_prop is None else t_prop + t_net, network_s=t_net))
+    return out
