@@ -116,8 +116,10 @@ def time_to_reach(hist, level):
 
 def time_to_chamfer(net, batch, points, iters: int = 300, views: int = 8, res: int = 96):
     """Per scene of ``batch`` (an SQBatch with its ``points`` [S, 2048, 3]):
-    plain-init and proposal-init fits; the plain fit's final Chamfer is the
-    level both are timed to.  The proposal's time includes its network
+    plain-init and proposal-init fits with the same, configured number of
+    blocks (the reference's block stage is given it; k-means uses it, the
+    proposal keeps its k most likely slots); the plain fit's final Chamfer is
+    the level both are timed to.  The proposal's time includes its network
     forward.  Returns a list of dicts."""
     from .proposal import plain_init, predict
     out = []
@@ -129,7 +131,7 @@ def time_to_chamfer(net, batch, points, iters: int = 300, views: int = 8, res: i
         h_plain = fit.fit(plain, iters)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        prop = predict(net, points[s:s + 1].contiguous())[0]
+        prop = predict(net, points[s:s + 1].contiguous(), counts=[k])[0]
         torch.cuda.synchronize()
         t_net = time.perf_counter() - t0
         h_prop = fit.fit(prop, iters)
@@ -139,3 +141,44 @@ def time_to_chamfer(net, batch, points, iters: int = 300, views: int = 8, res: i
                         proposal_start=h_prop[0][1], plain_start=h_plain[0][1], proposal_final=h_prop[-1][1],
                         proposal_time=None if t_prop is None else t_prop + t_net, network_s=t_net))
     return out
+
+
+def main():
+    """python -m partgs_gb300.block_fit --scenes 32 --iters 300: time to the
+    plain fit's final Chamfer distance, proposal init against plain init,
+    on seeded held-out scenes; prints one JSON line."""
+    import argparse
+    import json
+
+    import numpy as np
+
+    from . import sq_data as D
+    from .train_proposal import WEIGHTS, load_npz
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--scenes", type=int, default=32)
+    ap.add_argument("--iters", type=int, default=300)
+    ap.add_argument("--seed", type=int, default=4242)
+    ap.add_argument("--weights", default=WEIGHTS)
+    a = ap.parse_args()
+    net = load_npz(a.weights)
+    b = D.sample_sq_batch(a.scenes, torch.Generator().manual_seed(a.seed))
+    pts, _ = D.SceneRenderer(res=96).points(b, seed=a.seed)
+    time_to_chamfer(net, b, pts[:1], iters=20)                     # warm-up (library load, first launches)
+    res = time_to_chamfer(net, b, pts, iters=a.iters)
+    reached = [r for r in res if r["proposal_time"] is not None]
+    ratios = [r["proposal_time"] / r["plain_time"] for r in reached]
+    print(json.dumps({
+        "scenes": a.scenes, "iters": a.iters, "reached": len(reached),
+        "time_ratio_median": float(np.median(ratios)) if ratios else None,
+        "time_ratio_p90": float(np.percentile(ratios, 90)) if ratios else None,
+        "plain_start_chamfer": float(np.mean([r["plain_start"] for r in res])),
+        "proposal_start_chamfer": float(np.mean([r["proposal_start"] for r in res])),
+        "plain_final_chamfer": float(np.mean([r["plain_final"] for r in res])),
+        "proposal_final_chamfer": float(np.mean([r["proposal_final"] for r in res])),
+        "plain_fit_s": float(np.mean([r["plain_time"] for r in res])),
+        "network_s": float(np.mean([r["network_s"] for r in res])),
+        "blocks_true_vs_proposed": [[r["k"], r["k_proposed"]] for r in res]}))
+
+
+if __name__ == "__main__":
+    main()

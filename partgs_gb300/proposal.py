@@ -214,17 +214,22 @@ class Trainer:
         return loss.detach()
 
 
-def predict(net: ProposalNet, pts: torch.Tensor, threshold: float = 0.5):
+def predict(net: ProposalNet, pts: torch.Tensor, threshold: float = 0.5, counts=None):
     """Per scene, the proposed superquadrics: a list of (semi, eps, quat,
-    trans) tensors [k, .] with existence probability above ``threshold``
-    (at least one)."""
+    trans) tensors [k, .].  With ``counts`` (the configured number of blocks
+    per scene, as the reference's block stage is given) the k most likely
+    slots; otherwise the slots with existence probability above
+    ``threshold`` (at least one)."""
     out, _ = net.forward(pts)
     semi, eps, quat, trans, logit = decode(out)
     res = []
     for s in range(out.shape[0]):
-        keep = torch.sigmoid(logit[s]) > threshold
-        if not bool(keep.any()):
-            keep = logit[s] == logit[s].max()
+        if counts is not None:
+            keep = logit[s].argsort(descending=True)[:int(counts[s])]
+        else:
+            keep = torch.sigmoid(logit[s]) > threshold
+            if not bool(keep.any()):
+                keep = logit[s] == logit[s].max()
         res.append((semi[s][keep], eps[s][keep], quat[s][keep], trans[s][keep]))
     return res
 

@@ -27,7 +27,7 @@ def test_proposal_init_is_closer_than_the_plain_init(sgr_lib):
     net = load_npz(_weights())
     b = D.sample_sq_batch(64, torch.Generator().manual_seed(2024))
     pts, _ = D.SceneRenderer(res=96).points(b, seed=2024)
-    pred = predict(net, pts)
+    pred = predict(net, pts, counts=b.counts.tolist())
     cp, cn = [], []
     for s in range(64):
         k = int(b.counts[s])
