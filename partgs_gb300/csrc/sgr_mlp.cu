@@ -23,10 +23,12 @@
 // Every wait is bounded: on timeout the kernel raises SGR_MLP_TIMEOUT in the
 // status word, waits once more (bounded) for its own MMAs, frees its tensor
 // memory and returns.
+#include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <mutex>
 
 #include "../../include/sgr.h"
 
@@ -121,6 +123,87 @@ __device__ __forceinline__ void stage(uint8_t* dst, const __nv_bfloat16* __restr
   }
 }
 
+// Epilogue of 16 accumulator columns [col0, col0 + 16) of one row: 16-byte
+// vector stores (loads of the mask, fp32 vector atomics) when the 16 columns
+// are in range and aligned, element by element otherwise.
+__device__ __forceinline__ void epilogue16(const sgr_gemm_args& a, long long row, long long col0,
+                                           const uint32_t (&v)[16]) {
+  float x[16];
+#pragma unroll
+  for (int e = 0; e < 16; ++e) {
+    x[e] = __uint_as_float(v[e]);
+    if (a.bias && col0 + e < a.N) x[e] += a.bias[col0 + e];
+  }
+  const bool vec = col0 + 16 <= a.N && (a.ldo & 7) == 0 && (reinterpret_cast<uintptr_t>(a.out) & 15) == 0 &&
+                   (a.epilogue != SGR_GEMM_MASK_BF16 ||
+                    ((a.ldmask & 7) == 0 && (reinterpret_cast<uintptr_t>(a.mask) & 15) == 0));
+  if (vec) {
+    const long long o = row * a.ldo + col0;
+    switch (a.epilogue) {
+      case SGR_GEMM_STORE_F32: {
+        float4* dst = reinterpret_cast<float4*>(static_cast<float*>(a.out) + o);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) dst[q] = make_float4(x[4 * q], x[4 * q + 1], x[4 * q + 2], x[4 * q + 3]);
+        return;
+      }
+      case SGR_GEMM_ADD_F32: {
+        float4* dst = reinterpret_cast<float4*>(static_cast<float*>(a.out) + o);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) atomicAdd(dst + q, make_float4(x[4 * q], x[4 * q + 1], x[4 * q + 2], x[4 * q + 3]));
+        return;
+      }
+      case SGR_GEMM_RELU_BF16:
+      case SGR_GEMM_MASK_BF16: {
+        if (a.epilogue == SGR_GEMM_MASK_BF16) {
+          const uint4* mp = reinterpret_cast<const uint4*>(static_cast<const __nv_bfloat16*>(a.mask) +
+                                                           row * a.ldmask + col0);
+          const uint4 m2[2] = {mp[0], mp[1]};
+          const __nv_bfloat16* mh = reinterpret_cast<const __nv_bfloat16*>(m2);
+#pragma unroll
+          for (int e = 0; e < 16; ++e) x[e] = __bfloat162float(mh[e]) > 0.0f ? x[e] : 0.0f;
+        } else {
+#pragma unroll
+          for (int e = 0; e < 16; ++e) x[e] = fmaxf(x[e], 0.0f);
+        }
+        uint4 w[2];
+        __nv_bfloat162* wh = reinterpret_cast<__nv_bfloat162*>(w);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) wh[q] = __floats2bfloat162_rn(x[2 * q], x[2 * q + 1]);
+        uint4* dst = reinterpret_cast<uint4*>(static_cast<__nv_bfloat16*>(a.out) + o);
+        dst[0] = w[0];
+        dst[1] = w[1];
+        return;
+      }
+      default:
+        return;
+    }
+  }
+#pragma unroll
+  for (int e = 0; e < 16; ++e) {
+    const long long col = col0 + e;
+    if (col >= a.N) break;
+    const long long o = row * a.ldo + col;
+    switch (a.epilogue) {
+      case SGR_GEMM_STORE_F32:
+        static_cast<float*>(a.out)[o] = x[e];
+        break;
+      case SGR_GEMM_ADD_F32:
+        atomicAdd(static_cast<float*>(a.out) + o, x[e]);
+        break;
+      case SGR_GEMM_RELU_BF16:
+        static_cast<__nv_bfloat16*>(a.out)[o] = __float2bfloat16(fmaxf(x[e], 0.0f));
+        break;
+      case SGR_GEMM_MASK_BF16: {
+        const float h = __bfloat162float(static_cast<const __nv_bfloat16*>(a.mask)[row * a.ldmask + col]);
+        static_cast<__nv_bfloat16*>(a.out)[o] = __float2bfloat16(h > 0.0f ? x[e] : 0.0f);
+        break;
+      }
+      default:
+        break;
+    }
+  }
+}
+
 template <int NT, bool A_T, bool B_T>
 __global__ void __launch_bounds__(kThreads) k_gemm_tc(const sgr_gemm_args a) {
   extern __shared__ __align__(1024) uint8_t smem[];
@@ -205,31 +288,7 @@ __global__ void __launch_bounds__(kThreads) k_gemm_tc(const sgr_gemm_args a) {
           : "memory");
       asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
       if (row >= a.M) continue;
-#pragma unroll
-      for (int e = 0; e < 16; ++e) {
-        const long long col = (long long)n0 + c0 + e;
-        if (col >= a.N) break;
-        float x = __uint_as_float(v[e]);
-        if (a.bias) x += a.bias[col];
-        switch (a.epilogue) {
-          case SGR_GEMM_STORE_F32:
-            static_cast<float*>(a.out)[row * a.ldo + col] = x;
-            break;
-          case SGR_GEMM_ADD_F32:
-            atomicAdd(static_cast<float*>(a.out) + row * a.ldo + col, x);
-            break;
-          case SGR_GEMM_RELU_BF16:
-            static_cast<__nv_bfloat16*>(a.out)[row * a.ldo + col] = __float2bfloat16(fmaxf(x, 0.0f));
-            break;
-          case SGR_GEMM_MASK_BF16: {
-            const float h = __bfloat162float(static_cast<const __nv_bfloat16*>(a.mask)[row * a.ldmask + col]);
-            static_cast<__nv_bfloat16*>(a.out)[row * a.ldo + col] = __float2bfloat16(h > 0.0f ? x : 0.0f);
-            break;
-          }
-          default:
-            break;
-        }
-      }
+      epilogue16(a, row, (long long)n0 + c0, v);
     }
   }
   asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
@@ -238,6 +297,194 @@ __global__ void __launch_bounds__(kThreads) k_gemm_tc(const sgr_gemm_args a) {
     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(NT) : "memory");
   }
+}
+
+// ---------------------------------------------------------------------------
+// K-major operands: TMA-fed, multi-stage form.
+//
+// A TMA copy of a box of 8 columns x R rows (no swizzle) lands as R rows of
+// 16 bytes, contiguous: the no-swizzle K-major core-matrix layout with 8-row
+// groups 128 bytes apart (SBO) and adjacent 8-column slices R * 16 bytes
+// apart (LBO).  A K chunk of 64 is 8 such copies per operand.  Thread 0 of
+// warp 0 issues the copies of stage s once the MMAs that last read it have
+// committed to empty[s]; thread 0 of warp 1 waits for full[s] (the copies'
+// byte count), issues the four MMAs and commits them to empty[s].  After the
+// last chunk the MMAs commit to `done`, and all four warps run the
+// epilogue.  Out-of-range rows and columns are zero-filled by the TMA unit.
+// ---------------------------------------------------------------------------
+constexpr int kStages = 4;
+
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, int x, int y, uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];\n" ::
+          "r"(dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(bar)
+      : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(bar), "r"(bytes) : "memory");
+}
+
+template <int NT>
+__global__ void __launch_bounds__(kThreads) k_gemm_tma(const sgr_gemm_args a, const __grid_constant__ CUtensorMap map_a,
+                                                       const __grid_constant__ CUtensorMap map_b, int ns) {
+  extern __shared__ __align__(1024) uint8_t smem[];
+  constexpr uint32_t kBytesA = kTM * kKC * 2, kBytesB = NT * kKC * 2, kStage = kBytesA + kBytesB;
+  __shared__ __align__(8) uint64_t s_full[kStages], s_empty[kStages], s_done;
+  __shared__ uint32_t s_tmem;
+  __shared__ int s_fail;
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int m0 = blockIdx.x * kTM, n0 = blockIdx.y * NT;
+  const int chunks = (int)((a.K + kKC - 1) / kKC);
+
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_addr(&s_tmem)),
+                 "r"(NT)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+  }
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < ns; ++i) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_addr(&s_full[i])) : "memory");
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_addr(&s_empty[i])) : "memory");
+    }
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_addr(&s_done)) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    s_fail = 0;
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+  const uint32_t tmem = s_tmem;
+  const uint32_t base = (smem_addr(smem) + 127u) & ~127u;   // TMA destinations: 128-byte aligned
+
+  if (warp == 0 && lane == 0) {
+    // producer
+    for (int c = 0; c < chunks; ++c) {
+      const int st = c % ns;
+      if (c >= ns && !mbar_wait(smem_addr(&s_empty[st]), (uint32_t)((c / ns - 1) & 1))) {
+        s_fail = 1;
+        break;
+      }
+      const uint32_t full = smem_addr(&s_full[st]);
+      mbar_expect(full, kStage);
+      const uint32_t sa = base + st * kStage, sb = sa + kBytesA;
+      for (int kb = 0; kb < kKC / 8; ++kb) {
+        tma_load_2d(sa + kb * kTM * 16, &map_a, c * kKC + kb * 8, m0, full);
+        tma_load_2d(sb + kb * NT * 16, &map_b, c * kKC + kb * 8, n0, full);
+      }
+    }
+  } else if (warp == 1 && lane == 0) {
+    // MMA issuer
+    const uint32_t idesc = instr_desc(NT);
+    for (int c = 0; c < chunks; ++c) {
+      const int st = c % ns;
+      if (!mbar_wait(smem_addr(&s_full[st]), (uint32_t)((c / ns) & 1))) {
+        s_fail = 1;
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+      const uint32_t sa = base + st * kStage, sb = sa + kBytesA;
+#pragma unroll
+      for (int s = 0; s < kKC / 16; ++s) {
+        const uint64_t da = smem_desc(sa + 2u * s * kTM * 16, kTM * 16, 128u);
+        const uint64_t db = smem_desc(sb + 2u * s * NT * 16, NT * 16, 128u);
+        const uint32_t acc = (c > 0 || s > 0) ? 1u : 0u;
+        asm volatile(
+            "{\n .reg .pred p;\n setp.ne.u32 p, %4, 0;\n"
+            " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+            "l"(da), "l"(db), "r"(idesc), "r"(acc)
+            : "memory");
+      }
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                       smem_addr(&s_empty[st]))
+                   : "memory");
+    }
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                     smem_addr(&s_done))
+                 : "memory");
+  }
+  // everyone: wait for the accumulator (the issuer's last commit)
+  const bool ok = mbar_wait(smem_addr(&s_done), 0u);
+  asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+  __syncthreads();
+  if (!ok || s_fail) {
+    if (threadIdx.x == 0) atomicOr(a.status, (unsigned)SGR_MLP_TIMEOUT);
+  } else {
+    const long long row = (long long)m0 + 32 * warp + lane;
+#pragma unroll 1
+    for (int c0 = 0; c0 < NT; c0 += 16) {
+      uint32_t v[16];
+      const uint32_t taddr = tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)c0;
+      asm volatile(
+          "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+          : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+            "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
+          : "r"(taddr)
+          : "memory");
+      asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+      if (row >= a.M) continue;
+      epilogue16(a, row, (long long)n0 + c0, v);
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(NT) : "memory");
+  }
+}
+
+using EncodeTiled = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                 const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                 CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiled encode_fn() {
+  static std::once_flag once;
+  static EncodeTiled fn = nullptr;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiled>(p);
+  });
+  return fn;
+}
+
+// Tensor map of a row-major bf16 matrix [rows, cols] (ld elements per row)
+// read in boxes of 8 columns x box_rows rows.
+bool make_map(CUtensorMap* m, const void* base, long long rows, long long cols, long long ld, int box_rows) {
+  EncodeTiled enc = encode_fn();
+  if (!enc) return false;
+  const cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
+  const cuuint64_t strides[1] = {(cuuint64_t)ld * 2};
+  const cuuint32_t box[2] = {8u, (cuuint32_t)box_rows};
+  const cuuint32_t estr[2] = {1u, 1u};
+  return enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box, estr,
+             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+template <int NT>
+int launch_tma(const sgr_gemm_args& a, cudaStream_t st) {
+  alignas(64) CUtensorMap ma, mb;
+  if (!make_map(&ma, a.A, a.M, a.K, a.lda, kTM) || !make_map(&mb, a.B, a.N, a.K, a.ldb, NT)) return SGR_ERR_CUDA;
+  // as many stages as K chunks (up to kStages): short-K layers leave room
+  // for more CTAs per SM, whose loads overlap each other's epilogues
+  const long long chunks = (a.K + kKC - 1) / kKC;
+  const int ns = (int)(chunks < kStages ? (chunks < 1 ? 1 : chunks) : kStages);
+  const size_t smem = (size_t)ns * (kTM + NT) * kKC * 2 + 128;
+  if (cudaFuncSetAttribute(k_gemm_tma<NT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)((size_t)kStages * (kTM + NT) * kKC * 2 + 128)) != cudaSuccess)
+    return SGR_ERR_CUDA;
+  dim3 grid((unsigned)((a.M + kTM - 1) / kTM), (unsigned)((a.N + NT - 1) / NT), 1);
+  k_gemm_tma<NT><<<grid, kThreads, smem, st>>>(a, ma, mb, ns);
+  sgr::count_launches(1);
+  return cudaGetLastError() == cudaSuccess ? SGR_OK : SGR_ERR_CUDA;
 }
 
 template <int NT, bool A_T, bool B_T>
@@ -255,6 +502,7 @@ int launch(const sgr_gemm_args& a, cudaStream_t st) {
 
 template <int NT>
 int launch_nt(const sgr_gemm_args& a, cudaStream_t st) {
+  if (!a.a_trans && !a.b_trans && a.split_k == 0) return launch_tma<NT>(a, st);
   if (!a.a_trans && !a.b_trans) return launch<NT, false, false>(a, st);
   if (a.a_trans && a.b_trans) return launch<NT, true, true>(a, st);
   return SGR_ERR_UNSUPPORTED;
