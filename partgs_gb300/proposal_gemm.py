@@ -64,3 +64,34 @@ def gemm(a, b, out, epilogue, bias=None, mask=None, trans=False, split_k=0):
                     split_k, status_word(out.device).data_ptr())
     L.check(_lib().sgr_mlp_gemm(C.byref(args), torch.cuda.current_stream().cuda_stream), "sgr_mlp_gemm")
     return out
+
+
+def main():
+    """python -m partgs_gb300.proposal_gemm: CUDA-event timings of the
+    network's per-point layer shapes (262,144 rows), this GEMM against a
+    PyTorch bf16 matmul followed by ReLU."""
+    def timed(fn, n=20):
+        for _ in range(3):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(n):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / n * 1e-3
+    g = torch.Generator().manual_seed(0)
+    for M, N, K in ((262144, 64, 16), (262144, 128, 64), (262144, 256, 128), (262144, 128, 256)):
+        a = torch.randn(M, K, generator=g).to(torch.bfloat16).cuda()
+        b = torch.randn(N, K, generator=g).to(torch.bfloat16).cuda()
+        out = torch.empty(M, N, dtype=torch.bfloat16, device="cuda")
+        t = timed(lambda: gemm(a, b, out, RELU_BF16))
+        t_ref = timed(lambda: torch.relu(a @ b.t()))
+        nbytes = (M * K + N * K + M * N) * 2
+        print(f"M={M} N={N} K={K}: {t * 1e6:.1f} us, {2 * M * N * K / t / 1e12:.1f} TFLOP/s, "
+              f"{nbytes / t / 1e9:.0f} GB/s; torch matmul+relu {t_ref * 1e6:.1f} us")
+
+
+if __name__ == "__main__":
+    main()
