@@ -540,7 +540,7 @@ def _mapped_depth(variant, f, depth):
 
 
 def render_forward(pre, point_list, ranges, cam: Camera, s: Surfels, bg, variant=PLAIN, dtype=np.float64,
-                   amb_tol=2e-6, tiles=None):
+                   amb_tol=2e-6, tiles=None, alpha_tol=None):
     f = _f(dtype)
     gx, gy = pre["grid"]
     W, H = cam.width, cam.height
@@ -595,10 +595,14 @@ def render_forward(pre, point_list, ranges, cam: Camera, s: Surfels, bg, variant
         ok &= ~(alpha < f(1.0) / f(255.0))
         test_T = T * (1 - alpha)
         # ambiguity bookkeeping (only where a decision is close)
-        near_alpha = act & (np.abs(alpha - 1 / 255.0) <= amb_tol / 255.0)
+        # the alpha cutoff and the stop test take alpha_tol (default amb_tol):
+        # near the cutoff alpha carries the FP32 error of the splat
+        # intersection's cross product, which cancels for distant pixels
+        a_tol = amb_tol if alpha_tol is None else alpha_tol
+        near_alpha = act & (np.abs(alpha - 1 / 255.0) <= a_tol / 255.0)
         near_branch = act & (np.abs(rho3d - rho2d) <= amb_tol * np.maximum(rho3d, rho2d)) & (rho < 12.0)
         stop = ok & (test_T < f(1e-4))
-        near_stop = ok & (np.abs(test_T - 1e-4) <= amb_tol * 1e-4)
+        near_stop = ok & (np.abs(test_T - 1e-4) <= a_tol * 1e-4)
         acc = ok & ~stop
         near_med = acc & (np.abs(T - 0.5) <= amb_tol)
         amb |= near_alpha | near_branch | near_stop | near_med
@@ -678,12 +682,12 @@ def _gather_pixels(img, X, Y, inside):
 # full forward of one view
 # --------------------------------------------------------------------------
 def forward_view(s: Surfels, cam: Camera, bg, variant=PLAIN, dtype=np.float64, amb_tol=2e-6,
-                 tiles=None) -> ViewState:
+                 tiles=None, alpha_tol=None) -> ViewState:
     """Forward of one view; with ``tiles`` only those tiles are blended (the
     other pixels stay zero)."""
     pre = preprocess(s, cam, variant, dtype, amb_tol)
     point_list, ranges, keys = bin_tiles(pre)
-    rf = render_forward(pre, point_list, ranges, cam, s, bg, variant, dtype, amb_tol, tiles)
+    rf = render_forward(pre, point_list, ranges, cam, s, bg, variant, dtype, amb_tol, tiles, alpha_tol)
     st = ViewState(
         radii=pre["radii"], tiles_touched=pre["tiles_touched"], means2D=pre["means2D"],
         depths=pre["depths"], transmat=pre["transmat"], normal_opacity=pre["normal_opacity"],
