@@ -164,7 +164,7 @@ def run_gpu(args):
     targets = targets_host.to(dev)
 
     tr = SurfelTrainer(scene, cams, device=dev)
-    tr.capture(targets, warmup=3)            # sizes the cell lists from the eager warm-up steps
+    tr.capture(targets, warmup=3, autotune=True)   # cell size timed per workload; warm-up sizes the lists
     launches_per_step = tr.launches_per_step
     for _ in range(args.warmup):
         tr.replay()
@@ -252,7 +252,8 @@ def run_gpu(args):
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene and targets)",
             "config": dict(_workload_config(args.workload), keys=keys, cell_list_entries=nbins,
-                           cell_list_capacity=tr.raster.bin_capacity, parallelism=f"replicas x{ws}"),
+                           cell_list_capacity=tr.raster.bin_capacity, cell_tiles=tr.raster.cell_tiles,
+                           parallelism=f"replicas x{ws}"),
             "e2e": {"value": ws / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(targets_host.numel() * 4),
                     "d2h_bytes_per_step": 4},
             "roofline": roofline, "gpu_launches": int(launches_per_step) * args.steps, "clocks": clk}

@@ -72,6 +72,7 @@ extern "C" {
 #define SGR_VARIANT_PART 1
 #define SGR_MAX_SEMANTICS 16         /* the part variant's fixed register array, P1 forward.cu:317 */
 #define SGR_TILE 16                  /* tile edge in pixels, cuda_rasterizer/config.h:15-16 */
+#define SGR_DEFAULT_CELL_TILES 8     /* cell edge in tiles when sgr_batch.cell_tiles is 0 */
 
 /* One scene: a contiguous range of surfels seen by a contiguous range of views. */
 typedef struct sgr_scene_desc {
@@ -121,6 +122,8 @@ typedef struct sgr_batch {
     const float* colors_precomp;     /* [P,3] or NULL */
     const float* transmat_precomp;   /* [P,9] or NULL (single-view batches only) */
     const float* semantics;          /* [P,S] or NULL */
+    int32_t cell_tiles;              /* edge, in tiles, of the cells records are binned into: 1, 2, 4, 8 or 16;
+                                        0 for the default (SGR_DEFAULT_CELL_TILES) */
 } sgr_batch;
 
 /* Workspace sizes and the layout of the geometry workspace. */

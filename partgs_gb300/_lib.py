@@ -45,7 +45,7 @@ class Batch(C.Structure):
         ("semantic_channels", _i), ("prefiltered", _i), ("scale_modifier", _f),
         ("scenes", _p), ("views", _p), ("viewmatrix", _p), ("projmatrix", _p), ("campos", _p),
         ("background", _p), ("means3D", _p), ("scales", _p), ("rotations", _p), ("opacities", _p),
-        ("shs", _p), ("colors_precomp", _p), ("transmat_precomp", _p), ("semantics", _p),
+        ("shs", _p), ("colors_precomp", _p), ("transmat_precomp", _p), ("semantics", _p), ("cell_tiles", _i),
     ]
 
 

@@ -27,7 +27,7 @@ class _MultiViewFn(torch.autograd.Function):
         color, others, semantic, radii, state = _r.forward(
             cfg.variant, means3D, opacities, shs, colors_precomp, scales, rotations, None, semantics, cfg.viewset,
             cfg.bg, cfg.sh_degree, 1.0, False, bin_capacity=cfg.bin_capacity, tables=cfg.tables,
-            status_host=cfg.status)
+            status_host=cfg.status, cell_tiles=cfg.cell_tiles)
         ctx.state = state
         ctx.cfg = cfg
         ctx.op_shape = opacities.shape
@@ -53,12 +53,13 @@ class MultiViewRasterizer:
     once, so calls make no host-to-device copies."""
 
     def __init__(self, cameras, bg, sh_degree=3, variant=L.SGR_VARIANT_PLAIN, bin_capacity=None,
-                 scene_sizes=None, scene_views=None, num_surfels=None, device="cuda"):
+                 scene_sizes=None, scene_views=None, num_surfels=None, device="cuda", cell_tiles=0):
         dev = torch.device(device)
         self.cameras = list(cameras)
         self.variant = variant
         self.sh_degree = sh_degree
         self.bin_capacity = bin_capacity
+        self.cell_tiles = cell_tiles
         self.bg = torch.as_tensor(bg, dtype=torch.float32, device=dev)
         vm = torch.stack([torch.as_tensor(c.world_view_transform, dtype=torch.float32) for c in cameras])
         pm = torch.stack([torch.as_tensor(c.full_proj_transform, dtype=torch.float32) for c in cameras])

@@ -53,6 +53,9 @@ int check_batch(const sgr_batch* b) {
   if (b->num_scenes < 1 || b->num_views < 1 || b->height < 1 || b->width < 1) return SGR_ERR_INVALID_ARGUMENT;
   if (b->num_surfels < 0 || b->num_records < 0) return SGR_ERR_INVALID_ARGUMENT;
   if (b->semantic_channels < 0) return SGR_ERR_INVALID_ARGUMENT;
+  if (b->cell_tiles != 0 && b->cell_tiles != 1 && b->cell_tiles != 2 && b->cell_tiles != 4 && b->cell_tiles != 8 &&
+      b->cell_tiles != 16)
+    return SGR_ERR_INVALID_ARGUMENT;
   if (b->semantic_channels > SGR_MAX_SEMANTICS) return SGR_ERR_SEMANTIC_CHANNELS;
   if (b->variant == SGR_VARIANT_PLAIN && b->semantic_channels != 0) return SGR_ERR_INVALID_ARGUMENT;
   if (!b->scenes || !b->views || !b->viewmatrix || !b->projmatrix || !b->campos || !b->background)
@@ -105,8 +108,9 @@ int scratch_layout(const sgr_batch* b, long long cap, ScratchLayout& L) {
   (void)cap;
   int gx, gy;
   tile_grid(b, gx, gy);
-  if (!binning_supported(gx, gy)) return SGR_ERR_UNSUPPORTED;   // tile grid too large for the cell lists
-  const size_t bin = bin_scratch_bytes((long long)R, b->num_views, gx, gy);
+  const int B = cell_tiles_of(*b);
+  if (!binning_supported(gx, gy, B)) return SGR_ERR_UNSUPPORTED;   // cell size, or a grid too large for it
+  const size_t bin = bin_scratch_bytes((long long)R, b->num_views, gx, gy, B);
   L.bin = o;
   o = align_up(o + bin);
   L.end = o;
@@ -130,11 +134,12 @@ int sizes_impl(const sgr_batch* b, long long cap, sgr_sizes* s) {
   s->off_n_contrib = o; o = align_up(o + V * 2 * HW * 4);
   s->off_status = o; o = align_up(o + sizeof(Status));
   s->off_rects = o; o = align_up(o + R * 8);
-  const size_t cells = V * (size_t)bin_cells_x(gx) * bin_cells_y(gy);
+  const int B = cell_tiles_of(*b);
+  const size_t cells = V * (size_t)bin_cells(gx, B) * bin_cells(gy, B);
   s->off_bin_start = o; o = align_up(o + cells * 4);
   s->off_bin_count = o; o = align_up(o + cells * 4);
   s->off_tile_resume = o; o = align_up(o + V * gx * gy * 8);
-  s->cell_tiles = kBinTiles;
+  s->cell_tiles = B;
   s->geom_bytes = o;
   s->list_bytes = align_up((size_t)std::max(0LL, cap) * 4);
   ScratchLayout L;
@@ -173,6 +178,7 @@ GeomView geom_view(const sgr_batch* b, const sgr_sizes& s, void* geom, void* scr
   g.depth_keys_sorted = (sp && L) ? reinterpret_cast<unsigned long long*>(sp + L->depth_keys_sorted) : nullptr;
   g.tiles_x = s.tiles_x;
   g.tiles_y = s.tiles_y;
+  g.cell_tiles = s.cell_tiles;
   return g;
 }
 

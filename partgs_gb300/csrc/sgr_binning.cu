@@ -1,5 +1,5 @@
-// Cell lists: the records of each view binned into square cells of
-// kBinTiles x kBinTiles tiles, each cell's list in depth order.
+// Cell lists: the records of each view binned into square cells of B x B
+// tiles (the batch's cell_tiles), each cell's list in depth order.
 //
 // The reference emits one 64-bit key (tile << 32 | depth bits) per (surfel,
 // tile) pair in surfel order and radix-sorts them (cuda_rasterizer/
@@ -103,7 +103,7 @@ __global__ void __launch_bounds__(256) k_gather_rects(const uint32_t* __restrict
                                                       const int* __restrict__ radii,
                                                       unsigned long long* __restrict__ counts,
                                                       uint2* __restrict__ rects, Status* status, long long R,
-                                                      int gx, int gy) {
+                                                      int gx, int gy, int B) {
   __shared__ unsigned long long s_sum[8];
   const long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   unsigned int cells = 0;
@@ -118,7 +118,7 @@ __global__ void __launch_bounds__(256) k_gather_rects(const uint32_t* __restrict
       tile_rect(r2.y, r2.z, radii[r], gx, gy, x0, y0, x1, y1);
       out = pack_rect(x0, y0, x1, y1);
       int cx0, cy0, cx1, cy1;
-      cell_rect(out, kBinTiles, cx0, cy0, cx1, cy1);
+      cell_rect(out, B, cx0, cy0, cx1, cy1);
       cells = (unsigned int)((cx1 - cx0) * (cy1 - cy0));
     }
     rects[j] = out;
@@ -370,16 +370,14 @@ int run_cells(const sgr_batch& b, const GeomView& g, int B, bool ids, uint32_t* 
 
 }  // namespace
 
-int bin_cells_x(int gx) { return (gx + kBinTiles - 1) / kBinTiles; }
-int bin_cells_y(int gy) { return (gy + kBinTiles - 1) / kBinTiles; }
-
-bool binning_supported(int gx, int gy) {
-  const int cx = bin_cells_x(gx), cy = bin_cells_y(gy);
+bool binning_supported(int gx, int gy, int B) {
+  if (B != 1 && B != 2 && B != 4 && B != 8 && B != 16) return false;
+  const int cx = bin_cells(gx, B), cy = bin_cells(gy, B);
   return gx < 65536 && gy < 65536 && (size_t)(cx + 1) * (cy + 1) * 4 <= kMaxDynSmem && writer_warps(cx * cy) > 0;
 }
 
-size_t bin_scratch_bytes(long long R, int V, int gx, int gy) {
-  return cell_scratch(R, V, bin_cells_x(gx) * bin_cells_y(gy), false).end;
+size_t bin_scratch_bytes(long long R, int V, int gx, int gy, int B) {
+  return cell_scratch(R, V, bin_cells(gx, B) * bin_cells(gy, B), false).end;
 }
 
 size_t tile_list_scratch_bytes(long long R, int V, int gx, int gy) {
@@ -388,12 +386,13 @@ size_t tile_list_scratch_bytes(long long R, int V, int gx, int gy) {
 
 void launch_gather_rects(const GeomView& g, long long R, cudaStream_t st) {
   k_gather_rects<<<(unsigned)((R + 255) / 256), 256, 0, st>>>(g.depth_order, g.tiles_touched, g.records, g.radii,
-                                                               g.offsets, g.rects, g.status, R, g.tiles_x, g.tiles_y);
+                                                               g.offsets, g.rects, g.status, R, g.tiles_x, g.tiles_y,
+                                                               g.cell_tiles);
   count_launches();
 }
 
 int launch_binning(const sgr_batch& b, const GeomView& g, void* scratch, cudaStream_t st) {
-  return run_cells(b, g, kBinTiles, false, const_cast<uint32_t*>(g.bins), g.bin_capacity, SGR_FLAG_BIN_OVERFLOW,
+  return run_cells(b, g, g.cell_tiles, false, const_cast<uint32_t*>(g.bins), g.bin_capacity, SGR_FLAG_BIN_OVERFLOW,
                    g.bin_count, g.bin_start, nullptr, scratch, st);
 }
 

@@ -124,8 +124,9 @@ __device__ int stream_window(const GeomView& g, const uint32_t* __restrict__ lis
 // The cell list of tile (tx, ty) of view v: its start in g.bins and its
 // length, clipped to the entries the buffer holds.
 __device__ __forceinline__ void cell_list(const GeomView& g, int v, int tx, int ty, const uint32_t*& list, int& len) {
-  const int cx = (g.tiles_x + kBinTiles - 1) / kBinTiles, cy = (g.tiles_y + kBinTiles - 1) / kBinTiles;
-  const size_t cell = (size_t)v * cx * cy + (size_t)(ty / kBinTiles) * cx + (tx / kBinTiles);
+  const int B = g.cell_tiles;
+  const int cx = (g.tiles_x + B - 1) / B, cy = (g.tiles_y + B - 1) / B;
+  const size_t cell = (size_t)v * cx * cy + (size_t)(ty / B) * cx + (tx / B);
   const long long s = g.bin_start[cell];
   const long long n = g.bin_count[cell];
   list = g.bins + s;

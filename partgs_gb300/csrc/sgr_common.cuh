@@ -40,8 +40,11 @@ constexpr int kGradUsed = 18;
 // Records per chunk of the depth order, and list entries per streaming window
 // of a blend CTA (four per thread), sgr_binning.cu / sgr_blend.cu.
 constexpr int kChunk = 4 * kBlock;
-// Edge, in tiles, of the square cells records are binned into (sgr_binning.cu).
-constexpr int kBinTiles = 8;
+// Edge, in tiles, of the square cells records are binned into
+// (sgr_binning.cu): the batch's cell_tiles, or the default.
+__host__ __device__ inline int cell_tiles_of(const sgr_batch& b) {
+  return b.cell_tiles > 0 ? b.cell_tiles : SGR_DEFAULT_CELL_TILES;
+}
 
 // Host-side count of this library's kernel launches (sgr_kernel_launches).
 void count_launches(int n = 1);

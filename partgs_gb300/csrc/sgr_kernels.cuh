@@ -25,6 +25,7 @@ struct GeomView {
   uint2* tile_resume;                    // [V*tiles] (cell-list entries the forward scanned, tile entries found)
   const uint32_t* bins;                  // cell lists: depth-order positions
   long long bin_capacity;                // entries `bins` holds
+  int cell_tiles;                        // cell edge in tiles
   float* final_T;                        // [V][3][H][W]
   uint32_t* n_contrib;                   // [V][2][H][W]
   Status* status;
@@ -224,10 +225,9 @@ void launch_preprocess(const sgr_batch& b, const GeomView& g, cudaStream_t st);
 void launch_store_key_count(const GeomView& g, long long R, cudaStream_t st);
 // Cell lists (sgr_binning.cu).  binning_supported is false for tile grids
 // whose cell difference array does not fit in shared memory.
-int bin_cells_x(int gx);
-int bin_cells_y(int gy);
-bool binning_supported(int gx, int gy);
-size_t bin_scratch_bytes(long long R, int V, int gx, int gy);
+inline int bin_cells(int g, int B) { return (g + B - 1) / B; }
+bool binning_supported(int gx, int gy, int B);
+size_t bin_scratch_bytes(long long R, int V, int gx, int gy, int B);
 size_t tile_list_scratch_bytes(long long R, int V, int gx, int gy);
 void launch_gather_rects(const GeomView& g, long long R, cudaStream_t st);
 int launch_binning(const sgr_batch& b, const GeomView& g, void* scratch, cudaStream_t st);

@@ -158,13 +158,18 @@ class SurfelTrainer:
         self.opt.step()
         return loss
 
-    def capture(self, targets, warmup=3, headroom=1.25):
+    def capture(self, targets, warmup=3, headroom=1.25, autotune=False):
         """Captures step() into a CUDA graph reading ``self.targets``.
 
-        Without a cell-list capacity, the eager warm-up steps size it
-        (``headroom`` times the largest entry count they saw); after replays,
-        ``self.raster.counts()`` reports the flags (SGR_FLAG_BIN_OVERFLOW
-        when the parameters have drifted past the capacity)."""
+        With ``autotune`` the cell size is picked first by timing eager steps
+        (``autotune.tune_cells``; parameters restored).  Without a cell-list
+        capacity, the eager warm-up steps size it (``headroom`` times the
+        largest entry count they saw); after replays, ``self.raster.counts()``
+        reports the flags (SGR_FLAG_BIN_OVERFLOW when the parameters have
+        drifted past the capacity)."""
+        if autotune:
+            from .autotune import tune_cells
+            tune_cells(self, targets)
         self.targets = targets.clone()
         s = torch.cuda.Stream()
         s.wait_stream(torch.cuda.current_stream())
