@@ -30,7 +30,7 @@
  * (surfel, tile) keys, which it learns with a blocking device-to-host copy
  * (cuda_rasterizer/rasterizer_impl.cu:282), and writes and sorts every key.
  * Here the records are put in depth order once and binned into cells of
- * 8x8 tiles; each tile's list is streamed out of its cell's list by the
+ * B x B tiles (sgr_batch.cell_tiles); each tile's list is streamed out of its cell's list by the
  * blend kernels, so no per-tile list is written.  The forward is split in
  * two calls: sgr_forward_geometry counts, on the device, the keys (the
  * reference's num_rendered) and the (record, cell) entries the cell lists
