@@ -354,6 +354,36 @@ typedef struct sgr_adam_args {
  * step count; the call increments it first.  Never synchronises. */
 int sgr_adam_step(const sgr_adam_args* args, float* step, void* stream);
 
+/* ---- point-level parameter activations ---------------------------------- */
+
+/* The training step's parameter getters (scene/gaussian_model.py:198-218):
+ * scales = exp(log_scaling), rotations = F.normalize(rotation),
+ * opacities = sigmoid(opacity_logit), shs = cat(features_dc, features_rest),
+ * and their adjoints.  Device pointers; P surfels, M = sh_coeffs. */
+typedef struct sgr_activate_args {
+    int64_t P;
+    int32_t sh_coeffs;           /* M, 1..16 */
+    const float* log_scaling;    /* [P,2] */
+    const float* rotation;       /* [P,4] */
+    const float* opacity_logit;  /* [P] */
+    const float* features_dc;    /* [P,1,3] */
+    const float* features_rest;  /* [P,M-1,3] */
+    float* scales;               /* forward outputs: [P,2], [P,4], [P], [P,M,3] */
+    float* rotations;
+    float* opacities;
+    float* shs;
+    float* d_log_scaling;        /* backward outputs, the inputs' shapes */
+    float* d_rotation;
+    float* d_opacity_logit;
+    float* d_features_dc;
+    float* d_features_rest;
+} sgr_activate_args;
+
+int sgr_activate_forward(const sgr_activate_args* args, void* stream);
+/* Upstream gradients may be NULL (zero). */
+int sgr_activate_backward(const sgr_activate_args* args, const float* d_scales, const float* d_rotations,
+                          const float* d_opacities, const float* d_shs, void* stream);
+
 /* ---- proposal network: BF16 tensor-core GEMM --------------------------- */
 
 /* Epilogues of sgr_mlp_gemm (x = accumulator + bias) */

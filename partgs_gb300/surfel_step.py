@@ -8,7 +8,8 @@ loss between rendered normals and normals from the median depth map
 then an Adam update (scene/gaussian_model.py:266, eps 1e-15; one launch,
 optim.py).  Parameters use
 the reference's activations: exp scales, normalised quaternions, sigmoid
-opacity, concatenated SH features (scene/gaussian_model.py:198-218).
+opacity, concatenated SH features (scene/gaussian_model.py:198-218), in one
+CUDA kernel each way (activations.py).
 
 ``SurfelTrainer.capture()`` records the whole step (forward, losses,
 backward, optimiser) in one CUDA graph; ``replay()`` runs it.
@@ -21,6 +22,7 @@ import torch
 import torch.nn.functional as F
 
 from . import _lib
+from .activations import activate
 from .batched import MultiViewRasterizer
 from .optim import SurfelAdam
 
@@ -126,10 +128,8 @@ class SurfelTrainer:
         return [self.xyz, self.features_dc, self.features_rest, self.opacity_logit, self.log_scaling, self.rotation]
 
     def loss_fn(self, targets):
-        scales = torch.exp(self.log_scaling)
-        rots = F.normalize(self.rotation)
-        opac = torch.sigmoid(self.opacity_logit)
-        shs = torch.cat((self.features_dc, self.features_rest), dim=1)
+        scales, rots, opac, shs = activate(self.log_scaling, self.rotation, self.opacity_logit, self.features_dc,
+                                           self.features_rest)
         color, allmap, _, _ = self.raster(self.xyz, opac, shs, scales, rots)
         if self.point_loss is not None:
             return self.point_loss(color, allmap, targets)
