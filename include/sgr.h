@@ -384,6 +384,22 @@ int sgr_activate_forward(const sgr_activate_args* args, void* stream);
 int sgr_activate_backward(const sgr_activate_args* args, const float* d_scales, const float* d_rotations,
                           const float* d_opacities, const float* d_shs, void* stream);
 
+/* ---- Chamfer evaluation (utils/blender_eval.py:25-111) ------------------- */
+
+/* Exact nearest neighbour in r (m points, xyz float) of each of the n points
+ * of q: dist [n] (Euclidean) and, unless NULL, idx [n] (first minimum). */
+int sgr_nn_search(const float* q, int64_t n, const float* r, int64_t m, float* dist, int32_t* idx, void* stream);
+
+/* The reference's radius downsample: in index order, point i is kept unless
+ * an earlier kept point lies within `radius` (distance <= radius, fp64 like
+ * the reference).  pts [n,3] float64 on the device, lo / hi their bounding
+ * box on the host; state [n] receives 1 (kept) or 2 (removed); rounds (host,
+ * may be NULL) the number of parallel rounds.  Synchronises the host once
+ * per round. */
+size_t sgr_downsample_scratch_bytes(int64_t n);
+int sgr_radius_downsample(const double* pts, int64_t n, const double* lo, const double* hi, double radius,
+                          uint8_t* state, void* scratch, size_t scratch_bytes, int32_t* rounds, void* stream);
+
 /* ---- proposal network: BF16 tensor-core GEMM --------------------------- */
 
 /* Epilogues of sgr_mlp_gemm (x = accumulator + bias) */
