@@ -384,6 +384,54 @@ int sgr_activate_forward(const sgr_activate_args* args, void* stream);
 int sgr_activate_backward(const sgr_activate_args* args, const float* d_scales, const float* d_rotations,
                           const float* d_opacities, const float* d_shs, void* stream);
 
+/* ---- block-stage superquadric losses -------------------------------------
+ * games/block_mesh_splatting/scene/block_gaussian_model.py:522-582: the ray
+ * coverage (ray_in_mask), uncoverage (ray_out_mask) and occupancy
+ * (primitive_opacity) losses over a view's ray samples, and the overlap loss
+ * over random points of every block, with the SDF of
+ * games/block_mesh_splatting/utils/superquadric.py:25-46 (as_sdf=2). */
+
+#define SGR_SQ_MAX_BLOCKS 64
+
+typedef struct sgr_sq_loss_args {
+    int32_t n_blocks;            /* 1 .. SGR_SQ_MAX_BLOCKS */
+    float ratio;                 /* ratio_block_scene */
+    const float* S;              /* [n,3] block scales (get_mesh_scaling) */
+    const float* R;              /* [n,3,3] row-major rotation matrices */
+    const float* T;              /* [n,3] translations */
+    const float* eps1;           /* [n] */
+    const float* eps2;           /* [n] */
+    const float* occ_logit;      /* [n] sq_occ (alpha = sigmoid); NULL: 0 */
+    /* ray losses (n_rays = 0: none; losses[0..2] = 0) */
+    int32_t n_rays, n_samples;
+    const float* ray_origin;     /* [n_rays,3] camera centre per ray */
+    const float* ray_dir;        /* [n_rays,3] pixel point minus centre */
+    const float* ray_jitter;     /* [n_rays,n_samples] uniform [0,1) */
+    const float* ray_label;      /* [n_rays] mask value at the ray's pixel */
+    float near, far;
+    /* overlap loss (n_overlap = 0: none; losses[3] = 0) */
+    int32_t n_overlap;           /* points per block (OVERLAP_N_POINTS) */
+    const float* overlap_unit;   /* [n_blocks,n_overlap,3] uniform in [-1,1] */
+    const float* overlap_noise;  /* [n_blocks] N(0,1) added to occ_logit; NULL: 0 */
+    float overlap_temperature;   /* OVERLAP_TEMPERATURE */
+    float overlap_max_blocks;    /* OVERLAP_N_BLOCKS */
+    /* workspace (sgr_sq_scratch_bytes), outputs and gradients */
+    void* scratch;
+    size_t scratch_bytes;
+    float* losses;               /* [4] device: ray_in_mask, ray_out_mask, primitive_opacity, overlap */
+    float *d_S, *d_R, *d_T, *d_eps1, *d_eps2, *d_occ_logit;   /* written (not accumulated) by the backward */
+} sgr_sq_loss_args;
+
+size_t sgr_sq_scratch_bytes(const sgr_sq_loss_args* args);
+/* Forward: losses[4]; keeps each ray's minimum and occupancy choice in the
+ * scratch for the backward.  Two launches. */
+int sgr_sq_losses_forward(const sgr_sq_loss_args* args, void* stream);
+/* Backward from d_losses[4] (device) to the block parameters, after the
+ * forward with the same arguments and scratch.  Two launches. */
+int sgr_sq_losses_backward(const sgr_sq_loss_args* args, const float* d_losses, void* stream);
+/* The SDF (implicit_sq, as_sdf=2) of points [m,3] to every block: out [n,m]. */
+int sgr_sq_sdf(const sgr_sq_loss_args* args, const float* points, int64_t n_points, float* out, void* stream);
+
 /* ---- Chamfer evaluation (utils/blender_eval.py:25-111) ------------------- */
 
 /* Exact nearest neighbour in r (m points, xyz float) of each of the n points

@@ -9,7 +9,9 @@ first argument, default /root/reference).  It imports, unmodified:
 * utils/point_utils.py         depth_to_normal (normals from a depth map)
 * games/block_mesh_splatting/scene/block_gaussian_model.py
                                update_alpha / get_verts / prepare_scaling_rot / get_opacity
-                               (the superquadric -> surfel binding), differentiated by autograd
+                               (the superquadric -> surfel binding), differentiated by autograd;
+                               summarize_losses' ray and overlap terms (sq_losses.npz, with
+                               scene/cameras.py cast_rays and utils/superquadric.py implicit_sq)
 
 Packages the reference imports but this path does not use (open3d, trimesh,
 pytorch3d, plyfile, simple_knn, PIL, seaborn, matplotlib, iopath) are stubbed
@@ -75,6 +77,110 @@ def _cpu_only():
         k.pop("device", None)
         return real_arange(*a, **k)
     torch.arange = arange
+
+
+def sq_losses(bgm, ref_root):
+    """tests/golden/sq_losses.npz: the block-stage losses of summarize_losses
+    (ray coverage / uncoverage / occupancy over a 16x12 view's rays, and the
+    overlap term with 64 points per block), in float64, and their gradients
+    to the block parameters by autograd.  The camera's own cast_rays makes the
+    ray samples; torch.randperm / torch.rand / torch.randn_like are fed the
+    stored draws."""
+    from scene.cameras import Camera
+    from utils.graphics_utils import getWorld2View2
+    g = torch.Generator().manual_seed(1)
+    torch.set_default_dtype(torch.float64)
+    N, H, W, P, ratio = 4, 12, 16, 64, 0.25
+    S = (torch.rand(N, 3, generator=g) + 0.6).requires_grad_(True)
+    q = torch.randn(N, 4, generator=g)
+    q = q / q.norm(dim=1, keepdim=True)
+    w_, x, y, z = q.unbind(1)
+    R = torch.stack([1 - 2 * (y * y + z * z), 2 * (x * y - w_ * z), 2 * (x * z + w_ * y),
+                     2 * (x * y + w_ * z), 1 - 2 * (x * x + z * z), 2 * (y * z - w_ * x),
+                     2 * (x * z - w_ * y), 2 * (y * z + w_ * x), 1 - 2 * (x * x + y * y)], 1)
+    R = R.reshape(N, 3, 3).detach().requires_grad_(True)
+    T = ((torch.rand(N, 3, generator=g) - 0.5) * 0.3).requires_grad_(True)
+    eps1 = (torch.rand(N, 1, generator=g) * 1.6 + 0.2).requires_grad_(True)
+    eps2 = (torch.rand(N, 1, generator=g) * 1.6 + 0.2).requires_grad_(True)
+    sq_occ = (torch.randn(N, 1, generator=g) * 0.5 + 3.0).requires_grad_(True)   # overlapping, opaque blocks
+    perm = torch.randperm(H * W, generator=g)
+    jitter = torch.rand(H * W, 128, 1, generator=g)
+    unit01 = torch.rand(N, P, 3, generator=g)
+    noise = torch.randn(N, 1, generator=g)
+    mask = (torch.rand(H, W, generator=g) < 0.5).double()
+
+    ang = 0.4
+    c = np.array([3 * math.sin(ang), 0.3, 3 * math.cos(ang)])
+    fwd = -c / np.linalg.norm(c)
+    right = np.cross([0, 1.0, 0], fwd)
+    right /= np.linalg.norm(right)
+    down = np.cross(fwd, right)
+    Rc = np.stack([right, down, fwd], 1)
+    Tc = -Rc.T @ c
+    fovx = math.radians(50)
+    fovy = 2 * math.atan(math.tan(fovx / 2) * H / W)
+    K = torch.zeros((3, 3), dtype=torch.float32)
+    K[0, 0] = (W / 2.0) / math.tan(fovx / 2.0)
+    K[1, 1] = (H / 2.0) / math.tan(fovy / 2.0)
+    K[0, 2] = W / 2.0
+    K[1, 2] = H / 2.0
+    K[2, 2] = 1.0
+    wv = torch.tensor(getWorld2View2(Rc, Tc)).transpose(0, 1).float()
+    recorded = {}
+    cam = types.SimpleNamespace(image_height=H, image_width=W, data_device="cpu", K=K, world_view_transform=wv,
+                                original_mask=mask)
+    cam.invert = types.MethodType(Camera.invert, cam)
+    cam.cam2world = types.MethodType(Camera.cam2world, cam)
+
+    def cast_rays(**kw):
+        pts, idx = Camera.cast_rays(cam, **kw)
+        recorded["points"] = pts
+        return pts, idx
+    cam.cast_rays = cast_rays
+
+    real_rand, real_randperm, real_randn_like = torch.rand, torch.randperm, torch.randn_like
+
+    def rand(*shape, **k):
+        shape = tuple(shape[0]) if len(shape) == 1 and isinstance(shape[0], (tuple, list)) else shape
+        if shape == (H * W, 128, 1):
+            return jitter.clone()
+        if shape == (N, P, 3):
+            return unit01.clone()
+        raise AssertionError(f"unexpected torch.rand{shape}")
+
+    model = bgm.BlockGaussianModel.__new__(bgm.BlockGaussianModel)
+    model.n_blocks = N
+    model.ratio_block_scene = ratio
+    model.coarse_learning = True
+    model.opacity_activation = torch.sigmoid
+    model.sq_occ = sq_occ
+    model._blocks_SRT = (S, R, T)
+    model._blocks_eps = (eps1, eps2)
+    opt = types.SimpleNamespace(rgb_weight=1.0, lambda_dssim=0.2, primtive_scale_weight=0.0, parsimony_weight=0.0,
+                                data_type="blender", ray_coverage_weigth=10.0, ray_uncoverage_weigth=100.0,
+                                occupancy_weight=0.02, overlap_weight=2.0)
+    image = torch.rand(3, H, W, generator=g)
+    n_points = bgm.OVERLAP_N_POINTS
+    bgm.OVERLAP_N_POINTS = P
+    torch.rand, torch.randperm, torch.randn_like = rand, (lambda *a, **k: perm.clone()), (lambda t: noise.clone())
+    try:
+        _, loss, parts = model.summarize_losses(image, image.clone(), cam, opt)
+    finally:
+        torch.rand, torch.randperm, torch.randn_like = real_rand, real_randperm, real_randn_like
+        bgm.OVERLAP_N_POINTS = n_points
+    loss.backward()
+    out = dict(S=S, R=R, T=T, eps1=eps1, eps2=eps2, sq_occ=sq_occ)
+    res = {f"in_{k}": v.detach().numpy() for k, v in out.items()}
+    res.update({f"grad_{k}": v.grad.numpy() for k, v in out.items()})
+    res.update(K=K.numpy(), world_view=wv.numpy(), height=H, width=W, ratio=ratio, near=2.0, far=5.0,
+               ray_idx=perm.numpy(), jitter=jitter[..., 0].numpy(), mask=mask.numpy(), unit01=unit01.numpy(),
+               noise=noise[:, 0].numpy(), weights=np.array([10.0, 100.0, 0.02, 2.0]),
+               points_head=recorded["points"][:, :8].detach().numpy(),
+               losses=np.array([float(parts[k].detach()) for k in ("ray_in_mask", "ray_out_mask", "primitive_opacity",
+                                                          "overlap")]))
+    torch.set_default_dtype(torch.float32)
+    np.savez_compressed(os.path.join(HERE, "sq_losses.npz"), **res)
+    print("wrote", os.path.join(HERE, "sq_losses.npz"), res["losses"])
 
 
 def main(ref_root="/root/reference"):
@@ -194,5 +300,19 @@ def main(ref_root="/root/reference"):
     print("wrote", os.path.join(HERE, "reference_python.npz"), sorted(out))
 
 
+def main_sq(ref_root="/root/reference"):
+    sys.path.insert(0, ref_root)
+    _stub_modules()
+    _cpu_only()
+    import games.block_mesh_splatting.scene.block_gaussian_model as bgm
+    sq_losses(bgm, ref_root)
+
+
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    args = [a for a in sys.argv[1:] if not a.startswith("--")]
+    root = args[0] if args else "/root/reference"
+    if "--sq" in sys.argv:   # only the superquadric-loss fixture
+        main_sq(root)
+    else:
+        main(root)
+        main_sq(root)
