@@ -384,6 +384,18 @@ int sgr_activate_forward(const sgr_activate_args* args, void* stream);
 int sgr_activate_backward(const sgr_activate_args* args, const float* d_scales, const float* d_rotations,
                           const float* d_opacities, const float* d_shs, void* stream);
 
+/* ---- densification statistics (train.py:293-297) ------------------------- */
+
+/* For every surfel and each of its scene's views (device scene / view tables
+ * of the batch) where radii[record] > 0: max_radii2D = max(max_radii2D,
+ * radius), grad_accum += grad_scale * |dmeans2D[record][0:2]|, denom += 1
+ * (scene/gaussian_model.py:515-517), views in order.  radii [R] int32 and
+ * dmeans2D [R,3] as the forward and backward wrote them; max_radii2D,
+ * grad_accum, denom [num_surfels] updated in place. */
+int sgr_densify_stats(const sgr_scene_desc* scenes, int32_t num_scenes, const sgr_view_desc* views,
+                      int32_t num_surfels, const int32_t* radii, const float* dmeans2D, float grad_scale,
+                      float* max_radii2D, float* grad_accum, float* denom, void* stream);
+
 /* ---- block-stage superquadric losses -------------------------------------
  * games/block_mesh_splatting/scene/block_gaussian_model.py:522-582: the ray
  * coverage (ray_in_mask), uncoverage (ray_out_mask) and occupancy

@@ -77,6 +77,19 @@ class SurfelAdam:
         """Gradients are already cleared by ``step``; kept for the optimiser
         interface."""
 
+    def replace(self, params, moments):
+        """New parameter tensors (same groups, new sizes) with their carried
+        (exp_avg, exp_avg_sq); the step count is kept, as torch's Adam keeps
+        each parameter's step through the reference's optimiser surgery."""
+        if len(params) != len(self.entries):
+            raise ValueError("one tensor per parameter group")
+        entries = []
+        for (_, lr, _, _), p, (m, v) in zip(self.entries, params, moments):
+            if p.grad is None:
+                p.grad = torch.zeros_like(p)
+            entries.append((p, lr, m.contiguous(), v.contiguous()))
+        self.entries = entries
+
     def state_tensors(self):
         """The moment buffers and the step count (for snapshots)."""
         return [t for _, _, m, v in self.entries for t in (m, v)] + [self.step_count]

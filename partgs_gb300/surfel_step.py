@@ -91,7 +91,7 @@ class SurfelTrainer:
 
     def __init__(self, scene, cameras, bin_capacity=None, lambda_dssim=0.2, lambda_dist=1000.0,
                  lambda_normal=0.05, depth_ratio=1.0, bg=(0.0, 0.0, 0.0), device="cuda", extent=3.0,
-                 fused_loss=True):
+                 fused_loss=True, densify_stats=False):
         dev = torch.device(device)
         self.xyz = scene.means3D.detach().clone().to(dev).requires_grad_(True)
         self.log_scaling = torch.log(scene.scales).detach().clone().to(dev).requires_grad_(True)
@@ -123,6 +123,12 @@ class SurfelTrainer:
         self.targets = None
         self.graph = None
         self.loss = None
+        self._radii = None
+        # densification statistics, updated by every step (and captured with it)
+        self.stats = None
+        if densify_stats:
+            from .densify import DensifyStats
+            self.stats = DensifyStats(scene.P, dev)
 
     def params(self):
         return [self.xyz, self.features_dc, self.features_rest, self.opacity_logit, self.log_scaling, self.rotation]
@@ -130,7 +136,8 @@ class SurfelTrainer:
     def loss_fn(self, targets):
         scales, rots, opac, shs = activate(self.log_scaling, self.rotation, self.opacity_logit, self.features_dc,
                                            self.features_rest)
-        color, allmap, _, _ = self.raster(self.xyz, opac, shs, scales, rots)
+        color, allmap, _, radii = self.raster(self.xyz, opac, shs, scales, rots)
+        self._radii = radii
         if self.point_loss is not None:
             return self.point_loss(color, allmap, targets)
         return self.reference_loss(color, allmap, targets)
@@ -155,6 +162,11 @@ class SurfelTrainer:
         gradients it consumes."""
         loss = self.loss_fn(targets)
         loss.backward()
+        if self.stats is not None:
+            # the batch loss averages its views: scale the per-view screen-space
+            # gradients back to what a single-view iteration sees
+            self.stats.update(self.raster.tables, self._radii, self.raster.last_means2D_grad,
+                              grad_scale=float(self.raster.num_views))
         self.opt.step()
         return loss
 
@@ -196,6 +208,43 @@ class SurfelTrainer:
 
     def _state(self):
         return [p.detach() for p in self.params()] + self.opt.state_tensors()
+
+    def densify_and_prune(self, max_grad, min_opacity, extent, max_screen_size=None, percent_dense=0.01,
+                          generator=None):
+        """The reference's densify_and_prune on this trainer's surfels, from the
+        statistics the steps gathered (``densify_stats=True``); parameters and
+        Adam moments are replaced, so a captured graph is dropped (capture
+        again).  Returns the new surfel count."""
+        from .densify import densify_and_prune
+        if self.stats is None:
+            raise RuntimeError("densification statistics are off (SurfelTrainer(..., densify_stats=True))")
+        params = dict(zip(("xyz", "f_dc", "f_rest", "opacity", "scaling", "rotation"),
+                          (p.detach() for p in self.params())))
+        adam = {k: (m, v) for k, (_, _, m, v) in zip(params, self.opt.entries)}
+        params, _, adam, self.stats = densify_and_prune(params, self.stats, max_grad, min_opacity, extent,
+                                                        max_screen_size, percent_dense, adam=adam,
+                                                        generator=generator)
+        self._replace(params, adam)
+        return int(self.xyz.shape[0])
+
+    def reset_opacity(self):
+        """opacity = logit(min(opacity, 0.01)) with its moments cleared."""
+        from .densify import reset_opacity
+        with torch.no_grad():
+            params, adam = reset_opacity({"opacity": self.opacity_logit.detach()},
+                                         {"opacity": (self.opt.entries[3][2], self.opt.entries[3][3])})
+            self.opacity_logit.copy_(params["opacity"])
+            for dst, src in zip(self.opt.entries[3][2:], adam["opacity"]):
+                dst.copy_(src)
+
+    def _replace(self, params, adam):
+        new = [params[k].contiguous().requires_grad_(True) for k in params]
+        (self.xyz, self.features_dc, self.features_rest, self.opacity_logit, self.log_scaling,
+         self.rotation) = new
+        self.opt.replace(new, [adam[k] for k in params])
+        self.graph = None
+        self.loss = None
+        self.raster.set_capacity(None)
 
     def snapshot(self):
         """Copies of the parameters and the optimiser state."""

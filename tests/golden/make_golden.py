@@ -300,6 +300,102 @@ def main(ref_root="/root/reference"):
     print("wrote", os.path.join(HERE, "reference_python.npz"), sorted(out))
 
 
+def densify(ref_root):
+    """tests/golden/densify.npz: TwoGaussianModel's densify_and_prune (clone,
+    split with the stored normal draws, prune, optimiser state surgery) and
+    reset_opacity on 400 surfels, the statistics of train.py:293-297 over
+    three iterations, and both models' PLY attribute lists."""
+    import games.block_mesh_splatting.scene.two_gaussian_model as tgm
+    import scene.gaussian_model as gm
+    from utils import general_utils
+    g = torch.Generator().manual_seed(2)
+    P, M = 400, 16
+    real_zeros, real_normal = torch.zeros, torch.normal
+
+    def zeros(*a, **k):
+        k.pop("device", None)
+        return real_zeros(*a, **k)
+
+    model = tgm.TwoGaussianModel.__new__(tgm.TwoGaussianModel)
+    gm.GaussianModel.setup_functions(model) if hasattr(gm.GaussianModel, "setup_functions") else None
+    model.scaling_activation, model.scaling_inverse_activation = torch.exp, torch.log
+    model.opacity_activation, model.inverse_opacity_activation = torch.sigmoid, general_utils.inverse_sigmoid
+    model.rotation_activation = torch.nn.functional.normalize
+    model.percent_dense = 0.01
+    model.max_sh_degree = 3
+    raw = {"xyz": torch.randn(P, 3, generator=g), "f_dc": torch.randn(P, 1, 3, generator=g),
+           "f_rest": torch.randn(P, M - 1, 3, generator=g) * 0.1,
+           "opacity": torch.randn(P, 1, generator=g) * 2 - 1,
+           "scaling": torch.log(torch.rand(P, 2, generator=g) * 0.05 + 0.005),
+           "rotation": torch.randn(P, 4, generator=g)}
+    attr = {"xyz": "_xyz", "f_dc": "_features_dc", "f_rest": "_features_rest", "opacity": "_opacity",
+            "scaling": "_scaling", "rotation": "_rotation"}
+    for k, v in raw.items():
+        setattr(model, attr[k], torch.nn.Parameter(v.clone()))
+    model._semantic = torch.rand(P, 4, generator=g)
+    model.optimizer = torch.optim.Adam([{"params": [getattr(model, attr[k])], "lr": 0.01, "name": k} for k in raw],
+                                       lr=0.0, eps=1e-15)
+    for k in raw:   # one step so every parameter has Adam moments to carry
+        getattr(model, attr[k]).grad = torch.randn(raw[k].shape, generator=g)
+    model.optimizer.step()
+    out = {f"in_{k}": getattr(model, attr[k]).detach().numpy().copy() for k in raw}
+    for k in raw:
+        st = model.optimizer.state[getattr(model, attr[k])]
+        out[f"in_m_{k}"], out[f"in_v_{k}"] = st["exp_avg"].numpy().copy(), st["exp_avg_sq"].numpy().copy()
+    out["in_semantic"] = model._semantic.numpy().copy()
+    # statistics: three views' radii and screen-space gradients
+    model.xyz_gradient_accum = torch.zeros(P, 1)
+    model.denom = torch.zeros(P, 1)
+    model.max_radii2D = torch.zeros(P)
+    radii = (torch.rand(3, P, generator=g) * 30).int() * (torch.rand(3, P, generator=g) < 0.7).int()
+    g2d = torch.randn(3, P, 3, generator=g) * 2e-4
+    for it in range(3):
+        vis = radii[it] > 0
+        model.max_radii2D[vis] = torch.max(model.max_radii2D[vis], radii[it][vis])
+        vp = types.SimpleNamespace(grad=g2d[it])
+        model.add_densification_stats(vp, vis)
+    out.update(stats_radii=radii.numpy(), stats_grad=g2d.numpy(), stats_accum=model.xyz_gradient_accum.numpy().copy(),
+               stats_denom=model.denom.numpy().copy(), stats_max_radii=model.max_radii2D.numpy().copy())
+    # densify and prune with grad threshold 2e-4, min opacity 0.05, extent 1.5, screen size 20
+    grads = model.xyz_gradient_accum / model.denom
+    grads[grads.isnan()] = 0.0
+    n_split = None
+    draws = {}
+
+    def normal(mean, std, *a, **k):
+        x = real_normal(torch.zeros_like(mean), torch.ones_like(std), generator=g) * std + mean
+        draws["split"] = x.detach().clone()
+        return x
+    torch.zeros, torch.normal = zeros, normal
+    general_utils.torch.zeros = zeros
+    try:
+        model.densify_and_prune(2e-4, 0.05, 1.5, 20)
+    finally:
+        torch.zeros, torch.normal = real_zeros, real_normal
+    out["split_samples"] = draws["split"].numpy()
+    for k in raw:
+        t = getattr(model, attr[k])
+        out[f"out_{k}"] = t.detach().numpy()
+        st = model.optimizer.state[t]
+        out[f"out_m_{k}"], out[f"out_v_{k}"] = st["exp_avg"].detach().numpy(), st["exp_avg_sq"].detach().numpy()
+    out["out_semantic"] = model._semantic.detach().numpy()
+    out["densify_args"] = np.array([2e-4, 0.05, 1.5, 20, 0.01])
+    # reset_opacity on the densified set
+    torch.zeros = zeros
+    try:
+        model.reset_opacity()
+    finally:
+        torch.zeros = real_zeros
+    t = model._opacity
+    out["reset_opacity"] = t.detach().numpy()
+    out["reset_m_opacity"] = model.optimizer.state[t]["exp_avg"].detach().numpy()
+    # PLY attribute lists (construct_list_of_attributes of both models)
+    out["ply_attrs_two"] = np.array(tgm.TwoGaussianModel.construct_list_of_attributes(model))
+    out["ply_attrs_plain"] = np.array(gm.GaussianModel.construct_list_of_attributes(model))
+    np.savez_compressed(os.path.join(HERE, "densify.npz"), **out)
+    print("wrote", os.path.join(HERE, "densify.npz"), P, "->", out["out_xyz"].shape[0])
+
+
 def main_sq(ref_root="/root/reference"):
     sys.path.insert(0, ref_root)
     _stub_modules()
@@ -308,11 +404,21 @@ def main_sq(ref_root="/root/reference"):
     sq_losses(bgm, ref_root)
 
 
+def main_densify(ref_root="/root/reference"):
+    sys.path.insert(0, ref_root)
+    _stub_modules()
+    _cpu_only()
+    densify(ref_root)
+
+
 if __name__ == "__main__":
     args = [a for a in sys.argv[1:] if not a.startswith("--")]
     root = args[0] if args else "/root/reference"
     if "--sq" in sys.argv:   # only the superquadric-loss fixture
         main_sq(root)
+    elif "--densify" in sys.argv:   # only the densification fixture
+        main_densify(root)
     else:
         main(root)
         main_sq(root)
+        main_densify(root)
