@@ -254,10 +254,11 @@ def run_gpu(args):
         "depth_order": 8 * R_,
     }[dom]
     achieved = alg_bytes / (phases[dom] * 1e-3) / 1e9
-    traffic = None
+    traffic, inst = None, None
     try:
         tj = json.load(open(os.path.join(ROOT, "profiles", "roofline_traffic.json")))
         traffic = tj.get(args.workload, {}).get(dom)
+        inst = tj.get(args.workload, {}).get(dom + "_warp_inst")
     except (OSError, ValueError):
         pass
     roofline = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": hbm_peak,
@@ -265,6 +266,17 @@ def run_gpu(args):
                 "algorithmic_bytes": int(alg_bytes), "launch_ms": round(phases[dom], 3),
                 "peak_source": "measured" if "hbm_gbs" in peaks else "fallback",
                 "phase_ms": {k: round(v, 3) for k, v in phases.items()}}
+    if inst:
+        # The blend kernels are bound by instruction issue: warp instructions
+        # per launch (one ncu capture of this workload) over the live launch
+        # time, against one warp instruction per scheduler per SM clock.
+        sms = torch.cuda.get_device_properties(dev).multi_processor_count
+        clock_mhz = peaks.get("sm_max_mhz", 2070.0)
+        issue_peak = sms * 4 * clock_mhz * 1e6
+        issue = inst / (phases[dom] * 1e-3)
+        roofline["issue"] = {"achieved": round(issue / 1e12, 4), "peak": round(issue_peak / 1e12, 4),
+                             "unit": "Twarp-inst/s", "frac": round(issue / issue_peak, 4),
+                             "warp_inst_per_launch": int(inst)}
 
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
