@@ -498,7 +498,8 @@ __device__ __forceinline__ void bwd_update(BwdPixel<VARIANT>& q, const BwdGeom& 
     dmd_dd = (kFarP0 * kNearP0) / (kFarP0 - kNearP0) * (inv_d * inv_d);
   } else {
     m_d = mapped_depth_p1(c_d);
-    dmd_dd = (float)((kFarP1 * kNearP1) / ((kFarP1 - kNearP1) * c_d * c_d));
+    const float inv_d = __frcp_rn(c_d);
+    dmd_dd = kDmdP1f * (inv_d * inv_d);
   }
   if (pos == q.median_contributor - 1) {
     dL_dz += q.dL_dmedian;
@@ -558,8 +559,13 @@ __device__ __forceinline__ void bwd_update(BwdPixel<VARIANT>& q, const BwdGeom& 
 #define SGR_BWD_MIN_CTAS 4
 #endif
 
+#ifndef SGR_PART_BWD_MIN_CTAS
+#define SGR_PART_BWD_MIN_CTAS 1
+#endif
+
 template <int VARIANT>
-__global__ void __launch_bounds__(BwdShape<VARIANT>::NT, (VARIANT == SGR_VARIANT_PLAIN) ? SGR_BWD_MIN_CTAS : 1)
+__global__ void __launch_bounds__(BwdShape<VARIANT>::NT,
+                                  (VARIANT == SGR_VARIANT_PLAIN) ? SGR_BWD_MIN_CTAS : SGR_PART_BWD_MIN_CTAS)
     k_render_bwd(const sgr_batch b, GeomView g,
                                                                       const sgr_bwd_inputs in,
                                                                       float* __restrict__ grads,

@@ -62,10 +62,18 @@ __device__ __forceinline__ void intersect(float pxf, float pyf, V3 Tu, V3 Tv, V3
   f.depth = f.use3d ? (f.sx * Tw.x + f.sy * Tw.y) + Tw.z : Tw.z;
 }
 
-// Mapped depth of the part variant, evaluated in double as its macros do
-// (P1/cr/forward.cu:415).
+// Mapped depth of the part variant, (far d - far near) / ((far - near) d)
+// (P1/cr/forward.cu:415).  The reference evaluates it in double (its macros
+// are double); here it is fp32 with the constants rounded once.  It feeds
+// only the distortion and depth terms, never a decision, and differs from
+// the double result by a few fp32 ulps.  (A double division per fragment
+// costs more than the rest of the fragment on this GPU.)
+constexpr float kFarP1f = (float)kFarP1;
+constexpr float kFarNearP1f = (float)(kFarP1 * kNearP1);
+constexpr float kRangeP1f = (float)(kFarP1 - kNearP1);
+constexpr float kDmdP1f = (float)((kFarP1 * kNearP1) / (kFarP1 - kNearP1));   // d m / d depth = this / depth^2
 __device__ __forceinline__ float mapped_depth_p1(float depth) {
-  return (float)((kFarP1 * depth - kFarP1 * kNearP1) / ((kFarP1 - kNearP1) * depth));
+  return (kFarP1f * depth - kFarNearP1f) / (kRangeP1f * depth);
 }
 
 // View-dependent colour from degree <= 3 SH (P0/cr/forward.cu:20-71).
