@@ -177,14 +177,13 @@ struct FwdPixel {
   float C[3], N[3];
   float D, M1, M2, dist, med_depth, med_weight;
   int med_contrib;
-  float Sem[kSemSlots<VARIANT>];
 };
 
 // One fragment of the forward for one pixel: entry j of the staged batch,
 // list position contributor - 1 (P0/cr/forward.cu:349-430).
 template <int VARIANT>
 __device__ __forceinline__ void fwd_fragment(FwdPixel<VARIANT>& q, const float4 (*s_rec)[kBlock], const float* s_sem,
-                                             int j, uint32_t contributor, int S) {
+                                             int j, uint32_t contributor, int S, float* sem_acc) {
   if (q.done) return;
   const float4 r0 = s_rec[0][j], r1 = s_rec[1][j], r2 = s_rec[2][j];
   const V3 Tu = v3(r0.x, r0.y, r0.z), Tv = v3(r0.w, r1.x, r1.y), Tw = v3(r1.z, r1.w, r2.x);
@@ -253,14 +252,21 @@ __device__ __forceinline__ void fwd_fragment(FwdPixel<VARIANT>& q, const float4 
     q.C[0] += r4.x * alpha * q.T;
     q.C[1] += r4.y * alpha * q.T;
     q.C[2] += r4.z * alpha * q.T;
-    for (int c = 0; c < S; ++c) q.Sem[c] += s_sem[c * kBlock + j] * alpha * q.T;
+    for (int c = 0; c < S; ++c) sem_acc[c * FwdShape::NT] += s_sem[c * kBlock + j] * alpha * q.T;
   }
   q.T = test_T;
   q.last_contributor = contributor;
 }
 
+// Resident CTAs per SM the part variant's kernels are compiled for (80
+// registers; the semantic sums and gradients live in shared memory).
+#ifndef SGR_PART_FWD_MIN_CTAS
+#define SGR_PART_FWD_MIN_CTAS 3
+#endif
+
 template <int VARIANT>
-__global__ void __launch_bounds__(FwdShape::NT) k_render_fwd(const sgr_batch b, GeomView g, sgr_fwd_outputs out) {
+__global__ void __launch_bounds__(FwdShape::NT, (VARIANT == SGR_VARIANT_PLAIN) ? 0 : SGR_PART_FWD_MIN_CTAS)
+    k_render_fwd(const sgr_batch b, GeomView g, sgr_fwd_outputs out) {
   using Shape = FwdShape;
   constexpr int PX = Shape::PX, NT = Shape::NT, NW = Shape::NW, ROWS = Shape::ROWS, NS = kSemSlots<VARIANT>;
   const int tiles_per_view = g.tiles_x * g.tiles_y;
@@ -282,6 +288,9 @@ __global__ void __launch_bounds__(FwdShape::NT) k_render_fwd(const sgr_batch b, 
   __shared__ float s_sem[NS * kBlock];
   __shared__ uint32_t s_ring[kRing];
   __shared__ int s_count[32];
+  // part variant: each thread's semantic sums, one column per thread
+  __shared__ float s_semacc[NS][(VARIANT == SGR_VARIANT_PART) ? NT : 1];
+  float* sem_acc = (VARIANT == SGR_VARIANT_PART) ? &s_semacc[0][threadIdx.x] : nullptr;
 
   const uint32_t* list;
   int len;
@@ -304,8 +313,8 @@ __global__ void __launch_bounds__(FwdShape::NT) k_render_fwd(const sgr_batch b, 
     for (int c = 0; c < 3; ++c) Q.C[c] = Q.N[c] = 0.f;
     Q.D = Q.M1 = Q.M2 = Q.dist = Q.med_depth = Q.med_weight = 0.f;
     Q.med_contrib = -1;
-#pragma unroll
-    for (int c = 0; c < NS; ++c) Q.Sem[c] = 0.f;
+    if (VARIANT == SGR_VARIANT_PART)
+      for (int c = 0; c < S; ++c) sem_acc[c * NT] = 0.f;   // one pixel per thread in this variant
     done = done && Q.done;
   }
 
@@ -338,7 +347,7 @@ __global__ void __launch_bounds__(FwdShape::NT) k_render_fwd(const sgr_batch b, 
       done = true;
 #pragma unroll
       for (int i = 0; i < PX; ++i) {
-        fwd_fragment<VARIANT>(q[i], s_rec, s_sem, j, contributor, S);
+        fwd_fragment<VARIANT>(q[i], s_rec, s_sem, j, contributor, S, sem_acc);
         done = done && q[i].done;
       }
     }
@@ -377,7 +386,7 @@ __global__ void __launch_bounds__(FwdShape::NT) k_render_fwd(const sgr_batch b, 
     if (VARIANT == SGR_VARIANT_PART) {
       oth[pix + 7 * HW] = Q.med_weight;
       float* sem = out.semantic + (size_t)v * S * HW;
-      for (int c = 0; c < S; ++c) sem[pix + c * HW] = Q.Sem[c];
+      for (int c = 0; c < S; ++c) sem[pix + c * HW] = sem_acc[c * NT];
     }
   }
 }
@@ -412,7 +421,7 @@ struct BwdPixel {
   float dL_ddepth, dL_daccum, dL_dreg, dL_dmedian, dL_dmaxw;
   float accum_rec[3], last_color[3], last_normal[3], accum_normal[3];
   float last_alpha, last_depth, accum_depth, accum_alpha, last_dL_dT;
-  float dsem_pix[NS], accum_sem[NS], last_sem[NS];
+  float sem_w;   // part variant: alpha T of the pixel's fragment of the current entry
 };
 
 // Geometry of one backward fragment (P0/cr/backward.cu:290-330): the
@@ -465,11 +474,11 @@ __device__ __forceinline__ void bwd_alpha(const float4& r1, const float4& r2, Bw
 }
 
 // Stage 3: the pixel's recurrences and its share of the entry's 18 gradient
-// values (gv) and semantic gradients (gsem), for a live fragment.
+// values (gv), for a live fragment; the part variant also keeps the
+// fragment's weight for its semantic gradients.
 template <int VARIANT>
 __device__ __forceinline__ void bwd_update(BwdPixel<VARIANT>& q, const BwdGeom& f, const float4& r1, const float4& r2,
-                                           const float4& r3, const float4& r4, const float* s_sem, int j, int pos,
-                                           int S, float (&gv)[32], float (&gsem)[32]) {
+                                           const float4& r3, const float4& r4, int pos, float (&gv)[32]) {
   const float Twx = r1.z, Twy = r1.w;
   const float alpha = f.alpha, G = f.G, c_d = f.c_d;
   const float inv_1ma = __frcp_rn(1.f - alpha);
@@ -484,12 +493,9 @@ __device__ __forceinline__ void bwd_update(BwdPixel<VARIANT>& q, const BwdGeom& 
     dL_dalpha += (col[ch] - q.accum_rec[ch]) * q.dL_dpixel[ch];
     gv[14 + ch] += wgt * q.dL_dpixel[ch];
   }
-  if (VARIANT == SGR_VARIANT_PART) {
-    for (int c = 0; c < S; ++c) {
-      q.accum_sem[c] = q.last_alpha * q.last_sem[c] + (1.f - q.last_alpha) * q.accum_sem[c];
-      q.last_sem[c] = s_sem[c * kBlock + j];
-    }
-  }
+  // The reference's semantic recurrence (accumulated and last semantics,
+  // P1/cr/backward.cu:358-368) feeds only an alpha-gradient term that it
+  // leaves commented out (:365), so it is not computed here.
   float dL_dz = 0.0f, dL_dweight = 0.f;
   float m_d, dmd_dd;
   if (VARIANT == SGR_VARIANT_PLAIN) {
@@ -548,9 +554,7 @@ __device__ __forceinline__ void bwd_update(BwdPixel<VARIANT>& q, const BwdGeom& 
     gv[8] += dL_dz;
   }
   gv[17] += G * dL_dalpha;
-  if (VARIANT == SGR_VARIANT_PART) {
-    for (int c = 0; c < S; ++c) gsem[c] += wgt * q.dsem_pix[c];
-  }
+  if (VARIANT == SGR_VARIANT_PART) q.sem_w = wgt;   // dL/dsemantic[c] += wgt dL/dpixel_semantic[c]
 }
 
 // Resident CTAs per SM the plain backward is compiled for (registers per
@@ -560,7 +564,7 @@ __device__ __forceinline__ void bwd_update(BwdPixel<VARIANT>& q, const BwdGeom& 
 #endif
 
 #ifndef SGR_PART_BWD_MIN_CTAS
-#define SGR_PART_BWD_MIN_CTAS 1
+#define SGR_PART_BWD_MIN_CTAS 3
 #endif
 
 template <int VARIANT>
@@ -589,7 +593,7 @@ __global__ void __launch_bounds__(BwdShape<VARIANT>::NT,
   __shared__ uint32_t s_id[kBlock];
   __shared__ uint8_t s_mask[kBlock];
   __shared__ uint8_t s_list[NW][kBlock];
-  __shared__ float s_sem[NS * kBlock];
+  __shared__ float s_dsem[NS][NT];   // part variant: each thread's dL/dpixel semantics
   __shared__ int s_max[NW];
   __shared__ uint32_t s_ring[kRing];
   __shared__ int s_count[32];
@@ -628,11 +632,10 @@ __global__ void __launch_bounds__(BwdShape<VARIANT>::NT,
     Q.dL_dmedian = inside ? doth[pix + 5 * HW] : 0.f;
     Q.dL_dreg = inside ? doth[pix + 6 * HW] : 0.f;
     Q.dL_dmaxw = (VARIANT == SGR_VARIANT_PART && inside) ? doth[pix + 7 * HW] : 0.f;
-#pragma unroll
-    for (int c = 0; c < NS; ++c) Q.dsem_pix[c] = Q.accum_sem[c] = Q.last_sem[c] = 0.f;
-    if (VARIANT == SGR_VARIANT_PART && inside) {
+    Q.sem_w = 0.f;
+    if (VARIANT == SGR_VARIANT_PART) {   // one pixel per thread in this variant
       const float* ds = in.dL_dsemantic + (size_t)v * S * HW;
-      for (int c = 0; c < S; ++c) Q.dsem_pix[c] = ds[pix + c * HW];
+      for (int c = 0; c < S; ++c) s_dsem[c][threadIdx.x] = inside ? ds[pix + c * HW] : 0.f;
     }
     Q.final_D = inside ? fT[pix + HW] : 0.f;
     Q.final_D2 = inside ? fT[pix + 2 * HW] : 0.f;
@@ -680,10 +683,6 @@ __global__ void __launch_bounds__(BwdShape<VARIANT>::NT,
 #pragma unroll
       for (int k = 0; k < kRecF4 - 1; ++k) s_rec[k][e] = rec[k];
       s_mask[e] = (uint8_t)strip_mask<ROWS, NW>(rec[5], strip);
-      if (VARIANT == SGR_VARIANT_PART) {
-        const float* sem = b.semantics + (size_t)(sid_base + (int)r) * S;
-        for (int c = 0; c < S; ++c) s_sem[c * kBlock + e] = sem[c];
-      }
     }
     __syncthreads();
     const int cnt = warp_survivors(s_mask, n, warp, lane, s_list[warp]);
@@ -694,9 +693,6 @@ __global__ void __launch_bounds__(BwdShape<VARIANT>::NT,
       float gv[32];
 #pragma unroll
       for (int u = 0; u < 32; ++u) gv[u] = 0.f;
-      float gsem[32];
-#pragma unroll
-      for (int u = 0; u < 32; ++u) gsem[u] = 0.f;
       const float4 r0 = s_rec[0][j], r1 = s_rec[1][j], r2 = s_rec[2][j];
       const float reach = s_rec[3][j].w;
       BwdGeom f[PX];
@@ -714,15 +710,20 @@ __global__ void __launch_bounds__(BwdShape<VARIANT>::NT,
       const float4 r3 = s_rec[3][j], r4 = s_rec[4][j];
 #pragma unroll
       for (int i = 0; i < PX; ++i)
-        if (f[i].live) bwd_update<VARIANT>(q[i], f[i], r1, r2, r3, r4, s_sem, j, pos, S, gv, gsem);
+        if (f[i].live) bwd_update<VARIANT>(q[i], f[i], r1, r2, r3, r4, pos, gv);
       {
         int which;
         const float total = warp_sum18(gv, lane, which);
         const uint32_t r = s_id[j];
         if (which >= 0 && total != 0.f) atomicAdd(grads + (size_t)r * kGradF + which, total);
         if (VARIANT == SGR_VARIANT_PART && S > 0) {
-          const float st = warp_transpose_sum(gsem, lane);
-          if (lane < S && st != 0.f) atomicAdd(dL_dsemantics + (size_t)(sid_base + (int)r) * S + lane, st);
+          const float w = f[0].live ? q[0].sem_w : 0.f;
+          float sv[32];
+#pragma unroll
+          for (int c = 0; c < SGR_MAX_SEMANTICS; ++c) sv[c] = (c < S) ? w * s_dsem[c][threadIdx.x] : 0.f;
+          int ch;
+          const float st = warp_sum16(sv, lane, ch);
+          if (ch >= 0 && ch < S && st != 0.f) atomicAdd(dL_dsemantics + (size_t)(sid_base + (int)r) * S + ch, st);
         }
       }
     }

@@ -229,6 +229,19 @@ __device__ __forceinline__ float warp_sum18(float (&v)[32], int lane, int& index
   return v[0];
 }
 
+// Warp sum of values 0..15 of every lane by halvings (16, 8, 4, 2 values,
+// then lane pairs: 16 shuffles).  Afterwards the even lanes hold the totals,
+// lane l that of value (l >> 1) & 15; `index` is -1 in the odd lanes.
+__device__ __forceinline__ float warp_sum16(float (&v)[32], int lane, int& index) {
+  fold_half<16>(v, (lane & 16) != 0, 16);
+  fold_half<8>(v, (lane & 8) != 0, 8);
+  fold_half<4>(v, (lane & 4) != 0, 4);
+  fold_half<2>(v, (lane & 2) != 0, 2);
+  fold_half<1>(v, (lane & 1) != 0, 1);
+  index = (lane & 1) ? -1 : (lane >> 1) & 15;
+  return v[0];
+}
+
 void launch_preprocess(const sgr_batch& b, const GeomView& g, cudaStream_t st);
 void launch_store_key_count(const GeomView& g, long long R, cudaStream_t st);
 // Cell lists (sgr_binning.cu).  binning_supported is false for tile grids
