@@ -141,8 +141,10 @@ __device__ __forceinline__ void cell_list(const GeomView& g, int v, int tx, int 
 // The backward of the plain variant uses PX = 2: per-entry work (shared-
 // memory loads, the loop, the warp reduction of the gradients) is shared by
 // two pixels.  The forward keeps PX = 1: its pixels terminate independently
-// and it has no reduction to share; so does the part variant's backward,
-// whose 48 floats of per-pixel semantic state would not fit twice.
+// and it has no reduction to share.  The part variant's backward keeps
+// PX = 1 as well: at 3 CTAs of 256 threads it beats two pixels per thread
+// at 3 or 4 CTAs of 128 (49.5 ms against 56.3 and 50.7 on 500k surfels x 16
+// views, 8 semantic channels).
 // ---------------------------------------------------------------------------
 template <int PX_>
 struct BlendShape {
@@ -152,8 +154,11 @@ struct BlendShape {
   static constexpr int ROWS = kTile / NW;                             // strip height
 };
 using FwdShape = BlendShape<1>;
+#ifndef SGR_PART_BWD_PX
+#define SGR_PART_BWD_PX 1
+#endif
 template <int VARIANT>
-using BwdShape = BlendShape<(VARIANT == SGR_VARIANT_PLAIN) ? 2 : 1>;
+using BwdShape = BlendShape<(VARIANT == SGR_VARIANT_PLAIN) ? 2 : SGR_PART_BWD_PX>;
 template <int VARIANT>
 constexpr int kSemSlots = (VARIANT == SGR_VARIANT_PART) ? SGR_MAX_SEMANTICS : 1;
 
@@ -593,7 +598,7 @@ __global__ void __launch_bounds__(BwdShape<VARIANT>::NT,
   __shared__ uint32_t s_id[kBlock];
   __shared__ uint8_t s_mask[kBlock];
   __shared__ uint8_t s_list[NW][kBlock];
-  __shared__ float s_dsem[NS][NT];   // part variant: each thread's dL/dpixel semantics
+  __shared__ float s_dsem[NS][NT * PX];   // part variant: each pixel's dL/dpixel semantics
   __shared__ int s_max[NW];
   __shared__ uint32_t s_ring[kRing];
   __shared__ int s_count[32];
@@ -633,9 +638,9 @@ __global__ void __launch_bounds__(BwdShape<VARIANT>::NT,
     Q.dL_dreg = inside ? doth[pix + 6 * HW] : 0.f;
     Q.dL_dmaxw = (VARIANT == SGR_VARIANT_PART && inside) ? doth[pix + 7 * HW] : 0.f;
     Q.sem_w = 0.f;
-    if (VARIANT == SGR_VARIANT_PART) {   // one pixel per thread in this variant
+    if (VARIANT == SGR_VARIANT_PART) {
       const float* ds = in.dL_dsemantic + (size_t)v * S * HW;
-      for (int c = 0; c < S; ++c) s_dsem[c][threadIdx.x] = inside ? ds[pix + c * HW] : 0.f;
+      for (int c = 0; c < S; ++c) s_dsem[c][threadIdx.x * PX + i] = inside ? ds[pix + c * HW] : 0.f;
     }
     Q.final_D = inside ? fT[pix + HW] : 0.f;
     Q.final_D2 = inside ? fT[pix + 2 * HW] : 0.f;
@@ -717,10 +722,15 @@ __global__ void __launch_bounds__(BwdShape<VARIANT>::NT,
         const uint32_t r = s_id[j];
         if (which >= 0 && total != 0.f) atomicAdd(grads + (size_t)r * kGradF + which, total);
         if (VARIANT == SGR_VARIANT_PART && S > 0) {
-          const float w = f[0].live ? q[0].sem_w : 0.f;
           float sv[32];
 #pragma unroll
-          for (int c = 0; c < SGR_MAX_SEMANTICS; ++c) sv[c] = (c < S) ? w * s_dsem[c][threadIdx.x] : 0.f;
+          for (int c = 0; c < SGR_MAX_SEMANTICS; ++c) {
+            float t = 0.f;
+#pragma unroll
+            for (int i = 0; i < PX; ++i)
+              if (f[i].live && c < S) t += q[i].sem_w * s_dsem[c][threadIdx.x * PX + i];
+            sv[c] = t;
+          }
           int ch;
           const float st = warp_sum16(sv, lane, ch);
           if (ch >= 0 && ch < S && st != 0.f) atomicAdd(dL_dsemantics + (size_t)(sid_base + (int)r) * S + ch, st);
