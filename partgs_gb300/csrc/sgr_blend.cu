@@ -187,8 +187,9 @@ struct FwdPixel {
 // One fragment of the forward for one pixel: entry j of the staged batch,
 // list position contributor - 1 (P0/cr/forward.cu:349-430).
 template <int VARIANT>
-__device__ __forceinline__ void fwd_fragment(FwdPixel<VARIANT>& q, const float4 (*s_rec)[kBlock], const float* s_sem,
-                                             int j, uint32_t contributor, int S, float* sem_acc) {
+__device__ __forceinline__ void fwd_fragment(FwdPixel<VARIANT>& q, const float4 (*s_rec)[kBlock],
+                                             const float4* s_sem4, int j, uint32_t contributor, int S,
+                                             float4* sem_acc4) {
   if (q.done) return;
   const float4 r0 = s_rec[0][j], r1 = s_rec[1][j], r2 = s_rec[2][j];
   const V3 Tu = v3(r0.x, r0.y, r0.z), Tv = v3(r0.w, r1.x, r1.y), Tw = v3(r1.z, r1.w, r2.x);
@@ -257,7 +258,16 @@ __device__ __forceinline__ void fwd_fragment(FwdPixel<VARIANT>& q, const float4 
     q.C[0] += r4.x * alpha * q.T;
     q.C[1] += r4.y * alpha * q.T;
     q.C[2] += r4.z * alpha * q.T;
-    for (int c = 0; c < S; ++c) sem_acc[c * FwdShape::NT] += s_sem[c * kBlock + j] * alpha * q.T;
+    // four channels at a time; channels past S are zero in the staged values
+    for (int g4 = 0; g4 < (S + 3) / 4; ++g4) {
+      const float4 x = s_sem4[g4 * kBlock + j];
+      float4 a = sem_acc4[g4 * FwdShape::NT];
+      a.x += x.x * alpha * q.T;
+      a.y += x.y * alpha * q.T;
+      a.z += x.z * alpha * q.T;
+      a.w += x.w * alpha * q.T;
+      sem_acc4[g4 * FwdShape::NT] = a;
+    }
   }
   q.T = test_T;
   q.last_contributor = contributor;
@@ -290,12 +300,13 @@ __global__ void __launch_bounds__(FwdShape::NT, (VARIANT == SGR_VARIANT_PLAIN) ?
   __shared__ float4 s_rec[kRecF4 - 1][kBlock];
   __shared__ uint8_t s_mask[kBlock];
   __shared__ uint8_t s_list[NW][kBlock];
-  __shared__ float s_sem[NS * kBlock];
+  constexpr int NS4 = (NS + 3) / 4;
+  __shared__ float4 s_sem4[NS4 * kBlock];   // staged semantics, four channels per float4
   __shared__ uint32_t s_ring[kRing];
   __shared__ int s_count[32];
   // part variant: each thread's semantic sums, one column per thread
-  __shared__ float s_semacc[NS][(VARIANT == SGR_VARIANT_PART) ? NT : 1];
-  float* sem_acc = (VARIANT == SGR_VARIANT_PART) ? &s_semacc[0][threadIdx.x] : nullptr;
+  __shared__ float4 s_semacc4[NS4][(VARIANT == SGR_VARIANT_PART) ? NT : 1];
+  float4* sem_acc4 = (VARIANT == SGR_VARIANT_PART) ? &s_semacc4[0][threadIdx.x] : nullptr;
 
   const uint32_t* list;
   int len;
@@ -319,7 +330,7 @@ __global__ void __launch_bounds__(FwdShape::NT, (VARIANT == SGR_VARIANT_PLAIN) ?
     Q.D = Q.M1 = Q.M2 = Q.dist = Q.med_depth = Q.med_weight = 0.f;
     Q.med_contrib = -1;
     if (VARIANT == SGR_VARIANT_PART)
-      for (int c = 0; c < S; ++c) sem_acc[c * NT] = 0.f;   // one pixel per thread in this variant
+      for (int g4 = 0; g4 < (S + 3) / 4; ++g4) sem_acc4[g4 * NT] = make_float4(0.f, 0.f, 0.f, 0.f);
     done = done && Q.done;
   }
 
@@ -341,7 +352,11 @@ __global__ void __launch_bounds__(FwdShape::NT, (VARIANT == SGR_VARIANT_PLAIN) ?
       s_mask[e] = (uint8_t)strip_mask<ROWS, NW>(rec[5], strip);
       if (VARIANT == SGR_VARIANT_PART) {
         const float* sem = b.semantics + (size_t)(sid_base + (int)r) * S;
-        for (int c = 0; c < S; ++c) s_sem[c * kBlock + e] = sem[c];
+        for (int g4 = 0; g4 < (S + 3) / 4; ++g4) {
+          const int c = 4 * g4;
+          s_sem4[g4 * kBlock + e] = make_float4(sem[c], c + 1 < S ? sem[c + 1] : 0.f, c + 2 < S ? sem[c + 2] : 0.f,
+                                                c + 3 < S ? sem[c + 3] : 0.f);
+        }
       }
     }
     __syncthreads();
@@ -352,7 +367,7 @@ __global__ void __launch_bounds__(FwdShape::NT, (VARIANT == SGR_VARIANT_PLAIN) ?
       done = true;
 #pragma unroll
       for (int i = 0; i < PX; ++i) {
-        fwd_fragment<VARIANT>(q[i], s_rec, s_sem, j, contributor, S, sem_acc);
+        fwd_fragment<VARIANT>(q[i], s_rec, s_sem4, j, contributor, S, sem_acc4);
         done = done && q[i].done;
       }
     }
@@ -391,7 +406,8 @@ __global__ void __launch_bounds__(FwdShape::NT, (VARIANT == SGR_VARIANT_PLAIN) ?
     if (VARIANT == SGR_VARIANT_PART) {
       oth[pix + 7 * HW] = Q.med_weight;
       float* sem = out.semantic + (size_t)v * S * HW;
-      for (int c = 0; c < S; ++c) sem[pix + c * HW] = sem_acc[c * NT];
+      const float* acc = reinterpret_cast<const float*>(sem_acc4);   // thread column: float4 stride NT
+      for (int c = 0; c < S; ++c) sem[pix + c * HW] = acc[(c >> 2) * 4 * NT + (c & 3)];
     }
   }
 }
