@@ -242,6 +242,18 @@ __device__ __forceinline__ float warp_sum16(float (&v)[32], int lane, int& index
   return v[0];
 }
 
+// The same for values 0..7 (8, 4, 2 values, then two pair sums: 9
+// shuffles): lane l with l % 4 == 0 holds the total of value l >> 2.
+__device__ __forceinline__ float warp_sum8(float (&v)[32], int lane, int& index) {
+  fold_half<8>(v, (lane & 16) != 0, 16);
+  fold_half<4>(v, (lane & 8) != 0, 8);
+  fold_half<2>(v, (lane & 4) != 0, 4);
+  fold_half<1>(v, (lane & 2) != 0, 2);
+  fold_half<1>(v, (lane & 1) != 0, 1);
+  index = (lane & 3) ? -1 : lane >> 2;
+  return v[0];
+}
+
 void launch_preprocess(const sgr_batch& b, const GeomView& g, cudaStream_t st);
 void launch_store_key_count(const GeomView& g, long long R, cudaStream_t st);
 // Cell lists (sgr_binning.cu).  binning_supported is false for tile grids

@@ -10,15 +10,18 @@ from tests._util import grad_error, image_error, oracle_camera, oracle_surfels, 
 pytestmark = pytest.mark.gpu
 
 
-@pytest.fixture(scope="module")
-def case(sgr_lib):
+@pytest.fixture(scope="module", params=[5, 13, 16], ids=lambda n: f"S{n}")
+def case(sgr_lib, request):
+    """S semantic channels: 5 (the 8-value reduction), 13 (the 16-value one,
+    with a partly filled float4 group) and 16 (the maximum)."""
+    S = request.param
     import partgs_gb300.diff_surfel_rasterization_part as dsrp
     from partgs_gb300 import raster
     from partgs_gb300.scenes import random_surfels
     from partgs_gb300.cameras import orbit_cameras
     scene = random_surfels(3000, seed=11)
     cam = orbit_cameras(1, 3.0, 96, 112, 55.0, seed=5)[0]
-    sem = torch.rand(scene.P, 5, generator=torch.Generator().manual_seed(2))
+    sem = torch.rand(scene.P, S, generator=torch.Generator().manual_seed(2))
     sc = scene.to("cuda")
     rs = settings(dsrp, cam, [0.3, 0.1, 0.2])
     means3D = sc.means3D.clone().requires_grad_(True)
@@ -51,7 +54,7 @@ def case(sgr_lib):
     st32 = O.forward_view(osf, ocam, np.array([0.3, 0.1, 0.2]), O.PART, np.float32)
     ref32 = O.backward_view(st32, ocam, osf, np.array([0.3, 0.1, 0.2]), dcol, doth, dsem, variant=O.PART,
                             dtype=np.float32)
-    return dict(img=img.detach().cpu().numpy(), sem=sem_img.detach().cpu().numpy(),
+    return dict(S=S, img=img.detach().cpu().numpy(), sem=sem_img.detach().cpu().numpy(),
                 allmap=allmap.detach().cpu().numpy(), radii=radii.cpu().numpy(), st=st, amb=amb, ref=ref,
                 st32=st32, ref32=ref32,
                 grads=dict(dL_dmeans3D=means3D.grad, dL_dsh=shs.grad, dL_dopacity=opac.grad,
@@ -61,7 +64,7 @@ def case(sgr_lib):
 
 def test_part_shapes(case):
     assert case["img"].shape == (3, 96, 112)
-    assert case["sem"].shape == (5, 96, 112)
+    assert case["sem"].shape == (case["S"], 96, 112)
     assert case["allmap"].shape == (8, 96, 112)
 
 
