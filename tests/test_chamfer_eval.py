@@ -60,3 +60,23 @@ def test_nn_indices_and_empty_inputs(sgr_lib):
     picked = ref.gather(1, i.long().cpu()[:, None])[:, 0]
     np.testing.assert_allclose(picked.numpy(), ref.min(dim=1).values.numpy(), rtol=1e-5, atol=1e-7)
     assert E.nn_distance(torch.zeros(0, 3).cuda(), r.cuda()).shape == (0,)
+
+
+def test_downsample_duplicates_and_single_points(sgr_lib):
+    """Exact duplicates (distance 0): only the first of each is kept; one
+    point is kept; points exactly one radius apart remove each other, as the
+    reference's inclusive radius test does."""
+    from partgs_gb300 import chamfer_eval as E
+    g = torch.Generator().manual_seed(4)
+    base = torch.rand(500, 3, generator=g, dtype=torch.float64)
+    pts = torch.cat([base, base[:100]], 0)[torch.randperm(600, generator=g)]
+    keep, _ = E.radius_downsample(pts.cuda(), 1e-5)
+    ref = O.downsample_mask(pts.numpy(), 1e-5)
+    np.testing.assert_array_equal(keep.cpu().numpy(), ref)
+    assert int(keep.sum()) == 500
+    one, rounds = E.radius_downsample(torch.zeros(1, 3, dtype=torch.float64).cuda(), 0.005)
+    assert bool(one[0]) and rounds == 1
+    line = torch.tensor([[0.0, 0, 0], [0.25, 0, 0], [0.5, 0, 0]], dtype=torch.float64)
+    keep, _ = E.radius_downsample(line.cuda(), 0.25)
+    np.testing.assert_array_equal(keep.cpu().numpy(), O.downsample_mask(line.numpy(), 0.25))
+    assert keep.tolist() == [True, False, True]

@@ -201,3 +201,22 @@ def test_trainer_gathers_statistics_and_densifies(sgr_lib):
     assert torch.isfinite(loss)
     tr.reset_opacity()
     assert float(torch.sigmoid(tr.opacity_logit.detach()).max()) <= 0.01 + 1e-6
+
+
+def test_densify_with_nothing_selected_and_everything_pruned():
+    """High thresholds select nothing: the surfels come back unchanged (the
+    reference's clone / split of an empty selection); a min opacity above
+    every surfel prunes all of them."""
+    d = _gold()
+    stats = D.DensifyStats(d["in_xyz"].shape[0], "cpu")
+    stats.grad_accum.copy_(torch.from_numpy(d["stats_accum"]))
+    stats.denom.copy_(torch.from_numpy(d["stats_denom"]))
+    params, sem, adam, st = D.densify_and_prune(_params(d), stats, 1e9, 0.0, 1.5, None, 0.01,
+                                                semantic=torch.from_numpy(d["in_semantic"]), adam=_adam(d))
+    for k in D.NAMES:
+        assert torch.equal(params[k], torch.from_numpy(d[f"in_{k}"])), k
+        assert torch.equal(adam[k][0], torch.from_numpy(d[f"in_m_{k}"])), k
+    assert st.num_surfels == d["in_xyz"].shape[0]
+    params, sem, adam, st = D.densify_and_prune(_params(d), stats, 1e9, 1.1, 1.5, None, 0.01,
+                                                semantic=torch.from_numpy(d["in_semantic"]), adam=_adam(d))
+    assert all(params[k].shape[0] == 0 for k in D.NAMES) and sem.shape[0] == 0 and st.num_surfels == 0

@@ -190,3 +190,20 @@ def test_kernels_on_the_reference_fixture(sgr_lib):
         _close(got.grad.double().cpu(), torch.from_numpy(d[f"grad_{name}"]), RTOL_G)
     for name, got in zip(("eps1", "eps2", "sq_occ"), e):
         _close(got.grad.double().cpu(), torch.from_numpy(d[f"grad_{name}"][:, 0]), RTOL_G)
+
+
+def test_the_largest_block_count(sgr_lib):
+    """SGR_SQ_MAX_BLOCKS (64) blocks: losses and gradients still match."""
+    from partgs_gb300 import sq_losses as Q
+    n = Q.MAX_BLOCKS
+    params = _blocks(n, 8)
+    rays, ovl = _rays(8, n_rays=256, samples=32), _ovl(n, 8, P=64)
+    w = torch.tensor([10.0, 100.0, 0.02, 2.0], device="cuda")
+    p1 = [t.clone().requires_grad_(True) for t in params]
+    (w * Q.sq_losses(*p1, RATIO, rays, ovl)).sum().backward()
+    p2 = [t.clone().requires_grad_(True) for t in params]
+    (w * _oracle(p2, rays, ovl)).sum().backward()
+    for a, b in zip(p1, p2):
+        _close(a.grad, b.grad, RTOL_G)
+    with pytest.raises(ValueError):
+        Q.sq_losses(*_blocks(n + 1, 9), RATIO, rays, None)
