@@ -6,9 +6,12 @@
 //   opacities = sigmoid(opacity_logit)               [P,1]
 //   shs       = cat(features_dc [P,1,3], features_rest [P,M-1,3])      [P,M,3]
 //
-// One thread per surfel; the surfel's values are read and written together,
-// so the whole transform is one pass over the parameters (HBM-bound: about
-// 440 bytes per surfel forward and backward at SH degree 3).
+// One launch each way.  Its first CTAs take one surfel per thread for the
+// small parameters; the rest copy the SH coefficients as one flat array of
+// P * M * 3 floats, a float per thread, so that consecutive threads touch
+// consecutive addresses (a thread per surfel would put a warp's SH accesses
+// 192 bytes apart).  The whole transform is one pass over the parameters
+// (HBM-bound: about 440 bytes per surfel forward and backward at SH degree 3).
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -21,7 +24,22 @@ void count_launches(int n);   // sgr_api.cu
 
 namespace sgract {
 
-__global__ void k_activate(sgr_activate_args a) {
+constexpr int kThreads = 256;
+
+// CTAs [0, surfel_ctas) take the per-surfel parameters, the rest the SH copy.
+__host__ __device__ inline long long surfel_ctas(long long P) { return (P + kThreads - 1) / kThreads; }
+
+__global__ void __launch_bounds__(kThreads) k_activate(sgr_activate_args a) {
+  const long long nb = surfel_ctas(a.P);
+  if (blockIdx.x >= nb) {   // shs[p, k] = k < 3 ? features_dc[p, k] : features_rest[p, k - 3]
+    const int row = a.sh_coeffs * 3;
+    const long long e = (long long)(blockIdx.x - nb) * kThreads + threadIdx.x;
+    if (e >= a.P * row) return;
+    const long long p = e / row;
+    const int k = (int)(e - p * row);
+    a.shs[e] = k < 3 ? a.features_dc[p * 3 + k] : a.features_rest[p * (row - 3) + (k - 3)];
+    return;
+  }
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.P) return;
   const float2 ls = reinterpret_cast<const float2*>(a.log_scaling)[i];
@@ -30,20 +48,28 @@ __global__ void k_activate(sgr_activate_args a) {
   const float n = fmaxf(sqrtf(q.x * q.x + q.y * q.y + q.z * q.z + q.w * q.w), 1e-12f);
   reinterpret_cast<float4*>(a.rotations)[i] = make_float4(q.x / n, q.y / n, q.z / n, q.w / n);
   a.opacities[i] = 1.0f / (1.0f + expf(-a.opacity_logit[i]));
-  const int M = a.sh_coeffs;
-  float* sh = a.shs + i * M * 3;
-  for (int c = 0; c < 3; ++c) sh[c] = a.features_dc[i * 3 + c];
-  const float* rest = a.features_rest + i * (M - 1) * 3;
-  for (int k = 0; k < (M - 1) * 3; ++k) sh[3 + k] = rest[k];
 }
 
 // Adjoints: d log_scaling = d scales * scales; d rotation = (d - r (r.d)) / n
 // (the normalisation's Jacobian; below the 1e-12 clamp, d / 1e-12, as
 // F.normalize's autograd gives); d logit = d opacities * s (1 - s); the SH
 // gradient split back into its two parameter tensors.
-__global__ void k_activate_bwd(sgr_activate_args a, const float* __restrict__ d_scales,
-                               const float* __restrict__ d_rotations, const float* __restrict__ d_opacities,
-                               const float* __restrict__ d_shs) {
+__global__ void __launch_bounds__(kThreads) k_activate_bwd(sgr_activate_args a, const float* __restrict__ d_scales,
+                                                           const float* __restrict__ d_rotations,
+                                                           const float* __restrict__ d_opacities,
+                                                           const float* __restrict__ d_shs) {
+  const long long nb = surfel_ctas(a.P);
+  if (blockIdx.x >= nb) {   // the SH gradient split back into its two tensors
+    const int row = a.sh_coeffs * 3;
+    const long long e = (long long)(blockIdx.x - nb) * kThreads + threadIdx.x;
+    if (e >= a.P * row) return;
+    const long long p = e / row;
+    const int k = (int)(e - p * row);
+    const float d = d_shs ? d_shs[e] : 0.0f;
+    if (k < 3) a.d_features_dc[p * 3 + k] = d;
+    else a.d_features_rest[p * (row - 3) + (k - 3)] = d;
+    return;
+  }
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.P) return;
   const float2 ls = reinterpret_cast<const float2*>(a.log_scaling)[i];
@@ -66,11 +92,6 @@ __global__ void k_activate_bwd(sgr_activate_args a, const float* __restrict__ d_
   reinterpret_cast<float4*>(a.d_rotation)[i] = dq;
   const float s = 1.0f / (1.0f + expf(-a.opacity_logit[i]));
   a.d_opacity_logit[i] = d_opacities ? d_opacities[i] * s * (1.0f - s) : 0.0f;
-  const int M = a.sh_coeffs;
-  const float* dsh = d_shs ? d_shs + i * M * 3 : nullptr;
-  for (int c = 0; c < 3; ++c) a.d_features_dc[i * 3 + c] = dsh ? dsh[c] : 0.0f;
-  float* drest = a.d_features_rest + i * (M - 1) * 3;
-  for (int k = 0; k < (M - 1) * 3; ++k) drest[k] = dsh ? dsh[3 + k] : 0.0f;
 }
 
 int check(const sgr_activate_args* a) {
@@ -91,7 +112,8 @@ int sgr_activate_forward(const sgr_activate_args* a, void* stream) {
   if (!a->log_scaling || !a->rotation || !a->opacity_logit || !a->features_dc || !a->scales || !a->rotations ||
       !a->opacities || !a->shs || (a->sh_coeffs > 1 && !a->features_rest))
     return SGR_ERR_INVALID_ARGUMENT;
-  k_activate<<<(unsigned)((a->P + 255) / 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(*a);
+  const long long ctas = surfel_ctas(a->P) + (a->P * a->sh_coeffs * 3 + kThreads - 1) / kThreads;
+  k_activate<<<(unsigned)ctas, kThreads, 0, static_cast<cudaStream_t>(stream)>>>(*a);
   sgr::count_launches(1);
   return cudaGetLastError() == cudaSuccess ? SGR_OK : SGR_ERR_CUDA;
 }
@@ -104,8 +126,9 @@ int sgr_activate_backward(const sgr_activate_args* a, const float* d_scales, con
   if (!a->log_scaling || !a->rotation || !a->opacity_logit || !a->d_log_scaling || !a->d_rotation ||
       !a->d_opacity_logit || !a->d_features_dc || (a->sh_coeffs > 1 && !a->d_features_rest))
     return SGR_ERR_INVALID_ARGUMENT;
-  k_activate_bwd<<<(unsigned)((a->P + 255) / 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(
-      *a, d_scales, d_rotations, d_opacities, d_shs);
+  const long long ctas = surfel_ctas(a->P) + (a->P * a->sh_coeffs * 3 + kThreads - 1) / kThreads;
+  k_activate_bwd<<<(unsigned)ctas, kThreads, 0, static_cast<cudaStream_t>(stream)>>>(*a, d_scales, d_rotations,
+                                                                                     d_opacities, d_shs);
   sgr::count_launches(1);
   return cudaGetLastError() == cudaSuccess ? SGR_OK : SGR_ERR_CUDA;
 }
