@@ -7,6 +7,8 @@ namespace sgr {
 // preprocess backward: one thread per surfel, summing over its scene's views
 // (P0/cr/backward.cu:443-630; P1/cr/backward.cu:473-671)
 // ---------------------------------------------------------------------------
+// sh and dsh_acc hold coefficient k, channel c at index (3 k + c) * STRIDE.
+template <int STRIDE>
 __device__ __forceinline__ void sh_backward(int deg, const float* sh, V3 dir_orig, uint32_t clamped, V3 dL_dRGB_in,
                                             float* dsh_acc, V3& dmean) {
   const float len = sqrtf(dot3(dir_orig, dir_orig));
@@ -15,11 +17,11 @@ __device__ __forceinline__ void sh_backward(int deg, const float* sh, V3 dir_ori
   g.x *= (clamped & 1u) ? 0 : 1;
   g.y *= (clamped & 2u) ? 0 : 1;
   g.z *= (clamped & 4u) ? 0 : 1;
-  auto c = [&](int k) { return v3(sh[3 * k], sh[3 * k + 1], sh[3 * k + 2]); };
+  auto c = [&](int k) { return v3(sh[3 * k * STRIDE], sh[(3 * k + 1) * STRIDE], sh[(3 * k + 2) * STRIDE]); };
   auto add = [&](int k, float coef) {
-    dsh_acc[3 * k] += coef * g.x;
-    dsh_acc[3 * k + 1] += coef * g.y;
-    dsh_acc[3 * k + 2] += coef * g.z;
+    dsh_acc[3 * k * STRIDE] += coef * g.x;
+    dsh_acc[(3 * k + 1) * STRIDE] += coef * g.y;
+    dsh_acc[(3 * k + 2) * STRIDE] += coef * g.z;
   };
   V3 dx = v3(0, 0, 0), dy = v3(0, 0, 0), dz = v3(0, 0, 0);
   const float x = dir.x, y = dir.y, z = dir.z;
@@ -66,11 +68,21 @@ __device__ __forceinline__ void sh_backward(int deg, const float* sh, V3 dir_ori
   dmean = dmean + dnormvdv(dir_orig, dL_ddir);
 }
 
+// The CTA's SH coefficients and their gradients live in shared memory,
+// coefficient-major ([3 M][128]: conflict-free per thread), loaded and
+// stored as contiguous runs of the [P, M, 3] arrays.
+constexpr int kPreBwdThreads = 128;
+#ifndef SGR_PREBWD_MIN_CTAS
+#define SGR_PREBWD_MIN_CTAS 4
+#endif
+
+// One surfel of the preprocess backward: sh and dsh point at its column of
+// the CTA's shared arrays (stride kPreBwdThreads).
 template <int VARIANT>
-__global__ void __launch_bounds__(128) k_preprocess_bwd(const sgr_batch b, GeomView g, const float* __restrict__ grads,
-                                                        sgr_bwd_outputs out) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= b.num_surfels) return;
+__device__ __forceinline__ void preprocess_bwd_surfel(const sgr_batch& b, const GeomView& g,
+                                                      const float* __restrict__ grads, const sgr_bwd_outputs& out,
+                                                      int i, const float* sh, float* dsh) {
+  const bool has_sh = b.shs != nullptr;
   const int s = find_scene(b.scenes, b.num_scenes, i);
   const sgr_scene_desc sd = b.scenes[s];
   const int local = i - sd.surfel_offset;
@@ -82,15 +94,6 @@ __global__ void __launch_bounds__(128) k_preprocess_bwd(const sgr_batch b, GeomV
   if (!precomp) {
     sc = make_float2(b.scales[2 * i + 0], b.scales[2 * i + 1]);
     q = reinterpret_cast<const float4*>(b.rotations)[i];
-  }
-  const int M = b.sh_coeffs;
-  const bool has_sh = b.shs != nullptr;
-  float sh[kMaxShCoeffs * 3];
-  float dsh[kMaxShCoeffs * 3];
-#pragma unroll
-  for (int k = 0; k < kMaxShCoeffs * 3; ++k) {
-    sh[k] = (has_sh && k < M * 3) ? b.shs[(size_t)i * M * 3 + k] : 0.f;
-    dsh[k] = 0.f;
   }
   const M3 R = quat_to_rot(q);
   V3 dmean = v3(0, 0, 0), dcol = v3(0, 0, 0);
@@ -265,7 +268,7 @@ __global__ void __launch_bounds__(128) k_preprocess_bwd(const sgr_batch b, GeomV
       for (int k = 0; k < 9; ++k) oT[k] = dT[k];
     if (has_sh) {
       const V3 cp = v3(b.campos[3 * v], b.campos[3 * v + 1], b.campos[3 * v + 2]);
-      sh_backward(b.sh_degree, sh, p - cp, __float_as_uint(rc4.w), dc, dsh, dmean);
+      sh_backward<kPreBwdThreads>(b.sh_degree, sh, p - cp, __float_as_uint(rc4.w), dc, dsh, dmean);
     }
   }
   if (out.dL_dmeans3D) {
@@ -284,15 +287,45 @@ __global__ void __launch_bounds__(128) k_preprocess_bwd(const sgr_batch b, GeomV
     out.dL_dcolors[3 * i + 1] = dcol.y;
     out.dL_dcolors[3 * i + 2] = dcol.z;
   }
-  if (out.dL_dsh && M > 0) {
-    float* o = out.dL_dsh + (size_t)i * M * 3;
-    for (int k = 0; k < M * 3; ++k) o[k] = k < kMaxShCoeffs * 3 ? dsh[k] : 0.f;
+}
+
+template <int VARIANT>
+__global__ void __launch_bounds__(kPreBwdThreads, SGR_PREBWD_MIN_CTAS)
+    k_preprocess_bwd(const sgr_batch b, GeomView g, const float* __restrict__ grads, sgr_bwd_outputs out) {
+  constexpr int NT = kPreBwdThreads;
+  __shared__ float s_sh[kMaxShCoeffs * 3][NT];
+  __shared__ float s_dsh[kMaxShCoeffs * 3][NT];
+  const int i0 = blockIdx.x * NT;
+  const int i = i0 + threadIdx.x;
+  const int M = b.sh_coeffs;
+  const int row = M * 3;
+  const int here = min(NT, b.num_surfels - i0);
+  const bool has_sh = b.shs != nullptr;
+#pragma unroll
+  for (int k = 0; k < kMaxShCoeffs * 3; ++k) {
+    s_sh[k][threadIdx.x] = 0.f;
+    s_dsh[k][threadIdx.x] = 0.f;
   }
+  __syncthreads();
+  if (has_sh)
+    for (int e = threadIdx.x; e < here * row; e += NT) {
+      const int t = e / row;
+      s_sh[e - t * row][t] = b.shs[(size_t)i0 * row + e];
+    }
+  __syncthreads();
+  if (i < b.num_surfels) preprocess_bwd_surfel<VARIANT>(b, g, grads, out, i, &s_sh[0][threadIdx.x],
+                                                          &s_dsh[0][threadIdx.x]);
+  __syncthreads();
+  if (out.dL_dsh && M > 0)
+    for (int e = threadIdx.x; e < here * row; e += NT) {
+      const int t = e / row;
+      out.dL_dsh[(size_t)i0 * row + e] = s_dsh[e - t * row][t];
+    }
 }
 
 void launch_preprocess_bwd(const sgr_batch& b, const GeomView& g, const float* grads, const sgr_bwd_outputs& out,
                            cudaStream_t st) {
-  const int threads = 128;
+  const int threads = kPreBwdThreads;
   const int blocks = (b.num_surfels + threads - 1) / threads;
   if (blocks == 0) return;
   if (b.variant == SGR_VARIANT_PLAIN) k_preprocess_bwd<SGR_VARIANT_PLAIN><<<blocks, threads, 0, st>>>(b, g, grads, out);
