@@ -30,6 +30,11 @@ class _MultiViewFn(torch.autograd.Function):
             status_host=cfg.status, cell_tiles=cfg.cell_tiles)
         ctx.state = state
         ctx.cfg = cfg
+        # sticky record of every forward since the last reset: flags OR-ed,
+        # largest cell-list entry count (device side, so captured steps keep it)
+        st = state.geom[state.sizes.off_status:state.sizes.off_status + L.STATUS_BYTES]
+        cfg.sticky[0:1].bitwise_or_(st[8:12].view(torch.int32).to(torch.int64))
+        torch.maximum(cfg.sticky[1:2], st[16:24].view(torch.int64), out=cfg.sticky[1:2])
         ctx.op_shape = opacities.shape
         ctx.has = (shs is not None, colors_precomp is not None, semantics is not None)
         ctx.mark_non_differentiable(radii)
@@ -74,6 +79,7 @@ class MultiViewRasterizer:
         P = num_surfels if num_surfels is not None else (sum(scene_sizes) if scene_sizes else None)
         self.tables = _r._tables(variant, P, self.viewset, dev) if P is not None else None
         self.status = torch.zeros(L.STATUS_BYTES, dtype=torch.uint8).pin_memory()
+        self.sticky = torch.zeros(2, dtype=torch.int64, device=dev)   # see sticky_counts()
         self.last_means2D_grad = None
 
     @property
@@ -82,6 +88,14 @@ class MultiViewRasterizer:
 
     def set_capacity(self, bin_capacity):
         self.bin_capacity = bin_capacity
+
+    def sticky_counts(self, reset: bool = False):
+        """(flags OR-ed over every forward since the last reset, largest
+        cell-list entry count among them); synchronises with the device."""
+        flags, most = (int(x) for x in self.sticky.tolist())
+        if reset:
+            self.sticky.zero_()
+        return flags, most
 
     def counts(self):
         """(key count, flags, cell-list entry count) of the last forward;

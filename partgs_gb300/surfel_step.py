@@ -206,6 +206,36 @@ class SurfelTrainer:
         self.graph.replay()
         return self.loss
 
+    def train(self, steps: int, check_every: int = 25, headroom: float = 1.25, max_recaptures: int = 4):
+        """Replays ``steps`` captured steps, checking every ``check_every``
+        steps whether any of them overflowed the cell lists.  If one did, the
+        interval is undone (parameters and Adam state restored), the step is
+        captured again with room for the largest entry count seen times
+        ``headroom``, and the interval runs again.  Returns the last loss."""
+        if self.graph is None:
+            raise RuntimeError("capture() first")
+        done, loss, recaptures = 0, self.loss, 0
+        self.raster.sticky_counts(reset=True)
+        while done < steps:
+            n = min(check_every, steps - done)
+            snap = self.snapshot()
+            for _ in range(n):
+                loss = self.replay()
+            flags, most = self.raster.sticky_counts(reset=True)
+            if flags & _lib.SGR_FLAG_BIN_OVERFLOW:
+                if recaptures == max_recaptures:
+                    raise RuntimeError(f"cell lists still overflow after {recaptures} re-captures")
+                recaptures += 1
+                self.restore(snap)
+                self.raster.set_capacity(int(most * headroom) + 4096)
+                self.capture(self.targets, warmup=1)
+                self.restore(snap)   # the capture's warm-up step is not part of the run
+                self.raster.sticky_counts(reset=True)
+                continue
+            done += n
+        self.recaptures = recaptures
+        return loss
+
     def _state(self):
         return [p.detach() for p in self.params()] + self.opt.state_tensors()
 

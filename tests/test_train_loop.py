@@ -1,0 +1,44 @@
+"""The checked training loop: an overflow of the cell lists inside a captured
+step is caught, the interval is undone and run again after a re-capture with
+room for the entries, and the run ends where a run with enough room from the
+start ends."""
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+
+def test_train_recovers_from_a_cell_list_overflow(sgr_lib):
+    from partgs_gb300 import _lib as L
+    from partgs_gb300.cameras import orbit_cameras
+    from partgs_gb300.scenes import random_surfels
+    from partgs_gb300.surfel_step import SurfelTrainer
+    scene, cams = random_surfels(3000, seed=6), orbit_cameras(3, 3.0, 64, 80, 55.0, seed=3)
+    targets = torch.rand(len(cams), 3, 64, 80, generator=torch.Generator().manual_seed(5)).cuda()
+    tr = SurfelTrainer(scene, cams)
+    tr.capture(targets, warmup=2)
+    start = tr.snapshot()
+    loss_ok = float(tr.train(6, check_every=3))
+    assert tr.recaptures == 0
+    ok = [p.detach().clone() for p in tr.params()]
+    _, _, entries = tr.raster.counts()
+
+    tr.restore(start)
+    tr.raster.set_capacity(max(1, entries // 3))        # far too small for this scene
+    tr.capture(targets, warmup=1)
+    tr.restore(start)
+    tr.replay()
+    flags, _ = tr.raster.sticky_counts(reset=True)
+    assert flags & L.SGR_FLAG_BIN_OVERFLOW                # the captured step overflows
+    tr.restore(start)
+    loss = tr.train(6, check_every=3)
+    assert tr.recaptures >= 1 and torch.isfinite(loss)
+    assert tr.raster.bin_capacity >= entries
+    # The two runs differ only in the order of the gradient atomics.  Adam's
+    # first steps move every element by about +-lr whatever its gradient's
+    # size, so an element whose gradient is near zero may step the other way:
+    # compare the losses, and require nearly every element to agree.
+    assert abs(float(loss) - loss_ok) <= 1e-3 * abs(loss_ok)
+    for a, b in zip(ok, tr.params()):
+        off = (a - b.detach()).abs() > 1e-5 * max(float(a.abs().max()), 1.0)
+        assert float(off.float().mean()) < 0.01
