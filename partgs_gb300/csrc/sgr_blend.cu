@@ -49,6 +49,69 @@ __device__ __forceinline__ uint32_t strip_mask(const float4& box, const Strip& s
   return m;
 }
 
+// True when some pixel centre (x, y), x in [xa, xb], may be within reach of
+// the record: rho2d <= c (the filter disk, radius sqrt(c / 2)) or
+// |p.xy|^2 <= c p.z^2 (the splat disk), the per-pixel test of the blends.
+// Along the row, p(x) = k(x) x l with l = y Tw - Tv and k(xa + u) =
+// (xa Tw - Tu) + u Tw, so p(u) = B + u A (B = k(xa) x l, A = Tw x l) and
+// |p.xy|^2 - c p.z^2 is a quadratic in u.  The expansion around the row's
+// first pixel keeps the cancellation of the blends' own k and l.  The test
+// is conservative: the threshold is raised by 1% and the interval widened
+// by half a pixel each side, far beyond the fp32 differences between this
+// form and the per-pixel one (checked on the bench scene's 6.6M (entry,
+// strip) pairs: no pair that reaches a pixel was rejected).  Non-finite
+// coefficients keep the entry.
+__device__ __forceinline__ bool row_reaches(const V3& Tu, const V3& Tv, const V3& Tw, float cx, float cy, float c,
+                                            float y, float xa, float xb) {
+  const float cc = c * 1.01f;
+  const float dy = cy - y;
+  const float h2 = 0.5f * cc - dy * dy;
+  if (h2 >= 0.0f) {
+    const float h = sqrtf(h2);
+    if (cx + h >= xa - 0.5f && cx - h <= xb + 0.5f) return true;
+  }
+  const V3 l = y * Tw - Tv;
+  const V3 A = cross3(Tw, l);
+  const V3 B = cross3(xa * Tw - Tu, l);
+  const float a = A.x * A.x + A.y * A.y - cc * (A.z * A.z);
+  const float bh = A.x * B.x + A.y * B.y - cc * (A.z * B.z);
+  const float e = B.x * B.x + B.y * B.y - cc * (B.z * B.z);
+  if (!(isfinite(a) && isfinite(bh) && isfinite(e))) return true;
+  const float ua = -0.5f, ub = (xb - xa) + 0.5f;
+  if ((a * ua + 2.0f * bh) * ua + e <= 0.0f || (a * ub + 2.0f * bh) * ub + e <= 0.0f) return true;
+  if (a > 0.0f) {
+    const float us = -bh / a;
+    if (us > ua && us < ub && e - bh * (bh / a) <= 0.0f) return true;
+  }
+  return false;
+}
+
+#ifndef SGR_EXACT_STRIPS
+#define SGR_EXACT_STRIPS 1
+#endif
+
+// strip_mask, then each strip it keeps is tested row by row with
+// row_reaches (rows outside the box are skipped).
+template <int ROWS, int NWARPS>
+__device__ __forceinline__ uint32_t strip_mask_rows(const float4& r0, const float4& r1, const float4& r2,
+                                                    float reach, const float4& box, const Strip& s) {
+  uint32_t m = strip_mask<ROWS, NWARPS>(box, s);
+  if (!SGR_EXACT_STRIPS || m == 0u) return m;
+  const V3 Tu = v3(r0.x, r0.y, r0.z), Tv = v3(r0.w, r1.x, r1.y), Tw = v3(r1.z, r1.w, r2.x);
+#pragma unroll
+  for (int w = 0; w < NWARPS; ++w) {
+    if (!((m >> w) & 1u)) continue;
+    bool any = false;
+    for (int r = 0; r < ROWS && !any; ++r) {
+      const float y = s.y0 + (float)(ROWS * w + r);
+      if (y < box.z || y > box.w) continue;
+      any = row_reaches(Tu, Tv, Tw, r2.y, r2.z, reach, y, s.x0, s.x1);
+    }
+    if (!any) m &= ~(1u << w);
+  }
+  return m;
+}
+
 // Compacts this warp's surviving slots of a staged batch into `list`, in
 // slot order; returns their number.
 __device__ __forceinline__ int warp_survivors(const uint8_t* mask, int n, int warp, int lane, uint8_t* list) {
@@ -349,7 +412,10 @@ __global__ void __launch_bounds__(FwdShape::NT, (VARIANT == SGR_VARIANT_PLAIN) ?
       const float4* rec = g.records + (size_t)r * kRecF4;
 #pragma unroll
       for (int k = 0; k < kRecF4 - 1; ++k) s_rec[k][e] = rec[k];
-      s_mask[e] = (uint8_t)strip_mask<ROWS, NW>(rec[5], strip);
+      {
+        const float4 a0 = s_rec[0][e], a1 = s_rec[1][e], a2 = s_rec[2][e];
+        s_mask[e] = (uint8_t)strip_mask_rows<ROWS, NW>(a0, a1, a2, s_rec[3][e].w, rec[5], strip);
+      }
       if (VARIANT == SGR_VARIANT_PART) {
         const float* sem = b.semantics + (size_t)(sid_base + (int)r) * S;
         for (int g4 = 0; g4 < (S + 3) / 4; ++g4) {
@@ -703,7 +769,10 @@ __global__ void __launch_bounds__(BwdShape<VARIANT>::NT,
       const float4* rec = g.records + (size_t)r * kRecF4;
 #pragma unroll
       for (int k = 0; k < kRecF4 - 1; ++k) s_rec[k][e] = rec[k];
-      s_mask[e] = (uint8_t)strip_mask<ROWS, NW>(rec[5], strip);
+      {
+        const float4 a0 = s_rec[0][e], a1 = s_rec[1][e], a2 = s_rec[2][e];
+        s_mask[e] = (uint8_t)strip_mask_rows<ROWS, NW>(a0, a1, a2, s_rec[3][e].w, rec[5], strip);
+      }
     }
     __syncthreads();
     const int cnt = warp_survivors(s_mask, n, warp, lane, s_list[warp]);
