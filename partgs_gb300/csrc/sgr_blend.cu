@@ -90,37 +90,54 @@ __device__ __forceinline__ bool row_reaches(const V3& Tu, const V3& Tv, const V3
 #ifndef SGR_EXACT_STRIPS
 #define SGR_EXACT_STRIPS 1
 #endif
+// SGR_BWD_SPLIT 1 gives the backward one strip bit per pixel row pair of a
+// thread, so that a warp skips a pixel whose rows an entry cannot reach.
+// Measured slower (blend backward 27.9 -> 33.2 ms on the 500k x 16 view
+// scene: the extra branches cost more than the skipped pixels), so it is off.
+#ifndef SGR_BWD_SPLIT
+#define SGR_BWD_SPLIT 0
+#endif
 
-// strip_mask, then each strip it keeps is tested row by row with
-// row_reaches (rows outside the box are skipped).
-template <int ROWS, int NWARPS>
+// The strips of a record, each split into SPLIT groups of rows: bit
+// w * SPLIT + g is set when group g of strip w (rows ROWS w + g ROWS/SPLIT
+// on) may reach the record -- the reach box first, then, for each group
+// the box admits, row_reaches on its rows inside the box.  With two pixels
+// per thread (two rows apart) the groups are the thread's pixels.
+template <int ROWS, int NWARPS, int SPLIT>
 __device__ __forceinline__ uint32_t strip_mask_rows(const float4& r0, const float4& r1, const float4& r2,
                                                     float reach, const float4& box, const Strip& s) {
-  uint32_t m = strip_mask<ROWS, NWARPS>(box, s);
-  if (!SGR_EXACT_STRIPS || m == 0u) return m;
+  constexpr int RG = ROWS / SPLIT;
+  static_assert(RG * SPLIT == ROWS && NWARPS * SPLIT <= 8, "strip groups");
+  if (box.y < s.x0 || box.x > s.x1) return 0u;
   const V3 Tu = v3(r0.x, r0.y, r0.z), Tv = v3(r0.w, r1.x, r1.y), Tw = v3(r1.z, r1.w, r2.x);
+  uint32_t m = 0u;
 #pragma unroll
   for (int w = 0; w < NWARPS; ++w) {
-    if (!((m >> w) & 1u)) continue;
-    bool any = false;
-    for (int r = 0; r < ROWS && !any; ++r) {
-      const float y = s.y0 + (float)(ROWS * w + r);
-      if (y < box.z || y > box.w) continue;
-      any = row_reaches(Tu, Tv, Tw, r2.y, r2.z, reach, y, s.x0, s.x1);
+#pragma unroll
+    for (int gi = 0; gi < SPLIT; ++gi) {
+      const float ya = s.y0 + (float)(ROWS * w + RG * gi);
+      if (!(box.w >= ya && box.z <= ya + (float)(RG - 1))) continue;
+      bool any = !SGR_EXACT_STRIPS;
+      for (int r = 0; r < RG && !any; ++r) {
+        const float y = ya + (float)r;
+        if (y < box.z || y > box.w) continue;
+        any = row_reaches(Tu, Tv, Tw, r2.y, r2.z, reach, y, s.x0, s.x1);
+      }
+      if (any) m |= 1u << (w * SPLIT + gi);
     }
-    if (!any) m &= ~(1u << w);
   }
   return m;
 }
 
 // Compacts this warp's surviving slots of a staged batch into `list`, in
 // slot order; returns their number.
+template <int SPLIT = 1>
 __device__ __forceinline__ int warp_survivors(const uint8_t* mask, int n, int warp, int lane, uint8_t* list) {
   int cnt = 0;
 #pragma unroll
   for (int k = 0; k < kWarps; ++k) {
     const int j = k * 32 + lane;
-    const bool keep = j < n && ((mask[j] >> warp) & 1u);
+    const bool keep = j < n && ((mask[j] >> (warp * SPLIT)) & ((1u << SPLIT) - 1u));
     const unsigned bal = __ballot_sync(0xffffffffu, keep);
     if (keep) list[cnt + __popc(bal & ((1u << lane) - 1u))] = (uint8_t)j;
     cnt += __popc(bal);
@@ -337,14 +354,18 @@ __device__ __forceinline__ void fwd_fragment(FwdPixel<VARIANT>& q, const float4 
   q.last_contributor = contributor;
 }
 
-// Resident CTAs per SM the part variant's kernels are compiled for (80
-// registers; the semantic sums and gradients live in shared memory).
+// Resident CTAs per SM the forward is compiled for: 4 for the plain variant
+// (64 registers), 3 for the part variant (80 registers; its semantic sums
+// and gradients live in shared memory).
+#ifndef SGR_FWD_MIN_CTAS
+#define SGR_FWD_MIN_CTAS 4
+#endif
 #ifndef SGR_PART_FWD_MIN_CTAS
 #define SGR_PART_FWD_MIN_CTAS 3
 #endif
 
 template <int VARIANT>
-__global__ void __launch_bounds__(FwdShape::NT, (VARIANT == SGR_VARIANT_PLAIN) ? 0 : SGR_PART_FWD_MIN_CTAS)
+__global__ void __launch_bounds__(FwdShape::NT, (VARIANT == SGR_VARIANT_PLAIN) ? SGR_FWD_MIN_CTAS : SGR_PART_FWD_MIN_CTAS)
     k_render_fwd(const sgr_batch b, GeomView g, sgr_fwd_outputs out) {
   using Shape = FwdShape;
   constexpr int PX = Shape::PX, NT = Shape::NT, NW = Shape::NW, ROWS = Shape::ROWS, NS = kSemSlots<VARIANT>;
@@ -415,7 +436,7 @@ __global__ void __launch_bounds__(FwdShape::NT, (VARIANT == SGR_VARIANT_PLAIN) ?
       for (int k = 0; k < kRecF4 - 1; ++k) s_rec[k][e] = rec[k];
       {
         const float4 a0 = s_rec[0][e], a1 = s_rec[1][e], a2 = s_rec[2][e];
-        s_mask[e] = (uint8_t)strip_mask_rows<ROWS, NW>(a0, a1, a2, s_rec[3][e].w, rec[5], strip);
+        s_mask[e] = (uint8_t)strip_mask_rows<ROWS, NW, 1>(a0, a1, a2, s_rec[3][e].w, rec[5], strip);
       }
       if (VARIANT == SGR_VARIANT_PART) {
         const float* sem = b.semantics + (size_t)(sid_base + (int)r) * S;
@@ -664,6 +685,9 @@ __global__ void __launch_bounds__(BwdShape<VARIANT>::NT,
                                                                       float* __restrict__ dL_dsemantics) {
   using Shape = BwdShape<VARIANT>;
   constexpr int PX = Shape::PX, NT = Shape::NT, NW = Shape::NW, ROWS = Shape::ROWS, NS = kSemSlots<VARIANT>;
+  // strip masks with one bit per pixel row pair of a thread, so a warp skips
+  // a pixel whose rows the entry cannot reach
+  constexpr int SPLIT = SGR_BWD_SPLIT ? PX : 1;
   const int tiles_per_view = g.tiles_x * g.tiles_y;
   const int tile = blockIdx.x;
   const int v = tile / tiles_per_view;
@@ -772,14 +796,15 @@ __global__ void __launch_bounds__(BwdShape<VARIANT>::NT,
       for (int k = 0; k < kRecF4 - 1; ++k) s_rec[k][e] = rec[k];
       {
         const float4 a0 = s_rec[0][e], a1 = s_rec[1][e], a2 = s_rec[2][e];
-        s_mask[e] = (uint8_t)strip_mask_rows<ROWS, NW>(a0, a1, a2, s_rec[3][e].w, rec[5], strip);
+        s_mask[e] = (uint8_t)strip_mask_rows<ROWS, NW, SPLIT>(a0, a1, a2, s_rec[3][e].w, rec[5], strip);
       }
     }
     __syncthreads();
-    const int cnt = warp_survivors(s_mask, n, warp, lane, s_list[warp]);
+    const int cnt = warp_survivors<SPLIT>(s_mask, n, warp, lane, s_list[warp]);
     for (int si = 0; si < cnt; ++si) {
       const int j = s_list[warp][si];
       const int pos = hi - 1 - j;
+      const uint32_t rows_live = (s_mask[j] >> (warp * SPLIT)) & ((1u << SPLIT) - 1u);   // which pixels may reach
       if (pos >= warp_max) continue;        // uniform: past every lane's last contributor
       float gv[32];
 #pragma unroll
@@ -789,12 +814,15 @@ __global__ void __launch_bounds__(BwdShape<VARIANT>::NT,
       BwdGeom f[PX];
       bool may = false;
 #pragma unroll
-      for (int i = 0; i < PX; ++i) may |= bwd_reach<VARIANT>(q[i], r0, r1, r2, reach, pos, f[i]);
+      for (int i = 0; i < PX; ++i) {
+        f[i].live = false;
+        if (SPLIT == 1 || ((rows_live >> i) & 1u)) may |= bwd_reach<VARIANT>(q[i], r0, r1, r2, reach, pos, f[i]);
+      }
       if (!__any_sync(0xffffffffu, may)) continue;  // uniform: no pixel of the warp within reach
       bool ok = false;
 #pragma unroll
       for (int i = 0; i < PX; ++i) {
-        bwd_alpha(r1, r2, f[i]);
+        if (SPLIT == 1 || ((rows_live >> i) & 1u)) bwd_alpha(r1, r2, f[i]);   // uniform
         ok |= f[i].live;
       }
       if (!__any_sync(0xffffffffu, ok)) continue;
