@@ -21,6 +21,7 @@
 #include <cuda_runtime.h>
 
 #include <cfloat>
+#include <climits>
 #include <cstdint>
 
 #include "../../include/sgr.h"
@@ -236,9 +237,12 @@ int sgr_radius_downsample(const double* pts, int64_t n, const double* lo, const 
       cudaSuccess)
     return SGR_ERR_CUDA;
   if (cudaMemsetAsync(sa, 0, n, st) != cudaSuccess) return SGR_ERR_CUDA;
-  int r = 0;
-  for (; r < 100000; ++r) {
-    unsigned long long left = 0;
+  // Every round decides at least the lowest-index undecided point (its
+  // earlier neighbours are all decided), so n rounds always suffice.
+  long long r = 0;
+  unsigned long long left = 1;
+  for (; r <= n && left != 0; ++r) {
+    left = 0;
     if (cudaMemsetAsync(count, 0, 8, st) != cudaSuccess) return SGR_ERR_CUDA;
     k_mis_round<<<blocks, 256, 0, st>>>(pts, n, lo3, inv, radius * radius, keys_sorted, ids_sorted, sa, sb, count);
     sgr::count_launches(1);
@@ -248,9 +252,9 @@ int sgr_radius_downsample(const double* pts, int64_t n, const double* lo, const 
     uint8_t* t = sa;
     sa = sb;
     sb = t;
-    if (left == 0) break;
   }
-  if (rounds) *rounds = r + 1;
+  if (left != 0) return SGR_ERR_CUDA;   // cannot happen: see above
+  if (rounds) *rounds = (int32_t)min(r, (long long)INT32_MAX);
   if (cudaMemcpyAsync(state, sa, n, cudaMemcpyDeviceToDevice, st) != cudaSuccess) return SGR_ERR_CUDA;
   return cudaGetLastError() == cudaSuccess ? SGR_OK : SGR_ERR_CUDA;
 }
