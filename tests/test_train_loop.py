@@ -2,6 +2,8 @@
 step is caught, the interval is undone and run again after a re-capture with
 room for the entries, and the run ends where a run with enough room from the
 start ends."""
+import math
+
 import pytest
 import torch
 
@@ -18,10 +20,13 @@ def test_train_recovers_from_a_cell_list_overflow(sgr_lib):
     tr = SurfelTrainer(scene, cams)
     tr.capture(targets, warmup=2)
     start = tr.snapshot()
-    loss_ok = float(tr.train(6, check_every=3))
+    loss_ok = float(tr.train(6, check_every=3).detach())
     assert tr.recaptures == 0
     ok = [p.detach().clone() for p in tr.params()]
     _, _, entries = tr.raster.counts()
+    tr.restore(start)                                   # a second clean run: the natural spread
+    tr.train(6, check_every=3)
+    again = [p.detach().clone() for p in tr.params()]
 
     tr.restore(start)
     tr.raster.set_capacity(max(1, entries // 3))        # far too small for this scene
@@ -31,14 +36,17 @@ def test_train_recovers_from_a_cell_list_overflow(sgr_lib):
     flags, _ = tr.raster.sticky_counts(reset=True)
     assert flags & L.SGR_FLAG_BIN_OVERFLOW                # the captured step overflows
     tr.restore(start)
-    loss = tr.train(6, check_every=3)
-    assert tr.recaptures >= 1 and torch.isfinite(loss)
+    loss = float(tr.train(6, check_every=3).detach())
+    assert tr.recaptures >= 1 and math.isfinite(loss)
     assert tr.raster.bin_capacity >= entries
-    # The two runs differ only in the order of the gradient atomics.  Adam's
-    # first steps move every element by about +-lr whatever its gradient's
-    # size, so an element whose gradient is near zero may step the other way:
-    # compare the losses, and require nearly every element to agree.
-    assert abs(float(loss) - loss_ok) <= 1e-3 * abs(loss_ok)
-    for a, b in zip(ok, tr.params()):
-        off = (a - b.detach()).abs() > 1e-5 * max(float(a.abs().max()), 1.0)
-        assert float(off.float().mean()) < 0.01
+    # Runs differ only in the order of the gradient atomics.  Adam's first
+    # steps move every element by about +-lr whatever its gradient's size, so
+    # an element whose gradient is near zero may step the other way.  The
+    # recovered run must be as close to the clean run as two clean runs are.
+    assert abs(loss - loss_ok) <= 1e-3 * abs(loss_ok)
+
+    def off(a, b):
+        return float(((a - b).abs() > 1e-5 * max(float(a.abs().max()), 1.0)).float().mean())
+
+    for a, c, b in zip(ok, again, tr.params()):
+        assert off(a, b.detach()) <= 3 * off(a, c) + 0.005
