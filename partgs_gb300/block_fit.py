@@ -73,15 +73,28 @@ class BlockFit:
         _, others, _, _ = raster(xyz, op, None, torch.exp(log_s), rot, colors_precomp=torch.ones_like(xyz))
         return others
 
-    def fit(self, init, iters: int = 300, eval_every: int = 10):
+    def fit(self, init, iters: int = 300, eval_every: int = 10, reg: bool = False):
         """Runs the fit from init (semi, eps, quat, trans); returns
-        [(fit seconds so far, Chamfer distance to the target)]."""
+        [(fit seconds so far, Chamfer distance to the target)].  With ``reg``
+        the block model's regularisers are added as summarize_losses adds
+        them (block_gaussian_model.py:584-648): ray coverage and uncoverage,
+        occupancy BCE and overlap against the target silhouettes, one view's
+        2048 rays x 128 samples per iteration, with the reference's weights."""
         raw = [t.detach().float().to(self.dev).clone().contiguous() for t in to_binding_params(*init)]
         sq_s, sq_eps, sq_r, sq_t = (t.requires_grad_(True) for t in raw)
         opt = SurfelAdam([{"params": [sq_s], "lr": LR["sq_s"]}, {"params": [sq_eps], "lr": LR["sq_eps"]},
                           {"params": [sq_r], "lr": LR["sq_r"]}, {"params": [sq_t], "lr": LR["sq_t"]}], eps=1e-15)
         hist = [(0.0, self.chamfer_of(sq_s, sq_eps, sq_r, sq_t))]
         elapsed = 0.0
+        self.last_reg = None
+        if reg:
+            from . import sq_losses as Q
+            gen = torch.Generator(device=self.dev).manual_seed(self.seed + 23)
+            occ = torch.full((sq_s.shape[0],), 4.6, device=self.dev)   # the fit's fixed block opacity logit
+            weights = torch.tensor([10.0, 100.0, 0.02, 2.0], device=self.dev)
+            Ks = [Q.intrinsics(c.height, c.width, c.fovx, c.fovy, self.dev) for c in self.cams]
+            wvs = [torch.as_tensor(c.world_view_transform, device=self.dev) for c in self.cams]
+        it = 0
         for it0 in range(0, iters, eval_every):
             torch.cuda.synchronize()
             t0 = time.perf_counter()
@@ -89,11 +102,23 @@ class BlockFit:
                 others = self.render(sq_s, sq_eps, sq_r, sq_t)
                 loss = (others[:, 1] - self.alpha_t).abs().mean() + \
                     (self.mask_t * (others[:, 5] - self.depth_t).abs()).mean()
+                if reg:
+                    v = it % len(self.cams)
+                    c = self.cams[v]
+                    rays = Q.cast_rays(Ks[v], wvs[v], c.height, c.width, self.mask_t[v], *Q.NEAR_FAR["blender"],
+                                       generator=gen)
+                    ovl = Q.overlap_samples(sq_s.shape[0], device=self.dev, generator=gen)
+                    S, R, T, e1, e2 = Q.block_frames(sq_s, sq_r, sq_t, sq_eps, SMIN)
+                    terms = Q.sq_losses(S, R, T, e1, e2, occ, RATIO, rays, ovl)
+                    loss = loss + (weights * terms.nan_to_num(0.0)).sum()
+                    self.last_reg = terms.detach()
+                it += 1
                 loss.backward()
                 opt.step()
             torch.cuda.synchronize()
             elapsed += time.perf_counter() - t0
             hist.append((elapsed, self.chamfer_of(sq_s, sq_eps, sq_r, sq_t)))
+        self.last_params = [t.detach() for t in (sq_s, sq_eps, sq_r, sq_t)]
         return hist
 
     def chamfer_of(self, sq_s, sq_eps, sq_r, sq_t):

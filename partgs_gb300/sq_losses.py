@@ -204,6 +204,25 @@ def sq_losses(S, R, T, eps1, eps2, occ_logit, ratio: float, rays: RaySamples | N
     return _SQLosses.apply(S, R, T, eps1, eps2, occ_logit, ratio, rays, ovl)
 
 
+def quaternion_to_rotation_matrix(q: torch.Tensor) -> torch.Tensor:
+    """[N,4] (w, x, y, z) to [N,3,3], the reference's convention
+    (games/block_mesh_splatting/utils/superquadric.py:93-101)."""
+    w, x, y, z = q.unbind(-1)
+    return torch.stack([1 - 2 * y ** 2 - 2 * z ** 2, 2 * x * y - 2 * z * w, 2 * x * z + 2 * y * w,
+                        2 * x * y + 2 * z * w, 1 - 2 * x ** 2 - 2 * z ** 2, 2 * y * z - 2 * x * w,
+                        2 * x * z - 2 * y * w, 2 * y * z + 2 * x * w, 1 - 2 * x ** 2 - 2 * y ** 2], -1).view(-1, 3, 3)
+
+
+def block_frames(sq_s, sq_r, sq_t, sq_eps, scale_block_min: float = 0.2):
+    """(S, R, T, eps1, eps2) of the block model's raw parameters, as
+    BlockGaussianModel builds _blocks_SRT and _blocks_eps
+    (block_gaussian_model.py:111-121, 189-192, 220-222); differentiable."""
+    S = torch.exp(sq_s) + scale_block_min
+    R = quaternion_to_rotation_matrix(torch.nn.functional.normalize(sq_r, dim=-1))
+    eps1, eps2 = (torch.sigmoid(sq_eps) * 1.8 + 0.1).unbind(-1)
+    return S, R, sq_t, eps1, eps2
+
+
 def implicit_sq(points, S, R, T, eps1, eps2, ratio: float) -> torch.Tensor:
     """SDF (as_sdf=2) of world points [M, 3] to every block: [N, M] (no gradient)."""
     lib = _lib()
