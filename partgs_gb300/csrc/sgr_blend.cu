@@ -12,9 +12,10 @@
 // time: the entries whose tile rectangle holds the tile go, in order, into a
 // ring of record ids in shared memory; their count gives list positions.
 // The forward records how far it scanned; the backward streams the same
-// span back to front.  256 ring entries at a time are staged; each entry's
-// reach box (sgr_common.cuh) is tested once against the tile's eight 16x2
-// pixel strips (one strip per warp), and each warp then walks only the
+// span back to front.  256 ring entries at a time are staged; each entry is
+// tested once against the warps' pixel strips (16x2 in the forward, 16x4 in
+// the backward): its reach box (sgr_common.cuh) first, then, for the strips
+// the box admits, row by row (row_reaches).  Each warp then walks only the
 // entries that can reach its strip, in list order.  Entries that cannot
 // reach a pixel are ones the reference skips at its alpha test, so outputs,
 // contributor counts and median indices are unchanged.  Per pixel, a
