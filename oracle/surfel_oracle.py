@@ -46,7 +46,6 @@ and the blend themselves are parity unpinned by a runnable reference.
 """
 from __future__ import annotations
 
-import math
 from dataclasses import dataclass, field
 
 import numpy as np

@@ -1,6 +1,5 @@
 """The oracle and the host-side code against golden vectors produced by the
 reference's own Python (tests/golden/make_golden.py)."""
-import math
 import os
 import types
 

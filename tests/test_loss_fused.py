@@ -3,7 +3,6 @@ operations (autograd, float64): value and gradients w.r.t. the rendered
 colour and aux maps."""
 import types
 
-import numpy as np
 import pytest
 import torch
 

@@ -3,7 +3,6 @@ timing) on two gloo ranks on the CPU."""
 import os
 import socket
 
-import torch
 import torch.distributed as dist
 import torch.multiprocessing as mp
 

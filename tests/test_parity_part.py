@@ -16,7 +16,6 @@ def case(sgr_lib, request):
     with a partly filled float4 group) and 16 (the maximum)."""
     S = request.param
     import partgs_gb300.diff_surfel_rasterization_part as dsrp
-    from partgs_gb300 import raster
     from partgs_gb300.scenes import random_surfels
     from partgs_gb300.cameras import orbit_cameras
     scene = random_surfels(3000, seed=11)
