@@ -450,6 +450,17 @@ int sgr_sq_sdf(const sgr_sq_loss_args* args, const float* points, int64_t n_poin
  * of q: dist [n] (Euclidean) and, unless NULL, idx [n] (first minimum). */
 int sgr_nn_search(const float* q, int64_t n, const float* r, int64_t m, float* dist, int32_t* idx, void* stream);
 
+/* The same search through a uniform cell grid over r (about two cells per
+ * point): the same distances and indices as sgr_nn_search, bit for bit, at
+ * a cost that grows with n + m instead of n m for surface-like point sets.
+ * lo / hi (host, 3 floats): a box holding every point of r, e.g. its
+ * bounding box.  Queries far from every point of r fall back to the
+ * brute-force scan inside the call.  Seven launches plus a CUB scan and
+ * sort; no host synchronisation. */
+size_t sgr_nn_grid_scratch_bytes(int64_t n, int64_t m, const float* lo, const float* hi);
+int sgr_nn_search_grid(const float* q, int64_t n, const float* r, int64_t m, const float* lo, const float* hi,
+                       float* dist, int32_t* idx, void* scratch, size_t scratch_bytes, void* stream);
+
 /* The reference's radius downsample: in index order, point i is kept unless
  * an earlier kept point lies within `radius` (distance <= radius, fp64 like
  * the reference).  pts [n,3] float64 on the device, lo / hi their bounding

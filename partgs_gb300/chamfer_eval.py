@@ -11,7 +11,8 @@ the reference's evaluate_mesh (utils/blender_eval.py:25-111):
    (``sgr_radius_downsample``);
 4. accuracy = mean of the nearest-GT distances of all samples below
    MAX_DIST, completeness = mean of the GT points' nearest-sample distances
-   (to the thinned set) below MAX_DIST (``sgr_nn_search``, exact);
+   (to the thinned set) below MAX_DIST (exact nearest neighbours:
+   ``sgr_nn_search_grid`` for large sets, ``sgr_nn_search`` for small);
 5. the score is their average.
 """
 from __future__ import annotations
@@ -32,6 +33,11 @@ def _lib():
     lib = L.load()
     lib.sgr_nn_search.restype = C.c_int
     lib.sgr_nn_search.argtypes = [_p, C.c_int64, _p, C.c_int64, _p, _p, _p]
+    f3 = C.POINTER(C.c_float)
+    lib.sgr_nn_grid_scratch_bytes.restype = C.c_size_t
+    lib.sgr_nn_grid_scratch_bytes.argtypes = [C.c_int64, C.c_int64, f3, f3]
+    lib.sgr_nn_search_grid.restype = C.c_int
+    lib.sgr_nn_search_grid.argtypes = [_p, C.c_int64, _p, C.c_int64, f3, f3, _p, _p, _p, C.c_size_t, _p]
     lib.sgr_downsample_scratch_bytes.restype = C.c_size_t
     lib.sgr_downsample_scratch_bytes.argtypes = [C.c_int64]
     lib.sgr_radius_downsample.restype = C.c_int
@@ -40,15 +46,35 @@ def _lib():
     return lib
 
 
-def nn_distance(q: torch.Tensor, r: torch.Tensor, with_index: bool = False):
-    """Nearest-neighbour distances (and indices) in r of every point of q."""
+GRID_MIN_PAIRS = 1 << 24     # below this many (query, point) pairs the brute-force scan is as fast
+
+
+def nn_distance(q: torch.Tensor, r: torch.Tensor, with_index: bool = False, method: str = "auto"):
+    """Nearest-neighbour distances (and indices) in r of every point of q.
+
+    method: "brute" (sgr_nn_search), "grid" (sgr_nn_search_grid, which
+    gives the same results bit for bit) or "auto" (the grid for large sets;
+    it reads r's bounding box on the host)."""
+    if method not in ("auto", "brute", "grid"):
+        raise ValueError(f"unknown method {method!r}")
+    lib = _lib()
     q = q.float().contiguous()
     r = r.float().contiguous()
-    dist = torch.empty(q.shape[0], device=q.device)
-    idx = torch.empty(q.shape[0], dtype=torch.int32, device=q.device) if with_index else None
-    L.check(_lib().sgr_nn_search(q.data_ptr(), q.shape[0], r.data_ptr(), r.shape[0], dist.data_ptr(),
-                                 idx.data_ptr() if idx is not None else None,
-                                 torch.cuda.current_stream().cuda_stream), "sgr_nn_search")
+    n, m = q.shape[0], r.shape[0]
+    dist = torch.empty(n, device=q.device)
+    idx = torch.empty(n, dtype=torch.int32, device=q.device) if with_index else None
+    ip = idx.data_ptr() if idx is not None else None
+    stream = torch.cuda.current_stream().cuda_stream
+    grid = method == "grid" or (method == "auto" and n * m >= GRID_MIN_PAIRS)
+    if grid and n > 0 and m > 0:
+        lo_t, hi_t = torch.aminmax(r, dim=0)
+        lo = (C.c_float * 3)(*lo_t.tolist())
+        hi = (C.c_float * 3)(*hi_t.tolist())
+        scratch = torch.empty(lib.sgr_nn_grid_scratch_bytes(n, m, lo, hi), dtype=torch.uint8, device=q.device)
+        L.check(lib.sgr_nn_search_grid(q.data_ptr(), n, r.data_ptr(), m, lo, hi, dist.data_ptr(), ip,
+                                       scratch.data_ptr(), scratch.numel(), stream), "sgr_nn_search_grid")
+    else:
+        L.check(lib.sgr_nn_search(q.data_ptr(), n, r.data_ptr(), m, dist.data_ptr(), ip, stream), "sgr_nn_search")
     return (dist, idx) if with_index else dist
 
 
@@ -186,6 +212,21 @@ def main(argv=None):
     print(f"samples {pcd.shape[0]} kept {int(keep.sum())} gt {gt.shape[0]} rounds {rounds}")
     print(f"sample {1e3 * (t1 - t0):.1f} ms, downsample {1e3 * (t2 - t1):.1f} ms, whole evaluation "
           f"{1e3 * (t3 - t2):.1f} ms; acc {acc:.6f} comp {comp:.6f} avg {avg:.6f}")
+    # the two searches of the evaluation, brute force against the grid
+    stl = torch.as_tensor(gt, dtype=torch.float32, device=pcd.device)
+    down = pcd[keep]
+    for name, q, r in (("samples->gt", pcd, stl), ("gt->kept", stl, down)):
+        res, ms = {}, {}
+        for method in ("brute", "grid"):
+            nn_distance(q, r, True, method)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            res[method] = nn_distance(q, r, True, method)
+            torch.cuda.synchronize()
+            ms[method] = 1e3 * (time.perf_counter() - t0)
+        same = all(torch.equal(x, y) for x, y in zip(res["brute"], res["grid"]))
+        print(f"nearest neighbours {name} ({q.shape[0]} x {r.shape[0]}): brute {ms['brute']:.2f} ms, "
+              f"grid {ms['grid']:.2f} ms, identical {same}")
 
 
 if __name__ == "__main__":

@@ -53,6 +53,8 @@ void count_launches(int n = 1);
 constexpr float kNearP0 = 0.2f;
 constexpr float kFarP0 = 100.0f;
 constexpr float kFilterSizeP0 = 0.707106f;
+// 1 / filter size^2.  Both variants scale by exactly 2: the part variant's
+// double constant 1 / 0.7071067811865476^2 times a float rounds to 2x.
 constexpr float kFilterInvSquareP0 = 2.0f;
 constexpr double kFilterSizeP1 = 0.7071067811865476;
 constexpr double kNearP1 = 0.2;

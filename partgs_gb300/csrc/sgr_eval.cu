@@ -1,10 +1,25 @@
 // Chamfer evaluation on the GPU (utils/blender_eval.py:25-111): exact
 // nearest neighbours between point sets and the radius downsample.
 //
-// Nearest neighbours (sgr_nn_search): brute force, exact in fp32.  Each
-// thread owns 4 query points; the reference points stream through shared
-// memory 1024 at a time and every thread tests all of them (squared
-// distances, first minimum kept on ties).
+// Nearest neighbours, brute force (sgr_nn_search): each thread owns 4 query
+// points; the reference points stream through shared memory 1024 at a time
+// and every thread tests all of them (squared distances, first minimum kept
+// on ties).
+//
+// Nearest neighbours through a cell grid (sgr_nn_search_grid): the same
+// squared distances in the same arithmetic, the same tie rule, so the same
+// distances and indices bit for bit.  The reference points are counted into
+// a uniform grid of about two cells per point and scattered in cell order;
+// the queries are sorted by cell, so a warp's queries search neighbouring
+// cells.  Each query visits shells of cells around its own (Chebyshev ring
+// k = 0, 1, ...), skipping cells whose box is farther than the best distance
+// so far, and stops once the best squared distance is below the squared
+// distance to every cell outside the searched cube.  The bounds carry a
+// margin that covers the fp32 rounding of the cell assignment, the cell
+// faces and the squared distances.  Queries still open after a number of
+// shells that grows with the cube root of the reference count (far from
+// every reference point, in a sparse region) are listed and finished by the
+// brute-force scan.
 //
 // Radius downsample (sgr_radius_downsample): the reference keeps point i of
 // its shuffled order unless an earlier kept point lies within the radius
@@ -17,6 +32,7 @@
 // synchronises the host to read the count of undecided points; this is an
 // evaluation path, not part of the training step.
 #include <cub/device/device_radix_sort.cuh>
+#include <cub/device/device_scan.cuh>
 
 #include <cuda_runtime.h>
 
@@ -36,19 +52,31 @@ constexpr int kNNThreads = 256;
 constexpr int kNNQ = 4;           // queries per thread
 constexpr int kNNTile = 1024;     // reference points per shared-memory tile
 
+// Squared distance, rounded the same way in every search kernel.
+__device__ __forceinline__ float nn_d2(float qx, float qy, float qz, float rx, float ry, float rz) {
+  const float dx = qx - rx, dy = qy - ry, dz = qz - rz;
+  return __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+}
+
+// Brute force over all of r.  With `list`, the queries are list[0 .. *count)
+// (the grid search's open queries) instead of 0 .. n.
 __global__ void __launch_bounds__(kNNThreads) k_nn(const float* __restrict__ q, long long n,
                                                   const float* __restrict__ r, long long m,
-                                                  float* __restrict__ dist, int* __restrict__ idx) {
+                                                  float* __restrict__ dist, int* __restrict__ idx,
+                                                  const int* __restrict__ list, const unsigned* __restrict__ count) {
   __shared__ float s_r[kNNTile * 3];
+  if (list) n = (long long)*count;
+  const long long q0 = ((long long)blockIdx.x * kNNThreads + threadIdx.x) * kNNQ;
+  if ((long long)blockIdx.x * kNNThreads * kNNQ >= n) return;   // uniform over the block
   float qx[kNNQ], qy[kNNQ], qz[kNNQ], best[kNNQ];
   int arg[kNNQ];
-  const long long q0 = ((long long)blockIdx.x * kNNThreads + threadIdx.x) * kNNQ;
 #pragma unroll
   for (int k = 0; k < kNNQ; ++k) {
     const long long i = q0 + k;
-    qx[k] = i < n ? q[3 * i] : 0.f;
-    qy[k] = i < n ? q[3 * i + 1] : 0.f;
-    qz[k] = i < n ? q[3 * i + 2] : 0.f;
+    const long long qi = i < n ? (list ? (long long)list[i] : i) : 0;
+    qx[k] = i < n ? q[3 * qi] : 0.f;
+    qy[k] = i < n ? q[3 * qi + 1] : 0.f;
+    qz[k] = i < n ? q[3 * qi + 2] : 0.f;
     best[k] = FLT_MAX;
     arg[k] = -1;
   }
@@ -61,8 +89,7 @@ __global__ void __launch_bounds__(kNNThreads) k_nn(const float* __restrict__ q, 
       const float rx = s_r[3 * j], ry = s_r[3 * j + 1], rz = s_r[3 * j + 2];
 #pragma unroll
       for (int k = 0; k < kNNQ; ++k) {
-        const float dx = qx[k] - rx, dy = qy[k] - ry, dz = qz[k] - rz;
-        const float d2 = dx * dx + dy * dy + dz * dz;
+        const float d2 = nn_d2(qx[k], qy[k], qz[k], rx, ry, rz);
         if (d2 < best[k]) {
           best[k] = d2;
           arg[k] = (int)(t0 + j);
@@ -74,10 +101,231 @@ __global__ void __launch_bounds__(kNNThreads) k_nn(const float* __restrict__ q, 
   for (int k = 0; k < kNNQ; ++k) {
     const long long i = q0 + k;
     if (i < n) {
-      dist[i] = sqrtf(best[k]);
-      if (idx) idx[i] = arg[k];
+      const long long qi = list ? (long long)list[i] : i;
+      dist[qi] = sqrtf(best[k]);
+      if (idx) idx[qi] = arg[k];
     }
   }
+}
+
+// ---- grid nearest neighbours -------------------------------------------------
+
+struct NNGrid {
+  float lox, loy, loz;   // grid origin (the reference points' box corner)
+  float h, inv;          // cell edge and its inverse
+  float margin;          // covers fp32 rounding of cell assignment, faces and distances
+  float hix, hiy, hiz;   // far corner of the reference points' box (inside lo + n h)
+  int nx, ny, nz;
+  int shells;            // shells a query searches before the brute-force scan takes it
+};
+
+__device__ __forceinline__ int grid_axis(float p, float lo, float inv, int n) {
+  return min(max((int)floorf((p - lo) * inv), 0), n - 1);
+}
+
+// Distance along one axis from p to cell c's slab [lo + c h, lo + (c+1) h].
+__device__ __forceinline__ float slab_gap(float p, int c, float lo, float h) {
+  const float a = lo + (float)c * h, b = lo + (float)(c + 1) * h;
+  return fmaxf(0.0f, fmaxf(a - p, p - b));
+}
+
+__global__ void k_grid_count(const float* __restrict__ r, long long m, NNGrid g, uint32_t* __restrict__ count) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= m) return;
+  const int x = grid_axis(r[3 * i], g.lox, g.inv, g.nx), y = grid_axis(r[3 * i + 1], g.loy, g.inv, g.ny),
+            z = grid_axis(r[3 * i + 2], g.loz, g.inv, g.nz);
+  atomicAdd(count + ((long long)z * g.ny + y) * g.nx + x, 1u);
+}
+
+// Reference points in cell order as (x, y, z, index bits); the order within
+// a cell does not matter (ties are decided by index).
+__global__ void k_grid_scatter(const float* __restrict__ r, long long m, NNGrid g, const uint32_t* __restrict__ start,
+                               uint32_t* __restrict__ cursor, float4* __restrict__ pts) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= m) return;
+  const float x = r[3 * i], y = r[3 * i + 1], z = r[3 * i + 2];
+  const long long c = ((long long)grid_axis(z, g.loz, g.inv, g.nz) * g.ny + grid_axis(y, g.loy, g.inv, g.ny)) * g.nx +
+                      grid_axis(x, g.lox, g.inv, g.nx);
+  const uint32_t at = start[c] + atomicAdd(cursor + c, 1u);
+  if (at < start[c + 1]) pts[at] = make_float4(x, y, z, __int_as_float((int)i));   // always: same cell as counted
+}
+
+__global__ void k_query_cells(const float* __restrict__ q, long long n, NNGrid g, uint32_t* __restrict__ keys,
+                              int* __restrict__ ids) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  keys[i] = (uint32_t)(((long long)grid_axis(q[3 * i + 2], g.loz, g.inv, g.nz) * g.ny +
+                        grid_axis(q[3 * i + 1], g.loy, g.inv, g.ny)) * g.nx +
+                       grid_axis(q[3 * i], g.lox, g.inv, g.nx));
+  ids[i] = (int)i;
+}
+
+// Squared lower bound of the distance from p to the grid cells outside the
+// cube [c - k, c + k] on each axis, or FLT_MAX when the cube holds the whole
+// grid.  Those cells lie in six slabs (beyond each face of the cube that is
+// inside the grid); the distance to a slab is taken inside the reference
+// points' box, so a query outside the box (or off a flat point set) gets its
+// distance to the points' part of the slab.
+__device__ __forceinline__ float outside_bound2(float px, float py, float pz, int cx, int cy, int cz, int k,
+                                                const NNGrid& g) {
+  const float ox = fmaxf(0.0f, fmaxf(g.lox - px, px - g.hix) - g.margin);
+  const float oy = fmaxf(0.0f, fmaxf(g.loy - py, py - g.hiy) - g.margin);
+  const float oz = fmaxf(0.0f, fmaxf(g.loz - pz, pz - g.hiz) - g.margin);
+  float b2 = FLT_MAX;
+  auto face = [&](float d, float o1, float o2) {
+    const float t = fmaxf(0.0f, fmaxf(d, 0.0f) - g.margin);
+    b2 = fminf(b2, t * t + o1 * o1 + o2 * o2);
+  };
+  if (cx - k > 0) face(px - (g.lox + (float)(cx - k) * g.h), oy, oz);
+  if (cx + k + 1 < g.nx) face((g.lox + (float)(cx + k + 1) * g.h) - px, oy, oz);
+  if (cy - k > 0) face(py - (g.loy + (float)(cy - k) * g.h), ox, oz);
+  if (cy + k + 1 < g.ny) face((g.loy + (float)(cy + k + 1) * g.h) - py, ox, oz);
+  if (cz - k > 0) face(pz - (g.loz + (float)(cz - k) * g.h), ox, oy);
+  if (cz + k + 1 < g.nz) face((g.loz + (float)(cz + k + 1) * g.h) - pz, ox, oy);
+  return b2;
+}
+
+// One thread per query, in cell order.  A cell is searched unless its box
+// lies farther than the best distance so far; the shell loop ends when the
+// best squared distance is below the bound of everything outside, with a
+// relative 2e-6 kept for the rounding of the squared distances, so no
+// unsearched point can have a smaller (or equal) computed squared distance.
+__global__ void __launch_bounds__(256) k_nn_grid(const float* __restrict__ q, const int* __restrict__ order,
+                                                 long long n, NNGrid g, const uint32_t* __restrict__ start,
+                                                 const float4* __restrict__ pts, float* __restrict__ dist,
+                                                 int* __restrict__ idx, int* __restrict__ open,
+                                                 unsigned* __restrict__ n_open) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const int qi = order[t];
+  const float px = q[3 * (long long)qi], py = q[3 * (long long)qi + 1], pz = q[3 * (long long)qi + 2];
+  const int cx = grid_axis(px, g.lox, g.inv, g.nx), cy = grid_axis(py, g.loy, g.inv, g.ny),
+            cz = grid_axis(pz, g.loz, g.inv, g.nz);
+  float best = FLT_MAX;
+  int arg = INT_MAX;
+  bool done = false;
+  for (int k = 0; k <= g.shells && !done; ++k) {
+    for (int dz = -k; dz <= k; ++dz) {
+      const int z = cz + dz;
+      if (z < 0 || z >= g.nz) continue;
+      const float gz = slab_gap(pz, z, g.loz, g.h);
+      for (int dy = -k; dy <= k; ++dy) {
+        const int y = cy + dy;
+        if (y < 0 || y >= g.ny) continue;
+        const float gy = slab_gap(py, y, g.loy, g.h);
+        const int step = (dz == -k || dz == k || dy == -k || dy == k) ? 1 : 2 * k;   // k = 0 takes the first
+        for (int dx = -k; dx <= k; dx += step) {
+          const int x = cx + dx;
+          if (x < 0 || x >= g.nx) continue;
+          const float gx = slab_gap(px, x, g.lox, g.h);
+          const float gap = fmaxf(0.0f, sqrtf(gx * gx + gy * gy + gz * gz) - g.margin);
+          if (gap * gap * (1.0f - 2e-6f) > best) continue;
+          const long long c = ((long long)z * g.ny + y) * g.nx + x;
+          const uint32_t e = start[c + 1];
+          for (uint32_t j = start[c]; j < e; ++j) {
+            const float4 rp = pts[j];
+            const float d2 = nn_d2(px, py, pz, rp.x, rp.y, rp.z);
+            const int id = __float_as_int(rp.w);
+            if (d2 < best || (d2 == best && id < arg)) {
+              best = d2;
+              arg = id;
+            }
+          }
+        }
+      }
+    }
+    const float b2 = outside_bound2(px, py, pz, cx, cy, cz, k, g);
+    done = b2 == FLT_MAX || best < b2 * (1.0f - 2e-6f);
+  }
+  if (done) {
+    dist[qi] = sqrtf(best);
+    if (idx) idx[qi] = arg == INT_MAX ? -1 : arg;
+  } else {
+    open[atomicAdd(n_open, 1u)] = qi;
+  }
+}
+
+struct NNLayout {
+  size_t start, cursor, pts, keys, keys_sorted, ids, ids_sorted, open, n_open, temp, temp_bytes, end;
+};
+
+// Grid shape for m reference points in the box [lo, hi]: about two cells
+// per point, at most 1024 cells on an axis, found by bisection on the edge.
+bool nn_grid(int64_t m, const float* lo, const float* hi, NNGrid& g) {
+  double ext[3], maxext = 0.0, maxabs = 0.0;
+  for (int a = 0; a < 3; ++a) {
+    if (!(hi[a] >= lo[a]) || !isfinite(lo[a]) || !isfinite(hi[a])) return false;
+    ext[a] = (double)hi[a] - (double)lo[a];
+    maxext = fmax(maxext, ext[a]);
+    maxabs = fmax(maxabs, fmax(fabs((double)lo[a]), fabs((double)hi[a])));
+  }
+  const double target = fmin(fmax(2.0 * (double)m, 1.0), (double)(1 << 26));
+  auto cells = [&](double h) {
+    double c = 1.0;
+    for (int a = 0; a < 3; ++a) c *= fmax(1.0, ceil(ext[a] / h));
+    return c;
+  };
+  double h = 1.0;
+  if (maxext > 0.0) {
+    double a = maxext / 1024.0, b = maxext * 2.0;   // cells(b) = 1
+    if (cells(a) <= target) {
+      b = a;
+    } else {
+      for (int it = 0; it < 100; ++it) {
+        const double mid = 0.5 * (a + b);
+        if (cells(mid) <= target) b = mid; else a = mid;
+      }
+    }
+    h = b * (1.0 + 1e-6);
+  }
+  int n[3];
+  for (int a = 0; a < 3; ++a) n[a] = maxext > 0.0 ? (int)fmax(1.0, ceil(ext[a] / h)) : 1;
+  g.lox = lo[0];
+  g.loy = lo[1];
+  g.loz = lo[2];
+  g.h = (float)h;
+  g.inv = (float)(1.0 / h);
+  g.nx = n[0];
+  g.ny = n[1];
+  g.nz = n[2];
+  g.hix = hi[0];
+  g.hiy = hi[1];
+  g.hiz = hi[2];
+  g.margin = (float)(1e-3 * h + 1e-6 * maxabs);
+  // A shell of radius k costs about 24 k^2 cell tests, the brute-force scan
+  // m distances: cap the shells where their total nears a tenth of m.
+  g.shells = (int)fmin(64.0, fmax(4.0, 0.5 * cbrt(0.1 * (double)m)));
+  return true;
+}
+
+NNLayout nn_layout(long long n, long long m, long long cells) {
+  auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
+  NNLayout L;
+  size_t o = 0;
+  L.start = o; o = al(o + (cells + 1) * 4);
+  L.cursor = o; o = al(o + cells * 4);
+  L.pts = o; o = al(o + m * 16);
+  L.keys = o; o = al(o + n * 4);
+  L.keys_sorted = o; o = al(o + n * 4);
+  L.ids = o; o = al(o + n * 4);
+  L.ids_sorted = o; o = al(o + n * 4);
+  L.open = o; o = al(o + n * 4);
+  L.n_open = o; o = al(o + 4);
+  size_t ts = 0, tr = 0;
+  cub::DeviceScan::ExclusiveSum(nullptr, ts, (uint32_t*)nullptr, (uint32_t*)nullptr, (int64_t)(cells + 1));
+  cub::DeviceRadixSort::SortPairs(nullptr, tr, (const uint32_t*)nullptr, (uint32_t*)nullptr, (const int*)nullptr,
+                                  (int*)nullptr, (int64_t)n, 0, 32);
+  L.temp = o;
+  L.temp_bytes = ts > tr ? ts : tr;
+  o = al(o + L.temp_bytes);
+  L.end = o;
+  return L;
+}
+
+int key_bits(long long cells) {
+  int b = 1;
+  while (b < 32 && (1ll << b) < cells) ++b;
+  return b;
 }
 
 // ---- radius downsample -------------------------------------------------------
@@ -201,8 +449,60 @@ int sgr_nn_search(const float* q, int64_t n, const float* r, int64_t m, float* d
   if (n == 0) return SGR_OK;
   if (m == 0) return SGR_ERR_INVALID_ARGUMENT;
   const long long blocks = (n + (long long)kNNThreads * kNNQ - 1) / ((long long)kNNThreads * kNNQ);
-  k_nn<<<(unsigned)blocks, kNNThreads, 0, static_cast<cudaStream_t>(stream)>>>(q, n, r, m, dist, idx);
+  k_nn<<<(unsigned)blocks, kNNThreads, 0, static_cast<cudaStream_t>(stream)>>>(q, n, r, m, dist, idx, nullptr,
+                                                                              nullptr);
   sgr::count_launches(1);
+  return cudaGetLastError() == cudaSuccess ? SGR_OK : SGR_ERR_CUDA;
+}
+
+size_t sgr_nn_grid_scratch_bytes(int64_t n, int64_t m, const float* lo, const float* hi) {
+  NNGrid g;
+  if (n < 0 || m < 0 || !lo || !hi || !nn_grid(m, lo, hi, g)) return 0;
+  return nn_layout(n, m, (long long)g.nx * g.ny * g.nz).end;
+}
+
+int sgr_nn_search_grid(const float* q, int64_t n, const float* r, int64_t m, const float* lo, const float* hi,
+                       float* dist, int32_t* idx, void* scratch, size_t scratch_bytes, void* stream) {
+  if (n < 0 || m < 0 || (n > 0 && (!q || !dist)) || (n > 0 && m > 0 && (!r || !lo || !hi)))
+    return SGR_ERR_INVALID_ARGUMENT;
+  if (m > 0x7fffffffLL || n > 0x7fffffffLL) return SGR_ERR_UNSUPPORTED;
+  if (n == 0) return SGR_OK;
+  if (m == 0) return SGR_ERR_INVALID_ARGUMENT;
+  NNGrid g;
+  if (!nn_grid(m, lo, hi, g)) return SGR_ERR_INVALID_ARGUMENT;
+  const long long cells = (long long)g.nx * g.ny * g.nz;
+  const NNLayout L = nn_layout(n, m, cells);
+  if (!scratch || scratch_bytes < L.end) return SGR_ERR_WORKSPACE;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  char* sp = static_cast<char*>(scratch);
+  auto* start = reinterpret_cast<uint32_t*>(sp + L.start);
+  auto* cursor = reinterpret_cast<uint32_t*>(sp + L.cursor);
+  auto* pts = reinterpret_cast<float4*>(sp + L.pts);
+  auto* keys = reinterpret_cast<uint32_t*>(sp + L.keys);
+  auto* keys_sorted = reinterpret_cast<uint32_t*>(sp + L.keys_sorted);
+  auto* ids = reinterpret_cast<int*>(sp + L.ids);
+  auto* ids_sorted = reinterpret_cast<int*>(sp + L.ids_sorted);
+  auto* open = reinterpret_cast<int*>(sp + L.open);
+  auto* n_open = reinterpret_cast<unsigned*>(sp + L.n_open);
+  const unsigned mb = (unsigned)((m + 255) / 256), nb = (unsigned)((n + 255) / 256);
+  if (cudaMemsetAsync(start, 0, (cells + 1) * 4, st) != cudaSuccess ||
+      cudaMemsetAsync(cursor, 0, cells * 4, st) != cudaSuccess || cudaMemsetAsync(n_open, 0, 4, st) != cudaSuccess)
+    return SGR_ERR_CUDA;
+  k_grid_count<<<mb, 256, 0, st>>>(r, m, g, start);
+  size_t tb = L.temp_bytes;
+  if (cub::DeviceScan::ExclusiveSum(sp + L.temp, tb, start, start, (int64_t)(cells + 1), st) != cudaSuccess)
+    return SGR_ERR_CUDA;
+  k_grid_scatter<<<mb, 256, 0, st>>>(r, m, g, start, cursor, pts);
+  k_query_cells<<<nb, 256, 0, st>>>(q, n, g, keys, ids);
+  tb = L.temp_bytes;
+  if (cub::DeviceRadixSort::SortPairs(sp + L.temp, tb, keys, keys_sorted, ids, ids_sorted, (int64_t)n, 0,
+                                      key_bits(cells), st) != cudaSuccess)
+    return SGR_ERR_CUDA;
+  k_nn_grid<<<nb, 256, 0, st>>>(q, ids_sorted, n, g, start, pts, dist, idx, open, n_open);
+  // the open queries (count known only on the device): blocks past it return at once
+  const long long blocks = (n + (long long)kNNThreads * kNNQ - 1) / ((long long)kNNThreads * kNNQ);
+  k_nn<<<(unsigned)blocks, kNNThreads, 0, st>>>(q, n, r, m, dist, idx, open, n_open);
+  sgr::count_launches(5);
   return cudaGetLastError() == cudaSuccess ? SGR_OK : SGR_ERR_CUDA;
 }
 

@@ -32,36 +32,6 @@ struct GeomView {
   int tiles_x, tiles_y;
 };
 
-// One pixel / surfel intersection (P0/cr/forward.cu:349-366).
-struct Frag {
-  V3 k, l, p;
-  float sx, sy, rho3d, rho2d, rho, depth, dx, dy;
-  bool use3d;
-};
-
-template <int VARIANT>
-__device__ __forceinline__ void intersect(float pxf, float pyf, V3 Tu, V3 Tv, V3 Tw, float cx, float cy, Frag& f) {
-  if (VARIANT == SGR_VARIANT_PLAIN) {
-    f.k = pxf * Tw - Tu;
-    f.l = pyf * Tw - Tv;
-  } else {
-    f.k = v3(-Tu.x + pxf * Tw.x, -Tu.y + pxf * Tw.y, -Tu.z + pxf * Tw.z);
-    f.l = v3(-Tv.x + pyf * Tw.x, -Tv.y + pyf * Tw.y, -Tv.z + pyf * Tw.z);
-  }
-  f.p = cross3(f.k, f.l);
-  f.sx = f.p.x / f.p.z;
-  f.sy = f.p.y / f.p.z;
-  f.rho3d = f.sx * f.sx + f.sy * f.sy;
-  f.dx = cx - pxf;
-  f.dy = cy - pyf;
-  // Both variants scale by 2: the part variant's double constant
-  // 1/(0.7071067811865476^2) times a float rounds to exactly 2x.
-  f.rho2d = kFilterInvSquareP0 * (f.dx * f.dx + f.dy * f.dy);
-  f.use3d = f.rho3d <= f.rho2d;
-  f.rho = fminf(f.rho3d, f.rho2d);
-  f.depth = f.use3d ? (f.sx * Tw.x + f.sy * Tw.y) + Tw.z : Tw.z;
-}
-
 // Mapped depth of the part variant, (far d - far near) / ((far - near) d)
 // (P1/cr/forward.cu:415).  The reference evaluates it in double (its macros
 // are double); here it is fp32 with the constants rounded once.  It feeds
