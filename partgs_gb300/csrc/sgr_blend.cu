@@ -22,7 +22,9 @@
 // fragment whose splat and filter distances both exceed the reach threshold
 // is rejected before the reciprocal and the exponential.  The splat-plane
 // coordinates take one reciprocal and two products instead of the
-// reference's two divisions (splat_coords).
+// reference's two divisions (splat_coords), and the exponential and the
+// backward's reciprocals are the hardware's approximate ones (splat_exp,
+// blend_rcp): a few 1e-7 relative on alpha, far inside the tolerances.
 #include "sgr_kernels.cuh"
 
 namespace sgr {
@@ -116,14 +118,22 @@ __device__ __forceinline__ bool row_reaches(const V3& Tu, const V3& Tv, const V3
 #endif
 
 // SGR_FAST_EXP 1: the splat weight exp(power) by the hardware's base-2
-// exponential (__expf) instead of expf.  SGR_FAST_RCP 1: the backward's
-// reciprocals of 1 - alpha and of the depth, and the forward's of the depth,
-// by the approximate reciprocal instead of the correctly rounded one.
+// exponential (__expf, within 2 + 1.2 |power| ulp: at most 8 ulp, 5e-7
+// relative, over the powers that pass the alpha cut-off) instead of expf.
+// SGR_FAST_RCP 1: the backward's reciprocals of 1 - alpha (transmittance
+// recovery) and of the depth, and the forward's of the depth, by the
+// approximate reciprocal (2 ulp) instead of the correctly rounded one.  Both
+// blends use the same forms, so their decisions agree bit for bit; the
+// parity tests (images 1e-5, gradients 1e-4 relative, contributor counts
+// exact) pass at the full bench size with both on.  Measured on the
+// 500k-surfel 16-view 800x600 step (with SGR_SPLAT_DIV 2): forward 10.61 ->
+// 10.16 ms, backward 24.76 -> 22.54 ms with both (the correctly rounded
+// reciprocal of 1 - alpha was most of it).
 #ifndef SGR_FAST_EXP
-#define SGR_FAST_EXP 0
+#define SGR_FAST_EXP 1
 #endif
 #ifndef SGR_FAST_RCP
-#define SGR_FAST_RCP 0
+#define SGR_FAST_RCP 1
 #endif
 
 __device__ __forceinline__ float splat_exp(float power) {

@@ -18,8 +18,9 @@
 // margin that covers the fp32 rounding of the cell assignment, the cell
 // faces and the squared distances.  Queries still open after a number of
 // shells that grows with the cube root of the reference count (far from
-// every reference point, in a sparse region) are listed and finished by the
-// brute-force scan.
+// every reference point, in a sparse region) are listed and searched the
+// same way in a second grid of cells four times wider; what that leaves
+// open is finished by the brute-force scan.
 //
 // Radius downsample (sgr_radius_downsample): the reference keeps point i of
 // its shuffled order unless an earlier kept point lies within the radius
@@ -185,16 +186,18 @@ __device__ __forceinline__ float outside_bound2(float px, float py, float pz, in
   return b2;
 }
 
-// One thread per query, in cell order.  A cell is searched unless its box
+// One thread per query, in cell order (order[0 .. n), or order[0 .. *n_in)
+// for the queries the finer level left open).  A cell is searched unless its box
 // lies farther than the best distance so far; the shell loop ends when the
 // best squared distance is below the bound of everything outside, with a
 // relative 2e-6 kept for the rounding of the squared distances, so no
 // unsearched point can have a smaller (or equal) computed squared distance.
 __global__ void __launch_bounds__(256) k_nn_grid(const float* __restrict__ q, const int* __restrict__ order,
-                                                 long long n, NNGrid g, const uint32_t* __restrict__ start,
-                                                 const float4* __restrict__ pts, float* __restrict__ dist,
-                                                 int* __restrict__ idx, int* __restrict__ open,
-                                                 unsigned* __restrict__ n_open) {
+                                                 long long n, const unsigned* __restrict__ n_in, NNGrid g,
+                                                 const uint32_t* __restrict__ start, const float4* __restrict__ pts,
+                                                 float* __restrict__ dist, int* __restrict__ idx,
+                                                 int* __restrict__ open, unsigned* __restrict__ n_open) {
+  if (n_in) n = (long long)*n_in;   // the previous level's open queries
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n) return;
   const int qi = order[t];
@@ -246,12 +249,14 @@ __global__ void __launch_bounds__(256) k_nn_grid(const float* __restrict__ q, co
 }
 
 struct NNLayout {
-  size_t start, cursor, pts, keys, keys_sorted, ids, ids_sorted, open, n_open, temp, temp_bytes, end;
+  size_t start, cursor, pts, start2, cursor2, pts2, keys, keys_sorted, ids, ids_sorted, open, n_open, open2, n_open2,
+      temp, temp_bytes, end;
 };
 
-// Grid shape for m reference points in the box [lo, hi]: about two cells
-// per point, at most 1024 cells on an axis, found by bisection on the edge.
-bool nn_grid(int64_t m, const float* lo, const float* hi, NNGrid& g) {
+// Grid shape for m reference points in the box [lo, hi]: about
+// `per_point` cells per point, at most 1024 cells on an axis, found by
+// bisection on the edge.
+bool nn_grid(int64_t m, const float* lo, const float* hi, NNGrid& g, double per_point) {
   double ext[3], maxext = 0.0, maxabs = 0.0;
   for (int a = 0; a < 3; ++a) {
     if (!(hi[a] >= lo[a]) || !isfinite(lo[a]) || !isfinite(hi[a])) return false;
@@ -259,7 +264,7 @@ bool nn_grid(int64_t m, const float* lo, const float* hi, NNGrid& g) {
     maxext = fmax(maxext, ext[a]);
     maxabs = fmax(maxabs, fmax(fabs((double)lo[a]), fabs((double)hi[a])));
   }
-  const double target = fmin(fmax(2.0 * (double)m, 1.0), (double)(1 << 26));
+  const double target = fmin(fmax(per_point * (double)m, 1.0), (double)(1 << 26));
   auto cells = [&](double h) {
     double c = 1.0;
     for (int a = 0; a < 3; ++a) c *= fmax(1.0, ceil(ext[a] / h));
@@ -298,21 +303,31 @@ bool nn_grid(int64_t m, const float* lo, const float* hi, NNGrid& g) {
   return true;
 }
 
-NNLayout nn_layout(long long n, long long m, long long cells) {
+// The fine level (two cells per point) and the coarse one (edge about four
+// times longer) that takes the queries the fine level leaves open.
+constexpr double kFinePerPoint = 2.0, kCoarsePerPoint = 2.0 / 64.0;
+
+NNLayout nn_layout(long long n, long long m, long long cells, long long cells2) {
   auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
   NNLayout L;
   size_t o = 0;
   L.start = o; o = al(o + (cells + 1) * 4);
   L.cursor = o; o = al(o + cells * 4);
   L.pts = o; o = al(o + m * 16);
+  L.start2 = o; o = al(o + (cells2 + 1) * 4);
+  L.cursor2 = o; o = al(o + cells2 * 4);
+  L.pts2 = o; o = al(o + m * 16);
   L.keys = o; o = al(o + n * 4);
   L.keys_sorted = o; o = al(o + n * 4);
   L.ids = o; o = al(o + n * 4);
   L.ids_sorted = o; o = al(o + n * 4);
   L.open = o; o = al(o + n * 4);
   L.n_open = o; o = al(o + 4);
+  L.open2 = o; o = al(o + n * 4);
+  L.n_open2 = o; o = al(o + 4);
   size_t ts = 0, tr = 0;
-  cub::DeviceScan::ExclusiveSum(nullptr, ts, (uint32_t*)nullptr, (uint32_t*)nullptr, (int64_t)(cells + 1));
+  cub::DeviceScan::ExclusiveSum(nullptr, ts, (uint32_t*)nullptr, (uint32_t*)nullptr,
+                                (int64_t)((cells > cells2 ? cells : cells2) + 1));
   cub::DeviceRadixSort::SortPairs(nullptr, tr, (const uint32_t*)nullptr, (uint32_t*)nullptr, (const int*)nullptr,
                                   (int*)nullptr, (int64_t)n, 0, 32);
   L.temp = o;
@@ -456,9 +471,11 @@ int sgr_nn_search(const float* q, int64_t n, const float* r, int64_t m, float* d
 }
 
 size_t sgr_nn_grid_scratch_bytes(int64_t n, int64_t m, const float* lo, const float* hi) {
-  NNGrid g;
-  if (n < 0 || m < 0 || !lo || !hi || !nn_grid(m, lo, hi, g)) return 0;
-  return nn_layout(n, m, (long long)g.nx * g.ny * g.nz).end;
+  NNGrid g, g2;
+  if (n < 0 || m < 0 || !lo || !hi || !nn_grid(m, lo, hi, g, kFinePerPoint) ||
+      !nn_grid(m, lo, hi, g2, kCoarsePerPoint))
+    return 0;
+  return nn_layout(n, m, (long long)g.nx * g.ny * g.nz, (long long)g2.nx * g2.ny * g2.nz).end;
 }
 
 int sgr_nn_search_grid(const float* q, int64_t n, const float* r, int64_t m, const float* lo, const float* hi,
@@ -468,10 +485,11 @@ int sgr_nn_search_grid(const float* q, int64_t n, const float* r, int64_t m, con
   if (m > 0x7fffffffLL || n > 0x7fffffffLL) return SGR_ERR_UNSUPPORTED;
   if (n == 0) return SGR_OK;
   if (m == 0) return SGR_ERR_INVALID_ARGUMENT;
-  NNGrid g;
-  if (!nn_grid(m, lo, hi, g)) return SGR_ERR_INVALID_ARGUMENT;
-  const long long cells = (long long)g.nx * g.ny * g.nz;
-  const NNLayout L = nn_layout(n, m, cells);
+  NNGrid g, g2;
+  if (!nn_grid(m, lo, hi, g, kFinePerPoint) || !nn_grid(m, lo, hi, g2, kCoarsePerPoint))
+    return SGR_ERR_INVALID_ARGUMENT;
+  const long long cells = (long long)g.nx * g.ny * g.nz, cells2 = (long long)g2.nx * g2.ny * g2.nz;
+  const NNLayout L = nn_layout(n, m, cells, cells2);
   if (!scratch || scratch_bytes < L.end) return SGR_ERR_WORKSPACE;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   char* sp = static_cast<char*>(scratch);
@@ -484,25 +502,39 @@ int sgr_nn_search_grid(const float* q, int64_t n, const float* r, int64_t m, con
   auto* ids_sorted = reinterpret_cast<int*>(sp + L.ids_sorted);
   auto* open = reinterpret_cast<int*>(sp + L.open);
   auto* n_open = reinterpret_cast<unsigned*>(sp + L.n_open);
+  auto* start2 = reinterpret_cast<uint32_t*>(sp + L.start2);
+  auto* cursor2 = reinterpret_cast<uint32_t*>(sp + L.cursor2);
+  auto* pts2 = reinterpret_cast<float4*>(sp + L.pts2);
+  auto* open2 = reinterpret_cast<int*>(sp + L.open2);
+  auto* n_open2 = reinterpret_cast<unsigned*>(sp + L.n_open2);
   const unsigned mb = (unsigned)((m + 255) / 256), nb = (unsigned)((n + 255) / 256);
   if (cudaMemsetAsync(start, 0, (cells + 1) * 4, st) != cudaSuccess ||
-      cudaMemsetAsync(cursor, 0, cells * 4, st) != cudaSuccess || cudaMemsetAsync(n_open, 0, 4, st) != cudaSuccess)
+      cudaMemsetAsync(cursor, 0, cells * 4, st) != cudaSuccess || cudaMemsetAsync(n_open, 0, 4, st) != cudaSuccess ||
+      cudaMemsetAsync(start2, 0, (cells2 + 1) * 4, st) != cudaSuccess ||
+      cudaMemsetAsync(cursor2, 0, cells2 * 4, st) != cudaSuccess || cudaMemsetAsync(n_open2, 0, 4, st) != cudaSuccess)
     return SGR_ERR_CUDA;
-  k_grid_count<<<mb, 256, 0, st>>>(r, m, g, start);
-  size_t tb = L.temp_bytes;
-  if (cub::DeviceScan::ExclusiveSum(sp + L.temp, tb, start, start, (int64_t)(cells + 1), st) != cudaSuccess)
-    return SGR_ERR_CUDA;
-  k_grid_scatter<<<mb, 256, 0, st>>>(r, m, g, start, cursor, pts);
+  size_t tb;
+  for (int level = 0; level < 2; ++level) {   // both grids: count, scan, scatter
+    const NNGrid& gl = level ? g2 : g;
+    uint32_t* sl = level ? start2 : start;
+    k_grid_count<<<mb, 256, 0, st>>>(r, m, gl, sl);
+    tb = L.temp_bytes;
+    if (cub::DeviceScan::ExclusiveSum(sp + L.temp, tb, sl, sl, (int64_t)((level ? cells2 : cells) + 1), st) !=
+        cudaSuccess)
+      return SGR_ERR_CUDA;
+    k_grid_scatter<<<mb, 256, 0, st>>>(r, m, gl, sl, level ? cursor2 : cursor, level ? pts2 : pts);
+  }
   k_query_cells<<<nb, 256, 0, st>>>(q, n, g, keys, ids);
   tb = L.temp_bytes;
   if (cub::DeviceRadixSort::SortPairs(sp + L.temp, tb, keys, keys_sorted, ids, ids_sorted, (int64_t)n, 0,
                                       key_bits(cells), st) != cudaSuccess)
     return SGR_ERR_CUDA;
-  k_nn_grid<<<nb, 256, 0, st>>>(q, ids_sorted, n, g, start, pts, dist, idx, open, n_open);
+  k_nn_grid<<<nb, 256, 0, st>>>(q, ids_sorted, n, nullptr, g, start, pts, dist, idx, open, n_open);
   // the open queries (count known only on the device): blocks past it return at once
+  k_nn_grid<<<nb, 256, 0, st>>>(q, open, n, n_open, g2, start2, pts2, dist, idx, open2, n_open2);
   const long long blocks = (n + (long long)kNNThreads * kNNQ - 1) / ((long long)kNNThreads * kNNQ);
-  k_nn<<<(unsigned)blocks, kNNThreads, 0, st>>>(q, n, r, m, dist, idx, open, n_open);
-  sgr::count_launches(5);
+  k_nn<<<(unsigned)blocks, kNNThreads, 0, st>>>(q, n, r, m, dist, idx, open2, n_open2);
+  sgr::count_launches(8);
   return cudaGetLastError() == cudaSuccess ? SGR_OK : SGR_ERR_CUDA;
 }
 
