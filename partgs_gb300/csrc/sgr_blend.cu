@@ -121,8 +121,9 @@ __device__ __forceinline__ bool row_reaches(const V3& Tu, const V3& Tv, const V3
 // exponential (__expf, within 2 + 1.2 |power| ulp: at most 8 ulp, 5e-7
 // relative, over the powers that pass the alpha cut-off) instead of expf.
 // SGR_FAST_RCP 1: the backward's reciprocals of 1 - alpha (transmittance
-// recovery) and of the depth, and the forward's of the depth, by the
-// approximate reciprocal (2 ulp) instead of the correctly rounded one.  Both
+// recovery) and of the depth, and the forward's of the depth (distortion
+// terms), by the approximate reciprocal (2 ulp) instead of the correctly
+// rounded one.  Both
 // blends use the same forms, so their decisions agree bit for bit; the
 // parity tests (images 1e-5, gradients 1e-4 relative, contributor counts
 // exact) pass at the full bench size with both on.  Measured on the
@@ -399,7 +400,7 @@ __device__ __forceinline__ void fwd_fragment(FwdPixel<VARIANT>& q, const float4 
     q.C[1] += r4.y * w;
     q.C[2] += r4.z * w;
   } else {
-    const float m = mapped_depth_p1(depth);
+    const float m = mapped_depth_p1(blend_rcp(depth));
     const float err = m * m * A + q.M2 - 2 * m * q.M1;
     q.dist += err * alpha * q.T;
     if (q.T > 0.5f) {
@@ -688,8 +689,8 @@ __device__ __forceinline__ void bwd_update(BwdPixel<VARIANT>& q, const BwdGeom& 
     m_d = kFarP0 / (kFarP0 - kNearP0) * (1 - kNearP0 * inv_d);
     dmd_dd = (kFarP0 * kNearP0) / (kFarP0 - kNearP0) * (inv_d * inv_d);
   } else {
-    m_d = mapped_depth_p1(c_d);
     const float inv_d = blend_rcp(c_d);
+    m_d = mapped_depth_p1(inv_d);
     dmd_dd = kDmdP1f * (inv_d * inv_d);
   }
   if (pos == q.median_contributor - 1) {

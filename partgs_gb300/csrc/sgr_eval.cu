@@ -16,11 +16,12 @@
 // so far, and stops once the best squared distance is below the squared
 // distance to every cell outside the searched cube.  The bounds carry a
 // margin that covers the fp32 rounding of the cell assignment, the cell
-// faces and the squared distances.  Queries still open after a number of
-// shells that grows with the cube root of the reference count (far from
-// every reference point, in a sparse region) are listed and searched the
-// same way in a second grid of cells four times wider; what that leaves
-// open is finished by the brute-force scan.
+// faces and the squared distances.  Slabs and rows of cells beyond the best
+// distance are skipped whole.  Queries still open after 6 shells (far from
+// every reference point: in an empty region or outside the points' box) are
+// listed and searched the same way in a second grid of cells eight times
+// wider, up to 64 shells; the rare query that leaves open is finished by the
+// brute-force scan.
 //
 // Radius downsample (sgr_radius_downsample): the reference keeps point i of
 // its shuffled order unless an earlier kept point lies within the radius
@@ -207,22 +208,26 @@ __global__ void __launch_bounds__(256) k_nn_grid(const float* __restrict__ q, co
   float best = FLT_MAX;
   int arg = INT_MAX;
   bool done = false;
+  // true when every point of a box at squared gap g2 is farther than best
+  auto beyond = [&](float g2) {
+    const float gap = fmaxf(0.0f, sqrtf(g2) - g.margin);
+    return gap * gap * (1.0f - 2e-6f) > best;
+  };
   for (int k = 0; k <= g.shells && !done; ++k) {
-    for (int dz = -k; dz <= k; ++dz) {
+    for (int dz = max(-k, -cz); dz <= min(k, g.nz - 1 - cz); ++dz) {
       const int z = cz + dz;
-      if (z < 0 || z >= g.nz) continue;
       const float gz = slab_gap(pz, z, g.loz, g.h);
-      for (int dy = -k; dy <= k; ++dy) {
+      if (beyond(gz * gz)) continue;                 // the whole slab
+      for (int dy = max(-k, -cy); dy <= min(k, g.ny - 1 - cy); ++dy) {
         const int y = cy + dy;
-        if (y < 0 || y >= g.ny) continue;
         const float gy = slab_gap(py, y, g.loy, g.h);
+        if (beyond(gy * gy + gz * gz)) continue;     // the whole row
         const int step = (dz == -k || dz == k || dy == -k || dy == k) ? 1 : 2 * k;   // k = 0 takes the first
         for (int dx = -k; dx <= k; dx += step) {
           const int x = cx + dx;
           if (x < 0 || x >= g.nx) continue;
           const float gx = slab_gap(px, x, g.lox, g.h);
-          const float gap = fmaxf(0.0f, sqrtf(gx * gx + gy * gy + gz * gz) - g.margin);
-          if (gap * gap * (1.0f - 2e-6f) > best) continue;
+          if (beyond(gx * gx + gy * gy + gz * gz)) continue;
           const long long c = ((long long)z * g.ny + y) * g.nx + x;
           const uint32_t e = start[c + 1];
           for (uint32_t j = start[c]; j < e; ++j) {
@@ -256,7 +261,7 @@ struct NNLayout {
 // Grid shape for m reference points in the box [lo, hi]: about
 // `per_point` cells per point, at most 1024 cells on an axis, found by
 // bisection on the edge.
-bool nn_grid(int64_t m, const float* lo, const float* hi, NNGrid& g, double per_point) {
+bool nn_grid(int64_t m, const float* lo, const float* hi, NNGrid& g, double per_point, int shells) {
   double ext[3], maxext = 0.0, maxabs = 0.0;
   for (int a = 0; a < 3; ++a) {
     if (!(hi[a] >= lo[a]) || !isfinite(lo[a]) || !isfinite(hi[a])) return false;
@@ -297,15 +302,16 @@ bool nn_grid(int64_t m, const float* lo, const float* hi, NNGrid& g, double per_
   g.hiy = hi[1];
   g.hiz = hi[2];
   g.margin = (float)(1e-3 * h + 1e-6 * maxabs);
-  // A shell of radius k costs about 24 k^2 cell tests, the brute-force scan
-  // m distances: cap the shells where their total nears a tenth of m.
-  g.shells = (int)fmin(64.0, fmax(4.0, 0.5 * cbrt(0.1 * (double)m)));
+  g.shells = shells;
   return true;
 }
 
-// The fine level (two cells per point) and the coarse one (edge about four
-// times longer) that takes the queries the fine level leaves open.
-constexpr double kFinePerPoint = 2.0, kCoarsePerPoint = 2.0 / 64.0;
+// The fine level (two cells per point, 6 shells) and the coarse one (edge
+// about eight times longer, shells until the cube holds the grid, up to 64)
+// that takes the queries the fine level leaves open: queries in empty
+// regions, and far outside the points' box.
+constexpr double kFinePerPoint = 2.0, kCoarsePerPoint = 2.0 / 512.0;
+constexpr int kFineShells = 6, kCoarseShells = 64;
 
 NNLayout nn_layout(long long n, long long m, long long cells, long long cells2) {
   auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
@@ -472,8 +478,8 @@ int sgr_nn_search(const float* q, int64_t n, const float* r, int64_t m, float* d
 
 size_t sgr_nn_grid_scratch_bytes(int64_t n, int64_t m, const float* lo, const float* hi) {
   NNGrid g, g2;
-  if (n < 0 || m < 0 || !lo || !hi || !nn_grid(m, lo, hi, g, kFinePerPoint) ||
-      !nn_grid(m, lo, hi, g2, kCoarsePerPoint))
+  if (n < 0 || m < 0 || !lo || !hi || !nn_grid(m, lo, hi, g, kFinePerPoint, kFineShells) ||
+      !nn_grid(m, lo, hi, g2, kCoarsePerPoint, kCoarseShells))
     return 0;
   return nn_layout(n, m, (long long)g.nx * g.ny * g.nz, (long long)g2.nx * g2.ny * g2.nz).end;
 }
@@ -486,7 +492,7 @@ int sgr_nn_search_grid(const float* q, int64_t n, const float* r, int64_t m, con
   if (n == 0) return SGR_OK;
   if (m == 0) return SGR_ERR_INVALID_ARGUMENT;
   NNGrid g, g2;
-  if (!nn_grid(m, lo, hi, g, kFinePerPoint) || !nn_grid(m, lo, hi, g2, kCoarsePerPoint))
+  if (!nn_grid(m, lo, hi, g, kFinePerPoint, kFineShells) || !nn_grid(m, lo, hi, g2, kCoarsePerPoint, kCoarseShells))
     return SGR_ERR_INVALID_ARGUMENT;
   const long long cells = (long long)g.nx * g.ny * g.nz, cells2 = (long long)g2.nx * g2.ny * g2.nz;
   const NNLayout L = nn_layout(n, m, cells, cells2);

@@ -33,18 +33,16 @@ struct GeomView {
 };
 
 // Mapped depth of the part variant, (far d - far near) / ((far - near) d)
-// (P1/cr/forward.cu:415).  The reference evaluates it in double (its macros
-// are double); here it is fp32 with the constants rounded once.  It feeds
-// only the distortion and depth terms, never a decision, and differs from
-// the double result by a few fp32 ulps.  (A double division per fragment
-// costs more than the rest of the fragment on this GPU.)
-constexpr float kFarP1f = (float)kFarP1;
-constexpr float kFarNearP1f = (float)(kFarP1 * kNearP1);
-constexpr float kRangeP1f = (float)(kFarP1 - kNearP1);
+// (P1/cr/forward.cu:415), written as kMdP1 - kDmdP1f / d so that the blends
+// need only a reciprocal of the depth.  The reference evaluates it in double
+// (its macros are double); here it is fp32 with the constants rounded once.
+// It feeds only the distortion and depth terms, never a decision, and
+// differs from the double result by a few fp32 ulps of its constant term.
+// (A double division per fragment costs more than the rest of the fragment
+// on this GPU.)
+constexpr float kMdP1 = (float)(kFarP1 / (kFarP1 - kNearP1));
 constexpr float kDmdP1f = (float)((kFarP1 * kNearP1) / (kFarP1 - kNearP1));   // d m / d depth = this / depth^2
-__device__ __forceinline__ float mapped_depth_p1(float depth) {
-  return (kFarP1f * depth - kFarNearP1f) / (kRangeP1f * depth);
-}
+__device__ __forceinline__ float mapped_depth_p1(float inv_depth) { return kMdP1 - kDmdP1f * inv_depth; }
 
 // View-dependent colour from degree <= 3 SH (P0/cr/forward.cu:20-71).
 __device__ __forceinline__ V3 sh_to_rgb(int deg, const float* sh, V3 pos, V3 campos, uint32_t& clamped) {
