@@ -597,6 +597,15 @@ __global__ void __launch_bounds__(FwdShape::NT, (VARIANT == SGR_VARIANT_PLAIN) ?
 // ---------------------------------------------------------------------------
 static_assert(kGradUsed == 18, "warp_sum18 reduces the 18 gradient values of a fragment");
 
+// SGR_BWD_DOT_REC 1: the backward's colour and normal recurrences
+// (accum_rec, accum_normal: P0/cr/backward.cu:365-395) run on their dot
+// products with dL/dpixel and dL/dnormal instead of per channel.  The
+// recurrences are linear, so the alpha gradient is the same sum; it saves
+// four channels' worth of registers and instructions per pixel.
+#ifndef SGR_BWD_DOT_REC
+#define SGR_BWD_DOT_REC 1
+#endif
+
 // Per-pixel state of the backward recurrences (P0/cr/backward.cu:160-260).
 template <int VARIANT>
 struct BwdPixel {
@@ -606,7 +615,13 @@ struct BwdPixel {
   int last_contributor, median_contributor;
   float dL_dpixel[3], dL_dnormal2D[3];
   float dL_ddepth, dL_daccum, dL_dreg, dL_dmedian, dL_dmaxw;
+#if SGR_BWD_DOT_REC
+  // the colour and normal recurrences kept as their dot products with the
+  // pixel's upstream gradient, the only way the alpha gradient uses them
+  float rec_dot, last_col_dot, nrm_dot, last_nrm_dot;
+#else
   float accum_rec[3], last_color[3], last_normal[3], accum_normal[3];
+#endif
   float last_alpha, last_depth, accum_depth, accum_alpha, last_dL_dT;
   float sem_w;   // part variant: alpha T of the pixel's fragment of the current entry
 };
@@ -672,6 +687,16 @@ __device__ __forceinline__ void bwd_update(BwdPixel<VARIANT>& q, const BwdGeom& 
   const float wgt = alpha * q.T;
   float dL_dalpha = 0.0f;
   const float col[3] = {r4.x, r4.y, r4.z};
+#if SGR_BWD_DOT_REC
+  {
+    const float cd = col[0] * q.dL_dpixel[0] + col[1] * q.dL_dpixel[1] + col[2] * q.dL_dpixel[2];
+    q.rec_dot = q.last_alpha * q.last_col_dot + (1.f - q.last_alpha) * q.rec_dot;
+    q.last_col_dot = cd;
+    dL_dalpha += cd - q.rec_dot;
+  }
+#pragma unroll
+  for (int ch = 0; ch < 3; ++ch) gv[14 + ch] += wgt * q.dL_dpixel[ch];
+#else
 #pragma unroll
   for (int ch = 0; ch < 3; ++ch) {
     q.accum_rec[ch] = q.last_alpha * q.last_color[ch] + (1.f - q.last_alpha) * q.accum_rec[ch];
@@ -679,6 +704,7 @@ __device__ __forceinline__ void bwd_update(BwdPixel<VARIANT>& q, const BwdGeom& 
     dL_dalpha += (col[ch] - q.accum_rec[ch]) * q.dL_dpixel[ch];
     gv[14 + ch] += wgt * q.dL_dpixel[ch];
   }
+#endif
   // The reference's semantic recurrence (accumulated and last semantics,
   // P1/cr/backward.cu:358-368) feeds only an alpha-gradient term that it
   // leaves commented out (:365), so it is not computed here.
@@ -710,6 +736,16 @@ __device__ __forceinline__ void bwd_update(BwdPixel<VARIANT>& q, const BwdGeom& 
   q.accum_alpha = __fadd_rn(q.last_alpha, __fmul_rn(1.f - q.last_alpha, q.accum_alpha));
   dL_dalpha += (1 - q.accum_alpha) * q.dL_daccum;
   const float nrm[3] = {r3.x, r3.y, r3.z};
+#if SGR_BWD_DOT_REC
+  {
+    const float nd = nrm[0] * q.dL_dnormal2D[0] + nrm[1] * q.dL_dnormal2D[1] + nrm[2] * q.dL_dnormal2D[2];
+    q.nrm_dot = q.last_alpha * q.last_nrm_dot + (1.f - q.last_alpha) * q.nrm_dot;
+    q.last_nrm_dot = nd;
+    dL_dalpha += nd - q.nrm_dot;
+  }
+#pragma unroll
+  for (int ch = 0; ch < 3; ++ch) gv[11 + ch] += alpha * q.T * q.dL_dnormal2D[ch];
+#else
 #pragma unroll
   for (int ch = 0; ch < 3; ++ch) {
     q.accum_normal[ch] = q.last_alpha * q.last_normal[ch] + (1.f - q.last_alpha) * q.accum_normal[ch];
@@ -717,6 +753,7 @@ __device__ __forceinline__ void bwd_update(BwdPixel<VARIANT>& q, const BwdGeom& 
     dL_dalpha += (nrm[ch] - q.accum_normal[ch]) * q.dL_dnormal2D[ch];
     gv[11 + ch] += alpha * q.T * q.dL_dnormal2D[ch];
   }
+#endif
   dL_dalpha *= q.T;
   q.last_alpha = alpha;
   dL_dalpha += (-q.T_final * inv_1ma) * q.bg_dot;
@@ -814,7 +851,9 @@ __global__ void __launch_bounds__(BwdShape<VARIANT>::NT,
     for (int c = 0; c < 3; ++c) {
       Q.dL_dpixel[c] = inside ? dpix[pix + c * HW] : 0.f;
       Q.dL_dnormal2D[c] = inside ? doth[pix + (2 + c) * HW] : 0.f;
+#if !SGR_BWD_DOT_REC
       Q.accum_rec[c] = Q.last_color[c] = Q.last_normal[c] = Q.accum_normal[c] = 0.f;
+#endif
     }
     Q.dL_ddepth = inside ? doth[pix] : 0.f;
     Q.dL_daccum = inside ? doth[pix + HW] : 0.f;
@@ -831,6 +870,9 @@ __global__ void __launch_bounds__(BwdShape<VARIANT>::NT,
     Q.final_A = 1 - Q.T_final;
     Q.bg_dot = bg[0] * Q.dL_dpixel[0] + bg[1] * Q.dL_dpixel[1] + bg[2] * Q.dL_dpixel[2];
     Q.last_alpha = Q.last_depth = Q.accum_depth = Q.accum_alpha = Q.last_dL_dT = 0.f;
+#if SGR_BWD_DOT_REC
+    Q.rec_dot = Q.last_col_dot = Q.nrm_dot = Q.last_nrm_dot = 0.f;
+#endif
     thread_max = max(thread_max, Q.last_contributor);
   }
 
