@@ -7,6 +7,8 @@ first argument, default /root/reference).  It imports, unmodified:
 * utils/graphics_utils.py      getWorld2View2, getProjectionMatrix (camera matrices)
 * utils/general_utils.py       rot_to_quat_batch (rotation matrix -> quaternion)
 * utils/point_utils.py         depth_to_normal (normals from a depth map)
+* utils/loss_utils.py          l1_loss, ssim: the photometric term of train.py:230-231, per view,
+                               differentiated by autograd (point_loss.npz)
 * games/block_mesh_splatting/scene/block_gaussian_model.py
                                update_alpha / get_verts / prepare_scaling_rot / get_opacity
                                (the superquadric -> surfel binding), differentiated by autograd;
@@ -396,6 +398,43 @@ def densify(ref_root):
     print("wrote", os.path.join(HERE, "densify.npz"), P, "->", out["out_xyz"].shape[0])
 
 
+def point_loss(ref_root):
+    """The reference's photometric loss, (1 - lambda_dssim) L1 + lambda_dssim
+    (1 - SSIM) (train.py:230-231, utils/loss_utils.py:6-7, 24-54), evaluated
+    one view at a time as its training loop does, in float64, with the
+    gradient w.r.t. the rendered image from autograd."""
+    from utils.loss_utils import l1_loss, ssim
+    g = torch.Generator().manual_seed(11)
+    V, H, W, lam = 2, 24, 40, 0.2
+    yy, xx = torch.meshgrid(torch.linspace(0, 1, H, dtype=torch.float64),
+                            torch.linspace(0, 1, W, dtype=torch.float64), indexing="ij")
+    base = 0.5 + 0.4 * torch.sin(7 * xx + 3 * yy)[None, None] * torch.rand(V, 3, 1, 1, generator=g, dtype=torch.float64)
+    target = (base + 0.05 * torch.rand(V, 3, H, W, generator=g, dtype=torch.float64)).clamp(0, 1)
+    image = (target + 0.1 * torch.randn(V, 3, H, W, generator=g, dtype=torch.float64)).clamp(0, 1)
+    out = dict(image=image.numpy(), target=target.numpy(), lambda_dssim=np.float64(lam))
+    l1s, ssims, losses, grads = [], [], [], []
+    for v in range(V):
+        img = image[v].clone().requires_grad_(True)
+        l1 = l1_loss(img, target[v])
+        s = ssim(img, target[v])
+        loss = (1.0 - lam) * l1 + lam * (1.0 - s)
+        loss.backward()
+        l1s.append(float(l1.detach()))
+        ssims.append(float(s.detach()))
+        losses.append(float(loss.detach()))
+        grads.append(img.grad.numpy())
+    out.update(l1=np.array(l1s), ssim=np.array(ssims), loss=np.array(losses), grad=np.stack(grads))
+    np.savez_compressed(os.path.join(HERE, "point_loss.npz"), **out)
+    print("wrote", os.path.join(HERE, "point_loss.npz"), "ssim", ssims)
+
+
+def main_loss(ref_root="/root/reference"):
+    sys.path.insert(0, ref_root)
+    _stub_modules()
+    _cpu_only()
+    point_loss(ref_root)
+
+
 def main_sq(ref_root="/root/reference"):
     sys.path.insert(0, ref_root)
     _stub_modules()
@@ -418,7 +457,10 @@ if __name__ == "__main__":
         main_sq(root)
     elif "--densify" in sys.argv:   # only the densification fixture
         main_densify(root)
+    elif "--loss" in sys.argv:   # only the photometric-loss fixture
+        main_loss(root)
     else:
         main(root)
         main_sq(root)
         main_densify(root)
+        main_loss(root)
