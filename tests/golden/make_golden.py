@@ -9,6 +9,11 @@ first argument, default /root/reference).  It imports, unmodified:
 * utils/point_utils.py         depth_to_normal (normals from a depth map)
 * utils/loss_utils.py          l1_loss, ssim: the photometric term of train.py:230-231, per view,
                                differentiated by autograd (point_loss.npz)
+* renderer/gaussian_renderer/__init__.py
+                               render()'s post-processing of the rasteriser's maps (world normal,
+                               expected / median / surface depth, surface normal), with the
+                               rasteriser call answered by given maps; the point loss of
+                               train.py:230-249 on its outputs (render_post.npz)
 * games/block_mesh_splatting/scene/block_gaussian_model.py
                                update_alpha / get_verts / prepare_scaling_rot / get_opacity
                                (the superquadric -> surfel binding), differentiated by autograd;
@@ -428,11 +433,94 @@ def point_loss(ref_root):
     print("wrote", os.path.join(HERE, "point_loss.npz"), "ssim", ssims)
 
 
+def render_post(ref_root):
+    """The reference renderer's post-processing and the point loss on it.
+
+    render() (renderer/gaussian_renderer/__init__.py:9-141) runs unmodified;
+    its rasteriser (diff_surfel_rasterization) is replaced by a stand-in that
+    returns a given image and allmap, so what is exercised is the code after
+    the call (:111-141: normal view -> world, expected depth with
+    nan_to_num, median depth, surf_depth by depth_ratio, surf_normal from
+    utils/point_utils.py depth_to_normal times the detached alpha).  The
+    loss on its outputs is train.py:230-231 (photometric, through
+    utils/loss_utils.py) plus :244-249 (normal consistency and distortion,
+    both weights active), in the reference's float32, with autograd
+    gradients w.r.t. the image and the allmap.  Two views, two depth ratios."""
+    sys.path.insert(0, ROOT)
+    from partgs_gb300.cameras import orbit_cameras
+    slot = {}
+
+    class _Rasterizer:
+        def __init__(self, raster_settings):
+            self.raster_settings = raster_settings
+
+        def __call__(self, **kw):
+            return slot["image"], torch.zeros(kw["means3D"].shape[0], dtype=torch.int32), slot["allmap"]
+
+    stub = types.ModuleType("diff_surfel_rasterization")
+    stub.GaussianRasterizationSettings = lambda **kw: types.SimpleNamespace(**kw)
+    stub.GaussianRasterizer = _Rasterizer
+    sys.modules["diff_surfel_rasterization"] = stub
+    real_zeros_like = torch.zeros_like
+
+    def zeros_like(*a, **k):
+        k.pop("device", None)
+        return real_zeros_like(*a, **k)
+    torch.zeros_like = zeros_like
+    from renderer.gaussian_renderer import render
+    from utils.loss_utils import l1_loss, ssim
+
+    V, H, W, lam, lam_dist, lam_normal = 2, 24, 32, 0.2, 1000.0, 0.05
+    cams = orbit_cameras(V, 3.0, H, W, 55.0, seed=4)
+    g = torch.Generator().manual_seed(12)
+    yy, xx = torch.meshgrid(torch.linspace(-1, 1, H), torch.linspace(-1, 1, W), indexing="ij")
+    image = torch.rand(V, 3, H, W, generator=g)
+    target = torch.rand(V, 3, H, W, generator=g)
+    alpha = 0.2 + 0.8 * torch.rand(V, 1, H, W, generator=g)
+    median = 2.5 + 0.3 * torch.sin(3 * xx + 1) * torch.cos(2 * yy) + 0.01 * torch.rand(V, 1, H, W, generator=g)
+    expected = median * alpha * (1 + 0.05 * torch.rand(V, 1, H, W, generator=g))
+    normal = torch.nn.functional.normalize(torch.randn(V, 3, H, W, generator=g), dim=1) * alpha
+    dist = 1e-3 * torch.rand(V, 1, H, W, generator=g)
+    allmap = torch.cat([expected, alpha, normal, median, dist], 1)
+    pc = types.SimpleNamespace(get_xyz=torch.zeros(4, 3), get_opacity=torch.ones(4, 1),
+                               get_scaling=torch.ones(4, 2), get_rotation=torch.ones(4, 4),
+                               get_features=torch.zeros(4, 16, 3), active_sh_degree=3, max_sh_degree=3)
+    out = dict(image=image.numpy(), target=target.numpy(), allmap=allmap.numpy(),
+               lambdas=np.array([lam, lam_dist, lam_normal]))
+    for ratio in (1.0, 0.4):
+        pipe = types.SimpleNamespace(compute_cov3D_python=False, convert_SHs_python=False, depth_ratio=ratio,
+                                     debug=False)
+        tag = f"r{int(ratio * 10)}"
+        losses, g_img, g_map = [], [], []
+        for v, c in enumerate(cams):
+            cam = types.SimpleNamespace(FoVx=c.fovx, FoVy=c.fovy, image_height=H, image_width=W,
+                                        world_view_transform=torch.as_tensor(c.world_view_transform),
+                                        full_proj_transform=torch.as_tensor(c.full_proj_transform),
+                                        camera_center=torch.as_tensor(c.camera_center), znear=0.01, zfar=100.0)
+            img = image[v].clone().requires_grad_(True)
+            am = allmap[v].clone().requires_grad_(True)
+            slot.update(image=img, allmap=am)
+            pkg = render(cam, pc, pipe, torch.zeros(3))
+            loss = (1.0 - lam) * l1_loss(pkg["render"], target[v]) + lam * (1.0 - ssim(pkg["render"], target[v]))
+            normal_error = (1 - (pkg["rend_normal"] * pkg["surf_normal"]).sum(dim=0))[None]
+            loss = loss + lam_dist * pkg["rend_dist"].mean() + lam_normal * normal_error.mean()
+            loss.backward()
+            losses.append(float(loss.detach()))
+            g_img.append(img.grad.numpy())
+            g_map.append(am.grad.numpy())
+        out.update({f"{tag}_loss": np.array(losses), f"{tag}_grad_image": np.stack(g_img),
+                    f"{tag}_grad_allmap": np.stack(g_map)})
+    torch.zeros_like = real_zeros_like
+    np.savez_compressed(os.path.join(HERE, "render_post.npz"), **out)
+    print("wrote", os.path.join(HERE, "render_post.npz"), {k: v for k, v in out.items() if k.endswith("_loss")})
+
+
 def main_loss(ref_root="/root/reference"):
     sys.path.insert(0, ref_root)
     _stub_modules()
     _cpu_only()
     point_loss(ref_root)
+    render_post(ref_root)
 
 
 def main_sq(ref_root="/root/reference"):
