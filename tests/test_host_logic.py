@@ -66,3 +66,17 @@ def test_workloads_are_seeded_and_shaped():
     np.testing.assert_allclose(a.rotations.norm(dim=1).numpy(), 1.0, rtol=1e-6)
     s = superquadric_surfels(1000, 4, seed=1)
     assert s.P == 1000 and torch.isfinite(s.means3D).all()
+
+
+@pytest.mark.parametrize("mod", [dsr, dsrp])
+def test_host_tensors_are_rejected_before_any_device_work(sgr_lib, mod):
+    """Inputs in host memory raise ValueError in the host layer, before any
+    pointer reaches the library (a kernel given a host address would fault)."""
+    r = mod.GaussianRasterizer(_settings(mod))
+    x = torch.zeros(4, 3)
+    extra = {"semantics": torch.zeros(4, 2)} if mod is dsrp else {}
+    launches = sgr_lib.sgr_kernel_launches()
+    with pytest.raises(ValueError, match="must be CUDA tensors"):
+        r(means3D=x, means2D=x, opacities=torch.ones(4, 1), colors_precomp=x, scales=torch.ones(4, 2),
+          rotations=torch.ones(4, 4), **extra)
+    assert sgr_lib.sgr_kernel_launches() == launches
