@@ -139,3 +139,22 @@ def test_backward_matches_finite_differences(name, shape_idx):
         fd = fd[:, :9]
     err = np.abs(an - fd).max() / max(1e-9, np.abs(fd).max())
     assert err < 2e-4, (name, err)
+
+
+def test_scale_modifier_applies_to_the_plain_variant_only():
+    """The plain variant scales the tangent axes by scale_modifier
+    (P0/cr/forward.cu:75-115, scale_to_mat(scale, mod)); the part variant's
+    computeTransMat builds its scale matrix with 1.0 whatever the modifier
+    (P1/cr/forward.cu:95).  The oracle keeps both."""
+    cam = _camera()
+
+    def render(variant, mod):
+        s = _one_surfel()
+        s.scale_modifier = mod
+        return O.forward_view(s, cam, np.zeros(3), variant, np.float64)
+
+    part_a, part_b = render(O.PART, 0.5), render(O.PART, 1.0)
+    np.testing.assert_array_equal(part_a.color, part_b.color)
+    np.testing.assert_array_equal(part_a.others, part_b.others)
+    plain_a, plain_b = render(O.PLAIN, 0.5), render(O.PLAIN, 1.0)
+    assert (plain_a.others[1] > 0).sum() < (plain_b.others[1] > 0).sum()      # a smaller footprint
