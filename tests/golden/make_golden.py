@@ -16,7 +16,8 @@ first argument, default /root/reference).  It imports, unmodified:
                                train.py:230-249 on its outputs (render_post.npz)
 * games/block_mesh_splatting/scene/block_gaussian_model.py
                                update_alpha / get_verts / prepare_scaling_rot / get_opacity
-                               (the superquadric -> surfel binding), differentiated by autograd;
+                               (the superquadric -> surfel binding), differentiated by autograd,
+                               on a grid and on an icosphere (bind_icosphere.npz);
                                summarize_losses' ray and overlap terms (sq_losses.npz, with
                                scene/cameras.py cast_rays and utils/superquadric.py implicit_sq)
 
@@ -307,6 +308,106 @@ def main(ref_root="/root/reference"):
     print("wrote", os.path.join(HERE, "reference_python.npz"), sorted(out))
 
 
+def icosphere(level: int):
+    """Unit icosphere: the icosahedron (vertices the cyclic permutations of
+    (0, +-1, +-phi), faces the vertex triples at mutual edge length 2,
+    wound outward), each level splitting every triangle into four at its
+    normalised edge midpoints.  Level 2: 162 vertices, 320 faces, with
+    vertices at the poles (0, +-1, 0)."""
+    phi = (1.0 + 5.0 ** 0.5) / 2.0
+    v = []
+    for a in (-1.0, 1.0):
+        for b in (-phi, phi):
+            v += [(0.0, a, b), (a, b, 0.0), (b, 0.0, a)]
+    v = np.array(v)
+    faces = []
+    n = len(v)
+    for i in range(n):
+        for j in range(i + 1, n):
+            for k in range(j + 1, n):
+                d = [np.linalg.norm(v[i] - v[j]), np.linalg.norm(v[j] - v[k]), np.linalg.norm(v[i] - v[k])]
+                if np.allclose(d, 2.0):
+                    f = [i, j, k]
+                    if np.dot(np.cross(v[j] - v[i], v[k] - v[i]), v[i] + v[j] + v[k]) < 0:
+                        f = [i, k, j]
+                    faces.append(f)
+    verts = list(v / np.linalg.norm(v, axis=1, keepdims=True))
+    for _ in range(level):
+        mid, out = {}, []
+
+        def m(a, b):
+            key = (min(a, b), max(a, b))
+            if key not in mid:
+                c = verts[a] + verts[b]
+                verts.append(c / np.linalg.norm(c))
+                mid[key] = len(verts) - 1
+            return mid[key]
+        for a, b, c in faces:
+            ab, bc, ca = m(a, b), m(b, c), m(c, a)
+            out += [[a, ab, ca], [b, bc, ab], [c, ca, bc], [ab, bc, ca]]
+        faces = out
+    return np.array(verts), np.array(faces, dtype=np.int64)
+
+
+def bind_icosphere(bgm):
+    """tests/golden/bind_icosphere.npz: the binding on the block model's own
+    topology type, a level-2 icosphere (dataset_readers.py:130, with eta =
+    asin(y) and omega = atan2(x, z) as :141-142), poles included, 3 splats
+    per face, 2 blocks; prepare_scaling_rot and its autograd gradients in the
+    reference's float32."""
+    g = torch.Generator().manual_seed(21)
+    verts, faces = icosphere(2)
+    vt = torch.tensor(verts, dtype=torch.float32)
+    eta, omega = torch.asin(vt[:, 1].clamp(-1, 1)), torch.atan2(vt[:, 0], vt[:, 2])
+    B, N, Fn = 2, 3, faces.shape[0]
+    model = bgm.BlockGaussianModel.__new__(bgm.BlockGaussianModel)
+    model.scaling_activation = torch.exp
+    model.rotation_activation = torch.nn.functional.normalize
+    model.opacity_activation = torch.sigmoid
+    model.ratio_block_scene = 0.25
+    model.scale_block_min = 0.2
+    model.per_gs_num = Fn * N
+    sq_s = torch.log(torch.rand(B, 3, generator=g) * 1.6 + 0.2).requires_grad_(True)
+    sq_r = torch.randn(B, 4, generator=g).requires_grad_(True)
+    sq_t = (torch.rand(B, 3, generator=g) - 0.5).requires_grad_(True)
+    sq_eps = (torch.randn(B, 2, generator=g) * 0.8).requires_grad_(True)
+    sq_occ = torch.randn(B, 1, generator=g).requires_grad_(True)
+    model.sq_s, model.sq_r, model.sq_t, model.sq_eps, model.sq_occ = sq_s, sq_r, sq_t, sq_eps, sq_occ
+    model.sq_eta = eta.expand(B, -1).contiguous()
+    model.sq_omega = omega.expand(B, -1).contiguous()
+    model.faces = torch.tensor(faces).expand(B, -1, -1).contiguous()
+    model._alpha = torch.rand(B, Fn, N, 3, generator=g)
+    model._scale = torch.rand(B, Fn * N, 1, generator=g) * 0.5 + 0.5
+    model.update_alpha()
+    model.prepare_scaling_rot()
+    opac = model.get_opacity
+    ups = {k: torch.randn(t.shape, generator=g) for k, t in
+           dict(xyz=model._xyz, scaling=model._scaling, rotation=model._rotation, opacity=opac).items()}
+    loss = sum((t * ups[k]).sum() for k, t in
+               dict(xyz=model._xyz, scaling=model._scaling, rotation=model._rotation, opacity=opac).items())
+    loss.backward()
+    out = {}
+    for k, v in dict(sq_s=sq_s, sq_r=sq_r, sq_t=sq_t, sq_eps=sq_eps, sq_occ=sq_occ).items():
+        out[f"in_{k}"] = v.detach().numpy()
+        out[f"grad_{k}"] = v.grad.numpy()
+    out.update(in_eta=model.sq_eta.numpy(), in_omega=model.sq_omega.numpy(), in_faces=model.faces.numpy(),
+               in_alpha=model._alpha.numpy(), in_scale=model._scale.numpy(), out_xyz=model._xyz.detach().numpy(),
+               out_scaling=model._scaling.detach().numpy(), out_rotation=model._rotation.detach().numpy(),
+               out_opacity=opac.detach().numpy(), **{f"upstream_{k}": v.numpy() for k, v in ups.items()})
+    np.savez_compressed(os.path.join(HERE, "bind_icosphere.npz"), **out)
+    print("wrote", os.path.join(HERE, "bind_icosphere.npz"), "vertices", len(verts), "faces", Fn,
+          "poles", int((np.abs(verts[:, 1]) > 1 - 1e-12).sum()))
+
+
+def main_bind_ico(ref_root="/root/reference"):
+    sys.path.insert(0, ref_root)
+    _stub_modules()
+    _cpu_only()
+    torch.set_default_dtype(torch.float32)
+    import games.block_mesh_splatting.scene.block_gaussian_model as bgm
+    bind_icosphere(bgm)
+
+
 def densify(ref_root):
     """tests/golden/densify.npz: TwoGaussianModel's densify_and_prune (clone,
     split with the stored normal draws, prune, optimiser state surgery) and
@@ -547,8 +648,11 @@ if __name__ == "__main__":
         main_densify(root)
     elif "--loss" in sys.argv:   # only the photometric-loss fixture
         main_loss(root)
+    elif "--bind-ico" in sys.argv:   # only the icosphere binding fixture
+        main_bind_ico(root)
     else:
         main(root)
         main_sq(root)
         main_densify(root)
         main_loss(root)
+        main_bind_ico(root)

@@ -80,3 +80,39 @@ def test_binding_gradients_match_reference(bind_case):
         ref = GOLD[f"bind_grad_{k}"]
         err = np.abs(p.grad.numpy() - ref).max() / max(1e-6, np.abs(ref).max())
         assert err < 2e-4, (k, err)
+
+
+ICO = np.load(os.path.join(os.path.dirname(__file__), "golden", "bind_icosphere.npz"))
+
+
+def _ico_inputs(dtype):
+    g = {k[len("in_"):]: torch.tensor(ICO[k]) for k in ICO.files if k.startswith("in_")}
+    alpha = g["alpha"].reshape(-1, g["alpha"].shape[2], 3)
+    return g, alpha.to(dtype)
+
+
+@pytest.mark.parametrize("dtype,tol", [(torch.float32, 1e-6), (torch.float64, 2e-5)])
+def test_binding_on_the_icosphere_matches_reference(dtype, tol):
+    """The block model's own topology type: a level-2 icosphere (162
+    vertices, 320 faces, vertices at both poles, where cos(eta) is a float32
+    rounding residue), 3 splats per face (tests/golden/bind_icosphere.npz)."""
+    g, alpha = _ico_inputs(dtype)
+    assert int((np.abs(ICO["in_eta"]) > 1.5707).sum()) >= 2                 # the poles
+    out = B.bind(*(g[k].to(dtype) for k in ("sq_s", "sq_r", "sq_t", "sq_eps", "sq_occ", "eta", "omega")), g["faces"],
+                 alpha, g["scale"].to(dtype), 0.25, 0.2)
+    for o, k in zip(out, ["xyz", "scaling", "rotation", "opacity"]):
+        np.testing.assert_allclose(o.detach().numpy(), ICO[f"out_{k}"], rtol=tol, atol=tol, err_msg=k)
+
+
+def test_binding_gradients_on_the_icosphere_match_reference():
+    g, alpha = _ico_inputs(torch.float64)
+    params = {k: g[k].clone().double().requires_grad_(True) for k in ["sq_s", "sq_r", "sq_t", "sq_eps", "sq_occ"]}
+    out = B.bind(params["sq_s"], params["sq_r"], params["sq_t"], params["sq_eps"], params["sq_occ"],
+                 g["eta"].double(), g["omega"].double(), g["faces"], alpha, g["scale"].double(), 0.25, 0.2)
+    loss = sum((o * torch.tensor(ICO[f"upstream_{k}"]).double()).sum()
+               for o, k in zip(out, ["xyz", "scaling", "rotation", "opacity"]))
+    loss.backward()
+    for k, p in params.items():
+        ref = ICO[f"grad_{k}"]
+        err = np.abs(p.grad.numpy() - ref).max() / max(1e-6, np.abs(ref).max())
+        assert err < 2e-4, (k, err)
