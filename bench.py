@@ -105,7 +105,9 @@ class ClockSampler:
 
 
 def run_reference(args):
-    """CPU restatement timed on the host (rank 0 only)."""
+    """CPU restatement timed on the host (rank 0 only): per step, the
+    per-surfel phases of one view (timed once) plus the blend of every tile
+    estimated from a fresh length-weighted sample of tiles, times the views."""
     ws, rank, _ = _dist()
     if rank != 0:
         return
@@ -115,23 +117,20 @@ def run_reference(args):
     t0 = time.perf_counter()
     est, desc, cores, d = CB.time_step(args.workload, 0, sample_tiles=procs, procs=procs)
     per_surfel = d["t_setup"] + d["t_prebwd"]
-    # further steps: fresh seeded tile samples, same per-surfel phase times
     ests = []
     import multiprocessing as mp
     CB._setup(args.workload, 0, 0, "float32")
     ranges = CB._W["ranges"]
-    nonempty = np.nonzero(ranges[:, 1] > ranges[:, 0])[0]
+    views = _workload_config(args.workload).get("views", 16)
     ctx = mp.get_context("spawn")
     with ctx.Pool(procs, initializer=CB._setup, initargs=(args.workload, 0, 0, "float32")) as pool:
-        pool.map(CB._render_tiles, [nonempty[i:i + 1] for i in range(procs)])
+        nonempty = np.nonzero(ranges[:, 1] > ranges[:, 0])[0]
+        pool.map(CB._render_tiles, [nonempty[i:i + 1] for i in range(procs)], chunksize=1)
         for step in range(args.warmup + args.steps):
             rng = np.random.default_rng(1000 + step)
-            tiles = np.sort(rng.choice(nonempty, size=procs, replace=False))
-            t1 = time.perf_counter()
-            pool.map(CB._render_tiles, [tiles[i:i + 1] for i in range(procs)])
-            tr = time.perf_counter() - t1
+            core_s, _ = CB.blend_estimate(pool, ranges, procs, rng)
             if step >= args.warmup:
-                ests.append((per_surfel + tr * d["tiles"] / procs) * 16)
+                ests.append((per_surfel + core_s / procs) * views)
     step_s = statistics.mean(ests)
     value = 1.0 / step_s
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
@@ -143,6 +142,191 @@ def run_reference(args):
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "wall_s": time.perf_counter() - t0}
     print(json.dumps(line), flush=True)
+
+
+# FP32 operations per visited fragment of the reference's blend loops
+# (P0/cr/forward.cu:349-412: 77; P0/cr/backward.cu:290-437: 195)
+FLOPS_PER_FRAGMENT = {"blend_fwd": 77, "blend_bwd": 195}
+
+
+def roofline_report(workload, phases, dom, tr, P, V, H, W, keys, nbins, dev):
+    """Per-phase rooflines of the eager step whose CUDA-event phase times are
+    ``phases`` (ms).  The blends are bound by instruction issue: warp
+    instructions per launch (one ncu count of this workload, committed under
+    profiles/) over the live launch time, against one warp instruction per
+    scheduler per SM clock; beside that, the effective FP32 rate of the
+    reference's algorithm (FLOPS_PER_FRAGMENT x the fragments counted on the
+    device) against the FP32 peak.  The other phases are bound by HBM:
+    algorithmic bytes per launch over the launch time, against the measured
+    copy bandwidth."""
+    import torch
+    from partgs_gb300 import _lib as L
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
+    hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
+    props = torch.cuda.get_device_properties(dev)
+    sms = props.multi_processor_count
+    clock_mhz = float(peaks.get("sm_max_mhz", 2070.0))
+    issue_peak = sms * 4 * clock_mhz * 1e6                 # warp instructions / s
+    fp32_peak = sms * 128 * 2 * clock_mhz * 1e6            # FMA = 2 operations, 128 lanes per SM
+    frag_fwd = tr.raster.fragments()
+    st = tr.raster.last_state
+    s = st.sizes
+    HW = H * W
+    nc = st.geom[s.off_n_contrib:s.off_n_contrib + V * 2 * HW * 4].view(torch.int32).reshape(V, 2, HW)
+    frag_bwd = int(nc[:, 0].sum().item())
+    R = P * V
+    tj = {}
+    try:
+        tj = json.load(open(os.path.join(ROOT, "profiles", "roofline_traffic.json"))).get(workload, {})
+    except (OSError, ValueError):
+        pass
+    alg_bytes = {
+        "preprocess": 232 * P + 87 * R + 96 * R,     # parameters once; per record: outputs + the 96-B record
+        "depth_order": 24 * R + 20 * R,              # sort of 12-B (key, index) pairs; rectangle gather
+        "binning": 3 * 8 * R + 4 * nbins,            # rectangles read by three passes; one 4-B id per entry
+        "preprocess_bwd": 583 * R,
+    }
+    per = {}
+    for name, ms in phases.items():
+        t = ms * 1e-3
+        e = {"ms": round(ms, 4)}
+        if name in FLOPS_PER_FRAGMENT:
+            frags = frag_fwd if name == "blend_fwd" else frag_bwd
+            inst = tj.get(name + "_warp_inst")
+            e.update(bound="issue", fragments=int(frags),
+                     fp32_effective={"achieved": round(FLOPS_PER_FRAGMENT[name] * frags / t / 1e12, 3),
+                                     "peak": round(fp32_peak / 1e12, 2), "unit": "TFLOP/s",
+                                     "frac": round(FLOPS_PER_FRAGMENT[name] * frags / t / fp32_peak, 4)})
+            if inst:
+                e.update(achieved=round(inst / t / 1e12, 4), peak=round(issue_peak / 1e12, 4), unit="Twarp-inst/s",
+                         frac=round(inst / t / issue_peak, 4), warp_inst_per_launch=int(inst))
+        else:
+            b = alg_bytes[name]
+            e.update(bound="hbm", achieved=round(b / t / 1e9, 1), peak=hbm_peak, unit="GB/s",
+                     frac=round(b / t / 1e9 / hbm_peak, 4), algorithmic_bytes=int(b))
+        traffic = tj.get(name)
+        if traffic:
+            e["traffic"] = int(traffic)
+            e["dram_gbs"] = round(traffic / t / 1e9, 1)
+        per[name] = e
+    top = dict(per[dom])
+    out = {"kernel": dom, "bound": top.get("bound"), "achieved": top.get("achieved"), "peak": top.get("peak"),
+           "unit": top.get("unit"), "frac": top.get("frac"), "traffic": top.get("traffic"),
+           "launch_ms": top["ms"], "peak_source": "measured" if "hbm_gbs" in peaks else "fallback",
+           "fragments_fwd": int(frag_fwd), "fragments_bwd": int(frag_bwd), "phases": per}
+    if "fp32_effective" in top:
+        out["fp32_effective"] = top["fp32_effective"]
+    return out
+
+
+def time_reference_cuda(workload_name, steps=3, warmup=1, device=None):
+    """The reference's own CUDA rasteriser (compiled unmodified for sm_103a by
+    ``oracle/ref_build.py``) on the same workload, the way the reference
+    trains: per view, the activations (scene/gaussian_model.py:198-218), its
+    ``GaussianRasterizer`` forward, the same loss in PyTorch operations
+    (L1 + D-SSIM, distortion, normal consistency, as train.py:229-250 /
+    ``SurfelTrainer.reference_loss``) divided by the view count, backward;
+    after all views, ``torch.optim.Adam`` (eps 1e-15, fused) and zero_grad.
+    Also times the rasteriser alone (forward + backward of every view
+    against fixed upstream gradients).  Returns a dict of per-step ms, or
+    None when the reference was not built."""
+    import torch
+    from oracle import ref_build, ref_cuda
+    if not ref_cuda.available():
+        try:
+            ref_build.build()
+        except Exception:
+            return None
+        if not ref_cuda.available():
+            return None
+    from partgs_gb300.scenes import workload
+    from partgs_gb300.surfel_step import DepthNormals, _gaussian_window, ssim
+    dev = device or torch.device("cuda")
+    mod = ref_cuda.load("plain")
+    scene, cams = workload(workload_name, 0)
+    V = len(cams)
+    g = torch.Generator().manual_seed(7)
+    targets = torch.rand(V, 3, cams[0].height, cams[0].width, generator=g).to(dev)
+    sets = [ref_cuda.settings(mod, c, [0.0, 0.0, 0.0], scene.sh_degree) for c in cams]
+    normals = [DepthNormals([c], dev) for c in cams]
+    window = _gaussian_window(device=dev)
+    xyz = scene.means3D.to(dev).clone().requires_grad_(True)
+    log_s = torch.log(scene.scales).to(dev).clone().requires_grad_(True)
+    rot = scene.rotations.to(dev).clone().requires_grad_(True)
+    op = scene.opacities.clamp(1e-4, 1 - 1e-4)
+    op_l = torch.log(op / (1 - op)).to(dev).clone().requires_grad_(True)
+    f_dc = scene.shs[:, :1].to(dev).clone().requires_grad_(True)
+    f_rest = scene.shs[:, 1:].to(dev).clone().requires_grad_(True)
+    opt = torch.optim.Adam([{"params": [xyz], "lr": 0.00048}, {"params": [f_dc], "lr": 0.0025},
+                            {"params": [f_rest], "lr": 0.0025 / 20.0}, {"params": [op_l], "lr": 0.05},
+                            {"params": [log_s], "lr": 0.005}, {"params": [rot], "lr": 0.001}], eps=1e-15,
+                           fused=True)
+
+    def view_loss(v):
+        scales = torch.exp(log_s)
+        rots = torch.nn.functional.normalize(rot)
+        opac = torch.sigmoid(op_l)
+        shs = torch.cat((f_dc, f_rest), dim=1)
+        m2 = torch.zeros_like(xyz, requires_grad=True)
+        color, radii, allmap = mod.GaussianRasterizer(sets[v])(means3D=xyz, means2D=m2, shs=shs,
+                                                               colors_precomp=None, opacities=opac,
+                                                               scales=scales, rotations=rots)
+        color, allmap, tgt = color[None], allmap[None], targets[v:v + 1]
+        l1 = torch.abs(color - tgt).mean()
+        loss = 0.8 * l1 + 0.2 * (1.0 - ssim(color, tgt, window))
+        alpha = allmap[:, 1:2]
+        rend_normal = torch.einsum("vchw,vcd->vdhw", allmap[:, 2:5], normals[v].view_to_world)
+        median = torch.nan_to_num(allmap[:, 5:6], 0, 0)
+        surf_normal = normals[v].normals(median) * alpha.detach()
+        normal_loss = 0.05 * (1 - (rend_normal * surf_normal).sum(dim=1)).mean()
+        return (loss + 1000.0 * allmap[:, 6:7].mean() + normal_loss) / V
+
+    def step():
+        for v in range(V):
+            view_loss(v).backward()
+        opt.step()
+        opt.zero_grad(set_to_none=False)
+
+    def timed(fn, n):
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(n):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / n
+
+    for _ in range(warmup):
+        step()
+    step_ms = timed(step, steps)
+
+    # rasteriser alone: forward + backward of every view, fixed inputs
+    with torch.no_grad():
+        a = (torch.exp(log_s), torch.nn.functional.normalize(rot), torch.sigmoid(op_l),
+             torch.cat((f_dc, f_rest), dim=1))
+    gr = torch.Generator(device=dev).manual_seed(3)
+    up_c = torch.randn(3, cams[0].height, cams[0].width, device=dev, generator=gr)
+    up_o = torch.randn(7, cams[0].height, cams[0].width, device=dev, generator=gr) * 0.1
+    leaves = [t.detach().clone().requires_grad_(True) for t in (xyz,) + a]
+
+    def raster_only():
+        for v in range(V):
+            m2 = torch.zeros_like(leaves[0], requires_grad=True)
+            color, radii, allmap = mod.GaussianRasterizer(sets[v])(
+                means3D=leaves[0], means2D=m2, shs=leaves[4], colors_precomp=None, opacities=leaves[3],
+                scales=leaves[1], rotations=leaves[2])
+            ((color * up_c).sum() + (allmap * up_o).sum()).backward()
+
+    raster_only()
+    raster_ms = timed(raster_only, steps)
+    return {"step_ms": step_ms, "raster_ms": raster_ms, "steps": steps, "warmup": warmup,
+            "what": "reference diff_surfel_rasterization (unmodified, nvcc -O3 sm_103a) through its own "
+                    "GaussianRasterizer, one view at a time; loss and Adam in PyTorch"}
 
 
 def run_gpu(args):
@@ -236,57 +420,28 @@ def run_gpu(args):
     lib.sgr_profile_enable(0)
     phases = {L.PHASES[i]: (msv[i] / max(1, cnt[i])) for i in range(6)}
     dom = max(phases, key=phases.get)
-    peaks = {}
-    try:
-        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
-    except OSError:
-        pass
-    hbm_peak = peaks.get("hbm_gbs", 6800.0)
-    HW = H * W
-    P = scene.P
-    R_ = P * V
-    alg_bytes = {  # algorithmic bytes per launch (one batched launch covers all views)
-        "blend_bwd": 112 * keys + 60 * HW * V,
-        "blend_fwd": 76 * keys + 60 * HW * V,
-        "binning": 20 * R_ + 12 * keys,
-        "preprocess": 232 * P + 87 * R_,
-        "preprocess_bwd": 583 * R_,
-        "depth_order": 8 * R_,
-    }[dom]
-    achieved = alg_bytes / (phases[dom] * 1e-3) / 1e9
-    traffic, inst = None, None
-    try:
-        tj = json.load(open(os.path.join(ROOT, "profiles", "roofline_traffic.json")))
-        traffic = tj.get(args.workload, {}).get(dom)
-        inst = tj.get(args.workload, {}).get(dom + "_warp_inst")
-    except (OSError, ValueError):
-        pass
-    roofline = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": hbm_peak,
-                "unit": "GB/s", "frac": round(achieved / hbm_peak, 4), "traffic": traffic,
-                "algorithmic_bytes": int(alg_bytes), "launch_ms": round(phases[dom], 3),
-                "peak_source": "measured" if "hbm_gbs" in peaks else "fallback",
-                "phase_ms": {k: round(v, 3) for k, v in phases.items()}}
-    if inst:
-        # The blend kernels are bound by instruction issue: warp instructions
-        # per launch (one ncu capture of this workload) over the live launch
-        # time, against one warp instruction per scheduler per SM clock.
-        sms = torch.cuda.get_device_properties(dev).multi_processor_count
-        clock_mhz = peaks.get("sm_max_mhz", 2070.0)
-        issue_peak = sms * 4 * clock_mhz * 1e6
-        issue = inst / (phases[dom] * 1e-3)
-        roofline["issue"] = {"achieved": round(issue / 1e12, 4), "peak": round(issue_peak / 1e12, 4),
-                             "unit": "Twarp-inst/s", "frac": round(issue / issue_peak, 4),
-                             "warp_inst_per_launch": int(inst)}
+    roofline = roofline_report(args.workload, phases, dom, tr, scene.P, V, H, W, keys, nbins, dev)
+    frag_fwd, frag_bwd = roofline["fragments_fwd"], roofline["fragments_bwd"]
 
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene and targets)",
             "config": dict(_workload_config(args.workload), keys=keys, cell_list_entries=nbins,
+                           fragments_fwd=frag_fwd, fragments_bwd=frag_bwd,
                            cell_list_capacity=tr.raster.bin_capacity, cell_tiles=tr.raster.cell_tiles,
                            parallelism=f"replicas x{ws}"),
             "e2e": {"value": ws / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(targets_host.numel() * 4),
                     "d2h_bytes_per_step": 4},
             "roofline": roofline, "gpu_launches": int(launches_per_step) * args.steps, "clocks": clk}
+    if rank == 0 and ws == 1 and not args.no_reference_cuda:
+        rc = time_reference_cuda(args.workload, device=dev)
+        if rc is None:
+            line["reference_cuda"] = {"unavailable": "reference extension not built (sources not staged)"}
+        else:
+            raster_ms = sum(phases.values())
+            rc.update(ours_step_ms=ms_per_step, ours_raster_ms=raster_ms,
+                      step_speedup=rc["step_ms"] / ms_per_step, raster_speedup=rc["raster_ms"] / raster_ms)
+            line["reference_cuda"] = {k: (round(v, 4) if isinstance(v, float) else v) for k, v in rc.items()}
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         from oracle import cpu_baseline as CB
         procs = os.cpu_count() or 1
@@ -303,9 +458,11 @@ def main():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference", "reference-cuda"])
     ap.add_argument("--workload", default="sq500k_16x800x600")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-reference-cuda", action="store_true",
+                    help="skip timing the reference's CUDA rasteriser on the same workload")
     ap.add_argument("--cell-tiles", type=int, default=0, choices=[0, 1, 2, 4, 8, 16],
                     help="cell edge in tiles (0: autotuned)")
     args = ap.parse_args()
@@ -313,6 +470,10 @@ def main():
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
+    elif args.impl == "reference-cuda":
+        print(json.dumps({"impl": "reference-cuda", "workload": args.workload,
+                          **(time_reference_cuda(args.workload, steps=args.steps, warmup=args.warmup) or
+                             {"unavailable": "reference extension not built"})}), flush=True)
     else:
         run_gpu(args)
 

@@ -62,11 +62,24 @@ extern "C" {
 #define SGR_ERR_KEY_CAPACITY 5       /* key capacity above 2^31 - 1 or below zero */
 #define SGR_ERR_CUDA 6               /* a CUDA runtime call failed; see sgr_last_error_message */
 
+/* Byte offsets in the 32-byte device status word (sgr_sizes.off_status).
+ * SGR_STATUS_FRAGMENTS counts the (pixel, list entry) pairs the reference's
+ * forward blend would visit: per pixel, the list entries up to and including
+ * the one that ends it (or the whole tile list), summed over the batch; the
+ * blend's algorithmic work unit (about 77 FP32 operations each). */
+#define SGR_STATUS_KEYS 0
+#define SGR_STATUS_FLAGS 8
+#define SGR_STATUS_BIN_ENTRIES 16
+#define SGR_STATUS_FRAGMENTS 24
+
 /* bits of the device status word (sgr_sizes.off_status), set by kernels */
 #define SGR_FLAG_KEY_OVERFLOW 1u     /* sgr_tile_lists: more (surfel, tile) keys than its capacity */
 #define SGR_FLAG_PREFILTERED 2u      /* prefiltered was set but a surfel failed the near test
                                         (the reference traps here, cuda_rasterizer/auxiliary.h:200-206) */
 #define SGR_FLAG_BIN_OVERFLOW 4u     /* more (record, cell) entries than the cell-list capacity */
+#define SGR_FLAG_LIST_INCONSISTENT 8u /* sgr_backward: a tile's cell list held fewer entries than its
+                                         forward blended (the workspace or the lists changed between the
+                                         calls); that tile's gradients are incomplete */
 
 #define SGR_VARIANT_PLAIN 0
 #define SGR_VARIANT_PART 1
@@ -142,7 +155,8 @@ typedef struct sgr_sizes {
     size_t off_ranges;           /* uint32[V*tiles][2] per-tile [start, end), written by sgr_tile_lists */
     size_t off_final_T;          /* float[V][3][H][W]: T, M1, M2 */
     size_t off_n_contrib;        /* uint32[V][2][H][W]: last contributor, median contributor */
-    size_t off_status;           /* uint64 key count, uint32 flags, uint32 pad, uint64 cell-list entries, pad */
+    size_t off_status;           /* uint64 key count, uint32 flags, uint32 pad, uint64 cell-list entries,
+                                    uint64 fragments the forward blend visited (see SGR_STATUS_FRAGMENTS) */
     size_t off_rects;            /* uint32[R][2] tile rectangle of each record in depth order */
     size_t off_bin_start;        /* uint32[V*cells] start of each cell list */
     size_t off_bin_count;        /* uint32[V*cells] length of each cell list */
@@ -245,6 +259,34 @@ int sgr_profile_read(float* ms, int32_t* count);
  * capture) since it was loaded, over all threads.  Instrumentation with no
  * counterpart in the reference. */
 uint64_t sgr_kernel_launches(void);
+
+/* Folds the status word at `status` (sgr_sizes.off_status of a geometry
+ * workspace) into a device record of two int64: sticky[0] |= its flags,
+ * sticky[1] = max(sticky[1], its cell-list entry count).  One one-thread
+ * kernel on `stream`, so a captured training step keeps the flags of every
+ * forward and backward it replays.  No counterpart in the reference (whose
+ * calls synchronise the host instead). */
+int sgr_status_accumulate(const void* status, int64_t* sticky, void* stream);
+
+/* ---- the sort and scans the forward uses -------------------------------- */
+
+/* Stable LSD radix sort of n (key, value) pairs on key bits [0, end_bit),
+ * 8 bits per pass: keys_out / vals_out in ascending key order, equal keys in
+ * input order.  Replaces the reference's cub::DeviceRadixSort::SortPairs
+ * (cuda_rasterizer/rasterizer_impl.cu:304-309), which sorts the same way;
+ * the forward calls it on (view << 32 | depth bits, record) pairs.  The
+ * inputs are not modified; temp must hold sgr_radix_sort_temp_bytes(n, key
+ * bytes) bytes.  key_bytes is 8 (uint64 keys) or 4 (uint32 keys). */
+size_t sgr_radix_sort_temp_bytes(int64_t n, int key_bytes);
+int sgr_radix_sort_pairs(const void* keys_in, void* keys_out, const uint32_t* vals_in, uint32_t* vals_out, int64_t n,
+                         int key_bytes, int end_bit, void* temp, size_t temp_bytes, void* stream);
+/* Prefix sums the forward uses: inclusive over uint64 (key offsets, the
+ * reference's cub::DeviceScan::InclusiveSum, rasterizer_impl.cu:278) and
+ * exclusive over uint32 (cell-list starts).  `in` may equal `out`; temp
+ * must hold sgr_prefix_sum_temp_bytes(n, element bytes) bytes. */
+size_t sgr_prefix_sum_temp_bytes(int64_t n, int elem_bytes);
+int sgr_inclusive_sum_u64(const uint64_t* in, uint64_t* out, int64_t n, void* temp, size_t temp_bytes, void* stream);
+int sgr_exclusive_sum_u32(const uint32_t* in, uint32_t* out, int64_t n, void* temp, size_t temp_bytes, void* stream);
 
 /* Near-plane visibility of P points in one view (present: uint8[P]). */
 int sgr_mark_visible(int32_t P, const float* means3D, const float* viewmatrix, const float* projmatrix,

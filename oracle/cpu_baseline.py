@@ -4,17 +4,18 @@ TEST / MEASUREMENT INFRASTRUCTURE ONLY (used by ``bench.py``'s
 ``cpu_baseline`` field and its ``--impl reference`` arm; never by the
 product path).
 
-The reference rasteriser itself cannot run on a CPU (it is CUDA code that
-also needs the absent glm headers), so the baseline is the oracle port
+The reference rasteriser itself cannot run on a CPU (it is CUDA code), so
+the baseline is the oracle port
 (``kind: "port"``): numpy FP32, the reference's per-pixel algorithm.  A full
 step of the 500k-surfel / 16-view / 800x600 workload would take hours on the
 host, so one bounded sample is timed and scaled:
 
 * per view, the per-surfel phases (preprocess, key binning, preprocess
   backward) are timed in full on one view;
-* the per-pixel phases (blend forward + backward) are timed on a seeded
-  sample of that view's tiles, spread over the host cores with a ``spawn``
-  process pool, and scaled by (tiles in the view / sampled tiles);
+* the per-pixel phases (blend forward + backward) are estimated for every
+  tile of that view from a seeded sample of tiles drawn with probability
+  proportional to their list length, each timed alone in a ``spawn``
+  process pool (Horvitz-Thompson), and divided over the host cores;
 * the step time is that per-view estimate times the number of views.
 """
 from __future__ import annotations
@@ -65,9 +66,35 @@ def _render_tiles(tiles):
     return time.perf_counter() - t0, int(rf["fragments"])
 
 
+def sample_tiles(ranges, k, rng):
+    """k tiles drawn with replacement, with probability proportional to their
+    list length (the blend's work grows with it), and those probabilities."""
+    lens = (ranges[:, 1] - ranges[:, 0]).astype(np.float64)
+    p = lens / lens.sum()
+    tiles = rng.choice(len(lens), size=k, replace=True, p=p)
+    return tiles, p[tiles]
+
+
+def blend_estimate(pool, ranges, k, rng):
+    """Single-core seconds of the blend forward + backward of every tile of
+    the view, estimated from k length-weighted tiles timed one per job
+    (Horvitz-Thompson: the mean of cost / probability), and the sampled
+    fragments."""
+    tiles, p = sample_tiles(ranges, k, rng)
+    res = pool.map(_render_tiles, [np.array([t]) for t in tiles], chunksize=1)
+    cost = np.array([r[0] for r in res])
+    return float(np.mean(cost / p)), int(sum(r[1] for r in res))
+
+
 def time_step(workload_name="sq500k_16x800x600", seed=0, sample_tiles=None, procs=None, dtype_name="float32"):
     """Estimated seconds per step of the oracle on ``procs`` host processes,
-    with the sample description."""
+    with the sample description.
+
+    Per view: the per-surfel phases (preprocess, binning, preprocess
+    backward) timed in full on one core; the blend forward + backward of
+    every tile estimated from a length-weighted sample of tiles (each timed
+    alone) and divided over the processes, as a tile-parallel host
+    implementation would run it; times the number of views."""
     import sys
     root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
     if root not in sys.path:
@@ -94,25 +121,20 @@ def time_step(workload_name="sq500k_16x800x600", seed=0, sample_tiles=None, proc
     O.preprocess_backward(st, rb, ocam, osf, O.PLAIN, dt)
     t_prebwd = time.perf_counter() - t0
     ntiles = ranges.shape[0]
-    nonempty = np.nonzero(ranges[:, 1] > ranges[:, 0])[0]
-    k = sample_tiles or max(procs, 2 * procs)
+    k = sample_tiles or 2 * procs
     rng = np.random.default_rng(seed)
-    tiles = np.sort(rng.choice(nonempty, size=min(k, len(nonempty)), replace=False))
-    chunks = [c for c in np.array_split(tiles, procs) if len(c)]
     ctx = mp.get_context("spawn")
-    with ctx.Pool(len(chunks), initializer=_setup, initargs=(workload_name, seed, 0, dtype_name)) as pool:
-        pool.map(_render_tiles, [c[:1] for c in chunks])     # warm-up in every worker
-        t0 = time.perf_counter()
-        res = pool.map(_render_tiles, chunks)
-        t_render = time.perf_counter() - t0
-    frags = sum(r[1] for r in res)
-    per_view = t_setup + t_prebwd + t_render * ntiles / len(tiles)
+    with ctx.Pool(procs, initializer=_setup, initargs=(workload_name, seed, 0, dtype_name)) as pool:
+        nonempty = np.nonzero(ranges[:, 1] > ranges[:, 0])[0]
+        pool.map(_render_tiles, [nonempty[i:i + 1] for i in range(procs)], chunksize=1)   # warm-up
+        blend_core_s, frags = blend_estimate(pool, ranges, k, rng)
+    per_view = t_setup + t_prebwd + blend_core_s / procs
     step = per_view * V
     sample = (f"view 0 of {V}: preprocess, binning and preprocess backward in full (1 core); blend forward + "
-              f"backward on {len(tiles)} of {ntiles} tiles (seeded, {frags} fragments) over {len(chunks)} "
-              f"processes, scaled by tiles; times {V} views")
-    return step, sample, len(chunks), dict(t_setup=t_setup, t_prebwd=t_prebwd, t_render_sample=t_render,
-                                            tiles_sampled=len(tiles), tiles=ntiles)
+              f"backward of all {ntiles} tiles estimated from {k} tiles drawn by list length (each timed alone, "
+              f"{frags} fragments; Horvitz-Thompson), divided over {procs} processes; times {V} views")
+    return step, sample, procs, dict(t_setup=t_setup, t_prebwd=t_prebwd, blend_core_s=blend_core_s,
+                                     tiles_sampled=k, tiles=ntiles)
 
 
 if __name__ == "__main__":

@@ -1,0 +1,178 @@
+"""Float64 central finite differences of the superquadric binding followed by
+the plain rasteriser, for checking the hand-written adjoint chain
+(``sgr_bind_backward`` after ``sgr_backward``) parameter by parameter.
+
+TEST INFRASTRUCTURE ONLY.
+
+The chain is the oracle's: ``binding_oracle.bind`` (prepare_scaling_rot,
+games/block_mesh_splatting/scene/block_gaussian_model.py:198-256) then
+``surfel_oracle.forward_view`` (the rasteriser, both in float64).  The loss
+is a fixed weighted sum of the rendered colour and the seven auxiliary maps
+of every view.
+
+A parameter of block b moves only block b's surfels, so each evaluation
+blends only the tiles those surfels' rectangles cover (one tile of margin);
+every other pixel is unchanged by construction.
+
+Discrete decisions (the alpha cut-off, the stop test, the 3D/2D branch, the
+median switch, a rectangle's rounding) make the loss jump.  Each evaluation
+returns the oracle's per-pixel decision signature; a pixel whose signature
+differs between the +h and -h evaluations is a "flip", and the checks leave
+such pixels out of both the difference and the analytic gradient (the loss
+restricted to the other pixels is smooth over [-h, +h]).
+
+Evaluations run in a ``spawn`` process pool.
+"""
+from __future__ import annotations
+
+import multiprocessing as mp
+import os
+
+import numpy as np
+
+NAMES = ["sq_s", "sq_r", "sq_t", "sq_eps", "sq_occ"]
+
+_W = {}
+
+
+def make_case(B=8, n_eta=50, n_omega=50, views=(0, 1), height=300, width=400, fovx=50.0, seed=0):
+    """The block-level workload's layout: B superquadrics with n_eta x n_omega
+    surfels each, cameras on a radius-3 sphere; seeded SH colours and loss
+    weights.  Returns a dict of numpy / torch inputs (float64)."""
+    import torch
+    from oracle import binding_oracle as Bo
+    from partgs_gb300.cameras import orbit_cameras
+    inp = Bo.random_binding_inputs(B=B, n_eta=n_eta, n_omega=n_omega, N=1, seed=seed)
+    cams_all = orbit_cameras(8, 3.0, height, width, fovx, seed=seed)
+    cams = [cams_all[v] for v in views]
+    P = inp["faces"].shape[0] * inp["faces"].shape[1]
+    shs = torch.randn(P, 16, 3, generator=torch.Generator().manual_seed(seed + 5), dtype=torch.float64) * 0.2
+    g = np.random.default_rng(seed + 6)
+    w_col = [g.standard_normal((3, height, width)) for _ in cams]
+    w_oth = [g.standard_normal((7, height, width)) * 0.1 for _ in cams]
+    return dict(inp=inp, cams=cams, shs=shs, w_col=w_col, w_oth=w_oth, B=B)
+
+
+def _camera(cam):
+    from oracle import surfel_oracle as O
+    return O.Camera(np.asarray(cam.world_view_transform, np.float64).reshape(-1),
+                    np.asarray(cam.full_proj_transform, np.float64).reshape(-1),
+                    np.asarray(cam.camera_center, np.float64), cam.tanfovx, cam.tanfovy, cam.height, cam.width)
+
+
+def _surfels(case, params):
+    from oracle import binding_oracle as Bo
+    from oracle import surfel_oracle as O
+    inp = case["inp"]
+    xyz, ls, rot, op = Bo.bind(*params, inp["eta"], inp["omega"], inp["faces"], inp["alpha_raw"], inp["scale"],
+                               inp["ratio_block_scene"], inp["scale_block_min"])
+    return O.Surfels(xyz.numpy(), op.numpy(), np.exp(ls.numpy()), rot.numpy(), shs=case["shs"].numpy(), sh_degree=3)
+
+
+def block_tiles(case, block):
+    """Per view, the tiles block `block`'s visible surfels cover, with one
+    tile of margin (sorted tile indices)."""
+    from oracle import surfel_oracle as O
+    inp = case["inp"]
+    s = _surfels(case, [inp[k] for k in NAMES])
+    per_block = inp["faces"].shape[1] * inp["alpha_raw"].shape[1]
+    out = []
+    for cam in case["cams"]:
+        pre = O.preprocess(s, _camera(cam), O.PLAIN, np.float64)
+        gx, gy = pre["grid"]
+        xmin, ymin, xmax, ymax = pre["rect"]
+        mask = np.zeros((gy, gx), bool)
+        for i in range(block * per_block, (block + 1) * per_block):
+            if pre["radii"][i] > 0:
+                mask[max(0, ymin[i] - 1):min(gy, ymax[i] + 1), max(0, xmin[i] - 1):min(gx, xmax[i] + 1)] = True
+        out.append(np.nonzero(mask.reshape(-1))[0])
+    return out
+
+
+def pixel_values(case, params, tiles_per_view):
+    """Per view: (weighted per-pixel loss contributions [H,W], decision
+    signature [H,W], pixel mask of the blended tiles [H,W])."""
+    from oracle import surfel_oracle as O
+    s = _surfels(case, params)
+    res = []
+    for v, cam in enumerate(case["cams"]):
+        st = O.forward_view(s, _camera(cam), np.zeros(3), O.PLAIN, np.float64, tiles=tiles_per_view[v])
+        val = (case["w_col"][v] * st.color).sum(0) + (case["w_oth"][v] * st.others).sum(0)
+        gx = (cam.width + 15) // 16
+        tmask = np.zeros(((cam.height + 15) // 16) * gx, bool)
+        tmask[tiles_per_view[v]] = True
+        yy, xx = np.mgrid[0:cam.height, 0:cam.width]
+        pmask = tmask[(yy // 16) * gx + (xx // 16)]
+        res.append((np.where(pmask, val, 0.0), st.extra["signature"], pmask))
+    return res
+
+
+def _init(case_kwargs):
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    if root not in sys.path:
+        sys.path.insert(0, root)
+    import torch
+    torch.set_num_threads(1)
+    case = make_case(**case_kwargs)
+    _W["case"] = case
+    _W["tiles"] = {}
+
+
+def _eval(job):
+    """job = (name, flat index, signed step): per view (values, signature)
+    on block b's tiles."""
+    case = _W["case"]
+    name, flat, delta = job
+    inp = case["inp"]
+    params = [inp[k].clone() for k in NAMES]
+    k = NAMES.index(name)
+    block = int(np.unravel_index(flat, params[k].shape)[0])
+    if block not in _W["tiles"]:
+        _W["tiles"][block] = block_tiles(case, block)
+    params[k].view(-1)[flat] += delta
+    res = pixel_values(case, params, _W["tiles"][block])
+    out = []
+    for val, sig, pm in res:
+        idx = np.flatnonzero(pm)
+        out.append((idx.astype(np.int32), val.reshape(-1)[idx], sig.reshape(-1)[idx]))
+    return out
+
+
+def parameter_list(case, blocks_full=None):
+    """(name, flat index) of every parameter (or every parameter of the
+    blocks in ``blocks_full`` plus the exponents and occupancy of all)."""
+    inp = case["inp"]
+    out = []
+    for name in NAMES:
+        t = inp[name]
+        per = t.numel() // case["B"]
+        for flat in range(t.numel()):
+            b = flat // per
+            if blocks_full is None or b in blocks_full or name in ("sq_eps", "sq_occ"):
+                out.append((name, flat))
+    return out
+
+
+def finite_differences(case_kwargs, params, h=1e-6, procs=None):
+    """Central differences of the loss for each (name, flat index) in
+    ``params``.  Returns a list of dicts: fd (all pixels), flips (their
+    count), and per view the flat indices of the pixels the block's tiles
+    cover, their difference quotients, and the flip mask (pixels whose
+    decisions differ between +h and -h)."""
+    procs = procs or min(16, os.cpu_count() or 1)
+    jobs = [(n, f, s * h) for n, f in params for s in (1, -1)]
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(procs, initializer=_init, initargs=(case_kwargs,)) as pool:
+        res = pool.map(_eval, jobs, chunksize=1)
+    out = []
+    for i, (n, f) in enumerate(params):
+        plus, minus = res[2 * i], res[2 * i + 1]
+        views = []
+        total = 0.0
+        for (idx, vp, sp), (_, vm, sm) in zip(plus, minus):
+            q = (vp - vm) / (2 * h)
+            views.append(dict(pixels=idx, quotient=q, flip=sp != sm))
+            total += float(q.sum())
+        out.append(dict(name=n, flat=f, fd=total, views=views, flips=int(sum(v["flip"].sum() for v in views))))
+    return out

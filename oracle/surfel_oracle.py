@@ -286,6 +286,25 @@ def _near_int(v, tol):
     return np.abs(v - np.round(v)) <= tol * np.maximum(1.0, np.abs(v))
 
 
+EPS32 = 2.0 ** -24       # unit roundoff of float32
+FP32_ROUNDINGS = 4       # roundings an FP32 evaluation of a short sum accumulates (a bound)
+
+
+def _near_int_abs(v, err):
+    """True where v lies within an absolute err of an integer."""
+    return np.abs(v - np.round(v)) <= err
+
+
+def _extent_err(h0, mag):
+    """Absolute FP32 error bound of sqrt(max(0, h0)) when h0 is a difference
+    whose terms sum to ``mag`` in magnitude: the cancellation in h0 leaves
+    an error of about FP32_ROUNDINGS * EPS32 * mag there, and the square
+    root divides it by 2 sqrt(h0)."""
+    dh0 = FP32_ROUNDINGS * EPS32 * mag
+    with np.errstate(divide="ignore", invalid="ignore"):
+        return np.where(h0 > dh0, dh0 / (2.0 * np.sqrt(np.maximum(h0, dh0))), np.sqrt(dh0))
+
+
 def _rect(px, py, radius, gx, gy, f):
     """getRect, P0/cr/auxiliary.h:67-77: truncation toward zero, clamped."""
     def trunc_clamp(v, hi):
@@ -390,6 +409,13 @@ def preprocess(s: Surfels, cam: Camera, variant=PLAIN, dtype=np.float64, amb_tol
             rad_in = np.maximum(ext, f(np.float32(3.0) * np.float32(FILTER_SIZE_P0)))
             radius = np.ceil(rad_in)
             amb |= (ext > 2.2) & _near_int(ext, amb_tol)
+            # the extent is a difference of products of pixel-scale terms: its
+            # FP32 evaluation can miss by far more than a relative 2e-6
+            ex = _extent_err(h0x, px * px + np.abs(np.sum(fv * Tu * Tu, 1)))
+            ey = _extent_err(h0y, py * py + np.abs(np.sum(fv * Tv * Tv, 1)))
+            e_ext = np.where(hx >= hy, ex, ey)
+            amb |= (ext > 2.2) & _near_int_abs(ext, e_ext)
+            rad_err = np.where(ext > 2.2, np.maximum(amb_tol * np.abs(ext), e_ext), 0.0)
         else:
             t = np.array([1.0, 1.0, -1.0], dtype=dtype)
             d = np.sum(t * Tw * Tw, 1)
@@ -405,13 +431,23 @@ def preprocess(s: Surfels, cam: Camera, variant=PLAIN, dtype=np.float64, amb_tol
             rad_in = 3.0 * np.maximum(ext, FILTER_SIZE_P1)
             radius = np.ceil(rad_in).astype(dtype)
             amb |= (ext > FILTER_SIZE_P1) & _near_int(rad_in, amb_tol)
+            ex = _extent_err(h0x, px * px + np.abs(np.sum(fv * Tu * Tu, 1)))
+            ey = _extent_err(h0y, py * py + np.abs(np.sum(fv * Tv * Tv, 1)))
+            e_ext = np.where(hx >= hy, ex, ey)
+            amb |= (ext > FILTER_SIZE_P1) & _near_int_abs(rad_in, 3.0 * e_ext)
+            rad_err = np.where(ext > FILTER_SIZE_P1, np.maximum(amb_tol * np.abs(rad_in), 3.0 * e_ext), 0.0)
+        # FP32 error bound of the screen centre (a short sum of products)
+        ctr_err = np.stack([FP32_ROUNDINGS * EPS32 * np.sum(np.abs(fv * Tu * Tw), 1),
+                            FP32_ROUNDINGS * EPS32 * np.sum(np.abs(fv * Tv * Tw), 1)], 1)
         radius = np.where(alive, radius, 0).astype(dtype)
         px = np.where(alive, px, 0).astype(dtype)
         py = np.where(alive, py, 0).astype(dtype)
         xmin, ymin, xmax, ymax = _rect(px, py, radius, gx, gy, f)
-        for v in ((px - radius) / f(BLOCK_X), (py - radius) / f(BLOCK_Y),
-                  (px + radius + f(BLOCK_X - 1)) / f(BLOCK_X), (py + radius + f(BLOCK_Y - 1)) / f(BLOCK_Y)):
-            amb |= _near_int(v, amb_tol) & (v > -1) & (v < max(gx, gy) + 1)
+        for v, ce in (((px - radius) / f(BLOCK_X), ctr_err[:, 0]), ((py - radius) / f(BLOCK_Y), ctr_err[:, 1]),
+                      ((px + radius + f(BLOCK_X - 1)) / f(BLOCK_X), ctr_err[:, 0]),
+                      ((py + radius + f(BLOCK_Y - 1)) / f(BLOCK_Y), ctr_err[:, 1])):
+            near = _near_int(v, amb_tol) | _near_int_abs(v, ce / BLOCK_X)
+            amb |= near & (v > -1) & (v < max(gx, gy) + 1)
     # a decision close to its threshold matters only for surfels that reach
     # the rectangle stage, or sit on the near plane
     amb = (amb & alive) | amb_near
@@ -438,6 +474,9 @@ def preprocess(s: Surfels, cam: Camera, variant=PLAIN, dtype=np.float64, amb_tol
         clamped=clamped,
         alive=alive,
         amb=amb,
+        rad_in=np.where(alive, rad_in, 0.0).astype(np.float64),
+        rad_err=np.where(alive, rad_err, 0.0).astype(np.float64),
+        ctr_err=ctr_err.astype(np.float64),
         grid=(gx, gy),
         focal=(fx, fy),
     )
@@ -567,6 +606,10 @@ def render_forward(pre, point_list, ranges, cam: Camera, s: Surfels, bg, variant
     med_contrib = np.full(shape, -1, np.int64)
     Sem = np.zeros(shape + (Sn,), dtype)
     amb = np.zeros(shape, bool)
+    # rolling hash of the discrete path per pixel (which list positions were
+    # blended, through which branch, and where the walk stopped): equal
+    # signatures mean the same decisions (finite-difference checks use it)
+    sig = np.zeros(shape, np.int64)
     frags = 0
     for j in range(L):
         if done.all():
@@ -644,6 +687,8 @@ def render_forward(pre, point_list, ranges, cam: Camera, s: Surfels, bg, variant
                 Sem = np.where(acc[..., None], Sem + sv * alpha[..., None] * T[..., None], Sem)
         T = np.where(acc, test_T, T)
         last_contributor = np.where(acc, contributor, last_contributor)
+        code = contributor * 4 + use3d.astype(np.int64) * 2 + med.astype(np.int64)
+        sig = np.where(acc, sig * np.int64(1000003) + code, sig)
 
     HW = (H, W)
     out = lambda a, fill=0: _scatter_pixels(a, X, Y, inside, HW, fill)  # noqa: E731
@@ -658,7 +703,8 @@ def render_forward(pre, point_list, ranges, cam: Camera, s: Surfels, bg, variant
         semantic = (np.stack([out(Sem[..., c]) for c in range(Sn)]) if Sn
                     else np.zeros((0, H, W), dtype=dtype))
     return dict(final_T=final_T, n_contrib=n_contrib, color=color, others=np.stack(others),
-                semantic=semantic, amb_pixel=out(amb).astype(bool), fragments=frags)
+                semantic=semantic, amb_pixel=out(amb).astype(bool), fragments=frags,
+                signature=out(sig * np.int64(31) + done.astype(np.int64)))
 
 
 def s_surfel_ids(idc):
@@ -694,32 +740,78 @@ def forward_view(s: Surfels, cam: Camera, bg, variant=PLAIN, dtype=np.float64, a
         final_T=rf["final_T"], n_contrib=rf["n_contrib"], color=rf["color"], others=rf["others"],
         semantic=rf["semantic"], amb_surfel=pre["amb"], amb_pixel=rf["amb_pixel"], fragments=rf["fragments"])
     st.extra["pre"] = pre
-    # An ambiguous surfel may or may not sit in the lists of the tiles along
-    # its rectangle's border.  Those tiles' lists (and list positions) are
-    # ambiguous; their pixels are ambiguous only where that surfel can reach
-    # the alpha cut-off.
+    st.extra["signature"] = rf["signature"]
+    # An ambiguous surfel's rectangle may come out one tile larger or
+    # smaller in FP32: the tiles inside some but not all of the rectangles
+    # its radius and centre can round to may or may not list it.  Those
+    # tiles' lists are ambiguous; so are, in them, the pixels the surfel can
+    # reach (alpha at the cut-off) and the pixels whose last contributor
+    # lies after the surfel's place in the list (their contributor count
+    # shifts by one).
     gx, gy = pre["grid"]
-    xmin, ymin, xmax, ymax = pre["rect"]
     amb_tiles = np.zeros((gy, gx), bool)
     f = _f(dtype)
+    last = st.n_contrib[0]
+    shift = np.zeros_like(st.amb_pixel)
     for i in np.nonzero(pre["amb"])[0]:
-        x0, x1 = max(0, xmin[i] - 1), min(gx, max(xmax[i], xmin[i] + 1) + 1)
-        y0, y1 = max(0, ymin[i] - 1), min(gy, max(ymax[i], ymin[i] + 1) + 1)
-        amb_tiles[y0:y1, x0:x1] = True
-        px0, px1 = x0 * BLOCK_X, min(cam.width, x1 * BLOCK_X)
-        py0, py1 = y0 * BLOCK_Y, min(cam.height, y1 * BLOCK_Y)
-        if px1 <= px0 or py1 <= py0:
+        cx, cy = pre["means2D"][i]
+        r_lo = np.ceil(max(pre["rad_in"][i] - pre["rad_err"][i], 0.0))
+        r_hi = np.ceil(pre["rad_in"][i] + pre["rad_err"][i])
+        ex, ey = pre["ctr_err"][i] + 1e-9
+        rects = [_rect(np.array([x]), np.array([y]), np.array([r]), gx, gy, np.float64)
+                 for x in (cx - ex, cx + ex) for y in (cy - ey, cy + ey) for r in (r_lo, r_hi)]
+        R = np.array([[int(c[0]) for c in rc] for rc in rects])       # [8, 4] xmin ymin xmax ymax
+        ux0, uy0, ux1, uy1 = R[:, 0].min(), R[:, 1].min(), R[:, 2].max(), R[:, 3].max()
+        ix0, iy0, ix1, iy1 = R[:, 0].max(), R[:, 1].max(), R[:, 2].min(), R[:, 3].min()
+        band = np.zeros((gy, gx), bool)
+        band[uy0:uy1, ux0:ux1] = True
+        if ix1 > ix0 and iy1 > iy0:
+            band[iy0:iy1, ix0:ix1] = False
+        if not band.any():
             continue
-        yy, xx = np.mgrid[py0:py1, px0:px1]
+        amb_tiles |= band
+        key_i = int(np.float32(pre["depths"][i]).view(np.uint32))
         off = 0.5 if variant == PART else 0.0
         tmi = pre["transmat"][i]
-        res = _intersect(variant, f, xx.astype(f) + f(off), yy.astype(f) + f(off),
-                         tmi[0:3], tmi[3:6], tmi[6:9], pre["means2D"][i])
-        with np.errstate(over="ignore", invalid="ignore"):
-            a = pre["normal_opacity"][i, 3] * np.exp(-0.5 * res[7])
-        st.amb_pixel[py0:py1, px0:px1] |= a >= (1.0 - 1e-3) / 255.0
+        for ty, tx in zip(*np.nonzero(band)):
+            px0, px1 = tx * BLOCK_X, min(cam.width, (tx + 1) * BLOCK_X)
+            py0, py1 = ty * BLOCK_Y, min(cam.height, (ty + 1) * BLOCK_Y)
+            yy, xx = np.mgrid[py0:py1, px0:px1]
+            res = _intersect(variant, f, xx.astype(f) + f(off), yy.astype(f) + f(off),
+                             tmi[0:3], tmi[3:6], tmi[6:9], pre["means2D"][i])
+            with np.errstate(over="ignore", invalid="ignore"):
+                a = pre["normal_opacity"][i, 3] * np.exp(-0.5 * res[7])
+            t = ty * gx + tx
+            lst = st.point_list[st.ranges[t, 0]:st.ranges[t, 1]]
+            dk = pre["depths"][lst].astype(np.float32).view(np.uint32).astype(np.int64)
+            place = int(np.sum((dk < key_i) | ((dk == key_i) & (lst < i))))   # the surfel's list position
+            st.amb_pixel[py0:py1, px0:px1] |= a >= (1.0 - 1e-3) / 255.0
+            shift[py0:py1, px0:px1] |= last[py0:py1, px0:px1] > place
+    st.extra["amb_count_pixel"] = st.amb_pixel | shift
     st.extra["amb_tiles"] = amb_tiles.reshape(-1)
     return st
+
+
+def fp32_sensitivity(st: ViewState, cam: Camera, s: Surfels, bg, variant=PLAIN, trials=2, seed=0):
+    """Per pixel, how far the FP64 blend moves when every surfel's
+    splat-to-pixel matrix and screen centre are rounded by one FP32 unit
+    (relative 2^-23, random signs, ``trials`` draws): [3+others, H, W] of
+    |change| relative to max(1, |value|).  Every FP32 implementation stores
+    those quantities rounded, so where this exceeds a tolerance the
+    algorithm itself is too ill-conditioned in FP32 (nearly edge-on splats,
+    long transmittance products) for two FP32 evaluations to agree to it."""
+    pre = st.extra["pre"]
+    rng = np.random.default_rng(seed)
+    base = np.concatenate([st.color, st.others])
+    worst = np.zeros_like(base)
+    for _ in range(trials):
+        p2 = dict(pre)
+        p2["transmat"] = pre["transmat"] * (1.0 + rng.choice([-1.0, 1.0], pre["transmat"].shape) * 2.0 ** -23)
+        p2["means2D"] = pre["means2D"] * (1.0 + rng.choice([-1.0, 1.0], pre["means2D"].shape) * 2.0 ** -23)
+        rf = render_forward(p2, st.point_list, st.ranges, cam, s, bg, variant, np.float64)
+        out = np.concatenate([rf["color"], rf["others"]])
+        worst = np.maximum(worst, np.abs(out - base) / np.maximum(1.0, np.abs(base)))
+    return worst
 
 
 # --------------------------------------------------------------------------

@@ -18,6 +18,7 @@ ABI_VERSION = 2
 SGR_FLAG_KEY_OVERFLOW = 1
 SGR_FLAG_PREFILTERED = 2
 SGR_FLAG_BIN_OVERFLOW = 4
+SGR_FLAG_LIST_INCONSISTENT = 8
 STATUS_BYTES = 32
 SGR_VARIANT_PLAIN = 0
 SGR_VARIANT_PART = 1
@@ -94,6 +95,12 @@ SIGNATURES = {
                                C.POINTER(BwdOutputs), _p]),
     "sgr_tile_lists": (C.c_int, [C.POINTER(Batch), _p, _p, C.c_int64, _p, C.c_size_t, _p]),
     "sgr_mark_visible": (C.c_int, [_i, _p, _p, _p, _p, _p]),
+    "sgr_status_accumulate": (C.c_int, [_p, _p, _p]),
+    "sgr_radix_sort_temp_bytes": (C.c_size_t, [C.c_int64, C.c_int]),
+    "sgr_radix_sort_pairs": (C.c_int, [_p, _p, _p, _p, C.c_int64, C.c_int, C.c_int, _p, C.c_size_t, _p]),
+    "sgr_prefix_sum_temp_bytes": (C.c_size_t, [C.c_int64, C.c_int]),
+    "sgr_inclusive_sum_u64": (C.c_int, [_p, _p, C.c_int64, _p, C.c_size_t, _p]),
+    "sgr_exclusive_sum_u32": (C.c_int, [_p, _p, C.c_int64, _p, C.c_size_t, _p]),
     "sgr_profile_enable": (C.c_int, [C.c_int]),
     "sgr_profile_read": (C.c_int, [C.POINTER(C.c_float), C.POINTER(C.c_int32)]),
     "sgr_bind_forward": (C.c_int, [C.POINTER(BindArgs), _p, _p, _p, _p, _p]),

@@ -30,11 +30,10 @@ class _MultiViewFn(torch.autograd.Function):
             status_host=cfg.status, cell_tiles=cfg.cell_tiles)
         ctx.state = state
         ctx.cfg = cfg
+        cfg.last_state = state                    # for inspection (bench counters)
         # sticky record of every forward since the last reset: flags OR-ed,
         # largest cell-list entry count (device side, so captured steps keep it)
-        st = state.geom[state.sizes.off_status:state.sizes.off_status + L.STATUS_BYTES]
-        cfg.sticky[0:1].bitwise_or_(st[8:12].view(torch.int32).to(torch.int64))
-        torch.maximum(cfg.sticky[1:2], st[16:24].view(torch.int64), out=cfg.sticky[1:2])
+        cfg.accumulate_status(state)
         ctx.op_shape = opacities.shape
         ctx.has = (shs is not None, colors_precomp is not None, semantics is not None)
         ctx.mark_non_differentiable(radii)
@@ -46,6 +45,7 @@ class _MultiViewFn(torch.autograd.Function):
     def backward(ctx, d_color, d_others, d_semantic, d_radii):
         cfg = ctx.cfg
         g = _r.backward(ctx.state, d_color, d_others, d_semantic if ctx.has[2] else None)
+        cfg.accumulate_status(ctx.state)          # flags the backward raised
         cfg.last_means2D_grad = g["dL_dmeans2D"]
         return (g["dL_dmeans3D"], g["dL_dopacity"].reshape(ctx.op_shape),
                 g["dL_dsh"] if ctx.has[0] else None, g["dL_dscales"], g["dL_drotations"],
@@ -81,6 +81,7 @@ class MultiViewRasterizer:
         self.status = torch.zeros(L.STATUS_BYTES, dtype=torch.uint8).pin_memory()
         self.sticky = torch.zeros(2, dtype=torch.int64, device=dev)   # see sticky_counts()
         self.last_means2D_grad = None
+        self.last_state = None
 
     @property
     def num_views(self):
@@ -97,10 +98,23 @@ class MultiViewRasterizer:
             self.sticky.zero_()
         return flags, most
 
+    def accumulate_status(self, state):
+        """Folds the status word of ``state``'s workspace into ``self.sticky``
+        (one library kernel on the current stream)."""
+        lib = L.load()
+        st = state.geom[state.sizes.off_status:state.sizes.off_status + L.STATUS_BYTES]
+        L.check(lib.sgr_status_accumulate(st.data_ptr(), self.sticky.data_ptr(), _r._stream()),
+                "sgr_status_accumulate")
+
     def counts(self):
         """(key count, flags, cell-list entry count) of the last forward;
         valid once the stream has passed that forward."""
         return _r.read_status(self.status)
+
+    def fragments(self):
+        """(pixel, list entry) pairs the last forward visited; valid once the
+        stream has passed that forward."""
+        return _r.read_fragments(self.status)
 
     def __call__(self, means3D, opacities, shs=None, scales=None, rotations=None, colors_precomp=None,
                  semantics=None):

@@ -20,7 +20,7 @@ OUT = HERE / "_lib"
 LIB = OUT / "libsgr.so"
 SOURCES = ["sgr_api.cu", "sgr_forward.cu", "sgr_blend.cu", "sgr_binning.cu", "sgr_backward.cu", "sgr_bind.cu",
            "sgr_loss.cu", "sgr_adam.cu", "sgr_mlp.cu", "sgr_activate.cu",
-           "sgr_eval.cu", "sgr_sq.cu", "sgr_densify.cu"]
+           "sgr_eval.cu", "sgr_sq.cu", "sgr_densify.cu", "sgr_sort.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

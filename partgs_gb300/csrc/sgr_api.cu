@@ -1,7 +1,5 @@
 // C ABI of the surfel rasteriser: argument checks, workspace layout and the
 // launch sequence of each phase.
-#include <cub/device/device_radix_sort.cuh>
-#include <cub/device/device_scan.cuh>
 
 #include <atomic>
 #include <cstdio>
@@ -93,14 +91,8 @@ int scratch_layout(const sgr_batch* b, long long cap, ScratchLayout& L) {
   L.depth_keys = o; o = align_up(o + R * 8);
   L.depth_vals = o; o = align_up(o + R * 4);
   L.depth_keys_sorted = o; o = align_up(o + R * 8);
-  size_t sort_a = 0, scan_a = 0;
-  if (R > 0) {
-    SGR_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, sort_a, (const unsigned long long*)nullptr,
-                                             (unsigned long long*)nullptr, (const uint32_t*)nullptr,
-                                             (uint32_t*)nullptr, (int64_t)R, 0, depth_key_bits(b)));
-    SGR_CUDA(cub::DeviceScan::InclusiveSum(nullptr, scan_a, (unsigned long long*)nullptr,
-                                           (unsigned long long*)nullptr, (int64_t)R));
-  }
+  const size_t sort_a = radix_sort_temp_bytes<unsigned long long>((long long)R);
+  const size_t scan_a = scan_temp_bytes<unsigned long long>((long long)R);
   L.temp_a = o;
   L.temp_a_bytes = std::max(sort_a, scan_a);
   o = align_up(o + L.temp_a_bytes);
@@ -187,6 +179,12 @@ int check_cap(long long cap) {
   return SGR_OK;
 }
 
+__global__ void k_status_accumulate(const Status* status, long long* sticky) {
+  sticky[0] |= (long long)status->flags;
+  const long long n = (long long)status->num_bin_entries;
+  if (n > sticky[1]) sticky[1] = n;
+}
+
 }  // namespace
 
 void count_launches(int n) { g_launches.fetch_add((unsigned long long)n, std::memory_order_relaxed); }
@@ -246,14 +244,14 @@ int sgr_forward_geometry(const sgr_batch* batch, void* geom, void* fwd_scratch, 
     }
     SGR_CUDA(cudaGetLastError());
     PhaseScope ph(SGR_PHASE_DEPTH_ORDER, st);
-    size_t tb = L.temp_a_bytes;
     char* sp = static_cast<char*>(fwd_scratch);
-    SGR_CUDA(cub::DeviceRadixSort::SortPairs(sp + L.temp_a, tb, g.depth_keys, g.depth_keys_sorted, g.depth_vals,
-                                             g.depth_order, (int64_t)R, 0, depth_key_bits(batch), st));
+    if ((rc = radix_sort_pairs<unsigned long long>(g.depth_keys, g.depth_keys_sorted, g.depth_vals, g.depth_order, R,
+                                                   depth_key_bits(batch), sp + L.temp_a, L.temp_a_bytes, st)))
+      return rc == SGR_ERR_CUDA ? cuda_fail(cudaGetLastError(), "depth sort") : rc;
     launch_gather_rects(g, R, st);
     SGR_CUDA(cudaGetLastError());
-    tb = L.temp_a_bytes;
-    SGR_CUDA(cub::DeviceScan::InclusiveSum(sp + L.temp_a, tb, g.offsets, g.offsets, (int64_t)R, st));
+    if ((rc = prefix_sum<unsigned long long, true>(g.offsets, g.offsets, R, sp + L.temp_a, L.temp_a_bytes, st)))
+      return rc == SGR_ERR_CUDA ? cuda_fail(cudaGetLastError(), "key offsets") : rc;
     launch_store_key_count(g, R, st);
     SGR_CUDA(cudaGetLastError());
   }
@@ -368,6 +366,15 @@ int sgr_profile_enable(int enable) {
 }
 
 int sgr_profile_read(float* ms, int32_t* count) { return PhaseTimer::get().read(ms, count); }
+
+int sgr_status_accumulate(const void* status, int64_t* sticky, void* stream) {
+  if (!status || !sticky) return SGR_ERR_INVALID_ARGUMENT;
+  k_status_accumulate<<<1, 1, 0, static_cast<cudaStream_t>(stream)>>>(static_cast<const sgr::Status*>(status),
+                                                                       reinterpret_cast<long long*>(sticky));
+  sgr::count_launches(1);
+  SGR_CUDA(cudaGetLastError());
+  return SGR_OK;
+}
 
 int sgr_mark_visible(int32_t P, const float* means3D, const float* viewmatrix, const float* projmatrix,
                      uint8_t* present, void* stream) {

@@ -13,8 +13,10 @@
 // its N surfels; the backward scatters triangle-vertex gradients into a
 // per-vertex buffer, and one CTA per superquadric reduces its vertices'
 // contributions without atomics.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
+#include <climits>
 #include <mutex>
 #include <string>
 
@@ -398,6 +400,11 @@ thread_local std::string g_bind_error;
 
 int check_args(const sgr_bind_args* a) {
   if (!a || a->B < 0 || a->V < 0 || a->F < 0 || a->N < 0) return SGR_ERR_INVALID_ARGUMENT;
+  // surfel, face and vertex indices are 32-bit in the kernels
+  if ((long long)a->B * a->F * (a->N > 0 ? a->N : 1) > INT_MAX || (long long)a->B * a->V * 3 > INT_MAX) {
+    sgr::set_last_error("superquadric binding: more than 2^31 - 1 surfels, faces or vertex coordinates");
+    return SGR_ERR_UNSUPPORTED;
+  }
   if (a->B > 0 && (!a->sq_s || !a->sq_r || !a->sq_t || !a->sq_eps || !a->sq_occ)) return SGR_ERR_INVALID_ARGUMENT;
   if ((size_t)a->B * a->F > 0 && (!a->eta || !a->omega || !a->faces || !a->alpha || !a->scale))
     return SGR_ERR_INVALID_ARGUMENT;
@@ -417,9 +424,40 @@ static __device__ __align__(256) unsigned char g_bind_static_scratch[kBindStatic
 
 std::mutex g_static_mu;
 void* g_static_ptr[kMaxDevices] = {};
+unsigned long long g_static_ctx[kMaxDevices] = {};   // id of the context the address belongs to
 
-// Device address of the array on the current device, looked up once per
-// device with that device current.
+// Id of the current device's current context, through the driver entry
+// points the runtime hands out (so the library does not link libcuda).
+int current_context_id(unsigned long long* id) {
+  using get_current_fn = CUresult (*)(CUcontext*);
+  using get_id_fn = CUresult (*)(CUcontext, unsigned long long*);
+  static get_current_fn get_current = nullptr;
+  static get_id_fn get_id = nullptr;
+  if (!get_current || !get_id) {
+    void* f0 = nullptr;
+    void* f1 = nullptr;
+    cudaDriverEntryPointQueryResult q0, q1;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f0, 12000, cudaEnableDefault, &q0) != cudaSuccess ||
+        cudaGetDriverEntryPointByVersion("cuCtxGetId", &f1, 12000, cudaEnableDefault, &q1) != cudaSuccess ||
+        q0 != cudaDriverEntryPointSuccess || q1 != cudaDriverEntryPointSuccess || !f0 || !f1) {
+      sgr::set_last_error("sgr_bind_backward_static: the driver does not provide cuCtxGetCurrent / cuCtxGetId");
+      return SGR_ERR_CUDA;
+    }
+    get_current = reinterpret_cast<get_current_fn>(f0);
+    get_id = reinterpret_cast<get_id_fn>(f1);
+  }
+  CUcontext ctx = nullptr;
+  if (get_current(&ctx) != CUDA_SUCCESS || !ctx || get_id(ctx, id) != CUDA_SUCCESS) {
+    sgr::set_last_error("sgr_bind_backward_static: no current CUDA context");
+    return SGR_ERR_CUDA;
+  }
+  return SGR_OK;
+}
+
+// Device address of the array on the current device, looked up with that
+// device current: once per device, and again when the device's context has
+// changed since (after cudaDeviceReset the module is loaded anew and the
+// array may sit elsewhere).
 int static_scratch(void** out) {
   int dev = -1;
   cudaError_t e = cudaGetDevice(&dev);
@@ -431,8 +469,16 @@ int static_scratch(void** out) {
     sgr::set_last_error("sgr_bind_backward_static: device ordinal beyond the supported 64");
     return SGR_ERR_UNSUPPORTED;
   }
+  // make the device's primary context current (initialised) before asking for it
+  if ((e = cudaSetDevice(dev)) != cudaSuccess) {
+    sgr::set_last_error(std::string("cudaSetDevice: ") + cudaGetErrorString(e));
+    return SGR_ERR_CUDA;
+  }
+  unsigned long long ctx = 0;
+  int rc = current_context_id(&ctx);
+  if (rc) return rc;
   std::lock_guard<std::mutex> lock(g_static_mu);
-  if (!g_static_ptr[dev]) {
+  if (!g_static_ptr[dev] || g_static_ctx[dev] != ctx) {
     void* p = nullptr;
     e = cudaGetSymbolAddress(&p, g_bind_static_scratch);
     if (e != cudaSuccess || !p) {
@@ -440,6 +486,7 @@ int static_scratch(void** out) {
       return SGR_ERR_CUDA;
     }
     g_static_ptr[dev] = p;
+    g_static_ctx[dev] = ctx;
   }
   *out = g_static_ptr[dev];
   return SGR_OK;
@@ -455,7 +502,7 @@ int sgr_bind_forward(const sgr_bind_args* a, float* xyz, float* log_scaling, flo
                      void* stream) {
   int rc = check_args(a);
   if (rc) return rc;
-  const int n = a->B * a->F;
+  const int n = (int)((long long)a->B * a->F);   // at most INT_MAX (check_args)
   if (n == 0 || a->N == 0) return SGR_OK;
   k_bind_forward<<<(n + 127) / 128, 128, 0, static_cast<cudaStream_t>(stream)>>>(*a, xyz, log_scaling, rotation,
                                                                                   opacity);
@@ -481,7 +528,7 @@ int sgr_bind_backward(const sgr_bind_args* a, const float* d_xyz, const float* d
   const size_t dv = ((size_t)a->B * a->V * 3 * 4 + 255) & ~(size_t)255;
   float* dop_face = reinterpret_cast<float*>(static_cast<char*>(scratch) + dv);
   if (cudaMemsetAsync(scratch, 0, sgr_bind_scratch_bytes(a), st) != cudaSuccess) return SGR_ERR_CUDA;
-  const int n = a->B * a->F;
+  const int n = (int)((long long)a->B * a->F);   // at most INT_MAX (check_args)
   if (n > 0 && a->N > 0) {
     k_bind_backward_faces<<<(n + 127) / 128, 128, 0, st>>>(*a, d_xyz, d_log_scaling, d_rotation, d_opacity, dvert,
                                                             dop_face);

@@ -35,7 +35,6 @@
 // With one-tile cells and record ids as entries, the same kernels write the
 // reference's exact per-tile lists and [start, end) ranges; that form is
 // kept for inspection and tests (sgr_tile_lists).
-#include <cub/device/device_scan.cuh>
 
 #include "sgr_kernels.cuh"
 
@@ -217,7 +216,13 @@ __global__ void k_cell_ranges(CellArgs a) {
   const unsigned long long s = a.cell_start[t], e = s + a.cell_count[t];
   const unsigned long long cap = (unsigned long long)a.capacity;
   if (a.ranges) a.ranges[t] = make_uint2((uint32_t)min(s, cap), (uint32_t)min(e, cap));
-  if (t == n - 1 && e > cap) atomicOr(&a.status->flags, a.overflow_flag);
+  // the 32-bit scan wraps past 2^32 entries: also test the exact 64-bit total
+  // the geometry phase counted
+  if (t == n - 1) {
+    const unsigned long long total =
+        a.overflow_flag == SGR_FLAG_KEY_OVERFLOW ? a.status->num_keys : a.status->num_bin_entries;
+    if (e > cap || total > cap) atomicOr(&a.status->flags, a.overflow_flag);
+  }
 }
 
 // 3. stable scatter of each chunk's records into the cell lists
@@ -307,8 +312,7 @@ CellScratch cell_scratch(long long R, int V, int ncell, bool own_counts) {
     s.count = o; o = al(o + cells * 4);
     s.start = o; o = al(o + cells * 4);
   }
-  size_t tb = 0;
-  cub::DeviceScan::ExclusiveSum(nullptr, tb, (uint32_t*)nullptr, (uint32_t*)nullptr, (int64_t)cells);
+  const size_t tb = scan_temp_bytes<uint32_t>((long long)cells);
   s.temp = o;
   s.temp_bytes = tb;
   o = al(o + tb);
@@ -358,8 +362,7 @@ int run_cells(const sgr_batch& b, const GeomView& g, int B, bool ids, uint32_t* 
   count_launches();
   k_cell_scan<<<(unsigned)((ncells + 255) / 256), 256, 0, st>>>(a);
   count_launches();
-  size_t tb = L.temp_bytes;
-  if (cub::DeviceScan::ExclusiveSum(sp + L.temp, tb, a.cell_count, a.cell_start, (int64_t)ncells, st) != cudaSuccess)
+  if (prefix_sum<uint32_t, false>(a.cell_count, a.cell_start, ncells, sp + L.temp, L.temp_bytes, st) != SGR_OK)
     return SGR_ERR_CUDA;
   k_cell_ranges<<<(unsigned)((ncells + 255) / 256), 256, 0, st>>>(a);
   count_launches();

@@ -336,6 +336,7 @@ struct FwdPixel {
   float C[3], N[3];
   float D, M1, M2, dist, med_depth, med_weight;
   int med_contrib;
+  uint32_t stop;   // list position (1-based) of the entry that ended the pixel, 0 while open
 };
 
 // One fragment of the forward for one pixel: entry j of the staged batch,
@@ -374,6 +375,7 @@ __device__ __forceinline__ void fwd_fragment(FwdPixel<VARIANT>& q, const float4 
   const float test_T = q.T * (1 - alpha);
   if (test_T < 0.0001f) {
     q.done = true;
+    q.stop = contributor;
     return;
   }
   const float4 r3 = s_rec[3][j], r4 = s_rec[4][j];
@@ -492,6 +494,7 @@ __global__ void __launch_bounds__(FwdShape::NT, (VARIANT == SGR_VARIANT_PLAIN) ?
     for (int c = 0; c < 3; ++c) Q.C[c] = Q.N[c] = 0.f;
     Q.D = Q.M1 = Q.M2 = Q.dist = Q.med_depth = Q.med_weight = 0.f;
     Q.med_contrib = -1;
+    Q.stop = 0;
     if (VARIANT == SGR_VARIANT_PART)
       for (int g4 = 0; g4 < (S + 3) / 4; ++g4) sem_acc4[g4 * NT] = make_float4(0.f, 0.f, 0.f, 0.f);
     done = done && Q.done;
@@ -540,6 +543,20 @@ __global__ void __launch_bounds__(FwdShape::NT, (VARIANT == SGR_VARIANT_PLAIN) ?
   }
 
   if (threadIdx.x == 0) g.tile_resume[tile] = make_uint2((uint32_t)scanned, (uint32_t)tail);
+  {
+    // fragments the reference's blend visits here: per pixel, the list
+    // entries up to the one that ended it, or the whole list
+    unsigned long long visited = 0;
+#pragma unroll
+    for (int i = 0; i < PX; ++i) {
+      int px, py;
+      pixel_of<Shape>(tx, ty, lane, warp, i, px, py);
+      if (px < W && py < H) visited += q[i].stop ? q[i].stop : (uint32_t)tail;
+    }
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1) visited += __shfl_xor_sync(0xffffffffu, visited, o);
+    if (lane == 0 && visited) atomicAdd(&g.status->num_fragments, visited);
+  }
   const size_t HW = (size_t)H * W;
   const float* bg = b.background;
   const int NO = (VARIANT == SGR_VARIANT_PLAIN) ? 7 : 8;
@@ -905,7 +922,10 @@ __global__ void __launch_bounds__(BwdShape<VARIANT>::NT,
       scan_end = i0;
     }
     const int n = min(kBlock, hi);
-    if (tail - head < n) break;                    // index inconsistent with the rectangles: stop
+    if (tail - head < n) {                         // index inconsistent with the rectangles: stop
+      if (threadIdx.x == 0) atomicOr(&g.status->flags, SGR_FLAG_LIST_INCONSISTENT);
+      break;
+    }
     __syncthreads();
     for (int e = threadIdx.x; e < n; e += NT) {
       const uint32_t r = s_ring[(head + e) & (kRing - 1)];

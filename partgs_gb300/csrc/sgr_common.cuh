@@ -191,7 +191,7 @@ struct Status {
   unsigned int flags;                   // SGR_FLAG_*
   unsigned int pad;
   unsigned long long num_bin_entries;   // (record, cell) pairs: the entries of the cell lists
-  unsigned long long pad2;
+  unsigned long long num_fragments;     // (pixel, list entry) pairs the forward blend visits
 };
 
 }  // namespace sgr

@@ -33,8 +33,6 @@
 // by packed cell key (CUB), 27 cells searched by binary search.  Each round
 // synchronises the host to read the count of undecided points; this is an
 // evaluation path, not part of the training step.
-#include <cub/device/device_radix_sort.cuh>
-#include <cub/device/device_scan.cuh>
 
 #include <cuda_runtime.h>
 
@@ -43,6 +41,7 @@
 #include <cstdint>
 
 #include "../../include/sgr.h"
+#include "sgr_sort.cuh"
 
 namespace sgr {
 void count_launches(int n);   // sgr_api.cu
@@ -331,11 +330,8 @@ NNLayout nn_layout(long long n, long long m, long long cells, long long cells2) 
   L.n_open = o; o = al(o + 4);
   L.open2 = o; o = al(o + n * 4);
   L.n_open2 = o; o = al(o + 4);
-  size_t ts = 0, tr = 0;
-  cub::DeviceScan::ExclusiveSum(nullptr, ts, (uint32_t*)nullptr, (uint32_t*)nullptr,
-                                (int64_t)((cells > cells2 ? cells : cells2) + 1));
-  cub::DeviceRadixSort::SortPairs(nullptr, tr, (const uint32_t*)nullptr, (uint32_t*)nullptr, (const int*)nullptr,
-                                  (int*)nullptr, (int64_t)n, 0, 32);
+  const size_t ts = sgr::scan_temp_bytes<uint32_t>((long long)((cells > cells2 ? cells : cells2) + 1));
+  const size_t tr = sgr::radix_sort_temp_bytes<uint32_t>((long long)n);
   L.temp = o;
   L.temp_bytes = ts > tr ? ts : tr;
   o = al(o + L.temp_bytes);
@@ -448,9 +444,7 @@ DSLayout ds_layout(long long n) {
   L.state_a = o; o = al(o + n);
   L.state_b = o; o = al(o + n);
   L.count = o; o = al(o + 8);
-  size_t tb = 0;
-  cub::DeviceRadixSort::SortPairs(nullptr, tb, (const unsigned long long*)nullptr, (unsigned long long*)nullptr,
-                                  (const int*)nullptr, (int*)nullptr, (int64_t)n, 0, 63);
+  const size_t tb = sgr::radix_sort_temp_bytes<unsigned long long>((long long)n);
   L.temp = o;
   L.temp_bytes = tb;
   o = al(o + tb);
@@ -519,21 +513,19 @@ int sgr_nn_search_grid(const float* q, int64_t n, const float* r, int64_t m, con
       cudaMemsetAsync(start2, 0, (cells2 + 1) * 4, st) != cudaSuccess ||
       cudaMemsetAsync(cursor2, 0, cells2 * 4, st) != cudaSuccess || cudaMemsetAsync(n_open2, 0, 4, st) != cudaSuccess)
     return SGR_ERR_CUDA;
-  size_t tb;
   for (int level = 0; level < 2; ++level) {   // both grids: count, scan, scatter
     const NNGrid& gl = level ? g2 : g;
     uint32_t* sl = level ? start2 : start;
     k_grid_count<<<mb, 256, 0, st>>>(r, m, gl, sl);
-    tb = L.temp_bytes;
-    if (cub::DeviceScan::ExclusiveSum(sp + L.temp, tb, sl, sl, (int64_t)((level ? cells2 : cells) + 1), st) !=
-        cudaSuccess)
+    if (sgr::prefix_sum<uint32_t, false>(sl, sl, (long long)((level ? cells2 : cells) + 1), sp + L.temp, L.temp_bytes,
+                                         st) != SGR_OK)
       return SGR_ERR_CUDA;
     k_grid_scatter<<<mb, 256, 0, st>>>(r, m, gl, sl, level ? cursor2 : cursor, level ? pts2 : pts);
   }
   k_query_cells<<<nb, 256, 0, st>>>(q, n, g, keys, ids);
-  tb = L.temp_bytes;
-  if (cub::DeviceRadixSort::SortPairs(sp + L.temp, tb, keys, keys_sorted, ids, ids_sorted, (int64_t)n, 0,
-                                      key_bits(cells), st) != cudaSuccess)
+  if (sgr::radix_sort_pairs<uint32_t>(keys, keys_sorted, reinterpret_cast<const uint32_t*>(ids),
+                                      reinterpret_cast<uint32_t*>(ids_sorted), (long long)n, key_bits(cells),
+                                      sp + L.temp, L.temp_bytes, st) != SGR_OK)
     return SGR_ERR_CUDA;
   k_nn_grid<<<nb, 256, 0, st>>>(q, ids_sorted, n, nullptr, g, start, pts, dist, idx, open, n_open);
   // the open queries (count known only on the device): blocks past it return at once
@@ -570,9 +562,9 @@ int sgr_radius_downsample(const double* pts, int64_t n, const double* lo, const 
   const unsigned blocks = (unsigned)((n + 255) / 256);
   k_cell_keys<<<blocks, 256, 0, st>>>(pts, n, lo3, inv, keys, ids);
   sgr::count_launches(1);
-  size_t tb = L.temp_bytes;
-  if (cub::DeviceRadixSort::SortPairs(sp + L.temp, tb, keys, keys_sorted, ids, ids_sorted, (int64_t)n, 0, 63, st) !=
-      cudaSuccess)
+  if (sgr::radix_sort_pairs<unsigned long long>(keys, keys_sorted, reinterpret_cast<const uint32_t*>(ids),
+                                                reinterpret_cast<uint32_t*>(ids_sorted), (long long)n, 63,
+                                                sp + L.temp, L.temp_bytes, st) != SGR_OK)
     return SGR_ERR_CUDA;
   if (cudaMemsetAsync(sa, 0, n, st) != cudaSuccess) return SGR_ERR_CUDA;
   // Every round decides at least the lowest-index undecided point (its

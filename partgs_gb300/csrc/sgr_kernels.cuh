@@ -3,6 +3,7 @@
 #pragma once
 
 #include "sgr_common.cuh"
+#include "sgr_sort.cuh"
 
 namespace sgr {
 

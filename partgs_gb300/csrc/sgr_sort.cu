@@ -1,0 +1,388 @@
+// Stable LSD radix sort of (key, record id) pairs and prefix sums, the
+// depth order and the offset / cell scans of the forward
+// (replacing the library sort and scans the reference calls,
+// cuda_rasterizer/rasterizer_impl.cu:278, 304-309).
+//
+// Sort: 8-bit digits, one pass per digit of bits [0, end_bit).  Each pass is
+// three kernels:
+//   1. k_radix_hist: per 2048-key tile, the 256-bin digit histogram, stored
+//      digit-major (hist[digit][tile]);
+//   2. k_radix_scan: per digit, the exclusive scan of its counts over the
+//      tiles, and the digit's total;
+//   3. k_radix_scatter: per tile, every key's rank among the tile's keys of
+//      its digit in input order (warp match + per-warp counts, round by
+//      round), the tile reordered by (digit, rank) in shared memory, then
+//      written out in digit runs: out[digit base + tile prefix + rank].
+// Equal digits keep their input order in every pass, so the result is the
+// stable order of the keys (ties by input position), the order of any
+// stable radix sort of the same bits.
+//
+// Scans: a 2048-element tile per CTA; per-tile sums, one CTA scanning those,
+// then each tile's scan plus its prefix.
+#include "sgr_kernels.cuh"
+
+namespace sgr {
+
+namespace {
+
+constexpr int kSortThreads = 256;
+constexpr int kSortItems = 8;
+constexpr int kSortTile = kSortThreads * kSortItems;   // 2048 keys per CTA
+constexpr int kBins = 256;
+constexpr int kSortWarps = kSortThreads / 32;
+
+inline long long tiles_of(long long n) { return (n + kSortTile - 1) / kSortTile; }
+
+template <class K>
+__device__ __forceinline__ uint32_t digit_of(K key, int shift) {
+  return (uint32_t)((key >> shift) & (K)(kBins - 1));
+}
+
+// Exclusive scan of one value per thread over a 256-thread CTA; returns the
+// CTA total in `total`.  Uses s_warp[kSortWarps].
+template <class T>
+__device__ __forceinline__ T block_exclusive_scan(T v, T* s_warp, T& total) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  T incl = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const T y = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += y;
+  }
+  if (lane == 31) s_warp[warp] = incl;
+  __syncthreads();
+  T before = 0, all = 0;
+#pragma unroll
+  for (int w = 0; w < kSortWarps; ++w) {
+    const T x = s_warp[w];
+    if (w < warp) before += x;
+    all += x;
+  }
+  __syncthreads();
+  total = all;
+  return before + incl - v;
+}
+
+template <class K>
+__global__ void __launch_bounds__(kSortThreads) k_radix_hist(const K* __restrict__ keys, long long n, int shift,
+                                                             uint32_t* __restrict__ hist, long long ntiles) {
+  __shared__ uint32_t s_cnt[kBins];
+  s_cnt[threadIdx.x] = 0;
+  __syncthreads();
+  const long long base = (long long)blockIdx.x * kSortTile;
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int k = 0; k < kSortItems; ++k) {
+    const long long i = base + k * kSortThreads + threadIdx.x;
+    const bool valid = i < n;
+    const uint32_t d = valid ? digit_of(keys[i], shift) : (uint32_t)kBins;
+    const unsigned peers = __match_any_sync(0xffffffffu, d);
+    if (valid && lane == __ffs(peers) - 1) atomicAdd(&s_cnt[d], (uint32_t)__popc(peers));
+  }
+  __syncthreads();
+  hist[(size_t)threadIdx.x * ntiles + blockIdx.x] = s_cnt[threadIdx.x];
+}
+
+// One CTA per digit: exclusive scan of its per-tile counts, in place.
+__global__ void __launch_bounds__(kSortThreads) k_radix_scan(uint32_t* __restrict__ hist, long long ntiles,
+                                                             uint32_t* __restrict__ totals) {
+  __shared__ uint32_t s_warp[kSortWarps];
+  uint32_t* h = hist + (size_t)blockIdx.x * ntiles;
+  uint32_t carry = 0;
+  for (long long c = 0; c < ntiles; c += kSortThreads) {
+    const long long i = c + threadIdx.x;
+    const uint32_t v = i < ntiles ? h[i] : 0u;
+    uint32_t tot;
+    const uint32_t ex = block_exclusive_scan<uint32_t>(v, s_warp, tot);
+    if (i < ntiles) h[i] = carry + ex;
+    carry += tot;
+  }
+  if (threadIdx.x == 0) totals[blockIdx.x] = carry;
+}
+
+template <class K>
+__global__ void __launch_bounds__(kSortThreads) k_radix_scatter(const K* __restrict__ keys_in,
+                                                                const uint32_t* __restrict__ vals_in,
+                                                                K* __restrict__ keys_out,
+                                                                uint32_t* __restrict__ vals_out, long long n,
+                                                                int shift, const uint32_t* __restrict__ hist,
+                                                                const uint32_t* __restrict__ totals,
+                                                                long long ntiles) {
+  __shared__ K s_keys[kSortTile];
+  __shared__ uint32_t s_vals[kSortTile];
+  __shared__ uint32_t s_wc[kSortWarps][kBins];     // this round's count of each digit per warp
+  __shared__ uint32_t s_run[kBins];                // keys of each digit ranked so far
+  __shared__ uint32_t s_local[kBins];              // start of each digit in the tile's order
+  __shared__ unsigned long long s_gbase[kBins];    // output position of the tile's first key of each digit
+  __shared__ unsigned long long s_warp64[kSortWarps];
+  __shared__ uint32_t s_warp32[kSortWarps];
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  const long long base = (long long)blockIdx.x * kSortTile;
+
+  // global start of digit t: all smaller digits, then the tiles before this one
+  {
+    unsigned long long tot;
+    const unsigned long long ex = block_exclusive_scan<unsigned long long>(totals[t], s_warp64, tot);
+    s_gbase[t] = ex + hist[(size_t)t * ntiles + blockIdx.x];
+  }
+  K key[kSortItems];
+  uint32_t val[kSortItems], dig[kSortItems];
+  s_run[t] = 0;
+#pragma unroll
+  for (int w = 0; w < kSortWarps; ++w) s_wc[w][t] = 0;
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < kSortItems; ++k) {
+    const long long i = base + k * kSortThreads + t;
+    const bool valid = i < n;
+    key[k] = valid ? keys_in[i] : (K)0;
+    val[k] = valid ? vals_in[i] : 0u;
+    dig[k] = valid ? digit_of(key[k], shift) : (uint32_t)kBins;
+    const unsigned peers = __match_any_sync(0xffffffffu, dig[k]);
+    if (valid && lane == __ffs(peers) - 1) atomicAdd(&s_run[dig[k]], (uint32_t)__popc(peers));
+  }
+  __syncthreads();
+  {
+    uint32_t tot;
+    const uint32_t cnt = s_run[t];
+    s_local[t] = block_exclusive_scan<uint32_t>(cnt, s_warp32, tot);
+    s_run[t] = 0;
+  }
+  __syncthreads();
+  uint32_t pos[kSortItems];
+#pragma unroll
+  for (int k = 0; k < kSortItems; ++k) {
+    const uint32_t d = dig[k];
+    const unsigned peers = __match_any_sync(0xffffffffu, d);
+    const uint32_t lrank = __popc(peers & ((1u << lane) - 1u));
+    if (d < kBins && lrank == 0) s_wc[warp][d] = __popc(peers);
+    __syncthreads();
+    if (d < kBins) {
+      uint32_t before = s_run[d];
+      for (int w = 0; w < warp; ++w) before += s_wc[w][d];
+      pos[k] = s_local[d] + before + lrank;
+    }
+    __syncthreads();
+    {
+      uint32_t add = 0;
+#pragma unroll
+      for (int w = 0; w < kSortWarps; ++w) {
+        add += s_wc[w][t];
+        s_wc[w][t] = 0;
+      }
+      s_run[t] += add;
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int k = 0; k < kSortItems; ++k) {
+    if (dig[k] < kBins) {
+      s_keys[pos[k]] = key[k];
+      s_vals[pos[k]] = val[k];
+    }
+  }
+  __syncthreads();
+  const int count = (int)min((long long)kSortTile, n - base);
+  for (int s = t; s < count; s += kSortThreads) {
+    const K kv = s_keys[s];
+    const uint32_t d = digit_of(kv, shift);
+    const unsigned long long dst = s_gbase[d] + (unsigned long long)(s - (int)s_local[d]);
+    keys_out[dst] = kv;
+    vals_out[dst] = s_vals[s];
+  }
+}
+
+// ---- scans ------------------------------------------------------------------
+
+template <class T>
+__global__ void __launch_bounds__(kSortThreads) k_scan_reduce(const T* __restrict__ in, long long n,
+                                                              T* __restrict__ partials) {
+  __shared__ T s_warp[kSortWarps];
+  const long long base = (long long)blockIdx.x * kSortTile;
+  T sum = 0;
+#pragma unroll
+  for (int k = 0; k < kSortItems; ++k) {
+    const long long i = base + k * kSortThreads + threadIdx.x;
+    if (i < n) sum += in[i];
+  }
+  T tot;
+  block_exclusive_scan<T>(sum, s_warp, tot);
+  if (threadIdx.x == 0) partials[blockIdx.x] = tot;
+}
+
+template <class T>
+__global__ void __launch_bounds__(kSortThreads) k_scan_partials(T* __restrict__ partials, long long ntiles) {
+  __shared__ T s_warp[kSortWarps];
+  T carry = 0;
+  for (long long c = 0; c < ntiles; c += kSortThreads) {
+    const long long i = c + threadIdx.x;
+    const T v = i < ntiles ? partials[i] : (T)0;
+    T tot;
+    const T ex = block_exclusive_scan<T>(v, s_warp, tot);
+    if (i < ntiles) partials[i] = carry + ex;
+    carry += tot;
+  }
+}
+
+// Each thread owns kSortItems consecutive elements of the tile.
+template <class T, bool INCLUSIVE>
+__global__ void __launch_bounds__(kSortThreads) k_scan_apply(const T* in, T* out, long long n,
+                                                             const T* __restrict__ partials) {
+  __shared__ T s_tile[kSortTile];
+  __shared__ T s_warp[kSortWarps];
+  const long long base = (long long)blockIdx.x * kSortTile;
+#pragma unroll
+  for (int k = 0; k < kSortItems; ++k) {
+    const long long i = base + k * kSortThreads + threadIdx.x;
+    s_tile[k * kSortThreads + threadIdx.x] = i < n ? in[i] : (T)0;
+  }
+  __syncthreads();
+  T v[kSortItems];
+  T run = 0;
+#pragma unroll
+  for (int k = 0; k < kSortItems; ++k) {
+    v[k] = s_tile[threadIdx.x * kSortItems + k];
+    run += v[k];
+  }
+  T tot;
+  T pre = block_exclusive_scan<T>(run, s_warp, tot) + partials[blockIdx.x];
+#pragma unroll
+  for (int k = 0; k < kSortItems; ++k) {
+    const T x = v[k];
+    if (INCLUSIVE) pre += x;
+    s_tile[threadIdx.x * kSortItems + k] = pre;
+    if (!INCLUSIVE) pre += x;
+  }
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < kSortItems; ++k) {
+    const long long i = base + k * kSortThreads + threadIdx.x;
+    if (i < n) out[i] = s_tile[k * kSortThreads + threadIdx.x];
+  }
+}
+
+size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+}  // namespace
+
+template <class K>
+size_t radix_sort_temp_bytes(long long n) {
+  if (n <= 0) return 0;
+  const long long nt = tiles_of(n);
+  return align256((size_t)n * sizeof(K)) + align256((size_t)n * 4) + align256((size_t)kBins * nt * 4) +
+         align256((size_t)kBins * 4);
+}
+
+template <class K>
+int radix_sort_pairs(const K* keys_in, K* keys_out, const uint32_t* vals_in, uint32_t* vals_out, long long n,
+                     int end_bit, void* temp, size_t temp_bytes, cudaStream_t st) {
+  if (n <= 0) return SGR_OK;
+  if (temp_bytes < radix_sort_temp_bytes<K>(n) || !temp) return SGR_ERR_WORKSPACE;
+  const long long nt = tiles_of(n);
+  char* p = static_cast<char*>(temp);
+  K* alt_keys = reinterpret_cast<K*>(p);
+  p += align256((size_t)n * sizeof(K));
+  uint32_t* alt_vals = reinterpret_cast<uint32_t*>(p);
+  p += align256((size_t)n * 4);
+  uint32_t* hist = reinterpret_cast<uint32_t*>(p);
+  p += align256((size_t)kBins * nt * 4);
+  uint32_t* totals = reinterpret_cast<uint32_t*>(p);
+  const int passes = (end_bit + 7) / 8;
+  const K* src_k = keys_in;
+  const uint32_t* src_v = vals_in;
+  for (int pass = 0; pass < passes; ++pass) {
+    // the last pass lands in the output buffers
+    const bool to_out = ((passes - 1 - pass) % 2) == 0;
+    K* dst_k = to_out ? keys_out : alt_keys;
+    uint32_t* dst_v = to_out ? vals_out : alt_vals;
+    const int shift = 8 * pass;
+    k_radix_hist<K><<<(unsigned)nt, kSortThreads, 0, st>>>(src_k, n, shift, hist, nt);
+    k_radix_scan<<<kBins, kSortThreads, 0, st>>>(hist, nt, totals);
+    k_radix_scatter<K><<<(unsigned)nt, kSortThreads, 0, st>>>(src_k, src_v, dst_k, dst_v, n, shift, hist, totals,
+                                                              nt);
+    count_launches(3);
+    src_k = dst_k;
+    src_v = dst_v;
+  }
+  if (passes == 0) {
+    if (cudaMemcpyAsync(keys_out, keys_in, (size_t)n * sizeof(K), cudaMemcpyDeviceToDevice, st) != cudaSuccess ||
+        cudaMemcpyAsync(vals_out, vals_in, (size_t)n * 4, cudaMemcpyDeviceToDevice, st) != cudaSuccess)
+      return SGR_ERR_CUDA;
+  }
+  return cudaGetLastError() == cudaSuccess ? SGR_OK : SGR_ERR_CUDA;
+}
+
+template <class T>
+size_t scan_temp_bytes(long long n) {
+  return n <= 0 ? 0 : align256((size_t)tiles_of(n) * sizeof(T));
+}
+
+template <class T, bool INCLUSIVE>
+int prefix_sum(const T* in, T* out, long long n, void* temp, size_t temp_bytes, cudaStream_t st) {
+  if (n <= 0) return SGR_OK;
+  if (temp_bytes < scan_temp_bytes<T>(n) || !temp) return SGR_ERR_WORKSPACE;
+  const long long nt = tiles_of(n);
+  T* partials = static_cast<T*>(temp);
+  k_scan_reduce<T><<<(unsigned)nt, kSortThreads, 0, st>>>(in, n, partials);
+  k_scan_partials<T><<<1, kSortThreads, 0, st>>>(partials, nt);
+  k_scan_apply<T, INCLUSIVE><<<(unsigned)nt, kSortThreads, 0, st>>>(in, out, n, partials);
+  count_launches(3);
+  return cudaGetLastError() == cudaSuccess ? SGR_OK : SGR_ERR_CUDA;
+}
+
+template size_t radix_sort_temp_bytes<unsigned long long>(long long);
+template size_t radix_sort_temp_bytes<uint32_t>(long long);
+template int radix_sort_pairs<unsigned long long>(const unsigned long long*, unsigned long long*, const uint32_t*,
+                                                  uint32_t*, long long, int, void*, size_t, cudaStream_t);
+template int radix_sort_pairs<uint32_t>(const uint32_t*, uint32_t*, const uint32_t*, uint32_t*, long long, int, void*,
+                                        size_t, cudaStream_t);
+template size_t scan_temp_bytes<unsigned long long>(long long);
+template size_t scan_temp_bytes<uint32_t>(long long);
+template int prefix_sum<unsigned long long, true>(const unsigned long long*, unsigned long long*, long long, void*,
+                                                  size_t, cudaStream_t);
+template int prefix_sum<uint32_t, false>(const uint32_t*, uint32_t*, long long, void*, size_t, cudaStream_t);
+
+}  // namespace sgr
+
+extern "C" {
+
+size_t sgr_radix_sort_temp_bytes(int64_t n, int key_bytes) {
+  if (key_bytes == 8) return sgr::radix_sort_temp_bytes<unsigned long long>(n);
+  if (key_bytes == 4) return sgr::radix_sort_temp_bytes<uint32_t>(n);
+  return 0;
+}
+
+int sgr_radix_sort_pairs(const void* keys_in, void* keys_out, const uint32_t* vals_in, uint32_t* vals_out, int64_t n,
+                         int key_bytes, int end_bit, void* temp, size_t temp_bytes, void* stream) {
+  if (n < 0 || (key_bytes != 4 && key_bytes != 8) || end_bit < 0 || end_bit > 8 * key_bytes)
+    return SGR_ERR_INVALID_ARGUMENT;
+  if (n > 0 && (!keys_in || !keys_out || !vals_in || !vals_out)) return SGR_ERR_INVALID_ARGUMENT;
+  if (n >= 0x7fffffffLL) return SGR_ERR_UNSUPPORTED;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (key_bytes == 8)
+    return sgr::radix_sort_pairs<unsigned long long>(static_cast<const unsigned long long*>(keys_in),
+                                                     static_cast<unsigned long long*>(keys_out), vals_in, vals_out, n,
+                                                     end_bit, temp, temp_bytes, st);
+  return sgr::radix_sort_pairs<uint32_t>(static_cast<const uint32_t*>(keys_in), static_cast<uint32_t*>(keys_out),
+                                         vals_in, vals_out, n, end_bit, temp, temp_bytes, st);
+}
+
+size_t sgr_prefix_sum_temp_bytes(int64_t n, int elem_bytes) {
+  if (elem_bytes == 8) return sgr::scan_temp_bytes<unsigned long long>(n);
+  if (elem_bytes == 4) return sgr::scan_temp_bytes<uint32_t>(n);
+  return 0;
+}
+
+int sgr_inclusive_sum_u64(const uint64_t* in, uint64_t* out, int64_t n, void* temp, size_t temp_bytes, void* stream) {
+  if (n < 0 || (n > 0 && (!in || !out))) return SGR_ERR_INVALID_ARGUMENT;
+  return sgr::prefix_sum<unsigned long long, true>(reinterpret_cast<const unsigned long long*>(in),
+                                                   reinterpret_cast<unsigned long long*>(out), n, temp, temp_bytes,
+                                                   static_cast<cudaStream_t>(stream));
+}
+
+int sgr_exclusive_sum_u32(const uint32_t* in, uint32_t* out, int64_t n, void* temp, size_t temp_bytes, void* stream) {
+  if (n < 0 || (n > 0 && (!in || !out))) return SGR_ERR_INVALID_ARGUMENT;
+  return sgr::prefix_sum<uint32_t, false>(in, out, n, temp, temp_bytes, static_cast<cudaStream_t>(stream));
+}
+
+}  // extern "C"

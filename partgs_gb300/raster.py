@@ -229,6 +229,12 @@ def forward(variant, means3D, opacities, shs, colors_precomp, scales, rotations,
     return color, others, semantic, radii, state
 
 
+def read_fragments(status_host: torch.Tensor) -> int:
+    """(pixel, list entry) pairs the forward blend visited, summed over the
+    batch, from a status copy taken after the forward."""
+    return int(status_host[24:32].view(torch.int64)[0])
+
+
 def read_status(status_host: torch.Tensor):
     """(key count, flags, cell-list entry count) from a status copy."""
     w = status_host[:L.STATUS_BYTES].view(torch.int64)

@@ -222,6 +222,9 @@ class SurfelTrainer:
             for _ in range(n):
                 loss = self.replay()
             flags, most = self.raster.sticky_counts(reset=True)
+            if flags & _lib.SGR_FLAG_LIST_INCONSISTENT:
+                raise RuntimeError("a backward found a cell list shorter than its forward used "
+                                   "(SGR_FLAG_LIST_INCONSISTENT): gradients of that step are incomplete")
             if flags & _lib.SGR_FLAG_BIN_OVERFLOW:
                 if recaptures == max_recaptures:
                     raise RuntimeError(f"cell lists still overflow after {recaptures} re-captures")

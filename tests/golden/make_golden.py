@@ -1,7 +1,7 @@
 """Generates tests/golden/reference_python.npz from the reference's own Python.
 
-Run in a checkout that has the PartGS reference next to it (the path is the
-first argument, default /root/reference).  It imports, unmodified:
+Run with a PartGS checkout: its root is the first argument, or the
+PARTGS_REFERENCE environment variable.  It imports, unmodified:
 
 * utils/sh_utils.py            eval_sh (SH colour)
 * utils/graphics_utils.py      getWorld2View2, getProjectionMatrix (camera matrices)
@@ -191,7 +191,7 @@ def sq_losses(bgm, ref_root):
     print("wrote", os.path.join(HERE, "sq_losses.npz"), res["losses"])
 
 
-def main(ref_root="/root/reference"):
+def main(ref_root):
     sys.path.insert(0, ref_root)
     _stub_modules()
     _cpu_only()
@@ -399,7 +399,7 @@ def bind_icosphere(bgm):
           "poles", int((np.abs(verts[:, 1]) > 1 - 1e-12).sum()))
 
 
-def main_bind_ico(ref_root="/root/reference"):
+def main_bind_ico(ref_root):
     sys.path.insert(0, ref_root)
     _stub_modules()
     _cpu_only()
@@ -616,7 +616,7 @@ def render_post(ref_root):
     print("wrote", os.path.join(HERE, "render_post.npz"), {k: v for k, v in out.items() if k.endswith("_loss")})
 
 
-def main_loss(ref_root="/root/reference"):
+def main_loss(ref_root):
     sys.path.insert(0, ref_root)
     _stub_modules()
     _cpu_only()
@@ -624,7 +624,7 @@ def main_loss(ref_root="/root/reference"):
     render_post(ref_root)
 
 
-def main_sq(ref_root="/root/reference"):
+def main_sq(ref_root):
     sys.path.insert(0, ref_root)
     _stub_modules()
     _cpu_only()
@@ -632,7 +632,7 @@ def main_sq(ref_root="/root/reference"):
     sq_losses(bgm, ref_root)
 
 
-def main_densify(ref_root="/root/reference"):
+def main_densify(ref_root):
     sys.path.insert(0, ref_root)
     _stub_modules()
     _cpu_only()
@@ -641,7 +641,10 @@ def main_densify(ref_root="/root/reference"):
 
 if __name__ == "__main__":
     args = [a for a in sys.argv[1:] if not a.startswith("--")]
-    root = args[0] if args else "/root/reference"
+    root = args[0] if args else os.environ.get("PARTGS_REFERENCE")
+    if not root:
+        raise SystemExit("usage: make_golden.py <PartGS checkout> [--sq|--densify|--loss|--bind-ico] "
+                         "(or set PARTGS_REFERENCE)")
     if "--sq" in sys.argv:   # only the superquadric-loss fixture
         main_sq(root)
     elif "--densify" in sys.argv:   # only the densification fixture

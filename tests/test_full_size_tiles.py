@@ -9,11 +9,11 @@ import pytest
 import torch
 
 from oracle import surfel_oracle as O
-from tests._util import grad_error, image_error
+from tests._util import grad_check, image_error
 
 pytestmark = pytest.mark.gpu
 
-IMG_TOL, AUX_TOL, GRAD_TOL, GRAD_TOL_TRANSMAT = 1e-5, 3e-5, 1e-4, 3e-4
+IMG_TOL, AUX_TOL = 1e-5, 3e-5
 N_TILES = 10
 
 
@@ -89,10 +89,11 @@ def test_radii(case):
     P = len(case["radii"])
     np.testing.assert_array_equal(case["radii"][~d], st.radii[~d])
     # fp32 against fp64 flips: about 1e-4 of the surfels; the oracles also
-    # flag those within 2e-6 (relative) of a rounding boundary: about 0.07%
+    # flag those within FP32 rounding of a boundary, counting the
+    # cancellation in the extent: about 0.25%
     flips = int((case["radii"] != st.radii).sum())
     assert flips <= 2e-4 * P, flips
-    assert d.sum() <= 1e-3 * P, int(d.sum())
+    assert d.sum() <= 4e-3 * P, int(d.sum())
     assert (case["radii"] > 0).sum() > 100_000
 
 
@@ -110,7 +111,6 @@ def test_gradients_from_sampled_tiles(case):
     g, r = case["grads"], case["ref_g"]
     names = ["dL_dcolors", "dL_dopacity", "dL_dmeans3D", "dL_dtransmat", "dL_dsh", "dL_dscales",
              "dL_drotations", "dL_dmeans2D"]
-    errs = {k: grad_error(g[k], r[k]) for k in names}
-    bad = {k: v for k, v in errs.items() if v > (GRAD_TOL_TRANSMAT if k == "dL_dtransmat" else GRAD_TOL)}
+    errs, bad = grad_check(g, r, names)
     assert not bad, errs
     assert float(np.abs(r["dL_dmeans3D"]).max()) > 0

@@ -5,7 +5,7 @@ import pytest
 import torch
 
 from oracle import surfel_oracle as O
-from tests._util import grad_error, image_error, oracle_camera, oracle_surfels, settings
+from tests._util import grad_check, grad_error, image_error, oracle_camera, oracle_surfels, settings
 
 pytestmark = pytest.mark.gpu
 
@@ -51,11 +51,9 @@ def case(sgr_lib, request):
     # the same algorithm in FP32 (numpy): its distance to FP64 is the
     # rounding floor any FP32 implementation of the reference sits at
     st32 = O.forward_view(osf, ocam, np.array([0.3, 0.1, 0.2]), O.PART, np.float32)
-    ref32 = O.backward_view(st32, ocam, osf, np.array([0.3, 0.1, 0.2]), dcol, doth, dsem, variant=O.PART,
-                            dtype=np.float32)
     return dict(S=S, img=img.detach().cpu().numpy(), sem=sem_img.detach().cpu().numpy(),
                 allmap=allmap.detach().cpu().numpy(), radii=radii.cpu().numpy(), st=st, amb=amb, ref=ref,
-                st32=st32, ref32=ref32,
+                st32=st32,
                 grads=dict(dL_dmeans3D=means3D.grad, dL_dsh=shs.grad, dL_dopacity=opac.grad,
                            dL_dscales=scales.grad, dL_drotations=rots.grad, dL_dsemantics=sem_d.grad,
                            dL_dmeans2D=means2D.grad))
@@ -89,10 +87,6 @@ def test_part_images(case):
 
 
 def test_part_gradients(case):
-    bad = {}
-    for k, v in case["grads"].items():
-        err = grad_error(v.cpu().numpy(), case["ref"][k])
-        tol = _floor(1e-4, grad_error(case["ref32"][k], case["ref"][k]))
-        if err > tol:
-            bad[k] = (err, tol)
-    assert not bad, bad
+    got = {k: v.cpu().numpy() for k, v in case["grads"].items()}
+    errs, bad = grad_check(got, case["ref"])
+    assert not bad, errs

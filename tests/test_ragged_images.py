@@ -11,13 +11,12 @@ import pytest
 import torch
 
 from oracle import surfel_oracle as O
-from tests._util import grad_error, image_error, oracle_camera, oracle_surfels, settings
+from tests._util import grad_check, grad_error, image_error, oracle_camera, oracle_surfels, settings
 
 pytestmark = pytest.mark.gpu
 
 IMG_TOL = 1e-5
 AUX_TOL = 3e-5
-GRAD_TOL = 1e-4
 BG = [0.3, 0.2, 0.6]
 
 
@@ -84,19 +83,11 @@ def test_partial_tiles(sgr_lib, hw, variant):
         loss = loss + (sem_img * torch.from_numpy(dsem).cuda()).sum()
     loss.backward()
     ref = O.backward_view(st, ocam, osf, np.array(BG), dcol, doth, dsem, variant=variant, dtype=np.float64)
-    ref32 = O.backward_view(st32, ocam, osf, np.array(BG), dcol, doth, dsem, variant=variant, dtype=np.float32)
     got = {name: leaves[leaf].grad for name, leaf in
            (("dL_dsh", "shs"), ("dL_dmeans3D", "means3D"), ("dL_dopacity", "opacities"),
             ("dL_dscales", "scales"), ("dL_drotations", "rotations"))}
     got["dL_dmeans2D"] = means2D.grad
     if variant == O.PART:
         got["dL_dsemantics"] = sem_d.grad
-    bad = {}
-    for name, t in got.items():
-        mine = t.cpu().numpy()
-        r64 = np.asarray(ref[name]).reshape(mine.shape)
-        r32 = np.asarray(ref32[name]).reshape(mine.shape)
-        err, tol = grad_error(mine, r64), _floor(GRAD_TOL, grad_error(r32, r64))
-        if err > tol:
-            bad[name] = (err, tol)
-    assert not bad, bad
+    errs, bad = grad_check({k: t.cpu().numpy() for k, t in got.items()}, ref)
+    assert not bad, errs

@@ -15,13 +15,12 @@ import pytest
 import torch
 
 from oracle import surfel_oracle as O
-from tests._util import grad_error, image_error, oracle_camera, oracle_surfels, settings
+from tests._util import grad_check, grad_error, image_error, oracle_camera, oracle_surfels, settings
 
 pytestmark = pytest.mark.gpu
 
 IMG_TOL = 1e-5
 AUX_TOL = 3e-5
-GRAD_TOL = 1e-4
 BG = [0.2, 0.4, 0.1]
 
 
@@ -79,21 +78,18 @@ def test_lower_sh_degree_with_sixteen_coefficients(base, deg, variant):
     loss.backward()
     dsem = np.zeros((3,) + st.color.shape[1:], np.float32) if variant == O.PART else None
     ref = O.backward_view(st, ocam, osf, np.array(BG), dcol, doth, dsem, variant=variant, dtype=np.float64)
-    ref32 = O.backward_view(st32, ocam, osf, np.array(BG), dcol, doth, dsem, variant=variant, dtype=np.float32)
 
     dsh = leaves["shs"].grad.cpu().numpy()
     used = (deg + 1) ** 2
     assert np.count_nonzero(dsh[:, used:]) == 0, "gradient reached coefficients above the active degree"
     assert np.abs(dsh[:, :used]).max() > 0
-    bad = {}
+    got, want = {}, {}
     for name, leaf in (("dL_dsh", "shs"), ("dL_dmeans3D", "means3D"), ("dL_dopacity", "opacities"),
                        ("dL_dscales", "scales"), ("dL_drotations", "rotations")):
         mine = leaves[leaf].grad.cpu().numpy()
         r64 = np.asarray(ref[name]).reshape(mine.shape)
-        r32 = np.asarray(ref32[name]).reshape(mine.shape)
         if name == "dL_dsh":
-            mine, r64, r32 = mine[:, :used], r64[:, :used], r32[:, :used]
-        err, tol = grad_error(mine, r64), _floor(GRAD_TOL, grad_error(r32, r64))
-        if err > tol:
-            bad[name] = (err, tol)
-    assert not bad, bad
+            mine, r64 = mine[:, :used], r64[:, :used]
+        got[name], want[name] = mine, r64
+    errs, bad = grad_check(got, want)
+    assert not bad, errs
