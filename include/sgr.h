@@ -51,7 +51,7 @@
 extern "C" {
 #endif
 
-#define SGR_ABI_VERSION 2
+#define SGR_ABI_VERSION 3
 
 /* status codes returned by every entry point */
 #define SGR_OK 0
@@ -80,6 +80,17 @@ extern "C" {
 #define SGR_FLAG_LIST_INCONSISTENT 8u /* sgr_backward: a tile's cell list held fewer entries than its
                                          forward blended (the workspace or the lists changed between the
                                          calls); that tile's gradients are incomplete */
+
+/* sgr_batch.blend_shape: the part of a 16x16 tile each warp of the blend
+ * kernels owns.  STRIP16: 16-pixel-wide rows (16x2 in the forward, 16x4 in
+ * the backward of the plain variant); PATCH8: 8-pixel-wide patches (8x4,
+ * 8x8).  Only the grouping of pixels into warps changes: every pixel still
+ * walks its 16x16 tile's list, so images and gradients are the same. */
+#define SGR_BLEND_STRIP16 0
+#define SGR_BLEND_PATCH8 1
+/* sgr_batch.tile_schedule */
+#define SGR_SCHEDULE_GRID 0
+#define SGR_SCHEDULE_QUEUE 1
 
 #define SGR_VARIANT_PLAIN 0
 #define SGR_VARIANT_PART 1
@@ -137,6 +148,10 @@ typedef struct sgr_batch {
     const float* semantics;          /* [P,S] or NULL */
     int32_t cell_tiles;              /* edge, in tiles, of the cells records are binned into: 1, 2, 4, 8 or 16;
                                         0 for the default (SGR_DEFAULT_CELL_TILES) */
+    int32_t blend_shape;             /* pixels of a tile each warp of the blends owns: SGR_BLEND_STRIP16 or
+                                        SGR_BLEND_PATCH8 (results identical; speed depends on splat sizes) */
+    int32_t tile_schedule;           /* SGR_SCHEDULE_GRID (one CTA per tile) or SGR_SCHEDULE_QUEUE (persistent
+                                        CTAs take tiles from a device queue, longest estimated first) */
 } sgr_batch;
 
 /* Workspace sizes and the layout of the geometry workspace. */
@@ -161,6 +176,7 @@ typedef struct sgr_sizes {
     size_t off_bin_start;        /* uint32[V*cells] start of each cell list */
     size_t off_bin_count;        /* uint32[V*cells] length of each cell list */
     size_t off_tile_resume;      /* uint32[V*tiles][2] cell-list entries the forward scanned, tile entries found */
+    size_t off_tile_queue;       /* uint32[V*tiles + 1]: tile order and head of the SGR_SCHEDULE_QUEUE queue */
     int32_t tiles_x, tiles_y;
     int32_t tile_key_bits;
     int32_t cell_tiles;          /* cell edge in tiles */
@@ -520,7 +536,7 @@ int sgr_radius_downsample(const double* pts, int64_t n, const double* lo, const 
 #define SGR_GEMM_ADD_F32 1     /* out[m,n] += x (fp32, atomic; with split_k) */
 #define SGR_GEMM_RELU_BF16 2   /* out[m,n] = bf16(max(x, 0)) */
 #define SGR_GEMM_MASK_BF16 3   /* out[m,n] = bf16(mask[m,n] > 0 ? x : 0): a ReLU's backward */
-#define SGR_MLP_TIMEOUT 1u     /* status bit: a wait for the tensor cores ran out */
+#define SGR_MLP_TIMEOUT 1u     /* status bit: a wait for the tensor cores or a copy ran out (1 s) */
 
 /* C[M,N] = A[M,K] . B[N,K]^T with bf16 operands, fp32 accumulation.  A is
  * row-major with K contiguous (lda elements per row) or, with a_trans, its
@@ -542,6 +558,9 @@ typedef struct sgr_gemm_args {
     int64_t ldmask;
     int64_t split_k;             /* 0, or K per CTA (a multiple of 64; SGR_GEMM_ADD_F32) */
     uint32_t* status;            /* device word, OR-ed with SGR_MLP_TIMEOUT */
+    int32_t skip_loads;          /* 0.  Nonzero (tests of the timeout path only): the TMA producer issues no
+                                    loads, so the MMA issuer's bounded wait runs out with nothing in flight
+                                    and the call reports SGR_MLP_TIMEOUT after about one second */
 } sgr_gemm_args;
 
 /* The GEMM of the point-set proposal network's layers and their backward

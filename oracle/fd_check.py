@@ -35,7 +35,7 @@ NAMES = ["sq_s", "sq_r", "sq_t", "sq_eps", "sq_occ"]
 _W = {}
 
 
-def make_case(B=8, n_eta=50, n_omega=50, views=(0, 1), height=300, width=400, fovx=50.0, seed=0):
+def make_case(B=8, n_eta=50, n_omega=50, views=(0,), height=300, width=400, fovx=50.0, seed=0):
     """The block-level workload's layout: B superquadrics with n_eta x n_omega
     surfels each, cameras on a radius-3 sphere; seeded SH colours and loss
     weights.  Returns a dict of numpy / torch inputs (float64)."""
@@ -137,6 +137,101 @@ def _eval(job):
         idx = np.flatnonzero(pm)
         out.append((idx.astype(np.int32), val.reshape(-1)[idx], sig.reshape(-1)[idx]))
     return out
+
+
+def _surfel_grads(case, v, wc, wo, tiles=None):
+    """FP64 oracle adjoint of sum(wc * colour + wo * others) of view v at the
+    case's parameters: per-surfel gradients (means3D, scales, rotations,
+    opacity) -- the rasteriser half of the chain."""
+    from oracle import surfel_oracle as O
+    cache = _W.setdefault("forward", {})
+    if v not in cache:          # the forward at the case's parameters, once per view and process
+        inp = case["inp"]
+        s = _surfels(case, [inp[k] for k in NAMES])
+        cam = _camera(case["cams"][v])
+        cache[v] = (s, cam, O.forward_view(s, cam, np.zeros(3), O.PLAIN, np.float64))
+    s, cam, st = cache[v]
+    g = O.backward_view(st, cam, s, np.zeros(3), wc, wo, variant=O.PLAIN, dtype=np.float64, tiles=tiles)
+    return [np.asarray(g[k], np.float64) for k in ("dL_dmeans3D", "dL_dscales", "dL_drotations", "dL_dopacity")]
+
+
+def _eval_grads(job):
+    """job = (key, view, flat pixel indices or None): the surfel gradients of
+    the loss restricted to those pixels (all pixels with None)."""
+    case = _W["case"]
+    key, v, pix = job
+    wc, wo = case["w_col"][v], case["w_oth"][v]
+    tiles = None
+    if pix is not None:
+        cam = case["cams"][v]
+        keep = np.zeros(cam.height * cam.width, bool)
+        keep[pix] = True
+        keep = keep.reshape(cam.height, cam.width)
+        wc, wo = wc * keep, wo * keep
+        gx = (cam.width + 15) // 16
+        tiles = np.unique((pix // cam.width) // 16 * gx + (pix % cam.width) // 16)
+    return key, _surfel_grads(case, v, wc, wo, tiles)
+
+
+def chain_to_parameters(case, surfel_grads):
+    """FP64 vector-Jacobian product of the binding (binding_oracle.bind,
+    autograd) for per-surfel gradients [means3D, scales, rotations,
+    opacity]: {name: gradient of each block parameter}."""
+    import torch
+    from oracle import binding_oracle as Bo
+    inp = case["inp"]
+    ps = [inp[k].clone().requires_grad_(True) for k in NAMES]
+    xyz, ls, rot, op = Bo.bind(*ps, inp["eta"], inp["omega"], inp["faces"], inp["alpha_raw"], inp["scale"],
+                               inp["ratio_block_scene"], inp["scale_block_min"])
+    gx, gs, gr, go = surfel_grads
+    scales = np.exp(ls.detach().numpy())      # the rasteriser takes exp(log_scaling)
+    loss = (xyz * torch.tensor(gx)).sum() + (ls * torch.tensor(gs * scales)).sum() + \
+        (rot * torch.tensor(gr)).sum() + (op * torch.tensor(go.reshape(-1, 1))).sum()
+    loss.backward()
+    return {k: p.grad.numpy().reshape(-1).copy() for k, p in zip(NAMES, ps)}
+
+
+def check(case_kwargs, params, h=1e-6, procs=None):
+    """Central differences of every parameter in ``params`` and the FP64
+    analytic gradient of the same (flip-masked) loss: the oracle's adjoint
+    of the rasteriser, then the binding's autograd.  Returns the
+    finite_differences records, each with ``an64`` (the analytic value of
+    the loss its ``fd`` differentiates, flip pixels left out) and
+    ``masks`` (per view, the flat pixel indices left out)."""
+    procs = procs or min(16, os.cpu_count() or 1)
+    case = make_case(**case_kwargs)
+    V = len(case["cams"])
+    jobs = [(n, f, sgn * h) for n, f in params for sgn in (1, -1)]
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(procs, initializer=_init, initargs=(case_kwargs,)) as pool:
+        full = pool.map_async(_eval_grads, [(("full", v), v, None) for v in range(V)], chunksize=1)
+        res = pool.map(_eval, jobs, chunksize=1)
+        out = []
+        corr_jobs = []
+        for i, (n, f) in enumerate(params):
+            plus, minus = res[2 * i], res[2 * i + 1]
+            views, fd, flips, masks = [], 0.0, 0, []
+            for v, ((idx, vp, sp), (_, vm, sm)) in enumerate(zip(plus, minus)):
+                q = (vp - vm) / (2 * h)
+                flip = sp != sm
+                views.append(dict(pixels=idx, quotient=q, flip=flip))
+                fd += float(q[~flip].sum())
+                flips += int(flip.sum())
+                masks.append(idx[flip])
+                if flip.any():
+                    corr_jobs.append(((i, v), v, idx[flip]))
+            out.append(dict(name=n, flat=f, fd=fd, views=views, flips=flips, masks=masks))
+        corr = dict(pool.map(_eval_grads, corr_jobs, chunksize=1))
+        full = dict(full.get())
+    g_full = [sum(full[("full", v)][k] for v in range(V)) for k in range(4)]
+    base = chain_to_parameters(case, g_full)
+    for i, r in enumerate(out):
+        a = float(base[r["name"]][r["flat"]])
+        for v in range(V):
+            if (i, v) in corr:
+                a -= float(chain_to_parameters(case, corr[(i, v)])[r["name"]][r["flat"]])
+        r["an64"] = a
+    return case, out
 
 
 def parameter_list(case, blocks_full=None):

@@ -14,12 +14,16 @@ LIB_PATH = _HERE / "_lib" / "libsgr.so"
 
 SGR_OK = 0
 SGR_ERR_CUDA = 6
-ABI_VERSION = 2
+ABI_VERSION = 3
 SGR_FLAG_KEY_OVERFLOW = 1
 SGR_FLAG_PREFILTERED = 2
 SGR_FLAG_BIN_OVERFLOW = 4
 SGR_FLAG_LIST_INCONSISTENT = 8
 STATUS_BYTES = 32
+SGR_BLEND_STRIP16 = 0
+SGR_BLEND_PATCH8 = 1
+SGR_SCHEDULE_GRID = 0
+SGR_SCHEDULE_QUEUE = 1
 SGR_VARIANT_PLAIN = 0
 SGR_VARIANT_PART = 1
 SGR_MAX_SEMANTICS = 16
@@ -47,6 +51,7 @@ class Batch(C.Structure):
         ("scenes", _p), ("views", _p), ("viewmatrix", _p), ("projmatrix", _p), ("campos", _p),
         ("background", _p), ("means3D", _p), ("scales", _p), ("rotations", _p), ("opacities", _p),
         ("shs", _p), ("colors_precomp", _p), ("transmat_precomp", _p), ("semantics", _p), ("cell_tiles", _i),
+        ("blend_shape", _i), ("tile_schedule", _i),
     ]
 
 
@@ -58,6 +63,7 @@ class Sizes(C.Structure):
         ("off_offsets", C.c_size_t), ("off_ranges", C.c_size_t), ("off_final_T", C.c_size_t),
         ("off_n_contrib", C.c_size_t), ("off_status", C.c_size_t), ("off_rects", C.c_size_t),
         ("off_bin_start", C.c_size_t), ("off_bin_count", C.c_size_t), ("off_tile_resume", C.c_size_t),
+        ("off_tile_queue", C.c_size_t),
         ("tiles_x", _i), ("tiles_y", _i), ("tile_key_bits", _i), ("cell_tiles", _i),
     ]
 

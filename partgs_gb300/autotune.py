@@ -1,19 +1,33 @@
-"""Workload autotuning of the rasteriser's cell size.
+"""Workload autotuning of the rasteriser's launch shape.
 
-Each blend CTA streams the list of the cell that holds its tile and keeps
-the entries whose rectangle holds the tile (sgr_binning.cu, sgr_blend.cu).
-Small cells mean short, dense lists but more (record, cell) entries to bin;
-large cells the reverse, and the best edge depends on the surfels' screen
-sizes and on the image.  ``tune_cells`` times whole training steps of a
-``SurfelTrainer`` for each candidate edge (parameters and optimiser state
-restored after each trial) and keeps the fastest; results are cached per
-workload shape for the process.
+Three knobs change speed but not results:
+
+* the cell size.  Each blend CTA streams the list of the cell that holds its
+  tile and keeps the entries whose rectangle holds the tile
+  (sgr_binning.cu, sgr_blend.cu).  Small cells mean short, dense lists but
+  more (record, cell) entries to bin; large cells the reverse.
+* the warp footprint (``blend_shape``): 16-pixel-wide strips or 8-pixel-wide
+  patches of the 16x16 tile per warp.  Compact patches let a warp skip more
+  entries whose splats miss it and keep more lanes busy on those that hit
+  it, at the price of more per-entry reach tests.
+* the tile schedule: one CTA per tile, or persistent CTAs taking tiles from
+  a device queue in decreasing order of estimated cost (uneven scenes).
+
+The best choice depends on the surfels' screen sizes, the image and the
+scene mix.  ``tune_cells`` times whole training steps of a ``SurfelTrainer``
+for each candidate cell edge, ``tune_blend`` then each footprint and
+schedule at that edge (parameters and optimiser state restored after each
+trial); results are cached per workload shape for the process.
 """
 from __future__ import annotations
 
 import torch
 
+from . import _lib as L
+
 CANDIDATES = (2, 4, 8, 16)
+SHAPES = (L.SGR_BLEND_STRIP16, L.SGR_BLEND_PATCH8)
+SCHEDULES = (L.SGR_SCHEDULE_GRID, L.SGR_SCHEDULE_QUEUE)
 _CACHE: dict = {}
 
 
@@ -22,10 +36,22 @@ def workload_key(trainer) -> tuple:
     return (int(trainer.xyz.shape[0]), r.num_views, r.viewset.height, r.viewset.width)
 
 
+def _time_steps(trainer, targets, steps):
+    trainer.step(targets)                      # first use of this configuration
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        trainer.step(targets)
+    e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / steps
+
+
 def tune_cells(trainer, targets, candidates=CANDIDATES, steps: int = 3, log=None) -> int:
     """Sets ``trainer.raster.cell_tiles`` to the fastest candidate for this
     workload and returns it, with {edge: ms per step} in ``last_timings``."""
-    key = workload_key(trainer)
+    key = ("cells",) + workload_key(trainer)
     if key in _CACHE:
         trainer.raster.cell_tiles = _CACHE[key]
         return _CACHE[key]
@@ -35,15 +61,7 @@ def tune_cells(trainer, targets, candidates=CANDIDATES, steps: int = 3, log=None
     for edge in candidates:
         trainer.raster.cell_tiles = edge
         trainer.raster.set_capacity(None)          # eager steps size the lists exactly
-        trainer.step(targets)                      # first use of this edge
-        torch.cuda.synchronize()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record()
-        for _ in range(steps):
-            trainer.step(targets)
-        e1.record()
-        torch.cuda.synchronize()
-        timings[edge] = e0.elapsed_time(e1) / steps
+        timings[edge] = _time_steps(trainer, targets, steps)
         trainer.restore(state)
         if log:
             log(f"cell edge {edge}: {timings[edge]:.2f} ms per step")
@@ -56,3 +74,34 @@ def tune_cells(trainer, targets, candidates=CANDIDATES, steps: int = 3, log=None
 
 
 tune_cells.last_timings = {}
+
+
+def tune_blend(trainer, targets, shapes=SHAPES, schedules=SCHEDULES, steps: int = 3, log=None) -> tuple:
+    """Sets ``trainer.raster.blend_shape`` and ``tile_schedule`` to the
+    fastest pair for this workload (at the current cell edge) and returns
+    it, with {(shape, schedule): ms per step} in ``last_timings``."""
+    key = ("blend", trainer.raster.cell_tiles) + workload_key(trainer)
+    r = trainer.raster
+    if key in _CACHE:
+        r.blend_shape, r.tile_schedule = _CACHE[key]
+        return _CACHE[key]
+    state = trainer.snapshot()
+    saved_capacity = r.bin_capacity
+    timings = {}
+    for shape in shapes:
+        for sched in schedules:
+            r.blend_shape, r.tile_schedule = shape, sched
+            r.set_capacity(None)
+            timings[(shape, sched)] = _time_steps(trainer, targets, steps)
+            trainer.restore(state)
+            if log:
+                log(f"blend shape {shape}, schedule {sched}: {timings[(shape, sched)]:.2f} ms per step")
+    best = min(timings, key=timings.get)
+    r.blend_shape, r.tile_schedule = best
+    r.set_capacity(saved_capacity)
+    tune_blend.last_timings = timings
+    _CACHE[key] = best
+    return best
+
+
+tune_blend.last_timings = {}

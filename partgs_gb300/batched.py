@@ -27,7 +27,8 @@ class _MultiViewFn(torch.autograd.Function):
         color, others, semantic, radii, state = _r.forward(
             cfg.variant, means3D, opacities, shs, colors_precomp, scales, rotations, None, semantics, cfg.viewset,
             cfg.bg, cfg.sh_degree, 1.0, False, bin_capacity=cfg.bin_capacity, tables=cfg.tables,
-            status_host=cfg.status, cell_tiles=cfg.cell_tiles)
+            status_host=cfg.status, cell_tiles=cfg.cell_tiles, blend_shape=cfg.blend_shape,
+            tile_schedule=cfg.tile_schedule)
         ctx.state = state
         ctx.cfg = cfg
         cfg.last_state = state                    # for inspection (bench counters)
@@ -58,13 +59,16 @@ class MultiViewRasterizer:
     once, so calls make no host-to-device copies."""
 
     def __init__(self, cameras, bg, sh_degree=3, variant=L.SGR_VARIANT_PLAIN, bin_capacity=None,
-                 scene_sizes=None, scene_views=None, num_surfels=None, device="cuda", cell_tiles=0):
+                 scene_sizes=None, scene_views=None, num_surfels=None, device="cuda", cell_tiles=0, blend_shape=0,
+                 tile_schedule=0):
         dev = torch.device(device)
         self.cameras = list(cameras)
         self.variant = variant
         self.sh_degree = sh_degree
         self.bin_capacity = bin_capacity
         self.cell_tiles = cell_tiles
+        self.blend_shape = blend_shape          # L.SGR_BLEND_*
+        self.tile_schedule = tile_schedule      # L.SGR_SCHEDULE_*
         self.bg = torch.as_tensor(bg, dtype=torch.float32, device=dev)
         vm = torch.stack([torch.as_tensor(c.world_view_transform, dtype=torch.float32) for c in cameras])
         pm = torch.stack([torch.as_tensor(c.full_proj_transform, dtype=torch.float32) for c in cameras])

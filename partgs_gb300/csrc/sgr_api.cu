@@ -56,6 +56,8 @@ int check_batch(const sgr_batch* b) {
     return SGR_ERR_INVALID_ARGUMENT;
   if (b->semantic_channels > SGR_MAX_SEMANTICS) return SGR_ERR_SEMANTIC_CHANNELS;
   if (b->variant == SGR_VARIANT_PLAIN && b->semantic_channels != 0) return SGR_ERR_INVALID_ARGUMENT;
+  if (b->blend_shape != SGR_BLEND_STRIP16 && b->blend_shape != SGR_BLEND_PATCH8) return SGR_ERR_INVALID_ARGUMENT;
+  if (b->tile_schedule != SGR_SCHEDULE_GRID && b->tile_schedule != SGR_SCHEDULE_QUEUE) return SGR_ERR_INVALID_ARGUMENT;
   if (!b->scenes || !b->views || !b->viewmatrix || !b->projmatrix || !b->campos || !b->background)
     return SGR_ERR_INVALID_ARGUMENT;
   if (b->num_surfels > 0) {
@@ -131,6 +133,7 @@ int sizes_impl(const sgr_batch* b, long long cap, sgr_sizes* s) {
   s->off_bin_start = o; o = align_up(o + cells * 4);
   s->off_bin_count = o; o = align_up(o + cells * 4);
   s->off_tile_resume = o; o = align_up(o + V * gx * gy * 8);
+  s->off_tile_queue = o; o = align_up(o + (V * gx * gy + 1) * 4);
   s->cell_tiles = B;
   s->geom_bytes = o;
   s->list_bytes = align_up((size_t)std::max(0LL, cap) * 4);
@@ -163,6 +166,7 @@ GeomView geom_view(const sgr_batch* b, const sgr_sizes& s, void* geom, void* scr
   g.bin_start = reinterpret_cast<uint32_t*>(gp + s.off_bin_start);
   g.bin_count = reinterpret_cast<uint32_t*>(gp + s.off_bin_count);
   g.tile_resume = reinterpret_cast<uint2*>(gp + s.off_tile_resume);
+  g.tile_queue = reinterpret_cast<uint32_t*>(gp + s.off_tile_queue);
   g.bins = nullptr;
   g.bin_capacity = 0;
   g.depth_keys = (sp && L) ? reinterpret_cast<unsigned long long*>(sp + L->depth_keys) : nullptr;

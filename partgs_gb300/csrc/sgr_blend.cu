@@ -25,6 +25,8 @@
 // reference's two divisions (splat_coords), and the exponential and the
 // backward's reciprocals are the hardware's approximate ones (splat_exp,
 // blend_rcp): a few 1e-7 relative on alpha, far inside the tolerances.
+#include <algorithm>
+
 #include "sgr_kernels.cuh"
 
 namespace sgr {
@@ -39,20 +41,6 @@ struct Strip {
   float x0, x1;       // pixel-centre x range of the tile
   float y0;           // pixel-centre y of the tile's first row
 };
-
-// Bit w set when the record's reach box meets strip w: rows
-// [ROWS*w, ROWS*w + ROWS) of the tile, one strip per warp.
-template <int ROWS, int NWARPS>
-__device__ __forceinline__ uint32_t strip_mask(const float4& box, const Strip& s) {
-  if (box.y < s.x0 || box.x > s.x1) return 0u;
-  uint32_t m = 0;
-#pragma unroll
-  for (int w = 0; w < NWARPS; ++w) {
-    const float ya = s.y0 + (float)(ROWS * w);
-    if (box.w >= ya && box.z <= ya + (float)(ROWS - 1)) m |= 1u << w;
-  }
-  return m;
-}
 
 // True when some pixel centre (x, y), x in [xa, xb], may be within reach of
 // the record: rho2d <= c (the filter disk, radius sqrt(c / 2)) or
@@ -171,30 +159,34 @@ __device__ __forceinline__ float splat_coords(float x, float y, float z, float& 
 #endif
 }
 
-// The strips of a record, each split into SPLIT groups of rows: bit
-// w * SPLIT + g is set when group g of strip w (rows ROWS w + g ROWS/SPLIT
-// on) may reach the record -- the reach box first, then, for each group
-// the box admits, row_reaches on its rows inside the box.  With two pixels
-// per thread (two rows apart) the groups are the thread's pixels.
-template <int ROWS, int NWARPS, int SPLIT>
+// The warp patches of a record, each split into SPLIT groups of rows: bit
+// w * SPLIT + g is set when group g of warp w's patch (WX x WY pixels; the
+// tile holds kTile / WX patches across) may reach the record -- the reach
+// box first, then, for each group the box admits, row_reaches on its rows
+// inside the box.  With two pixels per thread the groups are the thread's
+// pixels.
+template <int WX, int WY, int NWARPS, int SPLIT>
 __device__ __forceinline__ uint32_t strip_mask_rows(const float4& r0, const float4& r1, const float4& r2,
                                                     float reach, const float4& box, const Strip& s) {
-  constexpr int RG = ROWS / SPLIT;
-  static_assert(RG * SPLIT == ROWS && NWARPS * SPLIT <= 8, "strip groups");
+  constexpr int RG = WY / SPLIT;
+  constexpr int ACROSS = kTile / WX;
+  static_assert(RG * SPLIT == WY && NWARPS * SPLIT <= 8, "strip groups");
   if (box.y < s.x0 || box.x > s.x1) return 0u;
   const V3 Tu = v3(r0.x, r0.y, r0.z), Tv = v3(r0.w, r1.x, r1.y), Tw = v3(r1.z, r1.w, r2.x);
   uint32_t m = 0u;
 #pragma unroll
   for (int w = 0; w < NWARPS; ++w) {
+    const float xa = s.x0 + (float)((w % ACROSS) * WX), xb = xa + (float)(WX - 1);
+    if (ACROSS > 1 && (box.y < xa || box.x > xb)) continue;
 #pragma unroll
     for (int gi = 0; gi < SPLIT; ++gi) {
-      const float ya = s.y0 + (float)(ROWS * w + RG * gi);
+      const float ya = s.y0 + (float)((w / ACROSS) * WY + RG * gi);
       if (!(box.w >= ya && box.z <= ya + (float)(RG - 1))) continue;
       bool any = !SGR_EXACT_STRIPS;
       for (int r = 0; r < RG && !any; ++r) {
         const float y = ya + (float)r;
         if (y < box.z || y > box.w) continue;
-        any = row_reaches(Tu, Tv, Tw, r2.y, r2.z, reach, y, s.x0, s.x1);
+        any = row_reaches(Tu, Tv, Tw, r2.y, r2.z, reach, y, xa, xb);
       }
       if (any) m |= 1u << (w * SPLIT + gi);
     }
@@ -300,28 +292,47 @@ __device__ __forceinline__ void cell_list(const GeomView& g, int v, int tx, int 
 // at 3 or 4 CTAs of 128 (49.5 ms against 56.3 and 50.7 on 500k surfels x 16
 // views, 8 semantic channels).
 // ---------------------------------------------------------------------------
-template <int PX_>
+template <int PX_, int WX_ = kTile>
 struct BlendShape {
   static constexpr int PX = PX_;                                      // pixels per thread
   static constexpr int NT = kBlock / PX;                              // threads per CTA
-  static constexpr int NW = NT / 32;                                  // warps, one strip each
-  static constexpr int ROWS = kTile / NW;                             // strip height
+  static constexpr int NW = NT / 32;                                  // warps, one patch each
+  static constexpr int WX = WX_;                                      // patch width
+  static constexpr int LANE_ROWS = 32 / WX;                           // rows one pixel of each lane spans
+  static constexpr int WY = LANE_ROWS * PX;                           // patch height
+  static constexpr int ACROSS = kTile / WX;                           // patches across the tile
+  static constexpr int ROWS = WY;
+  static_assert(ACROSS * WX == kTile && (NW / ACROSS) * WY == kTile && NW % ACROSS == 0, "patches tile the tile");
 };
-using FwdShape = BlendShape<1>;
 #ifndef SGR_PART_BWD_PX
 #define SGR_PART_BWD_PX 1
 #endif
-template <int VARIANT>
-using BwdShape = BlendShape<(VARIANT == SGR_VARIANT_PLAIN) ? 2 : SGR_PART_BWD_PX>;
+template <int VARIANT, int WX = kTile>
+using FwdShapeT = BlendShape<1, WX>;
+template <int VARIANT, int WX = kTile>
+using BwdShapeT = BlendShape<(VARIANT == SGR_VARIANT_PLAIN) ? 2 : SGR_PART_BWD_PX, WX>;
+using FwdShape = BlendShape<1>;
 template <int VARIANT>
 constexpr int kSemSlots = (VARIANT == SGR_VARIANT_PART) ? SGR_MAX_SEMANTICS : 1;
 
-// Pixel i of a thread: column lane % 16, row ROWS * warp + lane / 16 + 2 i.
+// Pixel i of a thread: warp w owns patch (w % ACROSS, w / ACROSS) of WX x WY
+// pixels; lane l sits at column l % WX, row l / WX, and its pixel i
+// LANE_ROWS * i rows further down.  With WX = 16 a warp covers a 16 x 2 PX
+// strip (column lane % 16, row WY w + lane / 16 + 2 i).
 template <class Shape>
 __device__ __forceinline__ void pixel_of(int tx, int ty, int lane, int warp, int i, int& px, int& py) {
-  px = tx * kTile + (lane & (kTile - 1));
-  py = ty * kTile + Shape::ROWS * warp + (lane >> 4) + 2 * i;
+  px = tx * kTile + (warp % Shape::ACROSS) * Shape::WX + (lane % Shape::WX);
+  py = ty * kTile + (warp / Shape::ACROSS) * Shape::WY + lane / Shape::WX + Shape::LANE_ROWS * i;
 }
+
+// Tiles taken from a device queue by persistent CTAs (order == NULL: one CTA
+// per tile, tile = blockIdx.x).  `order` lists the tiles by decreasing
+// estimated cost (k_tile_order); `next` is the queue head.
+struct TileQueue {
+  const uint32_t* order;
+  uint32_t* next;
+  int count;
+};
 
 // ---------------------------------------------------------------------------
 // forward
@@ -444,13 +455,13 @@ __device__ __forceinline__ void fwd_fragment(FwdPixel<VARIANT>& q, const float4 
 #define SGR_PART_FWD_MIN_CTAS 3
 #endif
 
-template <int VARIANT>
-__global__ void __launch_bounds__(FwdShape::NT, (VARIANT == SGR_VARIANT_PLAIN) ? SGR_FWD_MIN_CTAS : SGR_PART_FWD_MIN_CTAS)
-    k_render_fwd(const sgr_batch b, GeomView g, sgr_fwd_outputs out) {
-  using Shape = FwdShape;
-  constexpr int PX = Shape::PX, NT = Shape::NT, NW = Shape::NW, ROWS = Shape::ROWS, NS = kSemSlots<VARIANT>;
+// The forward of one tile (all threads of the CTA).
+template <int VARIANT, int WX>
+__device__ __forceinline__ void render_fwd_tile(const sgr_batch& b, const GeomView& g, const sgr_fwd_outputs& out,
+                                                const int tile) {
+  using Shape = FwdShapeT<VARIANT, WX>;
+  constexpr int PX = Shape::PX, NT = Shape::NT, NW = Shape::NW, NS = kSemSlots<VARIANT>;
   const int tiles_per_view = g.tiles_x * g.tiles_y;
-  const int tile = blockIdx.x;
   const int v = tile / tiles_per_view;
   const int t = tile - v * tiles_per_view;
   const int ty = t / g.tiles_x, tx = t - ty * g.tiles_x;
@@ -517,7 +528,7 @@ __global__ void __launch_bounds__(FwdShape::NT, (VARIANT == SGR_VARIANT_PLAIN) ?
       for (int k = 0; k < kRecF4 - 1; ++k) s_rec[k][e] = rec[k];
       {
         const float4 a0 = s_rec[0][e], a1 = s_rec[1][e], a2 = s_rec[2][e];
-        s_mask[e] = (uint8_t)strip_mask_rows<ROWS, NW, 1>(a0, a1, a2, s_rec[3][e].w, rec[5], strip);
+        s_mask[e] = (uint8_t)strip_mask_rows<Shape::WX, Shape::WY, NW, 1>(a0, a1, a2, s_rec[3][e].w, rec[5], strip);
       }
       if (VARIANT == SGR_VARIANT_PART) {
         const float* sem = b.semantics + (size_t)(sid_base + (int)r) * S;
@@ -592,6 +603,27 @@ __global__ void __launch_bounds__(FwdShape::NT, (VARIANT == SGR_VARIANT_PLAIN) ?
       const float* acc = reinterpret_cast<const float*>(sem_acc4);   // thread column: float4 stride NT
       for (int c = 0; c < S; ++c) sem[pix + c * HW] = acc[(c >> 2) * 4 * NT + (c & 3)];
     }
+  }
+}
+
+// One CTA per tile, or persistent CTAs taking tiles from a queue.
+template <int VARIANT, int WX>
+__global__ void __launch_bounds__(FwdShape::NT, (VARIANT == SGR_VARIANT_PLAIN) ? SGR_FWD_MIN_CTAS : SGR_PART_FWD_MIN_CTAS)
+    k_render_fwd(const sgr_batch b, GeomView g, sgr_fwd_outputs out, TileQueue q) {
+  __shared__ int s_item;
+  for (int it = 0;; ++it) {
+    int tile;
+    if (q.order) {
+      __syncthreads();                             // the previous tile is done with shared memory
+      if (threadIdx.x == 0) s_item = (int)atomicAdd(q.next, 1u);
+      __syncthreads();
+      if (s_item >= q.count) return;
+      tile = (int)q.order[s_item];
+    } else {
+      if (it > 0) return;
+      tile = blockIdx.x;
+    }
+    render_fwd_tile<VARIANT, WX>(b, g, out, tile);
   }
 }
 
@@ -807,20 +839,17 @@ __device__ __forceinline__ void bwd_update(BwdPixel<VARIANT>& q, const BwdGeom& 
 #define SGR_PART_BWD_MIN_CTAS 3
 #endif
 
-template <int VARIANT>
-__global__ void __launch_bounds__(BwdShape<VARIANT>::NT,
-                                  (VARIANT == SGR_VARIANT_PLAIN) ? SGR_BWD_MIN_CTAS : SGR_PART_BWD_MIN_CTAS)
-    k_render_bwd(const sgr_batch b, GeomView g,
-                                                                      const sgr_bwd_inputs in,
-                                                                      float* __restrict__ grads,
-                                                                      float* __restrict__ dL_dsemantics) {
-  using Shape = BwdShape<VARIANT>;
-  constexpr int PX = Shape::PX, NT = Shape::NT, NW = Shape::NW, ROWS = Shape::ROWS, NS = kSemSlots<VARIANT>;
+// The backward of one tile (all threads of the CTA).
+template <int VARIANT, int WX>
+__device__ __forceinline__ void render_bwd_tile(const sgr_batch& b, const GeomView& g, const sgr_bwd_inputs& in,
+                                                float* __restrict__ grads, float* __restrict__ dL_dsemantics,
+                                                const int tile) {
+  using Shape = BwdShapeT<VARIANT, WX>;
+  constexpr int PX = Shape::PX, NT = Shape::NT, NW = Shape::NW, NS = kSemSlots<VARIANT>;
   // strip masks with one bit per pixel row pair of a thread, so a warp skips
   // a pixel whose rows the entry cannot reach
   constexpr int SPLIT = SGR_BWD_SPLIT ? PX : 1;
   const int tiles_per_view = g.tiles_x * g.tiles_y;
-  const int tile = blockIdx.x;
   const int v = tile / tiles_per_view;
   const int t = tile - v * tiles_per_view;
   const int ty = t / g.tiles_x, tx = t - ty * g.tiles_x;
@@ -935,7 +964,8 @@ __global__ void __launch_bounds__(BwdShape<VARIANT>::NT,
       for (int k = 0; k < kRecF4 - 1; ++k) s_rec[k][e] = rec[k];
       {
         const float4 a0 = s_rec[0][e], a1 = s_rec[1][e], a2 = s_rec[2][e];
-        s_mask[e] = (uint8_t)strip_mask_rows<ROWS, NW, SPLIT>(a0, a1, a2, s_rec[3][e].w, rec[5], strip);
+        s_mask[e] = (uint8_t)strip_mask_rows<Shape::WX, Shape::WY, NW, SPLIT>(a0, a1, a2, s_rec[3][e].w, rec[5],
+                                                                               strip);
       }
     }
     __syncthreads();
@@ -1006,25 +1036,144 @@ __global__ void __launch_bounds__(BwdShape<VARIANT>::NT,
   }
 }
 
+template <int VARIANT, int WX>
+__global__ void __launch_bounds__(BwdShapeT<VARIANT>::NT,
+                                  (VARIANT == SGR_VARIANT_PLAIN) ? SGR_BWD_MIN_CTAS : SGR_PART_BWD_MIN_CTAS)
+    k_render_bwd(const sgr_batch b, GeomView g, const sgr_bwd_inputs in, float* __restrict__ grads,
+                 float* __restrict__ dL_dsemantics, TileQueue q) {
+  __shared__ int s_item;
+  for (int it = 0;; ++it) {
+    int tile;
+    if (q.order) {
+      __syncthreads();
+      if (threadIdx.x == 0) s_item = (int)atomicAdd(q.next, 1u);
+      __syncthreads();
+      if (s_item >= q.count) return;
+      tile = (int)q.order[s_item];
+    } else {
+      if (it > 0) return;
+      tile = blockIdx.x;
+    }
+    render_bwd_tile<VARIANT, WX>(b, g, in, grads, dL_dsemantics, tile);
+  }
+}
+
+// Queue order of the tiles, by decreasing estimated cost: for the forward the
+// length of the tile's cell list, for the backward the tile-list entries its
+// forward found.  Tiles are bucketed by the bit length of their cost (one
+// CTA; order inside a bucket is whatever the atomics give: the blends'
+// results do not depend on the order tiles run in).  Also resets the queue.
+__global__ void __launch_bounds__(1024) k_tile_order(GeomView g, int n, int backward, uint32_t* order,
+                                                     uint32_t* next) {
+  __shared__ uint32_t s_cnt[33];
+  __shared__ uint32_t s_pos[33];
+  const int T = g.tiles_x * g.tiles_y;
+  const int B = g.cell_tiles;
+  const int cx = (g.tiles_x + B - 1) / B, cy = (g.tiles_y + B - 1) / B;
+  auto cost = [&](int tile) -> uint32_t {
+    if (backward) return g.tile_resume[tile].y;
+    const int v = tile / T, t = tile - v * T;
+    const int ty = t / g.tiles_x, tx = t - ty * g.tiles_x;
+    return g.bin_count[(size_t)v * cx * cy + (size_t)(ty / B) * cx + (tx / B)];
+  };
+  if (threadIdx.x < 33) s_cnt[threadIdx.x] = 0;
+  __syncthreads();
+  for (int i = threadIdx.x; i < n; i += blockDim.x) atomicAdd(&s_cnt[32 - __clz(cost(i))], 1u);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint32_t run = 0;
+    for (int k = 32; k >= 0; --k) {
+      s_pos[k] = run;
+      run += s_cnt[k];
+    }
+    *next = 0u;
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < n; i += blockDim.x) order[atomicAdd(&s_pos[32 - __clz(cost(i))], 1u)] = (uint32_t)i;
+}
+
+// Resident CTAs per SM of a kernel on the current device (queried once per
+// kernel and device).
+template <class F>
+int resident_ctas(F kernel, int threads) {
+  constexpr int kMaxDev = 64;
+  static int cache[kMaxDev] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDev) return 0;
+  if (cache[dev] == 0) {
+    int per_sm = 0, sms = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, 0) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+      return 0;
+    cache[dev] = per_sm * sms;
+  }
+  return cache[dev];
+}
+
+template <int VARIANT, int WX>
+void launch_fwd(const sgr_batch& b, const GeomView& g, const sgr_fwd_outputs& out, TileQueue q, unsigned tiles,
+                cudaStream_t st) {
+  auto* k = k_render_fwd<VARIANT, WX>;
+  unsigned grid = tiles;
+  if (q.order) {
+    k_tile_order<<<1, 1024, 0, st>>>(g, (int)tiles, 0, const_cast<uint32_t*>(q.order), q.next);
+    count_launches();
+    const int r = resident_ctas(k, FwdShape::NT);
+    grid = r > 0 ? std::min<unsigned>(tiles, (unsigned)r) : tiles;
+  }
+  k<<<grid, FwdShape::NT, 0, st>>>(b, g, out, q);
+}
+
+template <int VARIANT, int WX>
+void launch_bwd(const sgr_batch& b, const GeomView& g, const sgr_bwd_inputs& in, float* grads, float* dsem,
+                TileQueue q, unsigned tiles, cudaStream_t st) {
+  auto* k = k_render_bwd<VARIANT, WX>;
+  constexpr int NT = BwdShapeT<VARIANT>::NT;
+  unsigned grid = tiles;
+  if (q.order) {
+    k_tile_order<<<1, 1024, 0, st>>>(g, (int)tiles, 1, const_cast<uint32_t*>(q.order), q.next);
+    count_launches();
+    const int r = resident_ctas(k, NT);
+    grid = r > 0 ? std::min<unsigned>(tiles, (unsigned)r) : tiles;
+  }
+  k<<<grid, NT, 0, st>>>(b, g, in, grads, dsem, q);
+}
+
+TileQueue tile_queue(const sgr_batch& b, const GeomView& g, unsigned tiles) {
+  TileQueue q{nullptr, nullptr, (int)tiles};
+  if (b.tile_schedule == SGR_SCHEDULE_QUEUE && g.tile_queue) {
+    q.order = g.tile_queue;
+    q.next = g.tile_queue + tiles;
+  }
+  return q;
+}
+
 void launch_render_fwd(const sgr_batch& b, const GeomView& g, const sgr_fwd_outputs& out, cudaStream_t st) {
-  const unsigned blocks = (unsigned)(g.tiles_x * g.tiles_y) * (unsigned)b.num_views;
-  if (blocks == 0) return;
+  const unsigned tiles = (unsigned)(g.tiles_x * g.tiles_y) * (unsigned)b.num_views;
+  if (tiles == 0) return;
+  const TileQueue q = tile_queue(b, g, tiles);
+  const bool narrow = b.blend_shape == SGR_BLEND_PATCH8;
   if (b.variant == SGR_VARIANT_PLAIN)
-    k_render_fwd<SGR_VARIANT_PLAIN><<<blocks, FwdShape::NT, 0, st>>>(b, g, out);
+    narrow ? launch_fwd<SGR_VARIANT_PLAIN, 8>(b, g, out, q, tiles, st)
+           : launch_fwd<SGR_VARIANT_PLAIN, kTile>(b, g, out, q, tiles, st);
   else
-    k_render_fwd<SGR_VARIANT_PART><<<blocks, FwdShape::NT, 0, st>>>(b, g, out);
+    narrow ? launch_fwd<SGR_VARIANT_PART, 8>(b, g, out, q, tiles, st)
+           : launch_fwd<SGR_VARIANT_PART, kTile>(b, g, out, q, tiles, st);
   count_launches();
 }
 
 void launch_render_bwd(const sgr_batch& b, const GeomView& g, const sgr_bwd_inputs& in, float* grads,
                        float* dL_dsemantics, cudaStream_t st) {
-  const unsigned blocks = (unsigned)(g.tiles_x * g.tiles_y) * (unsigned)b.num_views;
-  if (blocks == 0) return;
+  const unsigned tiles = (unsigned)(g.tiles_x * g.tiles_y) * (unsigned)b.num_views;
+  if (tiles == 0) return;
+  const TileQueue q = tile_queue(b, g, tiles);
+  const bool narrow = b.blend_shape == SGR_BLEND_PATCH8;
   if (b.variant == SGR_VARIANT_PLAIN)
-    k_render_bwd<SGR_VARIANT_PLAIN>
-        <<<blocks, BwdShape<SGR_VARIANT_PLAIN>::NT, 0, st>>>(b, g, in, grads, dL_dsemantics);
+    narrow ? launch_bwd<SGR_VARIANT_PLAIN, 8>(b, g, in, grads, dL_dsemantics, q, tiles, st)
+           : launch_bwd<SGR_VARIANT_PLAIN, kTile>(b, g, in, grads, dL_dsemantics, q, tiles, st);
   else
-    k_render_bwd<SGR_VARIANT_PART><<<blocks, BwdShape<SGR_VARIANT_PART>::NT, 0, st>>>(b, g, in, grads, dL_dsemantics);
+    narrow ? launch_bwd<SGR_VARIANT_PART, 8>(b, g, in, grads, dL_dsemantics, q, tiles, st)
+           : launch_bwd<SGR_VARIANT_PART, kTile>(b, g, in, grads, dL_dsemantics, q, tiles, st);
   count_launches();
 }
 

@@ -24,6 +24,7 @@ struct GeomView {
   uint32_t* bin_start;                   // [V*cells] start of each cell list in `bins`
   uint32_t* bin_count;                   // [V*cells] length of each cell list
   uint2* tile_resume;                    // [V*tiles] (cell-list entries the forward scanned, tile entries found)
+  uint32_t* tile_queue;                  // [V*tiles + 1] queue order of the tiles, then the queue head
   const uint32_t* bins;                  // cell lists: depth-order positions
   long long bin_capacity;                // entries `bins` holds
   int cell_tiles;                        // cell edge in tiles

@@ -41,7 +41,9 @@ namespace sgrmlp {
 constexpr int kTM = 128;        // rows per CTA tile (= tensor-memory lanes)
 constexpr int kKC = 64;         // K per shared-memory chunk
 constexpr int kThreads = 128;
-constexpr unsigned kWaitLimit = 1u << 26;
+// Every mbarrier wait gives up after this long (a healthy wait takes
+// microseconds); the kernel then reports SGR_MLP_TIMEOUT.
+constexpr unsigned long long kWaitNs = 1000000000ull;   // 1 s
 
 __device__ __forceinline__ uint32_t smem_addr(const void* p) {
   return static_cast<uint32_t>(__cvta_generic_to_shared(p));
@@ -70,10 +72,22 @@ __device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
   return ok != 0;
 }
 
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;\n" : "=l"(t));
+  return t;
+}
+
+// Waits for phase `parity` of the barrier, at most kWaitNs.
 __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
-  for (unsigned it = 0; it < kWaitLimit; ++it)
-    if (mbar_try(bar, parity)) return true;
-  return false;
+  if (mbar_try(bar, parity)) return true;
+  const unsigned long long t0 = global_ns();
+  for (;;) {
+#pragma unroll 1
+    for (int k = 0; k < 64; ++k)
+      if (mbar_try(bar, parity)) return true;
+    if (global_ns() - t0 > kWaitNs) return false;
+  }
 }
 
 // Offset of element (row r, k) of a chunk in the core-matrix layout.
@@ -360,9 +374,11 @@ __global__ void __launch_bounds__(kThreads) k_gemm_tma(const sgr_gemm_args a, co
   const uint32_t tmem = s_tmem;
   const uint32_t base = (smem_addr(smem) + 127u) & ~127u;   // TMA destinations: 128-byte aligned
 
+  int issued = 0;                                    // producer: chunks whose loads were issued
   if (warp == 0 && lane == 0) {
-    // producer
-    for (int c = 0; c < chunks; ++c) {
+    // producer (a.skip_loads: issues nothing, so that the MMA issuer's wait
+    // runs out with no copy in flight -- the timeout path's test)
+    for (int c = 0; c < chunks && !a.skip_loads; ++c) {
       const int st = c % ns;
       if (c >= ns && !mbar_wait(smem_addr(&s_empty[st]), (uint32_t)((c / ns - 1) & 1))) {
         s_fail = 1;
@@ -375,6 +391,7 @@ __global__ void __launch_bounds__(kThreads) k_gemm_tma(const sgr_gemm_args a, co
         tma_load_2d(sa + kb * kTM * 16, &map_a, c * kKC + kb * 8, m0, full);
         tma_load_2d(sb + kb * NT * 16, &map_b, c * kKC + kb * 8, n0, full);
       }
+      issued = c + 1;
     }
   } else if (warp == 1 && lane == 0) {
     // MMA issuer
@@ -409,9 +426,16 @@ __global__ void __launch_bounds__(kThreads) k_gemm_tma(const sgr_gemm_args a, co
   // everyone: wait for the accumulator (the issuer's last commit)
   const bool ok = mbar_wait(smem_addr(&s_done), 0u);
   asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-  __syncthreads();
-  if (!ok || s_fail) {
-    if (threadIdx.x == 0) atomicOr(a.status, (unsigned)SGR_MLP_TIMEOUT);
+  // one decision for the whole CTA (the epilogue's tcgen05.ld needs every lane)
+  if (__syncthreads_or(!ok || s_fail)) {
+    if (threadIdx.x == 0) {
+      atomicOr(a.status, (unsigned)SGR_MLP_TIMEOUT);
+      // let the copies this CTA issued land before it gives its shared
+      // memory back: the last phase armed on each stage (bounded waits)
+      for (int c = issued - 1; c >= 0 && c >= issued - ns; --c)
+        mbar_wait(smem_addr(&s_full[c % ns]), (uint32_t)((c / ns) & 1));
+    }
+    __syncthreads();
   } else {
     const long long row = (long long)m0 + 32 * warp + lane;
 #pragma unroll 1

@@ -5,7 +5,7 @@
 //
 // Sort: 8-bit digits, one pass per digit of bits [0, end_bit).  Each pass is
 // three kernels:
-//   1. k_radix_hist: per 2048-key tile, the 256-bin digit histogram, stored
+//   1. k_radix_hist: per 4096-key tile, the 256-bin digit histogram, stored
 //      digit-major (hist[digit][tile]);
 //   2. k_radix_scan: per digit, the exclusive scan of its counts over the
 //      tiles, and the digit's total;
@@ -26,16 +26,21 @@ namespace sgr {
 namespace {
 
 constexpr int kSortThreads = 256;
+constexpr int kRadixItems = 16;
+constexpr int kRadixTile = kSortThreads * kRadixItems;   // 4096 keys per sort CTA
 constexpr int kSortItems = 8;
-constexpr int kSortTile = kSortThreads * kSortItems;   // 2048 keys per CTA
+constexpr int kSortTile = kSortThreads * kSortItems;     // 2048 elements per scan CTA
 constexpr int kBins = 256;
 constexpr int kSortWarps = kSortThreads / 32;
 
 inline long long tiles_of(long long n) { return (n + kSortTile - 1) / kSortTile; }
+inline long long radix_tiles_of(long long n) { return (n + kRadixTile - 1) / kRadixTile; }
 
+// The pass's digit: bits [shift, shift + 8) of the key, cut at the sort's
+// end bit (dmask keeps the digit's bits below it).
 template <class K>
-__device__ __forceinline__ uint32_t digit_of(K key, int shift) {
-  return (uint32_t)((key >> shift) & (K)(kBins - 1));
+__device__ __forceinline__ uint32_t digit_of(K key, int shift, uint32_t dmask) {
+  return (uint32_t)(key >> shift) & dmask;
 }
 
 // Exclusive scan of one value per thread over a 256-thread CTA; returns the
@@ -65,17 +70,18 @@ __device__ __forceinline__ T block_exclusive_scan(T v, T* s_warp, T& total) {
 
 template <class K>
 __global__ void __launch_bounds__(kSortThreads) k_radix_hist(const K* __restrict__ keys, long long n, int shift,
-                                                             uint32_t* __restrict__ hist, long long ntiles) {
+                                                             uint32_t dmask, uint32_t* __restrict__ hist,
+                                                             long long ntiles) {
   __shared__ uint32_t s_cnt[kBins];
   s_cnt[threadIdx.x] = 0;
   __syncthreads();
-  const long long base = (long long)blockIdx.x * kSortTile;
+  const long long base = (long long)blockIdx.x * kRadixTile;
   const int lane = threadIdx.x & 31;
 #pragma unroll
-  for (int k = 0; k < kSortItems; ++k) {
+  for (int k = 0; k < kRadixItems; ++k) {
     const long long i = base + k * kSortThreads + threadIdx.x;
     const bool valid = i < n;
-    const uint32_t d = valid ? digit_of(keys[i], shift) : (uint32_t)kBins;
+    const uint32_t d = valid ? digit_of(keys[i], shift, dmask) : (uint32_t)kBins;
     const unsigned peers = __match_any_sync(0xffffffffu, d);
     if (valid && lane == __ffs(peers) - 1) atomicAdd(&s_cnt[d], (uint32_t)__popc(peers));
   }
@@ -105,11 +111,13 @@ __global__ void __launch_bounds__(kSortThreads) k_radix_scatter(const K* __restr
                                                                 const uint32_t* __restrict__ vals_in,
                                                                 K* __restrict__ keys_out,
                                                                 uint32_t* __restrict__ vals_out, long long n,
-                                                                int shift, const uint32_t* __restrict__ hist,
+                                                                int shift, uint32_t dmask,
+                                                                const uint32_t* __restrict__ hist,
                                                                 const uint32_t* __restrict__ totals,
                                                                 long long ntiles) {
-  __shared__ K s_keys[kSortTile];
-  __shared__ uint32_t s_vals[kSortTile];
+  extern __shared__ __align__(16) unsigned char s_dyn[];   // the tile in (digit, rank) order: keys, then values
+  K* s_keys = reinterpret_cast<K*>(s_dyn);
+  uint32_t* s_vals = reinterpret_cast<uint32_t*>(s_dyn + sizeof(K) * kRadixTile);
   __shared__ uint32_t s_wc[kSortWarps][kBins];     // this round's count of each digit per warp
   __shared__ uint32_t s_run[kBins];                // keys of each digit ranked so far
   __shared__ uint32_t s_local[kBins];              // start of each digit in the tile's order
@@ -117,7 +125,7 @@ __global__ void __launch_bounds__(kSortThreads) k_radix_scatter(const K* __restr
   __shared__ unsigned long long s_warp64[kSortWarps];
   __shared__ uint32_t s_warp32[kSortWarps];
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
-  const long long base = (long long)blockIdx.x * kSortTile;
+  const long long base = (long long)blockIdx.x * kRadixTile;
 
   // global start of digit t: all smaller digits, then the tiles before this one
   {
@@ -125,19 +133,19 @@ __global__ void __launch_bounds__(kSortThreads) k_radix_scatter(const K* __restr
     const unsigned long long ex = block_exclusive_scan<unsigned long long>(totals[t], s_warp64, tot);
     s_gbase[t] = ex + hist[(size_t)t * ntiles + blockIdx.x];
   }
-  K key[kSortItems];
-  uint32_t val[kSortItems], dig[kSortItems];
+  K key[kRadixItems];
+  uint32_t val[kRadixItems], dig[kRadixItems];
   s_run[t] = 0;
 #pragma unroll
   for (int w = 0; w < kSortWarps; ++w) s_wc[w][t] = 0;
   __syncthreads();
 #pragma unroll
-  for (int k = 0; k < kSortItems; ++k) {
+  for (int k = 0; k < kRadixItems; ++k) {
     const long long i = base + k * kSortThreads + t;
     const bool valid = i < n;
     key[k] = valid ? keys_in[i] : (K)0;
     val[k] = valid ? vals_in[i] : 0u;
-    dig[k] = valid ? digit_of(key[k], shift) : (uint32_t)kBins;
+    dig[k] = valid ? digit_of(key[k], shift, dmask) : (uint32_t)kBins;
     const unsigned peers = __match_any_sync(0xffffffffu, dig[k]);
     if (valid && lane == __ffs(peers) - 1) atomicAdd(&s_run[dig[k]], (uint32_t)__popc(peers));
   }
@@ -149,9 +157,9 @@ __global__ void __launch_bounds__(kSortThreads) k_radix_scatter(const K* __restr
     s_run[t] = 0;
   }
   __syncthreads();
-  uint32_t pos[kSortItems];
+  uint32_t pos[kRadixItems];
 #pragma unroll
-  for (int k = 0; k < kSortItems; ++k) {
+  for (int k = 0; k < kRadixItems; ++k) {
     const uint32_t d = dig[k];
     const unsigned peers = __match_any_sync(0xffffffffu, d);
     const uint32_t lrank = __popc(peers & ((1u << lane) - 1u));
@@ -175,17 +183,17 @@ __global__ void __launch_bounds__(kSortThreads) k_radix_scatter(const K* __restr
     __syncthreads();
   }
 #pragma unroll
-  for (int k = 0; k < kSortItems; ++k) {
+  for (int k = 0; k < kRadixItems; ++k) {
     if (dig[k] < kBins) {
       s_keys[pos[k]] = key[k];
       s_vals[pos[k]] = val[k];
     }
   }
   __syncthreads();
-  const int count = (int)min((long long)kSortTile, n - base);
+  const int count = (int)min((long long)kRadixTile, n - base);
   for (int s = t; s < count; s += kSortThreads) {
     const K kv = s_keys[s];
-    const uint32_t d = digit_of(kv, shift);
+    const uint32_t d = digit_of(kv, shift, dmask);
     const unsigned long long dst = s_gbase[d] + (unsigned long long)(s - (int)s_local[d]);
     keys_out[dst] = kv;
     vals_out[dst] = s_vals[s];
@@ -268,7 +276,7 @@ size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 template <class K>
 size_t radix_sort_temp_bytes(long long n) {
   if (n <= 0) return 0;
-  const long long nt = tiles_of(n);
+  const long long nt = radix_tiles_of(n);
   return align256((size_t)n * sizeof(K)) + align256((size_t)n * 4) + align256((size_t)kBins * nt * 4) +
          align256((size_t)kBins * 4);
 }
@@ -278,7 +286,10 @@ int radix_sort_pairs(const K* keys_in, K* keys_out, const uint32_t* vals_in, uin
                      int end_bit, void* temp, size_t temp_bytes, cudaStream_t st) {
   if (n <= 0) return SGR_OK;
   if (temp_bytes < radix_sort_temp_bytes<K>(n) || !temp) return SGR_ERR_WORKSPACE;
-  const long long nt = tiles_of(n);
+  const long long nt = radix_tiles_of(n);
+  const size_t dyn = (sizeof(K) + 4) * (size_t)kRadixTile;
+  if (cudaFuncSetAttribute(k_radix_scatter<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn) != cudaSuccess)
+    return SGR_ERR_CUDA;
   char* p = static_cast<char*>(temp);
   K* alt_keys = reinterpret_cast<K*>(p);
   p += align256((size_t)n * sizeof(K));
@@ -296,10 +307,12 @@ int radix_sort_pairs(const K* keys_in, K* keys_out, const uint32_t* vals_in, uin
     K* dst_k = to_out ? keys_out : alt_keys;
     uint32_t* dst_v = to_out ? vals_out : alt_vals;
     const int shift = 8 * pass;
-    k_radix_hist<K><<<(unsigned)nt, kSortThreads, 0, st>>>(src_k, n, shift, hist, nt);
+    const int bits = end_bit - shift < 8 ? end_bit - shift : 8;
+    const uint32_t dmask = (1u << bits) - 1u;
+    k_radix_hist<K><<<(unsigned)nt, kSortThreads, 0, st>>>(src_k, n, shift, dmask, hist, nt);
     k_radix_scan<<<kBins, kSortThreads, 0, st>>>(hist, nt, totals);
-    k_radix_scatter<K><<<(unsigned)nt, kSortThreads, 0, st>>>(src_k, src_v, dst_k, dst_v, n, shift, hist, totals,
-                                                              nt);
+    k_radix_scatter<K><<<(unsigned)nt, kSortThreads, dyn, st>>>(src_k, src_v, dst_k, dst_v, n, shift, dmask, hist,
+                                                                totals, nt);
     count_launches(3);
     src_k = dst_k;
     src_v = dst_v;

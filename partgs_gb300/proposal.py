@@ -204,11 +204,14 @@ class Trainer:
         self.opt = SurfelAdam([{"params": [p], "lr": lr} for p in net.parameters()], eps=1e-8)
 
     def step(self, pts: torch.Tensor, target: SQBatch) -> float:
+        """One training step; raises if a tensor-core GEMM of its forward or
+        backward ran out of time (before the optimiser uses its gradients)."""
         out, cache = self.net.forward(pts)
         o = out.detach().requires_grad_(True)
         loss = slot_loss(o, target)
         (dout,) = torch.autograd.grad(loss, o)
         self.net.backward(cache, dout.contiguous())
+        G.check_status(pts.device)
         self.opt.step()
         self.net.refresh()
         return loss.detach()
@@ -221,6 +224,7 @@ def predict(net: ProposalNet, pts: torch.Tensor, threshold: float = 0.5, counts=
     slots; otherwise the slots with existence probability above
     ``threshold`` (at least one)."""
     out, _ = net.forward(pts)
+    G.check_status(pts.device)          # raises if a GEMM's wait ran out
     semi, eps, quat, trans, logit = decode(out)
     res = []
     for s in range(out.shape[0]):

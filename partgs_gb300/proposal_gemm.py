@@ -17,7 +17,7 @@ class GemmArgs(C.Structure):
     _fields_ = [("M", C.c_int64), ("N", C.c_int64), ("K", C.c_int64), ("A", _p), ("lda", C.c_int64),
                 ("a_trans", C.c_int32), ("B", _p), ("ldb", C.c_int64), ("b_trans", C.c_int32), ("bias", _p),
                 ("epilogue", C.c_int32), ("out", _p), ("ldo", C.c_int64), ("mask", _p), ("ldmask", C.c_int64),
-                ("split_k", C.c_int64), ("status", _p)]
+                ("split_k", C.c_int64), ("status", _p), ("skip_loads", C.c_int32)]
 
 
 _STATUS: dict = {}
@@ -38,7 +38,19 @@ def status_word(device) -> torch.Tensor:
     return _STATUS[key]
 
 
-def gemm(a, b, out, epilogue, bias=None, mask=None, trans=False, split_k=0):
+def check_status(device) -> None:
+    """Raises if any GEMM on ``device`` since the last check ran out of time
+    waiting for the tensor cores or a copy (its output is then incomplete),
+    and clears the word.  Synchronises with the device."""
+    w = status_word(device)
+    flags = int(w.item())
+    if flags:
+        w.zero_()
+        raise RuntimeError(f"tensor-core GEMM status {flags:#x}: a wait ran out (SGR_MLP_TIMEOUT); "
+                           "the outputs of the calls since the last check are incomplete")
+
+
+def gemm(a, b, out, epilogue, bias=None, mask=None, trans=False, split_k=0, skip_loads=False):
     """out (+)= epilogue(a . b^T + bias).  Without ``trans``: a [M, K], b
     [N, K] (bf16, K contiguous).  With it: a [K, M], b [K, N] (the reduction
     runs over their rows).  ``out`` is [M, N] (fp32, or bf16 for the ReLU
@@ -61,7 +73,7 @@ def gemm(a, b, out, epilogue, bias=None, mask=None, trans=False, split_k=0):
     args = GemmArgs(M, N, K, a.data_ptr(), a.shape[1], int(trans), b.data_ptr(), b.shape[1], int(trans),
                     bias.data_ptr() if bias is not None else None, epilogue, out.data_ptr(), N,
                     mask.data_ptr() if mask is not None else None, mask.shape[1] if mask is not None else 0,
-                    split_k, status_word(out.device).data_ptr())
+                    split_k, status_word(out.device).data_ptr(), int(bool(skip_loads)))
     L.check(_lib().sgr_mlp_gemm(C.byref(args), torch.cuda.current_stream().cuda_stream), "sgr_mlp_gemm")
     return out
 

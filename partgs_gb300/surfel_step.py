@@ -173,15 +173,17 @@ class SurfelTrainer:
     def capture(self, targets, warmup=3, headroom=1.25, autotune=False):
         """Captures step() into a CUDA graph reading ``self.targets``.
 
-        With ``autotune`` the cell size is picked first by timing eager steps
-        (``autotune.tune_cells``; parameters restored).  Without a cell-list
+        With ``autotune`` the cell size, then the blends' warp footprint and
+        tile schedule, are picked first by timing eager steps
+        (``autotune.tune_cells``, ``tune_blend``; parameters restored).  Without a cell-list
         capacity, the eager warm-up steps size it (``headroom`` times the
         largest entry count they saw); after replays, ``self.raster.counts()``
         reports the flags (SGR_FLAG_BIN_OVERFLOW when the parameters have
         drifted past the capacity)."""
         if autotune:
-            from .autotune import tune_cells
+            from .autotune import tune_blend, tune_cells
             tune_cells(self, targets)
+            tune_blend(self, targets)
         self.targets = targets.clone()
         s = torch.cuda.Stream()
         s.wait_stream(torch.cuda.current_stream())

@@ -1,6 +1,7 @@
-"""The cell-size autotuner: every candidate edge renders the same images
-(the cell lists only change how tiles find their lists), the tuner restores
-the parameters it trained through, and picks a candidate."""
+"""The launch-shape autotuners: every candidate cell edge, warp footprint
+and tile schedule renders the same images (they only change how tiles find
+their lists and how pixels and tiles are handed to warps and CTAs), the
+tuners restore the parameters they trained through, and pick a candidate."""
 import pytest
 import torch
 
@@ -34,5 +35,50 @@ def test_tuner_picks_a_candidate_and_restores_the_parameters(sgr_lib):
     best = autotune.tune_cells(tr, targets, candidates=(2, 8), steps=2)
     assert best in (2, 8) and tr.raster.cell_tiles == best
     assert set(autotune.tune_cells.last_timings) == {2, 8}
+    for p, q in zip(tr.params(), before):
+        assert torch.equal(p.detach(), q)
+
+
+def test_warp_footprint_and_schedule_do_not_change_the_results(sgr_lib):
+    """Both warp footprints and both tile schedules: identical images and
+    radii (every pixel walks the same list with the same arithmetic), and
+    gradients equal up to the order of the float atomics."""
+    from partgs_gb300 import _lib as L
+    from partgs_gb300.batched import MultiViewRasterizer
+    from partgs_gb300.cameras import orbit_cameras
+    from partgs_gb300.scenes import random_surfels
+    sc = random_surfels(3000, seed=52).to("cuda")
+    cams = orbit_cameras(3, 3.0, 96, 160, 55.0, seed=9)
+    g = torch.Generator(device="cuda").manual_seed(4)
+    up_c = torch.randn(3, 3, 96, 160, device="cuda", generator=g)
+    up_o = torch.randn(3, 7, 96, 160, device="cuda", generator=g) * 0.1
+    outs = []
+    for shape in (L.SGR_BLEND_STRIP16, L.SGR_BLEND_PATCH8):
+        for sched in (L.SGR_SCHEDULE_GRID, L.SGR_SCHEDULE_QUEUE):
+            leaves = [t.clone().requires_grad_(True) for t in (sc.means3D, sc.opacities, sc.shs, sc.scales,
+                                                                sc.rotations)]
+            mv = MultiViewRasterizer(cams, [0.1, 0.2, 0.3], 3, num_surfels=3000, blend_shape=shape,
+                                     tile_schedule=sched)
+            img, amap, _, radii = mv(*leaves)
+            ((img * up_c).sum() + (amap * up_o).sum()).backward()
+            outs.append((img.detach(), amap.detach(), radii, [t.grad for t in leaves]))
+    for img, amap, radii, grads in outs[1:]:
+        assert torch.equal(img, outs[0][0]) and torch.equal(amap, outs[0][1]) and torch.equal(radii, outs[0][2])
+        for a, b in zip(grads, outs[0][3]):
+            assert float((a - b).norm() / b.norm()) < 1e-5
+
+
+def test_blend_tuner_picks_a_pair(sgr_lib):
+    from partgs_gb300 import autotune
+    from partgs_gb300.cameras import orbit_cameras
+    from partgs_gb300.scenes import random_surfels
+    from partgs_gb300.surfel_step import SurfelTrainer
+    scene, cams = random_surfels(2500, seed=32), orbit_cameras(4, 3.0, 72, 88, 55.0, seed=14)
+    targets = torch.rand(len(cams), 3, 72, 88, generator=torch.Generator().manual_seed(10)).cuda()
+    tr = SurfelTrainer(scene, cams)
+    before = [p.detach().clone() for p in tr.params()]
+    best = autotune.tune_blend(tr, targets, steps=2)
+    assert best == (tr.raster.blend_shape, tr.raster.tile_schedule)
+    assert len(autotune.tune_blend.last_timings) == 4
     for p, q in zip(tr.params(), before):
         assert torch.equal(p.detach(), q)

