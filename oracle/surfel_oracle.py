@@ -343,6 +343,7 @@ def preprocess(s: Surfels, cam: Camera, variant=PLAIN, dtype=np.float64, amb_tol
 
     transmat = np.zeros((P, 9), dtype=dtype)
     normal = np.zeros((P, 3), dtype=dtype)
+    facing = np.ones(P, bool)      # the normal's orientation decision (the DUAL_VISIABLE flip)
     if s.transmat_precomp is not None:
         transmat[:] = s.transmat_precomp.astype(dtype)
         if variant == PLAIN:
@@ -378,6 +379,7 @@ def preprocess(s: Surfels, cam: Camera, variant=PLAIN, dtype=np.float64, amb_tol
             tn = R[:, :, 2] @ W3.T
             cosv = np.sum(-tn * pv, 1)
             alive &= cosv != 0
+            facing = cosv > 0
             tn = tn * np.where(cosv > 0, 1.0, -1.0).astype(dtype)[:, None]
             Tu = np.stack([fx * m0[:, 0] + cx * m0[:, 2], fx * m1[:, 0] + cx * m1[:, 2], fx * pv[:, 0] + cx * pv[:, 2]], 1)
             Tv = np.stack([fy * m0[:, 1] + cy * m0[:, 2], fy * m1[:, 1] + cy * m1[:, 2], fy * pv[:, 1] + cy * pv[:, 2]], 1)
@@ -389,6 +391,7 @@ def preprocess(s: Surfels, cam: Camera, variant=PLAIN, dtype=np.float64, amb_tol
         # DUAL_VISIABLE flip (P0/cr/forward.cu:209-214)
         cosv = -np.sum(p_view * normal, 1)
         alive &= cosv != 0
+        facing = cosv > 0
         normal = normal * np.where(cosv > 0, 1.0, -1.0).astype(dtype)[:, None]
 
     Tu, Tv, Tw = transmat[:, 0:3], transmat[:, 3:6], transmat[:, 6:9]
@@ -474,6 +477,7 @@ def preprocess(s: Surfels, cam: Camera, variant=PLAIN, dtype=np.float64, amb_tol
         clamped=clamped,
         alive=alive,
         amb=amb,
+        facing=facing,
         rad_in=np.where(alive, rad_in, 0.0).astype(np.float64),
         rad_err=np.where(alive, rad_err, 0.0).astype(np.float64),
         ctr_err=ctr_err.astype(np.float64),
@@ -607,8 +611,9 @@ def render_forward(pre, point_list, ranges, cam: Camera, s: Surfels, bg, variant
     Sem = np.zeros(shape + (Sn,), dtype)
     amb = np.zeros(shape, bool)
     # rolling hash of the discrete path per pixel (which list positions were
-    # blended, through which branch, and where the walk stopped): equal
-    # signatures mean the same decisions (finite-difference checks use it)
+    # blended, through which branch, with which normal orientation, and
+    # where the walk stopped): equal signatures mean the same decisions
+    # (finite-difference checks use it)
     sig = np.zeros(shape, np.int64)
     frags = 0
     for j in range(L):
@@ -687,7 +692,8 @@ def render_forward(pre, point_list, ranges, cam: Camera, s: Surfels, bg, variant
                 Sem = np.where(acc[..., None], Sem + sv * alpha[..., None] * T[..., None], Sem)
         T = np.where(acc, test_T, T)
         last_contributor = np.where(acc, contributor, last_contributor)
-        code = contributor * 4 + use3d.astype(np.int64) * 2 + med.astype(np.int64)
+        code = (contributor * 8 + use3d.astype(np.int64) * 4 + med.astype(np.int64) * 2
+                + pre["facing"][idc].astype(np.int64)[:, None])
         sig = np.where(acc, sig * np.int64(1000003) + code, sig)
 
     HW = (H, W)
