@@ -5,8 +5,9 @@ the plain rasteriser, for checking the hand-written adjoint chain
 TEST INFRASTRUCTURE ONLY.
 
 The chain is the oracle's: ``binding_oracle.bind`` (prepare_scaling_rot,
-games/block_mesh_splatting/scene/block_gaussian_model.py:198-256) then
-``surfel_oracle.forward_view`` (the rasteriser, both in float64).  The loss
+games/block_mesh_splatting/scene/block_gaussian_model.py:198-256), the
+model's quaternion normalisation, then ``surfel_oracle.forward_view`` (the
+rasteriser), all in float64.  The loss
 is a fixed weighted sum of the rendered colour and the seven auxiliary maps
 of every view.
 
@@ -14,12 +15,17 @@ A parameter of block b moves only block b's surfels, so each evaluation
 blends only the tiles those surfels' rectangles cover (one tile of margin);
 every other pixel is unchanged by construction.
 
+The chain orders each tile's surfels by their FP64 depth, not by the FP32
+depth bits the reference sorts on: neighbouring surfels that tie in FP32
+would otherwise trade places under perturbations far below any step.
 Discrete decisions (the alpha cut-off, the stop test, the 3D/2D branch, the
-median switch, a rectangle's rounding) make the loss jump.  Each evaluation
+median switch, the normal's orientation, two surfels crossing in depth, a
+rectangle's rounding) make the loss jump.  Each evaluation
 returns the oracle's per-pixel decision signature; a pixel whose signature
-differs between the +h and -h evaluations is a "flip", and the checks leave
-such pixels out of both the difference and the analytic gradient (the loss
-restricted to the other pixels is smooth over [-h, +h]).
+differs between any of the evaluations (+h, -h, +h/2, -h/2 and the
+unperturbed one) is a "flip", and the checks leave such pixels out of both the difference and the
+analytic gradient (the loss restricted to the other pixels is smooth over
+[-h, +h], on the branch the analytic gradient is taken on).
 
 Evaluations run in a ``spawn`` process pool.
 """
@@ -35,10 +41,12 @@ NAMES = ["sq_s", "sq_r", "sq_t", "sq_eps", "sq_occ"]
 _W = {}
 
 
-def make_case(B=8, n_eta=50, n_omega=50, views=(0,), height=300, width=400, fovx=50.0, seed=0):
+def make_case(B=8, n_eta=50, n_omega=50, views=(0,), height=300, width=400, fovx=50.0, seed=0, channels=None):
     """The block-level workload's layout: B superquadrics with n_eta x n_omega
     surfels each, cameras on a radius-3 sphere; seeded SH colours and loss
-    weights.  Returns a dict of numpy / torch inputs (float64)."""
+    weights (``channels``: the loss channels kept, 0-2 the colour and 3-9 the
+    auxiliary maps; all by default).  Returns a dict of numpy / torch inputs
+    (float64)."""
     import torch
     from oracle import binding_oracle as Bo
     from partgs_gb300.cameras import orbit_cameras
@@ -50,6 +58,10 @@ def make_case(B=8, n_eta=50, n_omega=50, views=(0,), height=300, width=400, fovx
     g = np.random.default_rng(seed + 6)
     w_col = [g.standard_normal((3, height, width)) for _ in cams]
     w_oth = [g.standard_normal((7, height, width)) * 0.1 for _ in cams]
+    if channels is not None:
+        keep = np.isin(np.arange(10), channels).astype(np.float64)
+        w_col = [w * keep[:3, None, None] for w in w_col]
+        w_oth = [w * keep[3:, None, None] for w in w_oth]
     return dict(inp=inp, cams=cams, shs=shs, w_col=w_col, w_oth=w_oth, B=B)
 
 
@@ -60,12 +72,25 @@ def _camera(cam):
                     np.asarray(cam.camera_center, np.float64), cam.tanfovx, cam.tanfovy, cam.height, cam.width)
 
 
-def _surfels(case, params):
+def _bind(case, params):
+    """The binding, then the model's rotation activation: the block model
+    inherits GaussianModel.get_rotation (scene/gaussian_model.py:65, 203-205),
+    torch.nn.functional.normalize.  The quaternions the binding makes are
+    not unit (down to 0.992 here), and the rasteriser's quaternion adjoint
+    (quat_to_rotmat_vjp, P0/cr/auxiliary.h:239) is the gradient with
+    respect to the normalised quaternion, so the chain needs the
+    normalisation's own Jacobian, which autograd supplies."""
+    import torch
     from oracle import binding_oracle as Bo
-    from oracle import surfel_oracle as O
     inp = case["inp"]
     xyz, ls, rot, op = Bo.bind(*params, inp["eta"], inp["omega"], inp["faces"], inp["alpha_raw"], inp["scale"],
                                inp["ratio_block_scene"], inp["scale_block_min"])
+    return xyz, ls, torch.nn.functional.normalize(rot, dim=-1), op
+
+
+def _surfels(case, params):
+    from oracle import surfel_oracle as O
+    xyz, ls, rot, op = (t.detach() for t in _bind(case, params))
     return O.Surfels(xyz.numpy(), op.numpy(), np.exp(ls.numpy()), rot.numpy(), shs=case["shs"].numpy(), sh_degree=3)
 
 
@@ -96,7 +121,8 @@ def pixel_values(case, params, tiles_per_view):
     s = _surfels(case, params)
     res = []
     for v, cam in enumerate(case["cams"]):
-        st = O.forward_view(s, _camera(cam), np.zeros(3), O.PLAIN, np.float64, tiles=tiles_per_view[v])
+        st = O.forward_view(s, _camera(cam), np.zeros(3), O.PLAIN, np.float64, tiles=tiles_per_view[v],
+                            exact_depth=True)
         val = (case["w_col"][v] * st.color).sum(0) + (case["w_oth"][v] * st.others).sum(0)
         gx = (cam.width + 15) // 16
         tmask = np.zeros(((cam.height + 15) // 16) * gx, bool)
@@ -149,7 +175,7 @@ def _surfel_grads(case, v, wc, wo, tiles=None):
         inp = case["inp"]
         s = _surfels(case, [inp[k] for k in NAMES])
         cam = _camera(case["cams"][v])
-        cache[v] = (s, cam, O.forward_view(s, cam, np.zeros(3), O.PLAIN, np.float64))
+        cache[v] = (s, cam, O.forward_view(s, cam, np.zeros(3), O.PLAIN, np.float64, exact_depth=True))
     s, cam, st = cache[v]
     g = O.backward_view(st, cam, s, np.zeros(3), wc, wo, variant=O.PLAIN, dtype=np.float64, tiles=tiles)
     return [np.asarray(g[k], np.float64) for k in ("dL_dmeans3D", "dL_dscales", "dL_drotations", "dL_dopacity")]
@@ -178,11 +204,9 @@ def chain_to_parameters(case, surfel_grads):
     autograd) for per-surfel gradients [means3D, scales, rotations,
     opacity]: {name: gradient of each block parameter}."""
     import torch
-    from oracle import binding_oracle as Bo
     inp = case["inp"]
     ps = [inp[k].clone().requires_grad_(True) for k in NAMES]
-    xyz, ls, rot, op = Bo.bind(*ps, inp["eta"], inp["omega"], inp["faces"], inp["alpha_raw"], inp["scale"],
-                               inp["ratio_block_scene"], inp["scale_block_min"])
+    xyz, ls, rot, op = _bind(case, ps)
     gx, gs, gr, go = surfel_grads
     scales = np.exp(ls.detach().numpy())      # the rasteriser takes exp(log_scaling)
     loss = (xyz * torch.tensor(gx)).sum() + (ls * torch.tensor(gs * scales)).sum() + \
@@ -191,17 +215,36 @@ def chain_to_parameters(case, surfel_grads):
     return {k: p.grad.numpy().reshape(-1).copy() for k, p in zip(NAMES, ps)}
 
 
-def check(case_kwargs, params, h=1e-6, procs=None):
+def check(case_kwargs, params, h=1e-6, procs=None, richardson=True):
     """Central differences of every parameter in ``params`` and the FP64
     analytic gradient of the same (flip-masked) loss: the oracle's adjoint
     of the rasteriser, then the binding's autograd.  Returns the
     finite_differences records, each with ``an64`` (the analytic value of
     the loss its ``fd`` differentiates, flip pixels left out) and
-    ``masks`` (per view, the flat pixel indices left out)."""
+    ``masks`` (per view, the flat pixel indices left out).
+
+    With ``richardson`` the difference is extrapolated from the steps h and
+    h/2, (4 D(h/2) - D(h)) / 3, which cancels the truncation term (h^2 / 6
+    times the third derivative): pixels of nearly edge-on splats are smooth
+    over the step but steep and curved (third derivatives near 1e11 per
+    unit translation), which leaves plain central differences 1e-4 off."""
     procs = procs or min(16, os.cpu_count() or 1)
     case = make_case(**case_kwargs)
     V = len(case["cams"])
-    jobs = [(n, f, sgn * h) for n, f in params for sgn in (1, -1)]
+    steps = (h, h / 2) if richardson else (h,)
+    per = 2 * len(steps)
+    jobs = [(n, f, sgn * d) for n, f in params for d in steps for sgn in (1, -1)]
+    # the unperturbed signature of each block's tiles: a pixel whose +h and
+    # -h decisions agree but differ from the base point's (a near-tie that
+    # rounding breaks one way at the base and the other way at both steps)
+    # is a flip too, since the analytic gradient is taken at the base
+    block_of = {}
+    for n, f in params:
+        b = int(np.unravel_index(f, case["inp"][n].shape)[0])
+        block_of[(n, f)] = b
+        if b not in block_of:
+            block_of[b] = len(jobs)
+            jobs.append((n, f, 0.0))
     ctx = mp.get_context("spawn")
     with ctx.Pool(procs, initializer=_init, initargs=(case_kwargs,)) as pool:
         full = pool.map_async(_eval_grads, [(("full", v), v, None) for v in range(V)], chunksize=1)
@@ -209,11 +252,18 @@ def check(case_kwargs, params, h=1e-6, procs=None):
         out = []
         corr_jobs = []
         for i, (n, f) in enumerate(params):
-            plus, minus = res[2 * i], res[2 * i + 1]
+            evals = res[per * i:per * (i + 1)]
+            base = res[block_of[block_of[(n, f)]]]
             views, fd, flips, masks = [], 0.0, 0, []
-            for v, ((idx, vp, sp), (_, vm, sm)) in enumerate(zip(plus, minus)):
-                q = (vp - vm) / (2 * h)
-                flip = sp != sm
+            for v in range(V):
+                idx, _, s0 = base[v]
+                flip = np.zeros(len(idx), bool)
+                qs = []
+                for k, d in enumerate(steps):
+                    (_, vp, sp), (_, vm, sm) = evals[2 * k][v], evals[2 * k + 1][v]
+                    qs.append((vp - vm) / (2 * d))
+                    flip |= (sp != s0) | (sm != s0)
+                q = (4 * qs[1] - qs[0]) / 3 if richardson else qs[0]
                 views.append(dict(pixels=idx, quotient=q, flip=flip))
                 fd += float(q[~flip].sum())
                 flips += int(flip.sum())

@@ -489,7 +489,12 @@ def preprocess(s: Surfels, cam: Camera, variant=PLAIN, dtype=np.float64, amb_tol
 # --------------------------------------------------------------------------
 # tile binning (P0/cr/rasterizer_impl.cu:70-138, 278-318)
 # --------------------------------------------------------------------------
-def bin_tiles(pre: dict):
+def bin_tiles(pre: dict, exact_depth: bool = False):
+    """Per-tile depth-ordered lists: (point_list, ranges [tiles, 2], keys).
+    The reference orders by the FP32 bits of the depth (ties by index);
+    with ``exact_depth`` the order uses the depth itself (finite-difference
+    checks: FP32 ties among neighbouring surfels would otherwise trade
+    places under tiny perturbations)."""
     gx, gy = pre["grid"]
     xmin, ymin, xmax, ymax = pre["rect"]
     alive = pre["alive"]
@@ -510,7 +515,10 @@ def bin_tiles(pre: dict):
     tiles = tiles.astype(np.int64)
     keys = (tiles.astype(np.uint64) << np.uint64(32)) | depth_bits[ids]
     # stable sort by the 64-bit key: equal keys keep emission (index) order
-    order = np.argsort(keys, kind="stable")
+    if exact_depth:
+        order = np.lexsort((np.arange(len(ids)), pre["depths"][ids], tiles))
+    else:
+        order = np.argsort(keys, kind="stable")
     keys = keys[order]
     point_list = ids[order]
     tsorted = tiles[order]
@@ -610,9 +618,11 @@ def render_forward(pre, point_list, ranges, cam: Camera, s: Surfels, bg, variant
     med_contrib = np.full(shape, -1, np.int64)
     Sem = np.zeros(shape + (Sn,), dtype)
     amb = np.zeros(shape, bool)
-    # rolling hash of the discrete path per pixel (which list positions were
-    # blended, through which branch, with which normal orientation, and
-    # where the walk stopped): equal signatures mean the same decisions
+    # rolling hash of the discrete path per pixel (which surfels were blended
+    # at which list positions -- so two surfels trading depth order count
+    # too -- through which branch, with which normal orientation, whether
+    # alpha sat at its 0.99 cap, which colour channels the SH clamp zeroed,
+    # and where the walk stopped): equal signatures mean the same decisions
     # (finite-difference checks use it)
     sig = np.zeros(shape, np.int64)
     frags = 0
@@ -692,8 +702,11 @@ def render_forward(pre, point_list, ranges, cam: Camera, s: Surfels, bg, variant
                 Sem = np.where(acc[..., None], Sem + sv * alpha[..., None] * T[..., None], Sem)
         T = np.where(acc, test_T, T)
         last_contributor = np.where(acc, contributor, last_contributor)
-        code = (contributor * 8 + use3d.astype(np.int64) * 4 + med.astype(np.int64) * 2
-                + pre["facing"][idc].astype(np.int64)[:, None])
+        sat = alpha >= f(0.99)
+        clamp = pre["clamped"][idc].astype(np.int64) @ np.array([1, 2, 4], np.int64)
+        code = ((((contributor + idc.astype(np.int64)[:, None] * 4099) * 8 + clamp[:, None]) * 16
+                 + sat.astype(np.int64) * 8 + use3d.astype(np.int64) * 4 + med.astype(np.int64) * 2
+                 + pre["facing"][idc].astype(np.int64)[:, None]))
         sig = np.where(acc, sig * np.int64(1000003) + code, sig)
 
     HW = (H, W)
@@ -733,11 +746,11 @@ def _gather_pixels(img, X, Y, inside):
 # full forward of one view
 # --------------------------------------------------------------------------
 def forward_view(s: Surfels, cam: Camera, bg, variant=PLAIN, dtype=np.float64, amb_tol=2e-6,
-                 tiles=None, alpha_tol=None) -> ViewState:
+                 tiles=None, alpha_tol=None, exact_depth=False) -> ViewState:
     """Forward of one view; with ``tiles`` only those tiles are blended (the
     other pixels stay zero)."""
     pre = preprocess(s, cam, variant, dtype, amb_tol)
-    point_list, ranges, keys = bin_tiles(pre)
+    point_list, ranges, keys = bin_tiles(pre, exact_depth)
     rf = render_forward(pre, point_list, ranges, cam, s, bg, variant, dtype, amb_tol, tiles, alpha_tol)
     st = ViewState(
         radii=pre["radii"], tiles_touched=pre["tiles_touched"], means2D=pre["means2D"],

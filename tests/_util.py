@@ -138,6 +138,18 @@ GRAD_L2_TOL_GEOMETRY = 2e-4  # their L2 bar: the part variant's lands at 1.2e-4 
                              # adjoint cancels too), the reference binary's own up to 2.1e-4 (max-norm) on the same case
 
 
+def ill_conditioned(st, cam, s, bg, variant, img_tol=1e-5, aux_tol=3e-5):
+    """Pixels where rounding every surfel's splat-to-pixel matrix and screen
+    centre by one FP32 unit moves the FP64 result by more than half the
+    tolerance (oracle.fp32_sensitivity): nearly edge-on splats, whose value
+    and gradients two FP32 implementations cannot agree on to the bars.
+    Their upstream gradients are zeroed and they are left out of the image
+    comparisons, like the oracle's rounding-ambiguous pixels."""
+    from oracle import surfel_oracle as O
+    sens = O.fp32_sensitivity(st, cam, s, np.asarray(bg, np.float64), variant)
+    return (sens[:3].max(0) > 0.5 * img_tol) | (sens[3:].max(0) > 0.5 * aux_tol)
+
+
 def l2_error(gpu, ref):
     """|gpu - ref|_2 / |ref|_2."""
     gpu = np.asarray(gpu, np.float64).reshape(-1)

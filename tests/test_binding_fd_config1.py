@@ -6,23 +6,28 @@ loss a fixed weighted sum of the colour and all seven auxiliary maps.
 
 All 104 parameters: sq_s (3), sq_r (4), sq_t (3), sq_eps (2: the exponents
 through signed_pow, games/block_mesh_splatting/utils/pytorch.py:28-29, and
-parametric_sq, utils/superquadric.py:10-14) and sq_occ (1), per block.
+parametric_sq, utils/superquadric.py:10-14) and sq_occ (1), per block.  The
+chain includes the model's quaternion normalisation (GaussianModel.get_rotation,
+scene/gaussian_model.py:203-205), as the reference's renderer applies it.
 
-A step of 1e-6 still flips discrete decisions (the alpha cut-off, the stop
-test, the median switch) at a few pixels for most parameters; the pixels
-whose decisions differ between +h and -h (the oracle's per-pixel decision
-signature) are left out of both sides for that parameter, so the loss
-differentiated is smooth over the step.  The flip counts are printed.
+Steps of 1e-6 and 5e-7 still flip discrete decisions (the alpha cut-off, the
+stop test, the median switch, two surfels crossing in depth) at a few
+pixels for most parameters; the pixels whose decisions differ between any
+two of the evaluations (the oracle's per-pixel decision signature) are left
+out of both sides for that parameter, so the loss differentiated is smooth
+over the step.  The flip counts are printed.  The differences are
+Richardson-extrapolated from the two steps: nearly edge-on splats give
+pixels smooth over the step but with third derivatives near 1e11, which
+leave plain central differences 1e-4 off.
 
 Two checks:
 1. the FP64 analytic gradient of the chain (the oracle's restatement of the
    rasteriser adjoint, then the binding's autograd) equals the differences
-   to 1e-5 relative per parameter (denominator floored at 1% of the largest
-   of its kind: a quaternion's radial component has no derivative, the
-   binding normalises it);
+   to 1e-6 relative per parameter (measured: at most 8e-8; denominator
+   floored at 1% of the largest of its kind);
 2. the library's FP32 chain (sgr_bind_backward after sgr_backward) against
-   the FP64 analytic gradient of the same loss: per parameter within 1% of
-   the largest of its kind, and within 1e-3 relative in the L2 norm over
+   the FP64 analytic gradient of the same loss: per parameter within 1e-3
+   of the largest of its kind, and within 5e-4 relative in the L2 norm over
    each kind.  FP32 is the limit there: the splat-to-pixel adjoint carries
    per-surfel rounding up to ~1e-4 of the largest surfel gradient (the
    reference's own FP32 CUDA lands as far from FP64), and a block parameter
@@ -35,10 +40,10 @@ from oracle import fd_check as F
 
 pytestmark = pytest.mark.gpu
 
-FD_TOL = 1e-5
+FD_TOL = 1e-6
 FLOOR = 1e-2
-FP32_PARAM_TOL = 1e-2       # of the kind's largest derivative
-FP32_L2_TOL = 1e-3
+FP32_PARAM_TOL = 1e-3       # of the kind's largest derivative
+FP32_L2_TOL = 5e-4
 H = 1e-6
 
 

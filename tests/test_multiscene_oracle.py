@@ -3,7 +3,12 @@ five scenes of log-uniform surfel counts, unequal view counts) rasterised
 forward and backward in one batched call, each scene's views against the
 FP64 oracle run on that scene alone: radii and contributor counts exact,
 images within 1e-5 (RGB) / 3e-5 (auxiliary maps), every surfel's gradients
-within the parity bars (tests._util.grad_check), for both tile schedules."""
+within the parity bars (tests._util.grad_check), for both tile schedules.
+Pixels the oracle finds ambiguous in FP32 rounding or ill-conditioned in
+FP32 (tests._util.ill_conditioned: 0.25% of them here, nearly edge-on
+splats of the superquadric surfaces; with them in, the oracle's own FP32
+restatement lands 5e-4 from FP64 on the position gradients, 1.5e-5 without)
+are left out of the images and get no upstream gradient."""
 import math
 
 import numpy as np
@@ -11,7 +16,7 @@ import pytest
 import torch
 
 from oracle import surfel_oracle as O
-from tests._util import grad_check, image_error, oracle_camera, oracle_surfels
+from tests._util import grad_check, ill_conditioned, image_error, oracle_camera, oracle_surfels
 
 pytestmark = pytest.mark.gpu
 
@@ -43,11 +48,13 @@ def batch(sgr_lib, request):
     for s, sc in enumerate(scenes):
         osf = oracle_surfels(sc)
         for cam in cams[s]:
-            o = O.forward_view(osf, oracle_camera(cam), np.array([0.2, 0.1, 0.3]), O.PLAIN, np.float64)
+            ocam = oracle_camera(cam)
+            o = O.forward_view(osf, ocam, np.array([0.2, 0.1, 0.3]), O.PLAIN, np.float64)
+            o.extra["skip"] = o.amb_pixel | ill_conditioned(o, ocam, osf, [0.2, 0.1, 0.3], O.PLAIN, IMG_TOL, AUX_TOL)
             dc = rng.standard_normal(o.color.shape).astype(np.float32)
             do = (rng.standard_normal(o.others.shape) * 0.1).astype(np.float32)
-            dc[:, o.amb_pixel] = 0
-            do[:, o.amb_pixel] = 0
+            dc[:, o.extra["skip"]] = 0
+            do[:, o.extra["skip"]] = 0
             st.append((s, o, osf, cam))
             dcol.append(dc)
             doth.append(do)
@@ -64,7 +71,8 @@ def test_images_contributors_radii(batch):
     offs = np.concatenate([[0], np.cumsum(batch["sizes"])])
     rec = 0
     for v, (s, o, _, _) in enumerate(batch["st"]):
-        amb = o.amb_pixel
+        amb = o.extra["skip"]
+        assert amb.mean() < 0.01
         assert max(image_error(batch["img"][v], o.color, amb)) <= IMG_TOL
         assert max(image_error(batch["amap"][v], o.others, amb)) <= AUX_TOL
         n = int(batch["sizes"][s])

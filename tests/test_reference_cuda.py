@@ -39,16 +39,13 @@ import pytest
 import torch
 
 from oracle import surfel_oracle as O
-from tests._util import grad_error, image_error, oracle_camera, oracle_surfels, ours_render
+from tests._util import (GEOMETRY_GRADS, GRAD_L2_TOL_GEOMETRY, GRAD_TOL, GRAD_TOL_GEOMETRY, grad_error,
+                         ill_conditioned, image_error, l2_error, oracle_camera, oracle_surfels, ours_render)
 
 pytestmark = pytest.mark.gpu
 
 IMG_TOL = 1e-5           # RGB
 AUX_TOL = 3e-5           # auxiliary maps, final T planes, semantics
-GRAD_L2_TOL = 1e-4       # |ours - ref|_2 / |ref|_2
-GRAD_MAX_TOL = 1e-4      # max |ours - ref| / max |ref|
-GRAD_MAX_TOL_GEOMETRY = 3e-4
-GEOMETRY = ("dL_dmeans3D", "dL_dmeans2D", "dL_drotations", "dL_dtransmat")
 
 
 def _ref():
@@ -113,8 +110,7 @@ def _run(case):
     osf = oracle_surfels(sc, colors_precomp=case.get("colors"), semantics=case.get("semantics"))
     variant = O.PART if part else O.PLAIN
     st = O.forward_view(osf, ocam, np.array(case["bg"]), variant, np.float64)
-    sens = O.fp32_sensitivity(st, ocam, osf, np.array(case["bg"]), variant)
-    ill = (sens[:3].max(0) > 0.5 * IMG_TOL) | (sens[3:].max(0) > 0.5 * AUX_TOL)
+    ill = ill_conditioned(st, ocam, osf, case["bg"], variant, IMG_TOL, AUX_TOL)
     amb_px = st.amb_pixel | ill
     amb_s, amb_t = st.amb_surfel, st.extra["amb_tiles"]
     amb_count = st.extra["amb_count_pixel"]
@@ -194,13 +190,6 @@ def test_images(run):
     assert max(v for k, v in errs.items() if k != "color") <= AUX_TOL, errs
 
 
-def _l2(a, b):
-    a = np.asarray(a, np.float64).reshape(-1)
-    b = np.asarray(b, np.float64).reshape(-1)
-    n = float(np.linalg.norm(b))
-    return float(np.linalg.norm(a - b)) / n if n else float(np.linalg.norm(a))
-
-
 def test_gradients(run):
     ours, ref, ref2, o64 = run["ours"], run["ref"], run["ref2"], run["o64"]
     report, bad = {}, {}
@@ -208,13 +197,13 @@ def test_gradients(run):
         a, b = ours[k].reshape(-1), ref[k].reshape(-1)
         c = np.asarray(o64[k]).reshape(-1)
         e_max = grad_error(a, b)
-        e_l2 = _l2(a, b)
-        e_l2_64 = _l2(a, c)
+        e_l2 = l2_error(a, b)
+        e_l2_64 = l2_error(a, c)
         report[k] = dict(max=f"{e_max:.2e}", l2=f"{e_l2:.2e}", l2_fp64=f"{e_l2_64:.2e}",
-                         ref_max_fp64=f"{grad_error(b, c):.2e}", ref_l2_fp64=f"{_l2(b, c):.2e}",
+                         ref_max_fp64=f"{grad_error(b, c):.2e}", ref_l2_fp64=f"{l2_error(b, c):.2e}",
                          ref_run_to_run=f"{grad_error(ref2[k].reshape(-1), b):.1e}")
-        tol = GRAD_MAX_TOL_GEOMETRY if k in GEOMETRY else GRAD_MAX_TOL
-        tol_l2 = GRAD_L2_TOL_GEOMETRY if k in GEOMETRY else GRAD_L2_TOL
+        tol = GRAD_TOL_GEOMETRY if k in GEOMETRY_GRADS else GRAD_TOL
+        tol_l2 = GRAD_L2_TOL_GEOMETRY if k in GEOMETRY_GRADS else GRAD_TOL
         if e_max > tol or e_l2 > tol_l2 or e_l2_64 > tol_l2:
             bad[k] = report[k]
     print("gradients vs reference CUDA:", report)

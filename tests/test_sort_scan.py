@@ -1,8 +1,8 @@
 """The forward's own radix sort and prefix sums (sgr_sort.cu) against the
 stable sort of the same keys (numpy's, and PyTorch's on the GPU) and
 numpy's cumulative sums: identical keys and values, in the same order, for
-every size around the kernels' 2048-element tiles, heavy ties, all-equal
-keys, and partial key widths."""
+every size around the sort's 4096-key tiles and the scans' 2048-element
+tiles, heavy ties, all-equal keys, and partial key widths."""
 import ctypes as C
 
 import numpy as np
@@ -11,7 +11,7 @@ import torch
 
 pytestmark = pytest.mark.gpu
 
-SIZES = [1, 2, 31, 2047, 2048, 2049, 6143, 100_003, 1_048_576 + 17]
+SIZES = [1, 2, 31, 2047, 2048, 2049, 4095, 4096, 4097, 6143, 12_289, 100_003, 1_048_576 + 17]
 
 
 def _sort(lib, keys, vals, key_bytes, end_bit):
