@@ -348,10 +348,19 @@ def run_gpu(args):
     targets = targets_host.to(dev)
 
     tr = SurfelTrainer(scene, cams, device=dev)
-    if args.cell_tiles:                            # a fixed cell size (profiling runs: no tuning launches)
+    fixed = bool(args.cell_tiles)
+    if fixed:                                      # a fixed launch shape (profiling runs: no tuning launches)
         tr.raster.cell_tiles = args.cell_tiles
-    # cell size timed per workload unless given; the warm-up steps size the lists
-    tr.capture(targets, warmup=3, autotune=not args.cell_tiles)
+        tr.raster.blend_shape = args.blend_shape
+        tr.raster.tile_schedule = args.tile_schedule
+    # cell size, warp footprint and tile schedule timed per workload unless
+    # given; the warm-up steps size the lists
+    tr.capture(targets, warmup=3, autotune=not fixed)
+    tuning = {}
+    if not fixed:
+        from partgs_gb300 import autotune as AT
+        tuning = {"cells_ms": {str(k): round(v, 3) for k, v in AT.tune_cells.last_timings.items()},
+                  "blend_ms": {f"shape{k[0]}_sched{k[1]}": round(v, 3) for k, v in AT.tune_blend.last_timings.items()}}
     launches_per_step = tr.launches_per_step
     for _ in range(args.warmup):
         tr.replay()
@@ -429,7 +438,9 @@ def run_gpu(args):
             "config": dict(_workload_config(args.workload), keys=keys, cell_list_entries=nbins,
                            fragments_fwd=frag_fwd, fragments_bwd=frag_bwd,
                            cell_list_capacity=tr.raster.bin_capacity, cell_tiles=tr.raster.cell_tiles,
-                           parallelism=f"replicas x{ws}"),
+                           blend_shape=["strip16", "patch8"][tr.raster.blend_shape],
+                           tile_schedule=["grid", "queue"][tr.raster.tile_schedule],
+                           autotune_ms=tuning or None, parallelism=f"replicas x{ws}"),
             "e2e": {"value": ws / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(targets_host.numel() * 4),
                     "d2h_bytes_per_step": 4},
             "roofline": roofline, "gpu_launches": int(launches_per_step) * args.steps, "clocks": clk}
@@ -611,7 +622,11 @@ def main():
     ap.add_argument("--no-reference-cuda", action="store_true",
                     help="skip timing the reference's CUDA rasteriser on the same workload")
     ap.add_argument("--cell-tiles", type=int, default=0, choices=[0, 1, 2, 4, 8, 16],
-                    help="cell edge in tiles (0: autotuned)")
+                    help="cell edge in tiles (0: cell edge, warp footprint and tile schedule autotuned)")
+    ap.add_argument("--blend-shape", type=int, default=0, choices=[0, 1],
+                    help="with --cell-tiles: the blends' warp footprint (0: 16x2 strips, 1: 8-wide patches)")
+    ap.add_argument("--tile-schedule", type=int, default=0, choices=[0, 1],
+                    help="with --cell-tiles: 0 a CTA per tile, 1 persistent CTAs on a tile queue")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -23,12 +23,13 @@
 //  2. per cell, an exclusive scan over the view's chunks gives each chunk's
 //     first position in the cell's list and the cell's total; the totals are
 //     scanned into each cell's start in one concatenated array;
-//  3. per chunk, every warp counts its own slice of records per cell, the
-//     block turns the counts into per-warp bases, then each warp walks its
-//     slice record by record (the lanes cover the record's cells, which are
-//     distinct) and writes the entry at its cell's next slot.  Within a
-//     cell, entries come in chunk order, then warp order, then record order:
-//     depth order.
+//  3. per chunk, every warp counts its own slice of records per cell (a
+//     2-D difference array of the slice's cell rectangles in shared memory,
+//     then prefix sums along x and y), the block turns the counts into
+//     per-warp bases, then each warp walks its slice record by record (the
+//     lanes cover the record's cells, which are distinct) and writes the
+//     entry at its cell's next slot.  Within a cell, entries come in chunk
+//     order, then warp order, then record order: depth order.
 // Cell-list entries are depth-order positions (the blend reads the
 // rectangle and the record id from them).
 //
@@ -57,7 +58,8 @@ struct CellArgs {
   long long capacity;                // entries `out` holds
   unsigned int overflow_flag;        // status flag raised when the lists exceed the capacity
   int V;
-  int B;                             // cell edge in tiles
+  int B;                             // cell edge in tiles (a power of two)
+  int lb;                            // log2(B)
   int cx, cy;                        // cells per view along x and y
   int warps;                         // warps of the list-writing CTA
   bool ids;                          // write record ids (else depth-order positions)
@@ -82,18 +84,22 @@ __device__ __forceinline__ bool chunk_span(const CellArgs& a, int c, int& v, int
   return true;
 }
 
-// Cell rectangle [x0, x1) x [y0, y1) of a packed tile rectangle; empty for an empty one.
-__device__ __forceinline__ void cell_rect(uint2 r, int B, int& x0, int& y0, int& x1, int& y1) {
+// Cell rectangle [x0, x1) x [y0, y1) of a packed tile rectangle, for cells
+// of 2^lb tiles; empty for an empty one.
+__device__ __forceinline__ void cell_rect(uint2 r, int lb, int& x0, int& y0, int& x1, int& y1) {
   unpack_rect(r, x0, y0, x1, y1);
   if (x0 >= x1 || y0 >= y1) {
     x0 = y0 = x1 = y1 = 0;
     return;
   }
-  x0 /= B;
-  y0 /= B;
-  x1 = (x1 + B - 1) / B;
-  y1 = (y1 + B - 1) / B;
+  const int m = (1 << lb) - 1;
+  x0 >>= lb;
+  y0 >>= lb;
+  x1 = (x1 + m) >> lb;
+  y1 = (y1 + m) >> lb;
 }
+
+__host__ __device__ __forceinline__ int log2_of(int B) { return B >= 16 ? 4 : B >= 8 ? 3 : B >= 4 ? 2 : B >= 2 ? 1 : 0; }
 
 // 0. tile rectangles and key counts in depth order; (record, cell) pair count
 __global__ void __launch_bounds__(256) k_gather_rects(const uint32_t* __restrict__ order,
@@ -117,7 +123,7 @@ __global__ void __launch_bounds__(256) k_gather_rects(const uint32_t* __restrict
       tile_rect(r2.y, r2.z, radii[r], gx, gy, x0, y0, x1, y1);
       out = pack_rect(x0, y0, x1, y1);
       int cx0, cy0, cx1, cy1;
-      cell_rect(out, B, cx0, cy0, cx1, cy1);
+      cell_rect(out, log2_of(B), cx0, cy0, cx1, cy1);
       cells = (unsigned int)((cx1 - cx0) * (cy1 - cy0));
     }
     rects[j] = out;
@@ -154,7 +160,7 @@ __global__ void __launch_bounds__(256) k_cell_hist(CellArgs a) {
   __syncthreads();
   for (int p = p0 + threadIdx.x; p < p1; p += blockDim.x) {
     int x0, y0, x1, y1;
-    cell_rect(a.rects[p], a.B, x0, y0, x1, y1);
+    cell_rect(a.rects[p], a.lb, x0, y0, x1, y1);
     if (x0 >= x1) continue;
     atomicAdd(&s_diff[y0 * W1 + x0], 1);
     atomicAdd(&s_diff[y0 * W1 + x1], -1);
@@ -237,38 +243,38 @@ __global__ void __launch_bounds__(256) k_cell_write(CellArgs a) {
   __syncthreads();
   const int per_warp = kChunk / a.warps;
   const int w0 = p0 + warp * per_warp, w1 = min(p1, w0 + per_warp);
+  const int cx = a.cx, cy = a.cy;
 
-  // walks this warp's records in order; for each, the lanes cover its cells
-  auto walk = [&](bool place) {
-    for (int g = w0; g < w1; g += 32) {
-      const int p = g + lane;
-      int x0 = 0, y0 = 0, x1 = 0, y1 = 0;
-      uint32_t e = 0;
-      if (p < w1) {
-        cell_rect(a.rects[p], a.B, x0, y0, x1, y1);
-        if (place) e = a.ids ? a.depth_order[p] : (uint32_t)p;
-      }
-      const int m = min(32, w1 - g);
-      for (int k = 0; k < m; ++k) {
-        const uint32_t ek = __shfl_sync(0xffffffffu, e, k);
-        const int ax = __shfl_sync(0xffffffffu, x0, k), ay = __shfl_sync(0xffffffffu, y0, k);
-        const int bx = __shfl_sync(0xffffffffu, x1, k), by = __shfl_sync(0xffffffffu, y1, k);
-        const int w = bx - ax, n = w * (by - ay);
-        for (int q = lane; q < n; q += 32) {
-          const int ty = ay + q / w, tx = ax + q - (q / w) * w;
-          const int t = ty * a.cx + tx;
-          if (!place) {
-            cnt[t] += 1;
-          } else {
-            const uint32_t pos = cnt[t]++;
-            if ((long long)pos < a.capacity) a.out[pos] = ek;
-          }
-        }
-        __syncwarp();
-      }
+  // this warp's count per cell: difference array of its records' cell
+  // rectangles (updates past the last column or row have no effect inside
+  // the grid and are dropped), then prefix sums along x and along y
+  for (int p = w0 + lane; p < w1; p += 32) {
+    int x0, y0, x1, y1;
+    cell_rect(a.rects[p], a.lb, x0, y0, x1, y1);
+    if (x0 >= x1) continue;
+    atomicAdd(&cnt[y0 * cx + x0], 1u);
+    if (x1 < cx) atomicAdd(&cnt[y0 * cx + x1], 0xffffffffu);
+    if (y1 < cy) {
+      atomicAdd(&cnt[y1 * cx + x0], 0xffffffffu);
+      if (x1 < cx) atomicAdd(&cnt[y1 * cx + x1], 1u);
     }
-  };
-  walk(false);
+  }
+  __syncwarp();
+  for (int y = lane; y < cy; y += 32) {
+    uint32_t run = 0;
+    for (int x = 0; x < cx; ++x) {
+      run += cnt[y * cx + x];
+      cnt[y * cx + x] = run;
+    }
+  }
+  __syncwarp();
+  for (int x = lane; x < cx; x += 32) {
+    uint32_t run = 0;
+    for (int y = 0; y < cy; ++y) {
+      run += cnt[y * cx + x];
+      cnt[y * cx + x] = run;
+    }
+  }
   __syncthreads();
   const uint32_t* cbase = a.chunk_base + (size_t)blockIdx.x * ncell;
   const uint32_t* cstart = a.cell_start + (size_t)v * ncell;
@@ -281,7 +287,33 @@ __global__ void __launch_bounds__(256) k_cell_write(CellArgs a) {
     }
   }
   __syncthreads();
-  walk(true);
+  // walk this warp's records in order; for each, the lanes cover its cells
+  for (int g = w0; g < w1; g += 32) {
+    const int p = g + lane;
+    uint2 r = make_uint2(0u, 0u);
+    uint32_t e = 0;
+    if (p < w1) {
+      r = a.rects[p];
+      e = a.ids ? a.depth_order[p] : (uint32_t)p;
+    }
+    const int m = min(32, w1 - g);
+    for (int k = 0; k < m; ++k) {
+      const uint32_t ek = __shfl_sync(0xffffffffu, e, k);
+      uint2 rk;
+      rk.x = __shfl_sync(0xffffffffu, r.x, k);
+      rk.y = __shfl_sync(0xffffffffu, r.y, k);
+      int ax, ay, bx, by;
+      cell_rect(rk, a.lb, ax, ay, bx, by);
+      const int w = bx - ax, n = w * (by - ay);
+      for (int q = lane; q < n; q += 32) {
+        const int qy = q / w;
+        const int t = (ay + qy) * cx + ax + (q - qy * w);
+        const uint32_t pos = cnt[t]++;
+        if ((long long)pos < a.capacity) a.out[pos] = ek;
+      }
+      __syncwarp();
+    }
+  }
 }
 
 constexpr size_t kMaxDynSmem = 220 * 1024;
@@ -346,6 +378,7 @@ int run_cells(const sgr_batch& b, const GeomView& g, int B, bool ids, uint32_t* 
   a.overflow_flag = overflow_flag;
   a.V = b.num_views;
   a.B = B;
+  a.lb = log2_of(B);
   a.cx = cx;
   a.cy = cy;
   a.warps = warps;

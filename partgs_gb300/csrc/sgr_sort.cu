@@ -3,16 +3,20 @@
 // (replacing the library sort and scans the reference calls,
 // cuda_rasterizer/rasterizer_impl.cu:278, 304-309).
 //
-// Sort: 8-bit digits, one pass per digit of bits [0, end_bit).  Each pass is
-// three kernels:
-//   1. k_radix_hist: per 4096-key tile, the 256-bin digit histogram, stored
+// Sort: digits of up to 9 bits, as few passes as cover bits [0, end_bit)
+// (36-bit (view, depth) keys: 4 passes of 9 bits).  Each pass is three
+// kernels:
+//   1. k_radix_hist: per 4096-key tile, the digit histogram, stored
 //      digit-major (hist[digit][tile]);
 //   2. k_radix_scan: per digit, the exclusive scan of its counts over the
 //      tiles, and the digit's total;
 //   3. k_radix_scatter: per tile, every key's rank among the tile's keys of
-//      its digit in input order (warp match + per-warp counts, round by
-//      round), the tile reordered by (digit, rank) in shared memory, then
-//      written out in digit runs: out[digit base + tile prefix + rank].
+//      its digit in input order, the tile reordered by (digit, rank) in
+//      shared memory, then written out in digit runs:
+//      out[digit base + tile prefix + rank].  A warp owns 512 consecutive
+//      keys of the tile and ranks them with warp-private digit counters
+//      (match_any per 32 keys, no block barrier); the warps' counts are
+//      then scanned per digit, so earlier warps' keys come first.
 // Equal digits keep their input order in every pass, so the result is the
 // stable order of the keys (ties by input position), the order of any
 // stable radix sort of the same bits.
@@ -27,17 +31,20 @@ namespace {
 
 constexpr int kSortThreads = 256;
 constexpr int kRadixItems = 16;
+constexpr int kWarpSpan = 32 * kRadixItems;              // 512 keys per warp
 constexpr int kRadixTile = kSortThreads * kRadixItems;   // 4096 keys per sort CTA
 constexpr int kSortItems = 8;
 constexpr int kSortTile = kSortThreads * kSortItems;     // 2048 elements per scan CTA
-constexpr int kBins = 256;
+constexpr int kMaxDigitBits = 9;
+constexpr int kBins = 1 << kMaxDigitBits;                // 512
+constexpr int kBinsPerThread = kBins / kSortThreads;     // 2
 constexpr int kSortWarps = kSortThreads / 32;
 
 inline long long tiles_of(long long n) { return (n + kSortTile - 1) / kSortTile; }
 inline long long radix_tiles_of(long long n) { return (n + kRadixTile - 1) / kRadixTile; }
 
-// The pass's digit: bits [shift, shift + 8) of the key, cut at the sort's
-// end bit (dmask keeps the digit's bits below it).
+// The pass's digit: bits [shift, shift + width) of the key (dmask keeps the
+// width, cut at the sort's end bit).
 template <class K>
 __device__ __forceinline__ uint32_t digit_of(K key, int shift, uint32_t dmask) {
   return (uint32_t)(key >> shift) & dmask;
@@ -68,25 +75,50 @@ __device__ __forceinline__ T block_exclusive_scan(T v, T* s_warp, T& total) {
   return before + incl - v;
 }
 
+// Exclusive scan over the kBins digits, thread t holding digits
+// t*kBinsPerThread .. +kBinsPerThread-1 (consecutive).
+template <class T>
+__device__ __forceinline__ void digits_exclusive_scan(const T (&v)[kBinsPerThread], T (&ex)[kBinsPerThread],
+                                                      T* s_warp) {
+  T sum = 0;
+#pragma unroll
+  for (int j = 0; j < kBinsPerThread; ++j) sum += v[j];
+  T tot;
+  T run = block_exclusive_scan<T>(sum, s_warp, tot);
+#pragma unroll
+  for (int j = 0; j < kBinsPerThread; ++j) {
+    ex[j] = run;
+    run += v[j];
+  }
+}
+
 template <class K>
 __global__ void __launch_bounds__(kSortThreads) k_radix_hist(const K* __restrict__ keys, long long n, int shift,
                                                              uint32_t dmask, uint32_t* __restrict__ hist,
                                                              long long ntiles) {
   __shared__ uint32_t s_cnt[kBins];
-  s_cnt[threadIdx.x] = 0;
+#pragma unroll
+  for (int j = 0; j < kBinsPerThread; ++j) s_cnt[j * kSortThreads + threadIdx.x] = 0;
   __syncthreads();
   const long long base = (long long)blockIdx.x * kRadixTile;
   const int lane = threadIdx.x & 31;
+  uint32_t d[kRadixItems];
+#pragma unroll
+  for (int k = 0; k < kRadixItems; ++k) {       // all loads first
+    const long long i = base + k * kSortThreads + threadIdx.x;
+    d[k] = i < n ? digit_of(keys[i], shift, dmask) : (uint32_t)kBins;
+  }
 #pragma unroll
   for (int k = 0; k < kRadixItems; ++k) {
-    const long long i = base + k * kSortThreads + threadIdx.x;
-    const bool valid = i < n;
-    const uint32_t d = valid ? digit_of(keys[i], shift, dmask) : (uint32_t)kBins;
-    const unsigned peers = __match_any_sync(0xffffffffu, d);
-    if (valid && lane == __ffs(peers) - 1) atomicAdd(&s_cnt[d], (uint32_t)__popc(peers));
+    const unsigned peers = __match_any_sync(0xffffffffu, d[k]);
+    if (d[k] < kBins && lane == __ffs(peers) - 1) atomicAdd(&s_cnt[d[k]], (uint32_t)__popc(peers));
   }
   __syncthreads();
-  hist[(size_t)threadIdx.x * ntiles + blockIdx.x] = s_cnt[threadIdx.x];
+#pragma unroll
+  for (int j = 0; j < kBinsPerThread; ++j) {
+    const int b = j * kSortThreads + threadIdx.x;
+    hist[(size_t)b * ntiles + blockIdx.x] = s_cnt[b];
+  }
 }
 
 // One CTA per digit: exclusive scan of its per-tile counts, in place.
@@ -118,75 +150,85 @@ __global__ void __launch_bounds__(kSortThreads) k_radix_scatter(const K* __restr
   extern __shared__ __align__(16) unsigned char s_dyn[];   // the tile in (digit, rank) order: keys, then values
   K* s_keys = reinterpret_cast<K*>(s_dyn);
   uint32_t* s_vals = reinterpret_cast<uint32_t*>(s_dyn + sizeof(K) * kRadixTile);
-  __shared__ uint32_t s_wc[kSortWarps][kBins];     // this round's count of each digit per warp
-  __shared__ uint32_t s_run[kBins];                // keys of each digit ranked so far
+  __shared__ uint32_t s_wc[kSortWarps][kBins];     // per warp: keys of each digit (then: keys in earlier warps)
   __shared__ uint32_t s_local[kBins];              // start of each digit in the tile's order
   __shared__ unsigned long long s_gbase[kBins];    // output position of the tile's first key of each digit
   __shared__ unsigned long long s_warp64[kSortWarps];
   __shared__ uint32_t s_warp32[kSortWarps];
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
   const long long base = (long long)blockIdx.x * kRadixTile;
+  const long long wbase = base + (long long)warp * kWarpSpan;
 
-  // global start of digit t: all smaller digits, then the tiles before this one
-  {
-    unsigned long long tot;
-    const unsigned long long ex = block_exclusive_scan<unsigned long long>(totals[t], s_warp64, tot);
-    s_gbase[t] = ex + hist[(size_t)t * ntiles + blockIdx.x];
-  }
   K key[kRadixItems];
-  uint32_t val[kRadixItems], dig[kRadixItems];
-  s_run[t] = 0;
+  uint32_t val[kRadixItems];
 #pragma unroll
-  for (int w = 0; w < kSortWarps; ++w) s_wc[w][t] = 0;
-  __syncthreads();
-#pragma unroll
-  for (int k = 0; k < kRadixItems; ++k) {
-    const long long i = base + k * kSortThreads + t;
-    const bool valid = i < n;
-    key[k] = valid ? keys_in[i] : (K)0;
-    val[k] = valid ? vals_in[i] : 0u;
-    dig[k] = valid ? digit_of(key[k], shift, dmask) : (uint32_t)kBins;
-    const unsigned peers = __match_any_sync(0xffffffffu, dig[k]);
-    if (valid && lane == __ffs(peers) - 1) atomicAdd(&s_run[dig[k]], (uint32_t)__popc(peers));
+  for (int k = 0; k < kRadixItems; ++k) {       // all loads first; a warp's keys are consecutive
+    const long long i = wbase + k * 32 + lane;
+    key[k] = i < n ? keys_in[i] : (K)0;
+    val[k] = i < n ? vals_in[i] : 0u;
   }
-  __syncthreads();
+#pragma unroll
+  for (int j = 0; j < kBinsPerThread; ++j)
+#pragma unroll
+    for (int w = 0; w < kSortWarps; ++w) s_wc[w][j * kSortThreads + t] = 0;
+  // global start of each digit: all smaller digits, then the tiles before this one
   {
-    uint32_t tot;
-    const uint32_t cnt = s_run[t];
-    s_local[t] = block_exclusive_scan<uint32_t>(cnt, s_warp32, tot);
-    s_run[t] = 0;
+    unsigned long long tot[kBinsPerThread], ex[kBinsPerThread];
+#pragma unroll
+    for (int j = 0; j < kBinsPerThread; ++j) tot[j] = totals[t * kBinsPerThread + j];
+    digits_exclusive_scan<unsigned long long>(tot, ex, s_warp64);   // (its barriers also cover the zeroing)
+#pragma unroll
+    for (int j = 0; j < kBinsPerThread; ++j) {
+      const int b = t * kBinsPerThread + j;
+      s_gbase[b] = ex[j] + hist[(size_t)b * ntiles + blockIdx.x];
+    }
   }
-  __syncthreads();
-  uint32_t pos[kRadixItems];
+  // rank within the warp, in input order: (digit << 16) | rank
+  uint32_t dr[kRadixItems];
+  const unsigned lt = (1u << lane) - 1u;
 #pragma unroll
   for (int k = 0; k < kRadixItems; ++k) {
-    const uint32_t d = dig[k];
+    const long long i = wbase + k * 32 + lane;
+    const uint32_t d = i < n ? digit_of(key[k], shift, dmask) : (uint32_t)kBins;
     const unsigned peers = __match_any_sync(0xffffffffu, d);
-    const uint32_t lrank = __popc(peers & ((1u << lane) - 1u));
-    if (d < kBins && lrank == 0) s_wc[warp][d] = __popc(peers);
-    __syncthreads();
-    if (d < kBins) {
-      uint32_t before = s_run[d];
-      for (int w = 0; w < warp; ++w) before += s_wc[w][d];
-      pos[k] = s_local[d] + before + lrank;
+    const int leader = __ffs(peers) - 1;
+    uint32_t before = 0;
+    if (lane == leader && d < kBins) {
+      before = s_wc[warp][d];
+      s_wc[warp][d] = before + (uint32_t)__popc(peers);
     }
-    __syncthreads();
-    {
-      uint32_t add = 0;
+    before = __shfl_sync(0xffffffffu, before, leader);
+    __syncwarp();
+    dr[k] = (d << 16) | (before + (uint32_t)__popc(peers & lt));
+  }
+  __syncthreads();
+  // per digit: exclusive prefix over the warps, and the tile's count
+  {
+    uint32_t cnt[kBinsPerThread], ex[kBinsPerThread];
+#pragma unroll
+    for (int j = 0; j < kBinsPerThread; ++j) {
+      const int b = t * kBinsPerThread + j;
+      uint32_t run = 0;
 #pragma unroll
       for (int w = 0; w < kSortWarps; ++w) {
-        add += s_wc[w][t];
-        s_wc[w][t] = 0;
+        const uint32_t c = s_wc[w][b];
+        s_wc[w][b] = run;
+        run += c;
       }
-      s_run[t] += add;
+      cnt[j] = run;
     }
-    __syncthreads();
+    digits_exclusive_scan<uint32_t>(cnt, ex, s_warp32);
+#pragma unroll
+    for (int j = 0; j < kBinsPerThread; ++j) s_local[t * kBinsPerThread + j] = ex[j];
   }
+  __syncthreads();
 #pragma unroll
   for (int k = 0; k < kRadixItems; ++k) {
-    if (dig[k] < kBins) {
-      s_keys[pos[k]] = key[k];
-      s_vals[pos[k]] = val[k];
+    const uint32_t d = dr[k] >> 16;
+    if (d < kBins) {
+      const uint32_t pos = s_local[d] + s_wc[warp][d] + (dr[k] & 0xffffu);
+      s_keys[pos] = key[k];
+      s_vals[pos] = val[k];
     }
   }
   __syncthreads();
@@ -298,7 +340,9 @@ int radix_sort_pairs(const K* keys_in, K* keys_out, const uint32_t* vals_in, uin
   uint32_t* hist = reinterpret_cast<uint32_t*>(p);
   p += align256((size_t)kBins * nt * 4);
   uint32_t* totals = reinterpret_cast<uint32_t*>(p);
-  const int passes = (end_bit + 7) / 8;
+  // as few passes as cover the bits, digits as even as possible
+  const int passes = (end_bit + kMaxDigitBits - 1) / kMaxDigitBits;
+  const int width = passes ? (end_bit + passes - 1) / passes : 0;
   const K* src_k = keys_in;
   const uint32_t* src_v = vals_in;
   for (int pass = 0; pass < passes; ++pass) {
@@ -306,8 +350,8 @@ int radix_sort_pairs(const K* keys_in, K* keys_out, const uint32_t* vals_in, uin
     const bool to_out = ((passes - 1 - pass) % 2) == 0;
     K* dst_k = to_out ? keys_out : alt_keys;
     uint32_t* dst_v = to_out ? vals_out : alt_vals;
-    const int shift = 8 * pass;
-    const int bits = end_bit - shift < 8 ? end_bit - shift : 8;
+    const int shift = width * pass;
+    const int bits = end_bit - shift < width ? end_bit - shift : width;
     const uint32_t dmask = (1u << bits) - 1u;
     k_radix_hist<K><<<(unsigned)nt, kSortThreads, 0, st>>>(src_k, n, shift, dmask, hist, nt);
     k_radix_scan<<<kBins, kSortThreads, 0, st>>>(hist, nt, totals);
