@@ -165,27 +165,30 @@ def _eval(job):
     return out
 
 
-def _surfel_grads(case, v, wc, wo, tiles=None):
+def _surfel_grads(case, v, wc, wo, tiles=None, exact=True):
     """FP64 oracle adjoint of sum(wc * colour + wo * others) of view v at the
     case's parameters: per-surfel gradients (means3D, scales, rotations,
-    opacity) -- the rasteriser half of the chain."""
+    opacity) -- the rasteriser half of the chain.  ``exact``: tiles ordered
+    by FP64 depth (the chain the differences see); else by the FP32 depth
+    bits, as the reference and the library sort."""
     from oracle import surfel_oracle as O
     cache = _W.setdefault("forward", {})
-    if v not in cache:          # the forward at the case's parameters, once per view and process
+    if (v, exact) not in cache:      # the forward at the case's parameters, once per view and process
         inp = case["inp"]
         s = _surfels(case, [inp[k] for k in NAMES])
         cam = _camera(case["cams"][v])
-        cache[v] = (s, cam, O.forward_view(s, cam, np.zeros(3), O.PLAIN, np.float64, exact_depth=True))
-    s, cam, st = cache[v]
+        cache[(v, exact)] = (s, cam, O.forward_view(s, cam, np.zeros(3), O.PLAIN, np.float64, exact_depth=exact))
+    s, cam, st = cache[(v, exact)]
     g = O.backward_view(st, cam, s, np.zeros(3), wc, wo, variant=O.PLAIN, dtype=np.float64, tiles=tiles)
     return [np.asarray(g[k], np.float64) for k in ("dL_dmeans3D", "dL_dscales", "dL_drotations", "dL_dopacity")]
 
 
 def _eval_grads(job):
-    """job = (key, view, flat pixel indices or None): the surfel gradients of
-    the loss restricted to those pixels (all pixels with None)."""
+    """job = (key, view, flat pixel indices or None[, exact]): the surfel
+    gradients of the loss restricted to those pixels (all pixels with None)."""
     case = _W["case"]
-    key, v, pix = job
+    key, v, pix = job[:3]
+    exact = job[3] if len(job) > 3 else True
     wc, wo = case["w_col"][v], case["w_oth"][v]
     tiles = None
     if pix is not None:
@@ -196,7 +199,7 @@ def _eval_grads(job):
         wc, wo = wc * keep, wo * keep
         gx = (cam.width + 15) // 16
         tiles = np.unique((pix // cam.width) // 16 * gx + (pix % cam.width) // 16)
-    return key, _surfel_grads(case, v, wc, wo, tiles)
+    return key, _surfel_grads(case, v, wc, wo, tiles, exact)
 
 
 def chain_to_parameters(case, surfel_grads):
@@ -221,7 +224,10 @@ def check(case_kwargs, params, h=1e-6, procs=None, richardson=True):
     of the rasteriser, then the binding's autograd.  Returns the
     finite_differences records, each with ``an64`` (the analytic value of
     the loss its ``fd`` differentiates, flip pixels left out) and
-    ``masks`` (per view, the flat pixel indices left out).
+    ``masks`` (per view, the flat pixel indices left out), and ``an64_ref``:
+    the same analytic gradient with each tile's surfels in the reference's
+    order (FP32 depth bits, then index), the one to hold an FP32
+    implementation of the reference's algorithm against.
 
     With ``richardson`` the difference is extrapolated from the steps h and
     h/2, (4 D(h/2) - D(h)) / 3, which cancels the truncation term (h^2 / 6
@@ -247,7 +253,8 @@ def check(case_kwargs, params, h=1e-6, procs=None, richardson=True):
             jobs.append((n, f, 0.0))
     ctx = mp.get_context("spawn")
     with ctx.Pool(procs, initializer=_init, initargs=(case_kwargs,)) as pool:
-        full = pool.map_async(_eval_grads, [(("full", v), v, None) for v in range(V)], chunksize=1)
+        full = pool.map_async(_eval_grads, [(("full", v, ex), v, None, ex) for v in range(V) for ex in (True, False)],
+                              chunksize=1)
         res = pool.map(_eval, jobs, chunksize=1)
         out = []
         corr_jobs = []
@@ -269,18 +276,19 @@ def check(case_kwargs, params, h=1e-6, procs=None, richardson=True):
                 flips += int(flip.sum())
                 masks.append(idx[flip])
                 if flip.any():
-                    corr_jobs.append(((i, v), v, idx[flip]))
+                    corr_jobs += [((i, v, ex), v, idx[flip], ex) for ex in (True, False)]
             out.append(dict(name=n, flat=f, fd=fd, views=views, flips=flips, masks=masks))
         corr = dict(pool.map(_eval_grads, corr_jobs, chunksize=1))
         full = dict(full.get())
-    g_full = [sum(full[("full", v)][k] for v in range(V)) for k in range(4)]
-    base = chain_to_parameters(case, g_full)
-    for i, r in enumerate(out):
-        a = float(base[r["name"]][r["flat"]])
-        for v in range(V):
-            if (i, v) in corr:
-                a -= float(chain_to_parameters(case, corr[(i, v)])[r["name"]][r["flat"]])
-        r["an64"] = a
+    for ex, key in ((True, "an64"), (False, "an64_ref")):
+        g_full = [sum(full[("full", v, ex)][k] for v in range(V)) for k in range(4)]
+        base = chain_to_parameters(case, g_full)
+        for i, r in enumerate(out):
+            a = float(base[r["name"]][r["flat"]])
+            for v in range(V):
+                if (i, v, ex) in corr:
+                    a -= float(chain_to_parameters(case, corr[(i, v, ex)])[r["name"]][r["flat"]])
+            r[key] = a
     return case, out
 
 

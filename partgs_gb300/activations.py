@@ -67,3 +67,28 @@ class _ActivateFn(torch.autograd.Function):
 def activate(log_scaling, rotation, opacity_logit, features_dc, features_rest):
     """(scales, rotations, opacities, shs) with autograd."""
     return _ActivateFn.apply(log_scaling, rotation, opacity_logit, features_dc, features_rest)
+
+
+def activate_forward(ins):
+    """The forward without autograd: ins = (log_scaling, rotation,
+    opacity_logit, features_dc, features_rest), contiguous; returns
+    (scales, rotations, opacities, shs)."""
+    P, M, dev = ins[0].shape[0], 1 + ins[4].shape[1], ins[0].device
+    scales = torch.empty(P, 2, device=dev)
+    rots = torch.empty(P, 4, device=dev)
+    opac = torch.empty(ins[2].shape, device=dev)
+    shs = torch.empty(P, M, 3, device=dev)
+    a = ActivateArgs(P, M, *(t.data_ptr() for t in ins), scales.data_ptr(), rots.data_ptr(), opac.data_ptr(),
+                     shs.data_ptr(), None, None, None, None, None)
+    L.check(_lib().sgr_activate_forward(C.byref(a), torch.cuda.current_stream().cuda_stream), "sgr_activate_forward")
+    return scales, rots, opac, shs
+
+
+def activate_backward(ins, ups, outs):
+    """The backward without autograd: gradients of (scales, rotations,
+    opacities, shs) in ``ups`` (None for none) written into ``outs``, one
+    contiguous buffer per input of ``ins`` (e.g. the parameters' ``.grad``)."""
+    P, M = ins[0].shape[0], 1 + ins[4].shape[1]
+    a = ActivateArgs(P, M, *(t.data_ptr() for t in ins), None, None, None, None, *(g.data_ptr() for g in outs))
+    L.check(_lib().sgr_activate_backward(C.byref(a), *(_ptr(u) for u in ups), torch.cuda.current_stream().cuda_stream),
+            "sgr_activate_backward")

@@ -24,17 +24,10 @@ from . import raster as _r
 class _MultiViewFn(torch.autograd.Function):
     @staticmethod
     def forward(ctx, means3D, opacities, shs, scales, rotations, colors_precomp, semantics, cfg):
-        color, others, semantic, radii, state = _r.forward(
-            cfg.variant, means3D, opacities, shs, colors_precomp, scales, rotations, None, semantics, cfg.viewset,
-            cfg.bg, cfg.sh_degree, 1.0, False, bin_capacity=cfg.bin_capacity, tables=cfg.tables,
-            status_host=cfg.status, cell_tiles=cfg.cell_tiles, blend_shape=cfg.blend_shape,
-            tile_schedule=cfg.tile_schedule)
+        color, others, semantic, radii, state = cfg.forward_state(means3D, opacities, shs, scales, rotations,
+                                                                  colors_precomp, semantics)
         ctx.state = state
         ctx.cfg = cfg
-        cfg.last_state = state                    # for inspection (bench counters)
-        # sticky record of every forward since the last reset: flags OR-ed,
-        # largest cell-list entry count (device side, so captured steps keep it)
-        cfg.accumulate_status(state)
         ctx.op_shape = opacities.shape
         ctx.has = (shs is not None, colors_precomp is not None, semantics is not None)
         ctx.mark_non_differentiable(radii)
@@ -44,10 +37,7 @@ class _MultiViewFn(torch.autograd.Function):
 
     @staticmethod
     def backward(ctx, d_color, d_others, d_semantic, d_radii):
-        cfg = ctx.cfg
-        g = _r.backward(ctx.state, d_color, d_others, d_semantic if ctx.has[2] else None)
-        cfg.accumulate_status(ctx.state)          # flags the backward raised
-        cfg.last_means2D_grad = g["dL_dmeans2D"]
+        g = ctx.cfg.backward_state(ctx.state, d_color, d_others, d_semantic if ctx.has[2] else None)
         return (g["dL_dmeans3D"], g["dL_dopacity"].reshape(ctx.op_shape),
                 g["dL_dsh"] if ctx.has[0] else None, g["dL_dscales"], g["dL_drotations"],
                 g["dL_dcolors"] if ctx.has[1] else None,
@@ -120,11 +110,38 @@ class MultiViewRasterizer:
         stream has passed that forward."""
         return _r.read_fragments(self.status)
 
-    def __call__(self, means3D, opacities, shs=None, scales=None, rotations=None, colors_precomp=None,
-                 semantics=None):
+    def _refresh_tables(self, means3D):
         if self.tables is None or self.tables[3] != int(means3D.shape[0]) * self.num_views and \
                 self.viewset.scene_sizes is None:
             self.tables = _r._tables(self.variant, int(means3D.shape[0]), self.viewset, means3D.device)
+
+    def forward_state(self, means3D, opacities, shs=None, scales=None, rotations=None, colors_precomp=None,
+                      semantics=None):
+        """The forward without autograd: (color, others, semantic, radii,
+        state), ``state`` to pass to ``backward_state``."""
+        self._refresh_tables(means3D)
+        color, others, semantic, radii, state = _r.forward(
+            self.variant, means3D, opacities, shs, colors_precomp, scales, rotations, None, semantics, self.viewset,
+            self.bg, self.sh_degree, 1.0, False, bin_capacity=self.bin_capacity, tables=self.tables,
+            status_host=self.status, cell_tiles=self.cell_tiles, blend_shape=self.blend_shape,
+            tile_schedule=self.tile_schedule)
+        self.last_state = state                   # for inspection (bench counters)
+        # sticky record of every forward since the last reset: flags OR-ed,
+        # largest cell-list entry count (device side, so captured steps keep it)
+        self.accumulate_status(state)
+        return color, others, semantic, radii, state
+
+    def backward_state(self, state, d_color, d_others, d_semantic=None, out=None):
+        """The backward of a ``forward_state`` call without autograd: the
+        gradient dict of ``raster.backward`` (``out``: buffers to write some
+        of them into)."""
+        g = _r.backward(state, d_color, d_others, d_semantic, out=out)
+        self.accumulate_status(state)             # flags the backward raised
+        self.last_means2D_grad = g["dL_dmeans2D"]
+        return g
+
+    def __call__(self, means3D, opacities, shs=None, scales=None, rotations=None, colors_precomp=None,
+                 semantics=None):
         color, others, semantic, radii = _MultiViewFn.apply(means3D, opacities, shs, scales, rotations,
                                                             colors_precomp, semantics, self)
         return color, others, (semantic if semantics is not None else None), radii

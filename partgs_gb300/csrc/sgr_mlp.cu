@@ -314,19 +314,33 @@ __global__ void __launch_bounds__(kThreads) k_gemm_tc(const sgr_gemm_args a) {
 }
 
 // ---------------------------------------------------------------------------
-// K-major operands: TMA-fed, multi-stage form.
+// K-major operands: persistent, TMA-fed, warp-specialised form.
 //
 // A TMA copy of a box of 8 columns x R rows (no swizzle) lands as R rows of
 // 16 bytes, contiguous: the no-swizzle K-major core-matrix layout with 8-row
 // groups 128 bytes apart (SBO) and adjacent 8-column slices R * 16 bytes
-// apart (LBO).  A K chunk of 64 is 8 such copies per operand.  Thread 0 of
-// warp 0 issues the copies of stage s once the MMAs that last read it have
-// committed to empty[s]; thread 0 of warp 1 waits for full[s] (the copies'
-// byte count), issues the four MMAs and commits them to empty[s].  After the
-// last chunk the MMAs commit to `done`, and all four warps run the
-// epilogue.  Out-of-range rows and columns are zero-filled by the TMA unit.
+// apart (LBO).  A K chunk of 64 is 8 such copies per operand.
+//
+// Each CTA stays resident and takes output tiles blockIdx.x, + gridDim.x, ...
+// Six warps:
+//   warp 0 (one thread): TMA producer; fills a ring of ns stages (A and B
+//     chunks), waiting on empty[s] before it reuses stage s;
+//   warp 1 (one thread): MMA issuer; per tile, into one of two tensor-memory
+//     accumulators (2 x NT columns), four MMAs per chunk once full[s] has
+//     its bytes, each chunk's MMAs committed to empty[s], the tile's last
+//     commit to tfull[b]; it waits on tempty[b] before reusing accumulator b;
+//   warps 2-5: epilogue; warp w reads tensor-memory lanes 32 (w % 4) .. + 31
+//     (rows of the tile) once tfull[b] fires, applies the epilogue, stores,
+//     and arrives on tempty[b].
+// So one tile's epilogue runs while the next tile's loads and MMAs do.
+// Every wait is bounded (kWaitNs) and also ends when another role has
+// failed; a failure raises SGR_MLP_TIMEOUT, the producer then waits
+// (bounded) for the copies it issued, everyone waits for the issuer's final
+// commit (all MMAs done), and only then is the tensor memory freed.
+// Out-of-range rows and columns are zero-filled by the TMA unit.
 // ---------------------------------------------------------------------------
 constexpr int kStages = 4;
+constexpr int kPersistThreads = 192;
 
 __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, int x, int y, uint32_t bar) {
   asm volatile(
@@ -340,22 +354,42 @@ __device__ __forceinline__ void mbar_expect(uint32_t bar, uint32_t bytes) {
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(bar), "r"(bytes) : "memory");
 }
 
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(bar) : "memory");
+}
+
+// mbar_wait that also gives up as soon as another role has raised `fail`.
+__device__ __forceinline__ bool mbar_wait_or_fail(uint32_t bar, uint32_t parity, const volatile int* fail) {
+  if (mbar_try(bar, parity)) return true;
+  const unsigned long long t0 = global_ns();
+  for (;;) {
+#pragma unroll 1
+    for (int k = 0; k < 64; ++k)
+      if (mbar_try(bar, parity)) return true;
+    if (*fail || global_ns() - t0 > kWaitNs) return false;
+  }
+}
+
 template <int NT>
-__global__ void __launch_bounds__(kThreads) k_gemm_tma(const sgr_gemm_args a, const __grid_constant__ CUtensorMap map_a,
-                                                       const __grid_constant__ CUtensorMap map_b, int ns) {
+__global__ void __launch_bounds__(kPersistThreads)
+    k_gemm_persist(const sgr_gemm_args a, const __grid_constant__ CUtensorMap map_a,
+                   const __grid_constant__ CUtensorMap map_b, int ns) {
   extern __shared__ __align__(1024) uint8_t smem[];
   constexpr uint32_t kBytesA = kTM * kKC * 2, kBytesB = NT * kKC * 2, kStage = kBytesA + kBytesB;
-  __shared__ __align__(8) uint64_t s_full[kStages], s_empty[kStages], s_done;
+  constexpr uint32_t kCols = 2 * NT;                 // two accumulators
+  __shared__ __align__(8) uint64_t s_full[kStages], s_empty[kStages], s_tfull[2], s_tempty[2], s_done;
   __shared__ uint32_t s_tmem;
   __shared__ int s_fail;
+  volatile int* fail = &s_fail;
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int m0 = blockIdx.x * kTM, n0 = blockIdx.y * NT;
+  const int tiles_n = (int)((a.N + NT - 1) / NT);
+  const int total = (int)((a.M + kTM - 1) / kTM) * tiles_n;
   const int chunks = (int)((a.K + kKC - 1) / kKC);
 
-  if (warp == 0) {
+  if (warp == 1) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_addr(&s_tmem)),
-                 "r"(NT)
+                 "r"(kCols)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
   }
@@ -363,6 +397,10 @@ __global__ void __launch_bounds__(kThreads) k_gemm_tma(const sgr_gemm_args a, co
     for (int i = 0; i < ns; ++i) {
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_addr(&s_full[i])) : "memory");
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_addr(&s_empty[i])) : "memory");
+    }
+    for (int b = 0; b < 2; ++b) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_addr(&s_tfull[b])) : "memory");
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 4;\n" ::"r"(smem_addr(&s_tempty[b])) : "memory");
     }
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_addr(&s_done)) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
@@ -375,89 +413,130 @@ __global__ void __launch_bounds__(kThreads) k_gemm_tma(const sgr_gemm_args a, co
   const uint32_t base = (smem_addr(smem) + 127u) & ~127u;   // TMA destinations: 128-byte aligned
 
   int issued = 0;                                    // producer: chunks whose loads were issued
-  if (warp == 0 && lane == 0) {
+  if (warp == 0) {
     // producer (a.skip_loads: issues nothing, so that the MMA issuer's wait
     // runs out with no copy in flight -- the timeout path's test)
-    for (int c = 0; c < chunks && !a.skip_loads; ++c) {
-      const int st = c % ns;
-      if (c >= ns && !mbar_wait(smem_addr(&s_empty[st]), (uint32_t)((c / ns - 1) & 1))) {
-        s_fail = 1;
-        break;
+    if (lane == 0 && !a.skip_loads) {
+      int g = 0;
+      for (int t = blockIdx.x; t < total && !*fail; t += gridDim.x) {
+        const int m0 = (t / tiles_n) * kTM, n0 = (t % tiles_n) * NT;
+        for (int c = 0; c < chunks; ++c, ++g) {
+          const int st = g % ns;
+          if (g >= ns && !mbar_wait_or_fail(smem_addr(&s_empty[st]), (uint32_t)((g / ns - 1) & 1), fail)) {
+            *fail = 1;
+            break;
+          }
+          const uint32_t full = smem_addr(&s_full[st]);
+          mbar_expect(full, kStage);
+          const uint32_t sa = base + st * kStage, sb = sa + kBytesA;
+          for (int kb = 0; kb < kKC / 8; ++kb) {
+            tma_load_2d(sa + kb * kTM * 16, &map_a, c * kKC + kb * 8, m0, full);
+            tma_load_2d(sb + kb * NT * 16, &map_b, c * kKC + kb * 8, n0, full);
+          }
+          issued = g + 1;
+        }
       }
-      const uint32_t full = smem_addr(&s_full[st]);
-      mbar_expect(full, kStage);
-      const uint32_t sa = base + st * kStage, sb = sa + kBytesA;
-      for (int kb = 0; kb < kKC / 8; ++kb) {
-        tma_load_2d(sa + kb * kTM * 16, &map_a, c * kKC + kb * 8, m0, full);
-        tma_load_2d(sb + kb * NT * 16, &map_b, c * kKC + kb * 8, n0, full);
-      }
-      issued = c + 1;
     }
-  } else if (warp == 1 && lane == 0) {
+  } else if (warp == 1) {
     // MMA issuer
-    const uint32_t idesc = instr_desc(NT);
-    for (int c = 0; c < chunks; ++c) {
-      const int st = c % ns;
-      if (!mbar_wait(smem_addr(&s_full[st]), (uint32_t)((c / ns) & 1))) {
-        s_fail = 1;
+    if (lane == 0) {
+      const uint32_t idesc = instr_desc(NT);
+      int g = 0, i = 0;
+      for (int t = blockIdx.x; t < total; t += gridDim.x, ++i) {
+        const int b = i & 1;
+        if (i >= 2 && !mbar_wait_or_fail(smem_addr(&s_tempty[b]), (uint32_t)(((i >> 1) - 1) & 1), fail)) {
+          *fail = 1;
+          break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+        const uint32_t acc_tmem = tmem + (uint32_t)(b * NT);
+        bool bad = false;
+        for (int c = 0; c < chunks; ++c, ++g) {
+          const int st = g % ns;
+          if (!mbar_wait_or_fail(smem_addr(&s_full[st]), (uint32_t)((g / ns) & 1), fail)) {
+            bad = true;
+            break;
+          }
+          asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+          const uint32_t sa = base + st * kStage, sb = sa + kBytesA;
+#pragma unroll
+          for (int s = 0; s < kKC / 16; ++s) {
+            const uint64_t da = smem_desc(sa + 2u * s * kTM * 16, kTM * 16, 128u);
+            const uint64_t db = smem_desc(sb + 2u * s * NT * 16, NT * 16, 128u);
+            const uint32_t acc = (c > 0 || s > 0) ? 1u : 0u;
+            asm volatile(
+                "{\n .reg .pred p;\n setp.ne.u32 p, %4, 0;\n"
+                " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(acc_tmem),
+                "l"(da), "l"(db), "r"(idesc), "r"(acc)
+                : "memory");
+          }
+          asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                           smem_addr(&s_empty[st]))
+                       : "memory");
+        }
+        if (bad) {
+          *fail = 1;
+          break;
+        }
+        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                         smem_addr(&s_tfull[b]))
+                     : "memory");
+      }
+      // tracks every MMA this thread issued: the teardown waits on it
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                       smem_addr(&s_done))
+                   : "memory");
+    }
+  } else {
+    // epilogue: this warp's quarter of the tensor-memory lanes (rows)
+    const int q = warp & 3;
+    int i = 0;
+    for (int t = blockIdx.x; t < total; t += gridDim.x, ++i) {
+      const int b = i & 1;
+      const bool ok = mbar_wait_or_fail(smem_addr(&s_tfull[b]), (uint32_t)((i >> 1) & 1), fail);
+      if (!__all_sync(0xffffffffu, ok)) {              // one decision per warp (tcgen05.ld needs every lane)
+        if (lane == 0) *fail = 1;
         break;
       }
       asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-      const uint32_t sa = base + st * kStage, sb = sa + kBytesA;
-#pragma unroll
-      for (int s = 0; s < kKC / 16; ++s) {
-        const uint64_t da = smem_desc(sa + 2u * s * kTM * 16, kTM * 16, 128u);
-        const uint64_t db = smem_desc(sb + 2u * s * NT * 16, NT * 16, 128u);
-        const uint32_t acc = (c > 0 || s > 0) ? 1u : 0u;
+      const long long row = (long long)(t / tiles_n) * kTM + 32 * q + lane;
+      const long long n0 = (long long)(t % tiles_n) * NT;
+#pragma unroll 1
+      for (int c0 = 0; c0 < NT; c0 += 16) {
+        uint32_t v[16];
+        const uint32_t taddr = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(b * NT + c0);
         asm volatile(
-            "{\n .reg .pred p;\n setp.ne.u32 p, %4, 0;\n"
-            " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
-            "l"(da), "l"(db), "r"(idesc), "r"(acc)
+            "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
+            "[%16];\n"
+            : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+              "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
+            : "r"(taddr)
             : "memory");
+        asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+        if (row < a.M && n0 + c0 < a.N) epilogue16(a, row, n0 + c0, v);
       }
-      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
-                       smem_addr(&s_empty[st]))
-                   : "memory");
+      asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+      __syncwarp();
+      if (lane == 0) mbar_arrive(smem_addr(&s_tempty[b]));
     }
-    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
-                     smem_addr(&s_done))
-                 : "memory");
   }
-  // everyone: wait for the accumulator (the issuer's last commit)
-  const bool ok = mbar_wait(smem_addr(&s_done), 0u);
-  asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-  // one decision for the whole CTA (the epilogue's tcgen05.ld needs every lane)
-  if (__syncthreads_or(!ok || s_fail)) {
+
+  // teardown: one decision for the whole CTA
+  if (__syncthreads_or(*fail)) {
     if (threadIdx.x == 0) {
       atomicOr(a.status, (unsigned)SGR_MLP_TIMEOUT);
       // let the copies this CTA issued land before it gives its shared
       // memory back: the last phase armed on each stage (bounded waits)
-      for (int c = issued - 1; c >= 0 && c >= issued - ns; --c)
-        mbar_wait(smem_addr(&s_full[c % ns]), (uint32_t)((c / ns) & 1));
-    }
-    __syncthreads();
-  } else {
-    const long long row = (long long)m0 + 32 * warp + lane;
-#pragma unroll 1
-    for (int c0 = 0; c0 < NT; c0 += 16) {
-      uint32_t v[16];
-      const uint32_t taddr = tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)c0;
-      asm volatile(
-          "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
-          : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
-            "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
-          : "r"(taddr)
-          : "memory");
-      asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
-      if (row >= a.M) continue;
-      epilogue16(a, row, (long long)n0 + c0, v);
+      for (int g = issued - 1; g >= 0 && g >= issued - ns; --g)
+        mbar_wait(smem_addr(&s_full[g % ns]), (uint32_t)((g / ns) & 1));
     }
   }
+  if (threadIdx.x == 32) mbar_wait(smem_addr(&s_done), 0u);   // every MMA has completed
   asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
   __syncthreads();
-  if (warp == 0) {
+  if (warp == 1) {
     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(NT) : "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(kCols) : "memory");
   }
 }
 
@@ -497,16 +576,25 @@ template <int NT>
 int launch_tma(const sgr_gemm_args& a, cudaStream_t st) {
   alignas(64) CUtensorMap ma, mb;
   if (!make_map(&ma, a.A, a.M, a.K, a.lda, kTM) || !make_map(&mb, a.B, a.N, a.K, a.ldb, NT)) return SGR_ERR_CUDA;
-  // as many stages as K chunks (up to kStages): short-K layers leave room
-  // for more CTAs per SM, whose loads overlap each other's epilogues
-  const long long chunks = (a.K + kKC - 1) / kKC;
-  const int ns = (int)(chunks < kStages ? (chunks < 1 ? 1 : chunks) : kStages);
+  const int ns = kStages;
   const size_t smem = (size_t)ns * (kTM + NT) * kKC * 2 + 128;
-  if (cudaFuncSetAttribute(k_gemm_tma<NT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)((size_t)kStages * (kTM + NT) * kKC * 2 + 128)) != cudaSuccess)
+  if (cudaFuncSetAttribute(k_gemm_persist<NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+      cudaSuccess)
     return SGR_ERR_CUDA;
-  dim3 grid((unsigned)((a.M + kTM - 1) / kTM), (unsigned)((a.N + NT - 1) / NT), 1);
-  k_gemm_tma<NT><<<grid, kThreads, smem, st>>>(a, ma, mb, ns);
+  // resident CTAs: by registers and shared memory, and by tensor memory
+  // (512 columns per SM, 2 NT per CTA: a CTA beyond that would wait in its
+  // allocation until another finished)
+  int dev = 0, sms = 0, per_sm = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gemm_persist<NT>, kPersistThreads, smem) !=
+          cudaSuccess)
+    return SGR_ERR_CUDA;
+  per_sm = per_sm < 512 / (2 * NT) ? per_sm : 512 / (2 * NT);
+  if (per_sm < 1) return SGR_ERR_UNSUPPORTED;
+  const long long tiles = ((a.M + kTM - 1) / kTM) * ((a.N + NT - 1) / NT);
+  const long long grid = tiles < (long long)sms * per_sm ? tiles : (long long)sms * per_sm;
+  k_gemm_persist<NT><<<(unsigned)grid, kPersistThreads, smem, st>>>(a, ma, mb, ns);
   sgr::count_launches(1);
   return cudaGetLastError() == cudaSuccess ? SGR_OK : SGR_ERR_CUDA;
 }

@@ -57,24 +57,30 @@ def camera_geometry(cameras, device="cuda"):
     return st(vw), st(basis), st(origin)
 
 
+def _loss_and_grads(color, others, target, cfg):
+    """The fused loss and its gradients with respect to the rendered maps."""
+    lib = _lib()
+    color = color.detach().contiguous()
+    others = others.detach().contiguous()
+    target = target.detach().contiguous()
+    V, _, H, W = color.shape
+    a = LossArgs(V, H, W, cfg.lambda_dssim, cfg.lambda_dist, cfg.lambda_normal, cfg.depth_ratio,
+                 color.data_ptr(), target.data_ptr(), others.data_ptr(), cfg.view_to_world.data_ptr(),
+                 cfg.ray_basis.data_ptr(), cfg.ray_origin.data_ptr())
+    loss = torch.empty((), dtype=torch.float32, device=color.device)
+    dcol = torch.empty_like(color)
+    doth = torch.empty_like(others)
+    scratch = torch.empty(lib.sgr_loss_scratch_bytes(C.byref(a)), dtype=torch.uint8, device=color.device)
+    L.check(lib.sgr_loss_forward_backward(C.byref(a), loss.data_ptr(), dcol.data_ptr(), doth.data_ptr(),
+                                          scratch.data_ptr(), torch.cuda.current_stream().cuda_stream),
+            "sgr_loss_forward_backward")
+    return loss, dcol, doth
+
+
 class _PointLossFn(torch.autograd.Function):
     @staticmethod
     def forward(ctx, color, others, target, cfg):
-        lib = _lib()
-        color = color.detach().contiguous()
-        others = others.detach().contiguous()
-        target = target.detach().contiguous()
-        V, _, H, W = color.shape
-        a = LossArgs(V, H, W, cfg.lambda_dssim, cfg.lambda_dist, cfg.lambda_normal, cfg.depth_ratio,
-                     color.data_ptr(), target.data_ptr(), others.data_ptr(), cfg.view_to_world.data_ptr(),
-                     cfg.ray_basis.data_ptr(), cfg.ray_origin.data_ptr())
-        loss = torch.empty((), dtype=torch.float32, device=color.device)
-        dcol = torch.empty_like(color)
-        doth = torch.empty_like(others)
-        scratch = torch.empty(lib.sgr_loss_scratch_bytes(C.byref(a)), dtype=torch.uint8, device=color.device)
-        L.check(lib.sgr_loss_forward_backward(C.byref(a), loss.data_ptr(), dcol.data_ptr(), doth.data_ptr(),
-                                              scratch.data_ptr(), torch.cuda.current_stream().cuda_stream),
-                "sgr_loss_forward_backward")
+        loss, dcol, doth = _loss_and_grads(color, others, target, cfg)
         ctx.save_for_backward(dcol, doth)
         return loss
 
@@ -96,3 +102,8 @@ class PointLoss:
 
     def __call__(self, color, others, target):
         return _PointLossFn.apply(color, others, target, self)
+
+    def forward_backward(self, color, others, target):
+        """(loss, dL/dcolor, dL/dothers) without autograd: the three kernels
+        of the fused loss, nothing else."""
+        return _loss_and_grads(color, others, target, self)

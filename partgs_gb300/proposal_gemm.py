@@ -80,8 +80,13 @@ def gemm(a, b, out, epilogue, bias=None, mask=None, trans=False, split_k=0, skip
 
 def main():
     """python -m partgs_gb300.proposal_gemm: CUDA-event timings of the
-    network's per-point layer shapes (262,144 rows), this GEMM against a
-    PyTorch bf16 matmul followed by ReLU."""
+    network's per-point layer shapes at 128 and 256 scenes of 2,048 points
+    (262,144 and 524,288 rows), this GEMM (bias + ReLU fused, bf16 out)
+    against PyTorch's cuBLAS GEMM with the bias (F.linear) followed by ReLU.
+    One JSON line per shape.  Operands larger than the 129 MB L2 are read
+    from HBM every launch; the smaller ones partly stay in L2 for both."""
+    import json
+
     def timed(fn, n=20):
         for _ in range(3):
             fn()
@@ -94,15 +99,20 @@ def main():
         torch.cuda.synchronize()
         return e0.elapsed_time(e1) / n * 1e-3
     g = torch.Generator().manual_seed(0)
-    for M, N, K in ((262144, 64, 16), (262144, 128, 64), (262144, 256, 128), (262144, 128, 256)):
-        a = torch.randn(M, K, generator=g).to(torch.bfloat16).cuda()
-        b = torch.randn(N, K, generator=g).to(torch.bfloat16).cuda()
-        out = torch.empty(M, N, dtype=torch.bfloat16, device="cuda")
-        t = timed(lambda: gemm(a, b, out, RELU_BF16))
-        t_ref = timed(lambda: torch.relu(a @ b.t()))
-        nbytes = (M * K + N * K + M * N) * 2
-        print(f"M={M} N={N} K={K}: {t * 1e6:.1f} us, {2 * M * N * K / t / 1e12:.1f} TFLOP/s, "
-              f"{nbytes / t / 1e9:.0f} GB/s; torch matmul+relu {t_ref * 1e6:.1f} us")
+    for M in (262144, 524288):
+        for N, K in ((64, 16), (128, 64), (256, 128)):
+            a = torch.randn(M, K, generator=g).to(torch.bfloat16).cuda()
+            b = torch.randn(N, K, generator=g).to(torch.bfloat16).cuda()
+            bias = torch.randn(N, generator=g).cuda()
+            bias16 = bias.to(torch.bfloat16)
+            out = torch.empty(M, N, dtype=torch.bfloat16, device="cuda")
+            t = timed(lambda: gemm(a, b, out, RELU_BF16, bias=bias))
+            t_ref = timed(lambda: torch.relu(torch.nn.functional.linear(a, b, bias16)))
+            check_status(out.device)
+            nbytes = (M * K + N * K + M * N) * 2
+            print(json.dumps({"M": M, "N": N, "K": K, "us": round(t * 1e6, 2), "tflops": round(2 * M * N * K / t / 1e12, 1),
+                              "gbs": round(nbytes / t / 1e9), "cublas_linear_relu_us": round(t_ref * 1e6, 2),
+                              "speedup_vs_cublas": round(t_ref / t, 3)}), flush=True)
 
 
 if __name__ == "__main__":

@@ -249,9 +249,10 @@ def read_status(status_host: torch.Tensor):
     return int(w[0]), int(status_host[8:12].view(torch.int32)[0]), int(w[2])
 
 
-def backward(state: RasterState, dL_dcolor, dL_dothers, dL_dsemantic=None, need=None):
+def backward(state: RasterState, dL_dcolor, dL_dothers, dL_dsemantic=None, need=None, out=None):
     """Gradients of every surfel input.  Returns a dict of tensors shaped as
-    the reference's backward returns them."""
+    the reference's backward returns them; ``out`` may name buffers (float32,
+    contiguous, of those sizes) to write some of them into instead."""
     lib = L.load()
     b = state.batch
     device = state.geom.device
@@ -266,6 +267,10 @@ def backward(state: RasterState, dL_dcolor, dL_dothers, dL_dsemantic=None, need=
         dL_dmeans2D=e(R, 3), dL_dcolors=e(P, 3), dL_dopacity=e(P, 1), dL_dmeans3D=e(P, 3), dL_dtransmat=e(R, 9),
         dL_dsh=e(P, M, 3) if M > 0 else e(0), dL_dscales=e(P, 2), dL_drotations=e(P, 4),
         dL_dsemantics=e(P, S) if S > 0 else e(0))
+    for k, t in (out or {}).items():
+        if t.dtype != torch.float32 or not t.is_contiguous() or t.numel() != g[k].numel():
+            raise ValueError(f"output buffer for {k}: float32, contiguous, {g[k].numel()} elements")
+        g[k] = t
     inp = L.BwdInputs(dL_dcolor.data_ptr(), dL_dothers.data_ptr(), _ptr(dL_dsemantic))
     out = L.BwdOutputs(*(_ptr(g[k]) for k in ("dL_dmeans2D", "dL_dcolors", "dL_dopacity", "dL_dmeans3D",
                                                "dL_dtransmat", "dL_dsh", "dL_dscales", "dL_drotations",

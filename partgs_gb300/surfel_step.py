@@ -22,7 +22,7 @@ import torch
 import torch.nn.functional as F
 
 from . import _lib
-from .activations import activate
+from .activations import activate, activate_backward, activate_forward
 from .batched import MultiViewRasterizer
 from .optim import SurfelAdam
 
@@ -157,11 +157,33 @@ class SurfelTrainer:
         dist_loss = self.lambda_dist * allmap[:, 6:7].mean()
         return loss + dist_loss + normal_loss
 
+    def _fused_step(self, targets):
+        """Forward, fused loss and backward without autograd: the loss
+        kernels hand dL/dcolor and dL/dmaps to the rasteriser's backward,
+        which writes dL/dxyz into xyz.grad; the activation backward writes
+        the other parameters' gradients into their .grad buffers (which the
+        optimiser consumes and clears).  Only this library's kernels run."""
+        ins = [t.detach() for t in (self.log_scaling, self.rotation, self.opacity_logit, self.features_dc,
+                                    self.features_rest)]
+        scales, rots, opac, shs = activate_forward(ins)
+        color, allmap, _, radii, state = self.raster.forward_state(self.xyz.detach(), opac, shs, scales, rots)
+        self._radii = radii
+        loss, dcol, doth = self.point_loss.forward_backward(color, allmap, targets)
+        g = self.raster.backward_state(state, dcol, doth, out={"dL_dmeans3D": self.xyz.grad})
+        activate_backward(ins, (g["dL_dscales"], g["dL_drotations"], g["dL_dopacity"], g["dL_dsh"]),
+                          [self.log_scaling.grad, self.rotation.grad, self.opacity_logit.grad,
+                           self.features_dc.grad, self.features_rest.grad])
+        return loss
+
     def step(self, targets):
         """One eager step; returns the loss tensor.  The optimiser clears the
         gradients it consumes."""
-        loss = self.loss_fn(targets)
-        loss.backward()
+        if self.point_loss is not None:
+            with torch.no_grad():
+                loss = self._fused_step(targets)
+        else:
+            loss = self.loss_fn(targets)
+            loss.backward()
         if self.stats is not None:
             # the batch loss averages its views: scale the per-view screen-space
             # gradients back to what a single-view iteration sees

@@ -26,7 +26,10 @@ Two checks:
    to 1e-6 relative per parameter (measured: at most 8e-8; denominator
    floored at 1% of the largest of its kind);
 2. the library's FP32 chain (sgr_bind_backward after sgr_backward) against
-   the FP64 analytic gradient of the same loss: per parameter within 1e-3
+   the FP64 analytic gradient of the same loss with each tile's surfels in
+   the reference's order (FP32 depth bits, then index: surfels that tie in
+   FP32 depth blend in index order there, in FP64-depth order in check 1's
+   chain, which changes the result at those pixels): per parameter within 1e-3
    of the largest of its kind, and within 5e-4 relative in the L2 norm over
    each kind.  FP32 is the limit there: the splat-to-pixel adjoint carries
    per-surfel rounding up to ~1e-4 of the largest surfel gradient (the
@@ -115,20 +118,20 @@ def test_fp64_adjoint_equals_finite_differences(run):
 
 
 def test_library_fp32_chain(run):
-    kmax = _kind_max(run, "an64")
+    kmax = _kind_max(run, "an64_ref")
     bad, worst, l2 = [], {}, {}
     for r in run:
-        e = abs(r["an32"] - r["an64"])
+        e = abs(r["an32"] - r["an64_ref"])
         worst[r["name"]] = max(worst.get(r["name"], 0.0), e / kmax[r["name"]])
         if e > FP32_PARAM_TOL * kmax[r["name"]]:
-            bad.append((r["name"], r["flat"], r["an32"], r["an64"], r["flips"]))
+            bad.append((r["name"], r["flat"], r["an32"], r["an64_ref"], r["flips"]))
     for name in kmax:
         a = np.array([r["an32"] for r in run if r["name"] == name])
-        b = np.array([r["an64"] for r in run if r["name"] == name])
+        b = np.array([r["an64_ref"] for r in run if r["name"] == name])
         l2[name] = float(np.linalg.norm(a - b) / np.linalg.norm(b))
     print("FP32 chain vs FP64: worst |error| / kind max", {k: f"{v:.1e}" for k, v in worst.items()},
           "kind L2", {k: f"{v:.1e}" for k, v in l2.items()})
-    ranked = sorted(run, key=lambda r: -abs(r["an32"] - r["an64"]) / kmax[r["name"]])[:8]
-    print("largest:", [(r["name"], r["flat"], round(r["an32"], 4), round(r["an64"], 4), r["flips"]) for r in ranked])
+    ranked = sorted(run, key=lambda r: -abs(r["an32"] - r["an64_ref"]) / kmax[r["name"]])[:8]
+    print("largest:", [(r["name"], r["flat"], round(r["an32"], 4), round(r["an64_ref"], 4), r["flips"]) for r in ranked])
     assert not bad, bad
     assert max(l2.values()) <= FP32_L2_TOL, l2

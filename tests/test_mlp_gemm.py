@@ -1,6 +1,8 @@
 """The proposal network's tcgen05 BF16 GEMM against a PyTorch fp32 matmul of
 the same bf16 operands: every epilogue, each output-tile width (64, 128,
-256), ragged M, N and K, the transposed (weight-gradient) form with split K."""
+256), ragged M, N and K, the persistent form with many tiles per CTA (both
+tensor-memory accumulators cycled, several output-column tiles), the
+transposed (weight-gradient) form with split K."""
 import pytest
 import torch
 
@@ -35,6 +37,27 @@ def test_gemm_store_and_bias(sgr_lib, M, N, K):
     ref = _ref(a, b, bias)
     assert int(G.status_word("cuda").item()) == 0
     assert float((out - ref).abs().max()) <= TOL * float(ref.abs().max())
+
+
+@pytest.mark.parametrize("M,N,K", [(152 * 128 * 3 + 77, 256, 128), (60001, 384, 64), (40000, 64, 16)])
+def test_gemm_persistent_many_tiles(sgr_lib, M, N, K):
+    """More output tiles than resident CTAs: each CTA loops over tiles,
+    alternating its two accumulators, with the last row and column tiles
+    ragged."""
+    from partgs_gb300 import proposal_gemm as G
+    g = torch.Generator().manual_seed(M + N)
+    a, b = _bf((M, K), g), _bf((N, K), g)
+    bias = torch.randn(N, generator=g).cuda()
+    out = torch.full((M, N), float("nan"), device="cuda")
+    G.gemm(a, b, out, G.STORE_F32, bias=bias)
+    torch.cuda.synchronize()
+    ref = _ref(a, b, bias)
+    assert int(G.status_word("cuda").item()) == 0
+    assert float((out - ref).abs().max()) <= TOL * float(ref.abs().max())
+    out16 = torch.empty((M, N), dtype=torch.bfloat16, device="cuda")
+    G.gemm(a, b, out16, G.RELU_BF16, bias=bias)
+    ref16 = torch.relu(ref)
+    assert float((out16.float() - ref16).abs().max()) <= 1e-2 * float(ref16.abs().max())
 
 
 def test_gemm_relu_and_mask_epilogues(sgr_lib):

@@ -50,3 +50,28 @@ def test_train_recovers_from_a_cell_list_overflow(sgr_lib):
 
     for a, c, b in zip(ok, again, tr.params()):
         assert off(a, b.detach()) <= 3 * off(a, c) + 0.005
+
+
+def test_fused_step_gradients_equal_the_autograd_path(sgr_lib):
+    """The fused step (loss kernels -> rasteriser backward -> activation
+    backward into the .grad buffers, no autograd and no PyTorch kernels)
+    gives the loss and parameter gradients the autograd path through the
+    same kernels gives (up to the order of the gradient atomics)."""
+    from partgs_gb300.cameras import orbit_cameras
+    from partgs_gb300.scenes import random_surfels
+    from partgs_gb300.surfel_step import SurfelTrainer
+    scene, cams = random_surfels(3000, seed=8), orbit_cameras(3, 3.0, 64, 80, 55.0, seed=4)
+    targets = torch.rand(len(cams), 3, 64, 80, generator=torch.Generator().manual_seed(6)).cuda()
+    tr = SurfelTrainer(scene, cams)
+    with torch.no_grad():
+        loss_fused = float(tr._fused_step(targets))
+    fused = [p.grad.detach().clone() for p in tr.params()]
+    for p in tr.params():
+        p.grad.zero_()
+    loss_ag = tr.loss_fn(targets)
+    loss_ag.backward()
+    assert abs(float(loss_ag) - loss_fused) <= 1e-6 * abs(loss_fused)
+    for a, p in zip(fused, tr.params()):
+        b = p.grad
+        assert float(a.abs().max()) > 0
+        assert float((a - b).abs().max()) <= 1e-5 * float(b.abs().max()), p.shape
