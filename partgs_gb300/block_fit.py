@@ -22,6 +22,7 @@ import time
 
 import torch
 
+from . import _lib as L
 from .batched import MultiViewRasterizer
 from .binding import SuperquadricBinding
 from .cameras import orbit_cameras
@@ -189,19 +190,58 @@ class BatchFit:
         ld = (self.mask_t * (others[:, 5] - self.depth_t).abs()).mean(dim=(1, 2))
         return (la + ld).reshape(self.S, self.views).mean(1)
 
-    def fit(self, init, iters: int):
+    def fit(self, init, iters: int, capture: bool = False, headroom: float = 1.5):
         """Runs the fit from per-scene init sets; returns the fitted sets
         [(semi, eps, quat, trans)] (quaternions normalised, w >= 0) and the
-        per-scene loss of the last iteration."""
-        sq_s, sq_eps, sq_r, sq_t = (t.detach().clone().requires_grad_(True) for t in self.raw(init))
-        opt = SurfelAdam([{"params": [sq_s], "lr": LR["sq_s"]}, {"params": [sq_eps], "lr": LR["sq_eps"]},
-                          {"params": [sq_r], "lr": LR["sq_r"]}, {"params": [sq_t], "lr": LR["sq_t"]}], eps=1e-15)
-        last = None
-        for _ in range(iters):
-            per_scene = self.loss(self.render(sq_s, sq_eps, sq_r, sq_t))
-            per_scene.sum().backward()
-            opt.step()
-            last = per_scene.detach()
+        per-scene loss of the last iteration.  With ``capture`` one iteration
+        (binding, rasteriser, loss, backward, Adam) is captured in a CUDA
+        graph after an eager first iteration has sized the cell lists
+        (``headroom`` times its entry count), and replayed; if a replay
+        overflowed the lists, the fit runs again eagerly from the start."""
+        raw = [t.detach().clone() for t in self.raw(init)]
+
+        def run(graphed):
+            params = [t.clone().requires_grad_(True) for t in raw]
+            sq_s, sq_eps, sq_r, sq_t = params
+            opt = SurfelAdam([{"params": [sq_s], "lr": LR["sq_s"]}, {"params": [sq_eps], "lr": LR["sq_eps"]},
+                              {"params": [sq_r], "lr": LR["sq_r"]}, {"params": [sq_t], "lr": LR["sq_t"]}],
+                             eps=1e-15)
+
+            def step():
+                per_scene = self.loss(self.render(*params))
+                per_scene.sum().backward()
+                opt.step()
+                return per_scene.detach()
+
+            if not graphed:
+                self.raster.set_capacity(None)
+                last = None
+                for _ in range(iters):
+                    last = step()
+                return params, last, True
+            side = torch.cuda.Stream()
+            side.wait_stream(torch.cuda.current_stream())
+            with torch.cuda.stream(side):
+                self.raster.set_capacity(None)
+                last = step()                       # iteration 1, eager: sizes the lists
+                side.synchronize()
+                most = self.raster.counts()[2]
+            torch.cuda.current_stream().wait_stream(side)
+            self.raster.set_capacity(int(most * headroom) + 4096)
+            graph = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(graph):
+                out = step()
+            self.raster.sticky_counts(reset=True)
+            for _ in range(iters - 1):
+                graph.replay()
+            flags, _ = self.raster.sticky_counts(reset=True)
+            self.raster.set_capacity(None)
+            return params, out.clone(), not (flags & L.SGR_FLAG_BIN_OVERFLOW)
+
+        params, last, ok = run(capture and iters > 1)
+        if not ok:
+            params, last, ok = run(False)
+        sq_s, sq_eps, sq_r, sq_t = params
         with torch.no_grad():
             semi = RATIO * (torch.exp(sq_s) + SMIN)
             eps = torch.sigmoid(sq_eps) * 1.8 + 0.1

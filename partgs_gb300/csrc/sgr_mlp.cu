@@ -140,13 +140,15 @@ __device__ __forceinline__ void stage(uint8_t* dst, const __nv_bfloat16* __restr
 // Epilogue of 16 accumulator columns [col0, col0 + 16) of one row: 16-byte
 // vector stores (loads of the mask, fp32 vector atomics) when the 16 columns
 // are in range and aligned, element by element otherwise.
+// `bias`: the bias vector (indexed by output column), from shared or global
+// memory, or null.
 __device__ __forceinline__ void epilogue16(const sgr_gemm_args& a, long long row, long long col0,
-                                           const uint32_t (&v)[16]) {
+                                           const uint32_t (&v)[16], const float* bias) {
   float x[16];
 #pragma unroll
   for (int e = 0; e < 16; ++e) {
     x[e] = __uint_as_float(v[e]);
-    if (a.bias && col0 + e < a.N) x[e] += a.bias[col0 + e];
+    if (bias && col0 + e < a.N) x[e] += bias[col0 + e];
   }
   const bool vec = col0 + 16 <= a.N && (a.ldo & 7) == 0 && (reinterpret_cast<uintptr_t>(a.out) & 15) == 0 &&
                    (a.epilogue != SGR_GEMM_MASK_BF16 ||
@@ -302,7 +304,7 @@ __global__ void __launch_bounds__(kThreads) k_gemm_tc(const sgr_gemm_args a) {
           : "memory");
       asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
       if (row >= a.M) continue;
-      epilogue16(a, row, (long long)n0 + c0, v);
+      epilogue16(a, row, (long long)n0 + c0, v, a.bias);
     }
   }
   asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
@@ -329,9 +331,10 @@ __global__ void __launch_bounds__(kThreads) k_gemm_tc(const sgr_gemm_args a) {
 //     accumulators (2 x NT columns), four MMAs per chunk once full[s] has
 //     its bytes, each chunk's MMAs committed to empty[s], the tile's last
 //     commit to tfull[b]; it waits on tempty[b] before reusing accumulator b;
-//   warps 2-5: epilogue; warp w reads tensor-memory lanes 32 (w % 4) .. + 31
-//     (rows of the tile) once tfull[b] fires, applies the epilogue, stores,
-//     and arrives on tempty[b].
+//   warps 2-9: epilogue; warp w reads tensor-memory lanes 32 (w % 4) .. + 31
+//     (rows of the tile), columns of half (w - 2) / 4 of the tile, once
+//     tfull[b] fires, 32 columns per wait, applies the epilogue, stores, and
+//     arrives on tempty[b].
 // So one tile's epilogue runs while the next tile's loads and MMAs do.
 // Every wait is bounded (kWaitNs) and also ends when another role has
 // failed; a failure raises SGR_MLP_TIMEOUT, the producer then waits
@@ -340,7 +343,9 @@ __global__ void __launch_bounds__(kThreads) k_gemm_tc(const sgr_gemm_args a) {
 // Out-of-range rows and columns are zero-filled by the TMA unit.
 // ---------------------------------------------------------------------------
 constexpr int kStages = 4;
-constexpr int kPersistThreads = 192;
+constexpr int kEpiWarps = 8;
+constexpr int kBiasSmem = 1024;   // output columns whose bias the persistent GEMM keeps in shared memory
+constexpr int kPersistThreads = 64 + 32 * kEpiWarps;
 
 __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, int x, int y, uint32_t bar) {
   asm volatile(
@@ -371,7 +376,7 @@ __device__ __forceinline__ bool mbar_wait_or_fail(uint32_t bar, uint32_t parity,
 }
 
 template <int NT>
-__global__ void __launch_bounds__(kPersistThreads)
+__global__ void __launch_bounds__(kPersistThreads, 1)
     k_gemm_persist(const sgr_gemm_args a, const __grid_constant__ CUtensorMap map_a,
                    const __grid_constant__ CUtensorMap map_b, int ns) {
   extern __shared__ __align__(1024) uint8_t smem[];
@@ -380,9 +385,16 @@ __global__ void __launch_bounds__(kPersistThreads)
   __shared__ __align__(8) uint64_t s_full[kStages], s_empty[kStages], s_tfull[2], s_tempty[2], s_done;
   __shared__ uint32_t s_tmem;
   __shared__ int s_fail;
+  __shared__ float s_bias[kBiasSmem];
   volatile int* fail = &s_fail;
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  // the bias, once per CTA, into shared memory (the epilogue reads 16
+  // values per 16 columns; from global memory those loads were its stall)
+  const bool bias_smem = a.bias && a.N <= kBiasSmem;
+  if (bias_smem)
+    for (int c = threadIdx.x; c < (int)a.N; c += kPersistThreads) s_bias[c] = a.bias[c];
+  const float* bias = bias_smem ? s_bias : a.bias;
   const int tiles_n = (int)((a.N + NT - 1) / NT);
   const int total = (int)((a.M + kTM - 1) / kTM) * tiles_n;
   const int chunks = (int)((a.K + kKC - 1) / kKC);
@@ -400,7 +412,8 @@ __global__ void __launch_bounds__(kPersistThreads)
     }
     for (int b = 0; b < 2; ++b) {
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_addr(&s_tfull[b])) : "memory");
-      asm volatile("mbarrier.init.shared::cta.b64 [%0], 4;\n" ::"r"(smem_addr(&s_tempty[b])) : "memory");
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_addr(&s_tempty[b])), "r"(kEpiWarps)
+                   : "memory");
     }
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_addr(&s_done)) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
@@ -488,8 +501,11 @@ __global__ void __launch_bounds__(kPersistThreads)
                    : "memory");
     }
   } else {
-    // epilogue: this warp's quarter of the tensor-memory lanes (rows)
+    // epilogue: this warp's quarter of the tensor-memory lanes (rows) and
+    // half of the columns
     const int q = warp & 3;
+    constexpr int kHalf = NT / 2;
+    const int h0 = ((warp - 2) >> 2) * kHalf;
     int i = 0;
     for (int t = blockIdx.x; t < total; t += gridDim.x, ++i) {
       const int b = i & 1;
@@ -500,11 +516,11 @@ __global__ void __launch_bounds__(kPersistThreads)
       }
       asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
       const long long row = (long long)(t / tiles_n) * kTM + 32 * q + lane;
-      const long long n0 = (long long)(t % tiles_n) * NT;
+      const long long n0 = (long long)(t % tiles_n) * NT + h0;
 #pragma unroll 1
-      for (int c0 = 0; c0 < NT; c0 += 16) {
-        uint32_t v[16];
-        const uint32_t taddr = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(b * NT + c0);
+      for (int c0 = 0; c0 < kHalf; c0 += 32) {
+        uint32_t v[32];
+        const uint32_t taddr = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(b * NT + h0 + c0);
         asm volatile(
             "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
             "[%16];\n"
@@ -512,8 +528,21 @@ __global__ void __launch_bounds__(kPersistThreads)
               "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
             : "r"(taddr)
             : "memory");
+        if (c0 + 16 < kHalf)
+          asm volatile(
+              "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
+              "[%16];\n"
+              : "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]),
+                "=r"(v[23]), "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]),
+                "=r"(v[30]), "=r"(v[31])
+              : "r"(taddr + 16u)
+              : "memory");
         asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
-        if (row < a.M && n0 + c0 < a.N) epilogue16(a, row, n0 + c0, v);
+        if (row < a.M) {
+          if (n0 + c0 < a.N) epilogue16(a, row, n0 + c0, *reinterpret_cast<const uint32_t(*)[16]>(&v[0]), bias);
+          if (c0 + 16 < kHalf && n0 + c0 + 16 < a.N)
+            epilogue16(a, row, n0 + c0 + 16, *reinterpret_cast<const uint32_t(*)[16]>(&v[16]), bias);
+        }
       }
       asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
       __syncwarp();
@@ -578,22 +607,28 @@ int launch_tma(const sgr_gemm_args& a, cudaStream_t st) {
   if (!make_map(&ma, a.A, a.M, a.K, a.lda, kTM) || !make_map(&mb, a.B, a.N, a.K, a.ldb, NT)) return SGR_ERR_CUDA;
   const int ns = kStages;
   const size_t smem = (size_t)ns * (kTM + NT) * kKC * 2 + 128;
-  if (cudaFuncSetAttribute(k_gemm_persist<NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
-      cudaSuccess)
-    return SGR_ERR_CUDA;
-  // resident CTAs: by registers and shared memory, and by tensor memory
-  // (512 columns per SM, 2 NT per CTA: a CTA beyond that would wait in its
-  // allocation until another finished)
-  int dev = 0, sms = 0, per_sm = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess ||
-      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gemm_persist<NT>, kPersistThreads, smem) !=
-          cudaSuccess)
-    return SGR_ERR_CUDA;
-  per_sm = per_sm < 512 / (2 * NT) ? per_sm : 512 / (2 * NT);
-  if (per_sm < 1) return SGR_ERR_UNSUPPORTED;
+  // per device, once: the shared-memory attribute and the resident CTAs (by
+  // registers and shared memory, and by tensor memory: 512 columns per SM,
+  // 2 NT per CTA; a CTA beyond that would wait in its allocation until
+  // another finished)
+  constexpr int kMaxDev = 64;
+  static int resident[kMaxDev] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDev) return SGR_ERR_CUDA;
+  if (resident[dev] == 0) {
+    int sms = 0, per_sm = 0;
+    if (cudaFuncSetAttribute(k_gemm_persist<NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+            cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gemm_persist<NT>, kPersistThreads, smem) !=
+            cudaSuccess)
+      return SGR_ERR_CUDA;
+    per_sm = per_sm < 512 / (2 * NT) ? per_sm : 512 / (2 * NT);
+    if (per_sm < 1) return SGR_ERR_UNSUPPORTED;
+    resident[dev] = sms * per_sm;
+  }
   const long long tiles = ((a.M + kTM - 1) / kTM) * ((a.N + NT - 1) / NT);
-  const long long grid = tiles < (long long)sms * per_sm ? tiles : (long long)sms * per_sm;
+  const long long grid = tiles < (long long)resident[dev] ? tiles : (long long)resident[dev];
   k_gemm_persist<NT><<<(unsigned)grid, kPersistThreads, smem, st>>>(a, ma, mb, ns);
   sgr::count_launches(1);
   return cudaGetLastError() == cudaSuccess ? SGR_OK : SGR_ERR_CUDA;

@@ -258,6 +258,52 @@ def kmeans(points: torch.Tensor, k: int, iters: int = 20, g: torch.Generator | N
     return c
 
 
+def kmeans_batch(points: torch.Tensor, counts, iters: int = 20, seed: int = 0):
+    """Per scene s of points [S, n, 3], counts[s] k-means centres (k-means++
+    seeding, Lloyd steps), all scenes at once on the device: [S, 8, 3], the
+    slots past counts[s] zero."""
+    S, n, _ = points.shape
+    dev = points.device
+    K = MAX_SQ
+    k = torch.as_tensor(counts, device=dev).long()
+    g = torch.Generator(device=dev).manual_seed(seed)
+    ar = torch.arange(S, device=dev)
+    pts = points.float()
+    centres = torch.zeros(S, K, 3, device=dev)
+    first = torch.randint(n, (S,), generator=g, device=dev)
+    centres[:, 0] = pts[ar, first]
+    d = ((pts - centres[:, :1]) ** 2).sum(-1)
+    for j in range(1, K):
+        w = d / d.sum(1, keepdim=True).clamp(min=1e-12)
+        w = torch.where(w.sum(1, keepdim=True) > 0, w, torch.ones_like(w))
+        pick = torch.multinomial(w, 1, generator=g).squeeze(1)
+        centres[:, j] = pts[ar, pick]
+        d = torch.minimum(d, ((pts - centres[:, j:j + 1]) ** 2).sum(-1))
+    slot_on = torch.arange(K, device=dev)[None, :] < k[:, None]             # [S, K]
+    for _ in range(iters):
+        dist = torch.cdist(pts, centres)                                      # [S, n, K]
+        dist = dist.masked_fill(~slot_on[:, None, :], float("inf"))
+        onehot = torch.nn.functional.one_hot(dist.argmin(-1), K).float()     # [S, n, K]
+        num = onehot.sum(1)                                                   # [S, K]
+        sums = onehot.transpose(1, 2) @ pts                                   # [S, K, 3]
+        centres = torch.where((num > 0)[..., None], sums / num.clamp(min=1)[..., None], centres)
+    return centres * slot_on[..., None]
+
+
+def plain_init_batch(points: torch.Tensor, counts, seed: int = 0):
+    """plain_init for every scene of points [S, n, 3] at once (the k-means
+    of kmeans_batch): a list of (semi, eps, quat, trans) per scene."""
+    c = kmeans_batch(points, counts, seed=seed)
+    out = []
+    for s, k in enumerate(counts):
+        k = int(k)
+        semi = torch.full((k, 3), RATIO * (RATIO + SMIN), device=points.device)
+        eps = torch.ones(k, 2, device=points.device)
+        quat = torch.tensor([1.0, 0.0, 0.0, 0.0], device=points.device).expand(k, 4)
+        out.append((semi, eps, quat, c[s, :k]))
+    return out
+
+
 def plain_init(points: torch.Tensor, k: int, g: torch.Generator | None = None):
     """The reference's block initialisation for k blocks (utils/superquadric.py:
     112-120): k-means centres, identity rotation, sq_eps = 0 (exponents 1.0)

@@ -82,19 +82,31 @@ def main():
     """python -m partgs_gb300.proposal_gemm: CUDA-event timings of the
     network's per-point layer shapes at 128 and 256 scenes of 2,048 points
     (262,144 and 524,288 rows), this GEMM (bias + ReLU fused, bf16 out)
-    against PyTorch's cuBLAS GEMM with the bias (F.linear) followed by ReLU.
-    One JSON line per shape.  Operands larger than the 129 MB L2 are read
+    against PyTorch's cuBLAS GEMM with the bias (F.linear) followed by ReLU,
+    both as device time inside a CUDA graph.  One JSON line per shape.  Operands larger than the 129 MB L2 are read
     from HBM every launch; the smaller ones partly stay in L2 for both."""
     import json
 
     def timed(fn, n=20):
-        for _ in range(3):
-            fn()
+        """Device time per call: n calls captured in one CUDA graph, the
+        replay timed with CUDA events (so host launch overhead, which is
+        larger than the small layers' device time, is not measured)."""
+        s = torch.cuda.Stream()
+        s.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(s):
+            for _ in range(3):
+                fn()
+        torch.cuda.current_stream().wait_stream(s)
+        torch.cuda.synchronize()
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(graph):
+            for _ in range(n):
+                fn()
+        graph.replay()
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record()
-        for _ in range(n):
-            fn()
+        graph.replay()
         e1.record()
         torch.cuda.synchronize()
         return e0.elapsed_time(e1) / n * 1e-3

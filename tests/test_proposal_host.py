@@ -71,3 +71,27 @@ def test_plain_init_is_the_reference_block_init():
     xs = sorted(float(v) for v in c[:, 0])
     assert abs(xs[0] + 0.5) < 0.05 and abs(xs[1] - 0.5) < 0.05
     assert math.isclose(0.25 * (math.exp(math.log(0.25)) + 0.2), 0.1125)
+
+
+def test_kmeans_batch_finds_separated_clusters():
+    """The batched k-means of the labelling fits: on scenes of well-separated
+    blobs it puts one centre in each blob, per scene and with each scene's
+    own block count; slots past the count stay zero."""
+    from partgs_gb300.proposal import kmeans_batch
+    g = torch.Generator().manual_seed(0)
+    S, n = 5, 2048
+    counts = [1, 3, 8, 5, 2]
+    pts = torch.empty(S, n, 3)
+    truth = []
+    for s, k in enumerate(counts):
+        c = torch.randn(k, 3, generator=g) * 4.0
+        c = c + torch.arange(k)[:, None] * torch.tensor([10.0, 0.0, 0.0])     # blobs far apart
+        lab = torch.arange(n) % k
+        pts[s] = c[lab] + 0.05 * torch.randn(n, 3, generator=g)
+        truth.append(c)
+    got = kmeans_batch(pts, counts, seed=3)
+    assert got.shape == (S, 8, 3)
+    for s, k in enumerate(counts):
+        d = torch.cdist(truth[s], got[s, :k])
+        assert float(d.min(dim=1).values.max()) < 0.05, (s, d)       # every blob has a centre
+        assert bool((got[s, k:] == 0).all())
