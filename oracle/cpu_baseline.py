@@ -121,7 +121,7 @@ def time_step(workload_name="sq500k_16x800x600", seed=0, sample_tiles=None, proc
     O.preprocess_backward(st, rb, ocam, osf, O.PLAIN, dt)
     t_prebwd = time.perf_counter() - t0
     ntiles = ranges.shape[0]
-    k = sample_tiles or 2 * procs
+    k = sample_tiles or max(2 * procs, int(round(0.1 * ntiles)))   # default: a tenth of the tiles
     rng = np.random.default_rng(seed)
     ctx = mp.get_context("spawn")
     with ctx.Pool(procs, initializer=_setup, initargs=(workload_name, seed, 0, dtype_name)) as pool:

@@ -62,6 +62,7 @@ struct CellArgs {
   int lb;                            // log2(B)
   int cx, cy;                        // cells per view along x and y
   int warps;                         // warps of the list-writing CTA
+  int stage;                         // entries a list-writing CTA can stage in shared memory
   bool ids;                          // write record ids (else depth-order positions)
 };
 
@@ -233,7 +234,9 @@ __global__ void k_cell_ranges(CellArgs a) {
 
 // 3. stable scatter of each chunk's records into the cell lists
 __global__ void __launch_bounds__(256) k_cell_write(CellArgs a) {
-  extern __shared__ uint32_t s_cnt[];              // [warps][cells per view]
+  // [warps][cells per view] positions, then [cells + 1] chunk-run starts,
+  // [cells] list positions of those runs, then the staging area
+  extern __shared__ uint32_t s_cnt[];
   int v, p0, p1;
   if (!chunk_span(a, blockIdx.x, v, p0, p1)) return;
   const int ncell = a.cx * a.cy;
@@ -278,14 +281,47 @@ __global__ void __launch_bounds__(256) k_cell_write(CellArgs a) {
   __syncthreads();
   const uint32_t* cbase = a.chunk_base + (size_t)blockIdx.x * ncell;
   const uint32_t* cstart = a.cell_start + (size_t)v * ncell;
-  for (int t = threadIdx.x; t < ncell; t += blockDim.x) {
-    uint32_t run = cstart[t] + cbase[t];
+  uint32_t* s_run = s_cnt + (size_t)a.warps * ncell;      // [ncell + 1]: this chunk's run starts, staged order
+  uint32_t* s_dst = s_run + ncell + 1;                    // [ncell]: where each run goes in the lists
+  uint32_t* s_stage = s_dst + ncell;                      // [a.stage]
+  __shared__ uint32_t s_part[8];
+  // Each cell's entries from this chunk form one run in the cell's list.
+  // When the chunk's entries fit the staging area, they are placed there
+  // (cell-major) and each run is then written out contiguously; otherwise
+  // straight into the lists.  Runs: exclusive scan of the chunk's per-cell
+  // counts, each thread a contiguous range of cells.
+  const int per_t = (ncell + blockDim.x - 1) / blockDim.x;
+  const int c0 = min(ncell, (int)threadIdx.x * per_t), c1 = min(ncell, c0 + per_t);
+  uint32_t mine = 0;
+  for (int t = c0; t < c1; ++t)
+    for (int w = 0; w < a.warps; ++w) mine += s_cnt[(size_t)w * ncell + t];
+  uint32_t incl = mine;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += y;
+  }
+  if (lane == 31) s_part[warp] = incl;
+  __syncthreads();
+  uint32_t before = 0, total = 0;
+  for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+    if (w < warp) before += s_part[w];
+    total += s_part[w];
+  }
+  const bool staged = total <= (uint32_t)a.stage;                 // CTA-uniform
+  uint32_t run = before + incl - mine;
+  for (int t = c0; t < c1; ++t) {
+    s_run[t] = run;
+    s_dst[t] = cstart[t] + cbase[t];
+    uint32_t at = staged ? run : cstart[t] + cbase[t];
     for (int w = 0; w < a.warps; ++w) {
       const uint32_t n = s_cnt[(size_t)w * ncell + t];
-      s_cnt[(size_t)w * ncell + t] = run;
+      s_cnt[(size_t)w * ncell + t] = at;
+      at += n;
       run += n;
     }
   }
+  if (threadIdx.x == 0) s_run[ncell] = total;
   __syncthreads();
   // walk this warp's records in order; for each, the lanes cover its cells
   for (int g = w0; g < w1; g += 32) {
@@ -309,10 +345,19 @@ __global__ void __launch_bounds__(256) k_cell_write(CellArgs a) {
         const int qy = q / w;
         const int t = (ay + qy) * cx + ax + (q - qy * w);
         const uint32_t pos = cnt[t]++;
-        if ((long long)pos < a.capacity) a.out[pos] = ek;
+        if (staged) s_stage[pos] = ek;
+        else if ((long long)pos < a.capacity) a.out[pos] = ek;
       }
       __syncwarp();
     }
+  }
+  if (!staged) return;                               // CTA-uniform
+  __syncthreads();
+  // each warp writes whole runs, lanes over consecutive entries
+  for (int t = warp; t < ncell; t += blockDim.x >> 5) {
+    const uint32_t r0 = s_run[t], n = s_run[t + 1] - r0, d = s_dst[t];
+    for (uint32_t k = lane; k < n; k += 32)
+      if ((long long)(d + k) < a.capacity) a.out[d + k] = s_stage[r0 + k];
   }
 }
 
@@ -320,8 +365,22 @@ constexpr size_t kMaxDynSmem = 220 * 1024;
 constexpr size_t kAlignB = 256;
 size_t al(size_t x) { return (x + kAlignB - 1) & ~(kAlignB - 1); }
 
+// Staging area of the list writer, in entries: 6,144 (24 KB), less where
+// the per-warp counts leave less room.
+constexpr long long kStageEntries = 6144;
+
+size_t writer_smem(int warps, int ncell, int stage) {
+  return ((size_t)warps * ncell + 2 * (size_t)ncell + 1 + (size_t)stage) * 4;
+}
+
+int writer_stage(int warps, int ncell) {
+  const long long room = (long long)(kMaxDynSmem / 4) - (long long)warps * ncell - 2LL * ncell - 1;
+  return (int)std::max(0LL, std::min(kStageEntries, room));
+}
+
 int writer_warps(int ncell) {
-  const long long fit = (long long)(200 * 1024) / (4LL * std::max(1, ncell));
+  // per-warp counts, plus the run starts and destinations, within 200 KB
+  const long long fit = ((long long)(200 * 1024) / 4 - 2LL * ncell - 1) / std::max(1, ncell);
   return fit >= 8 ? 8 : fit >= 4 ? 4 : fit >= 2 ? 2 : fit >= 1 ? 1 : 0;
 }
 
@@ -382,6 +441,7 @@ int run_cells(const sgr_batch& b, const GeomView& g, int B, bool ids, uint32_t* 
   a.cx = cx;
   a.cy = cy;
   a.warps = warps;
+  a.stage = writer_stage(warps, ncell);
   a.ids = ids;
   const long long chunks = (b.num_records + kChunk - 1) / kChunk + b.num_views;
   const long long ncells = (long long)b.num_views * ncell;
@@ -399,7 +459,7 @@ int run_cells(const sgr_batch& b, const GeomView& g, int B, bool ids, uint32_t* 
     return SGR_ERR_CUDA;
   k_cell_ranges<<<(unsigned)((ncells + 255) / 256), 256, 0, st>>>(a);
   count_launches();
-  k_cell_write<<<(unsigned)chunks, warps * 32, (size_t)warps * ncell * 4, st>>>(a);
+  k_cell_write<<<(unsigned)chunks, warps * 32, writer_smem(warps, ncell, a.stage), st>>>(a);
   count_launches();
   return cudaGetLastError() == cudaSuccess ? SGR_OK : SGR_ERR_CUDA;
 }

@@ -159,6 +159,74 @@ __device__ __forceinline__ float splat_coords(float x, float y, float z, float& 
 #endif
 }
 
+// The reciprocal of p.z the plain variant's explicit geometry uses: the
+// approximate one (SGR_SPLAT_DIV 2) or the correctly rounded one (0, 1).
+__device__ __forceinline__ float splat_rcp(float z) {
+#if SGR_SPLAT_DIV == 2
+  return __fdividef(1.0f, z);
+#else
+  return __frcp_rn(z);
+#endif
+}
+
+// ---------------------------------------------------------------------------
+// Fragment geometry of the plain variant in an explicit order of IEEE
+// round-to-nearest operations, for one pixel (float) or for a thread's two
+// pixels at once (float2: the packed FP32 instructions, __ffma2_rn and
+// friends).  Both forms give identical results element by element, so the
+// forward (one pixel per thread) and the packed backward (two) make the
+// same decisions -- the near-plane, power and alpha tests -- bit for bit.
+// The operations follow P0/cr/forward.cu:349-378: k = px Tw - Tu,
+// l = py Tw - Tv, p = k x l (each component fma(a, b, -(c d))), the filter
+// distance 2 (dx^2 + dy^2), s = p.xy / p.z by one approximate reciprocal,
+// rho3d = sx^2 + sy^2, depth (sx Tw.x + sy Tw.y) + Tw.z on the 3D branch.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float lmul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float2 lmul(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float lfma(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ float2 lfma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float ladd(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float2 ladd(float2 a, float2 b) { return __fadd2_rn(a, b); }
+template <class T> __device__ __forceinline__ T bc(float s);
+template <> __device__ __forceinline__ float bc<float>(float s) { return s; }
+template <> __device__ __forceinline__ float2 bc<float2>(float s) { return make_float2(s, s); }
+
+template <class T>
+struct FragGeom {
+  T kx, ky, kz, lx, ly, lz, px, py, pz, dx, dy, rho2d;
+};
+
+// Stage 1: the ray-splat intersection and the filter distance.  npx, npy
+// are the negated pixel coordinates.
+template <class T>
+__device__ __forceinline__ void frag_intersect(T pxf, T pyf, T npx, T npy, const float4& r0, const float4& r1,
+                                               const float4& r2, FragGeom<T>& f) {
+  f.kx = lfma(pxf, bc<T>(r1.z), bc<T>(-r0.x));
+  f.ky = lfma(pxf, bc<T>(r1.w), bc<T>(-r0.y));
+  f.kz = lfma(pxf, bc<T>(r2.x), bc<T>(-r0.z));
+  f.lx = lfma(pyf, bc<T>(r1.z), bc<T>(-r0.w));
+  f.ly = lfma(pyf, bc<T>(r1.w), bc<T>(-r1.x));
+  f.lz = lfma(pyf, bc<T>(r2.x), bc<T>(-r1.y));
+  // -(c d) as (-c) d: -k by the same fma with negated operands (rounding is
+  // symmetric), so no product is negated
+  const T nkx = lfma(pxf, bc<T>(-r1.z), bc<T>(r0.x));
+  const T nky = lfma(pxf, bc<T>(-r1.w), bc<T>(r0.y));
+  const T nkz = lfma(pxf, bc<T>(-r2.x), bc<T>(r0.z));
+  f.px = lfma(f.ky, f.lz, lmul(nkz, f.ly));
+  f.py = lfma(f.kz, f.lx, lmul(nkx, f.lz));
+  f.pz = lfma(f.kx, f.ly, lmul(nky, f.lx));
+  f.dx = ladd(bc<T>(r2.y), npx);
+  f.dy = ladd(bc<T>(r2.z), npy);
+  f.rho2d = lmul(bc<T>(kFilterInvSquareP0), lfma(f.dx, f.dx, lmul(f.dy, f.dy)));
+}
+
+// The reach test's two squared lengths: |p.xy|^2 and reach p.z^2.
+template <class T>
+__device__ __forceinline__ void frag_reach_terms(const FragGeom<T>& f, float reach, T& pxy2, T& rpz2) {
+  pxy2 = lfma(f.px, f.px, lmul(f.py, f.py));
+  rpz2 = lmul(bc<T>(reach), lmul(f.pz, f.pz));
+}
+
 // The warp patches of a record, each split into SPLIT groups of rows: bit
 // w * SPLIT + g is set when group g of warp w's patch (WX x WY pixels; the
 // tile holds kTile / WX patches across) may reach the record -- the reach
@@ -359,29 +427,44 @@ __device__ __forceinline__ void fwd_fragment(FwdPixel<VARIANT>& q, const float4 
   if (q.done) return;
   const float4 r0 = s_rec[0][j], r1 = s_rec[1][j], r2 = s_rec[2][j];
   const V3 Tu = v3(r0.x, r0.y, r0.z), Tv = v3(r0.w, r1.x, r1.y), Tw = v3(r1.z, r1.w, r2.x);
-  V3 k, l;
-  if (VARIANT == SGR_VARIANT_PLAIN) {
-    k = q.pxf * Tw - Tu;
-    l = q.pyf * Tw - Tv;
-  } else {
-    k = v3(-Tu.x + q.pxf * Tw.x, -Tu.y + q.pxf * Tw.y, -Tu.z + q.pxf * Tw.z);
-    l = v3(-Tv.x + q.pyf * Tw.x, -Tv.y + q.pyf * Tw.y, -Tv.z + q.pyf * Tw.z);
-  }
-  const V3 p = cross3(k, l);
-  if (p.z == 0.0f) return;
-  const float dx = r2.y - q.pxf, dy = r2.z - q.pyf;
-  const float rho2d = kFilterInvSquareP0 * (dx * dx + dy * dy);
   const float reach = s_rec[3][j].w;
-  if (rho2d > reach && p.x * p.x + p.y * p.y > reach * (p.z * p.z)) return;
-  float sx, sy;
-  splat_coords(p.x, p.y, p.z, sx, sy);
-  const float rho3d = sx * sx + sy * sy;
-  const float rho = fminf(rho3d, rho2d);
-  const float depth = (rho3d <= rho2d) ? (sx * Tw.x + sy * Tw.y) + Tw.z : Tw.z;
-  if (depth < kNearP0) return;
-  const float power = -0.5f * rho;
-  if (power > 0.0f) return;
-  const float alpha = fminf(0.99f, r2.w * splat_exp(power));
+  float sx, sy, rho2d, depth, power, alpha;
+  if (VARIANT == SGR_VARIANT_PLAIN) {
+    // the explicit sequence the packed backward repeats
+    FragGeom<float> f;
+    frag_intersect<float>(q.pxf, q.pyf, -q.pxf, -q.pyf, r0, r1, r2, f);
+    if (f.pz == 0.0f) return;
+    rho2d = f.rho2d;
+    float pxy2, rpz2;
+    frag_reach_terms(f, reach, pxy2, rpz2);
+    if (rho2d > reach && pxy2 > rpz2) return;
+    const float iz = splat_rcp(f.pz);
+    sx = lmul(f.px, iz);
+    sy = lmul(f.py, iz);
+    const float rho3d = lfma(sx, sx, lmul(sy, sy));
+    const float rho = fminf(rho3d, rho2d);
+    depth = (rho3d <= rho2d) ? ladd(lfma(sx, Tw.x, lmul(sy, Tw.y)), Tw.z) : Tw.z;
+    if (depth < kNearP0) return;
+    power = lmul(-0.5f, rho);
+    if (power > 0.0f) return;
+    alpha = fminf(0.99f, lmul(r2.w, splat_exp(power)));
+  } else {
+    const V3 k = v3(-Tu.x + q.pxf * Tw.x, -Tu.y + q.pxf * Tw.y, -Tu.z + q.pxf * Tw.z);
+    const V3 l = v3(-Tv.x + q.pyf * Tw.x, -Tv.y + q.pyf * Tw.y, -Tv.z + q.pyf * Tw.z);
+    const V3 p = cross3(k, l);
+    if (p.z == 0.0f) return;
+    const float dx = r2.y - q.pxf, dy = r2.z - q.pyf;
+    rho2d = kFilterInvSquareP0 * (dx * dx + dy * dy);
+    if (rho2d > reach && p.x * p.x + p.y * p.y > reach * (p.z * p.z)) return;
+    splat_coords(p.x, p.y, p.z, sx, sy);
+    const float rho3d = sx * sx + sy * sy;
+    const float rho = fminf(rho3d, rho2d);
+    depth = (rho3d <= rho2d) ? (sx * Tw.x + sy * Tw.y) + Tw.z : Tw.z;
+    if (depth < kNearP0) return;
+    power = -0.5f * rho;
+    if (power > 0.0f) return;
+    alpha = fminf(0.99f, r2.w * splat_exp(power));
+  }
   if (alpha < 1.0f / 255.0f) return;
   const float test_T = q.T * (1 - alpha);
   if (test_T < 0.0001f) {
@@ -689,14 +772,22 @@ struct BwdGeom {
 template <int VARIANT>
 __device__ __forceinline__ bool bwd_reach(const BwdPixel<VARIANT>& q, const float4& r0, const float4& r1,
                                           const float4& r2, float reach, int pos, BwdGeom& f) {
-  const V3 Tu = v3(r0.x, r0.y, r0.z), Tv = v3(r0.w, r1.x, r1.y), Tw = v3(r1.z, r1.w, r2.x);
-  if (VARIANT == SGR_VARIANT_PLAIN) {
-    f.k = q.pxf * Tw - Tu;
-    f.l = q.pyf * Tw - Tv;
-  } else {
-    f.k = v3(-Tu.x + q.pxf * Tw.x, -Tu.y + q.pxf * Tw.y, -Tu.z + q.pxf * Tw.z);
-    f.l = v3(-Tv.x + q.pyf * Tw.x, -Tv.y + q.pyf * Tw.y, -Tv.z + q.pyf * Tw.z);
+  if (VARIANT == SGR_VARIANT_PLAIN) {   // the forward's explicit sequence
+    FragGeom<float> g;
+    frag_intersect<float>(q.pxf, q.pyf, -q.pxf, -q.pyf, r0, r1, r2, g);
+    f.k = v3(g.kx, g.ky, g.kz);
+    f.l = v3(g.lx, g.ly, g.lz);
+    f.p = v3(g.px, g.py, g.pz);
+    f.dx = g.dx;
+    f.dy = g.dy;
+    float pxy2, rpz2;
+    frag_reach_terms(g, reach, pxy2, rpz2);
+    f.live = pos < q.last_contributor && g.pz != 0.0f && !(g.rho2d > reach && pxy2 > rpz2);
+    return f.live;
   }
+  const V3 Tu = v3(r0.x, r0.y, r0.z), Tv = v3(r0.w, r1.x, r1.y), Tw = v3(r1.z, r1.w, r2.x);
+  f.k = v3(-Tu.x + q.pxf * Tw.x, -Tu.y + q.pxf * Tw.y, -Tu.z + q.pxf * Tw.z);
+  f.l = v3(-Tv.x + q.pyf * Tw.x, -Tv.y + q.pyf * Tw.y, -Tv.z + q.pyf * Tw.z);
   f.p = cross3(f.k, f.l);
   f.dx = r2.y - q.pxf;
   f.dy = r2.z - q.pyf;
@@ -708,9 +799,25 @@ __device__ __forceinline__ bool bwd_reach(const BwdPixel<VARIANT>& q, const floa
 
 // Stage 2: alpha and the remaining tests, with the forward's divisions so
 // that alpha and the tests agree with it bit for bit.
+template <int VARIANT>
 __device__ __forceinline__ void bwd_alpha(const float4& r1, const float4& r2, BwdGeom& f) {
   const float Twx = r1.z, Twy = r1.w, Twz = r2.x;
   const float pz = f.live ? f.p.z : 1.0f;
+  if (VARIANT == SGR_VARIANT_PLAIN) {   // the forward's explicit sequence
+    f.iz = splat_rcp(pz);
+    f.sx = lmul(f.p.x, f.iz);
+    f.sy = lmul(f.p.y, f.iz);
+    const float rho3d = lfma(f.sx, f.sx, lmul(f.sy, f.sy));
+    const float rho2d = lmul(kFilterInvSquareP0, lfma(f.dx, f.dx, lmul(f.dy, f.dy)));
+    f.use3d = rho3d <= rho2d;
+    const float rho = fminf(rho3d, rho2d);
+    f.c_d = f.use3d ? ladd(lfma(f.sx, Twx, lmul(f.sy, Twy)), Twz) : Twz;
+    const float power = lmul(-0.5f, rho);
+    f.G = splat_exp(power);
+    f.alpha = fminf(0.99f, lmul(r2.w, f.G));
+    f.live = f.live && !(f.c_d < kNearP0) && !(power > 0.0f) && !(f.alpha < 1.0f / 255.0f);
+    return;
+  }
   f.iz = splat_coords(f.p.x, f.p.y, pz, f.sx, f.sy);
   const float rho3d = f.sx * f.sx + f.sy * f.sy;
   const float rho2d = kFilterInvSquareP0 * (f.dx * f.dx + f.dy * f.dy);
@@ -829,6 +936,207 @@ __device__ __forceinline__ void bwd_update(BwdPixel<VARIANT>& q, const BwdGeom& 
   if (VARIANT == SGR_VARIANT_PART) q.sem_w = wgt;   // dL/dsemantic[c] += wgt dL/dpixel_semantic[c]
 }
 
+// ---------------------------------------------------------------------------
+// The plain backward's two pixels per thread as the two lanes of packed
+// FP32 operations (SGR_BWD_PACKED): the same recurrences as bwd_reach,
+// bwd_alpha and bwd_update, with the fragment geometry in the forward's
+// explicit sequence (frag_intersect), so the decisions -- which fragments
+// count -- are the forward's bit for bit.  A pixel that a fragment does not
+// reach keeps its state (per-lane selects) and adds nothing.
+// ---------------------------------------------------------------------------
+#ifndef SGR_BWD_PACKED
+#define SGR_BWD_PACKED 1
+#endif
+
+__device__ __forceinline__ float2 sel2(bool a, bool b, float2 x, float2 y) {
+  return make_float2(a ? x.x : y.x, b ? x.y : y.y);
+}
+
+// Per-pixel state of the backward recurrences, lane i = pixel i.
+struct BwdPair {
+  float pxf;                                 // both pixels share the column
+  float2 pyf, npx, npy;
+  float2 T, T_final, final_A, final_D, final_D2, bg_dot;
+  int last_contributor[2], median_contributor[2];
+  float2 dL_dpixel[3], dL_dnormal2D[3];
+  float2 dL_ddepth, dL_daccum, dL_dreg, dL_dmedian;
+  float2 rec_dot, last_col_dot, nrm_dot, last_nrm_dot;
+  float2 last_alpha, last_depth, accum_depth, accum_alpha, last_dL_dT;
+};
+
+__device__ __forceinline__ BwdPair to_pair(const BwdPixel<SGR_VARIANT_PLAIN> (&q)[2]) {
+  BwdPair p;
+  auto f2 = [](float a, float b) { return make_float2(a, b); };
+  p.pxf = q[0].pxf;
+  p.pyf = f2(q[0].pyf, q[1].pyf);
+  p.npx = f2(-q[0].pxf, -q[1].pxf);
+  p.npy = f2(-q[0].pyf, -q[1].pyf);
+  p.T = f2(q[0].T, q[1].T);
+  p.T_final = f2(q[0].T_final, q[1].T_final);
+  p.final_A = f2(q[0].final_A, q[1].final_A);
+  p.final_D = f2(q[0].final_D, q[1].final_D);
+  p.final_D2 = f2(q[0].final_D2, q[1].final_D2);
+  p.bg_dot = f2(q[0].bg_dot, q[1].bg_dot);
+  for (int i = 0; i < 2; ++i) {
+    p.last_contributor[i] = q[i].last_contributor;
+    p.median_contributor[i] = q[i].median_contributor;
+  }
+  for (int c = 0; c < 3; ++c) {
+    p.dL_dpixel[c] = f2(q[0].dL_dpixel[c], q[1].dL_dpixel[c]);
+    p.dL_dnormal2D[c] = f2(q[0].dL_dnormal2D[c], q[1].dL_dnormal2D[c]);
+  }
+  p.dL_ddepth = f2(q[0].dL_ddepth, q[1].dL_ddepth);
+  p.dL_daccum = f2(q[0].dL_daccum, q[1].dL_daccum);
+  p.dL_dreg = f2(q[0].dL_dreg, q[1].dL_dreg);
+  p.dL_dmedian = f2(q[0].dL_dmedian, q[1].dL_dmedian);
+  const float2 z = f2(0.f, 0.f);
+  p.rec_dot = p.last_col_dot = p.nrm_dot = p.last_nrm_dot = z;
+  p.last_alpha = p.last_depth = p.accum_depth = p.accum_alpha = p.last_dL_dT = z;
+  return p;
+}
+
+// Geometry of the two fragments of one entry (stages 1 and 2 of the
+// backward); live[i] is false when pixel i's fragment contributes nothing.
+struct BwdGeom2 {
+  FragGeom<float2> g;
+  float2 sx, sy, iz, G, alpha, c_d;
+  bool use3d[2], live[2];
+};
+
+// Stage 1: the reach test of both pixels.
+__device__ __forceinline__ bool bwd_reach2(const BwdPair& q, const float4& r0, const float4& r1, const float4& r2,
+                                           float reach, int pos, BwdGeom2& f) {
+  frag_intersect<float2>(make_float2(q.pxf, q.pxf), q.pyf, q.npx, q.npy, r0, r1, r2, f.g);
+  float2 pxy2, rpz2;
+  frag_reach_terms(f.g, reach, pxy2, rpz2);
+  f.live[0] = pos < q.last_contributor[0] && f.g.pz.x != 0.0f && !(f.g.rho2d.x > reach && pxy2.x > rpz2.x);
+  f.live[1] = pos < q.last_contributor[1] && f.g.pz.y != 0.0f && !(f.g.rho2d.y > reach && pxy2.y > rpz2.y);
+  return f.live[0] || f.live[1];
+}
+
+// Stage 2: alpha and the remaining tests, as the forward computes them.
+__device__ __forceinline__ void bwd_alpha2(const float4& r1, const float4& r2, BwdGeom2& f) {
+  const float Twx = r1.z, Twy = r1.w, Twz = r2.x;
+  f.iz = make_float2(splat_rcp(f.live[0] ? f.g.pz.x : 1.0f), splat_rcp(f.live[1] ? f.g.pz.y : 1.0f));
+  f.sx = lmul(f.g.px, f.iz);
+  f.sy = lmul(f.g.py, f.iz);
+  const float2 rho3d = lfma(f.sx, f.sx, lmul(f.sy, f.sy));
+  f.use3d[0] = rho3d.x <= f.g.rho2d.x;
+  f.use3d[1] = rho3d.y <= f.g.rho2d.y;
+  const float2 rho = make_float2(fminf(rho3d.x, f.g.rho2d.x), fminf(rho3d.y, f.g.rho2d.y));
+  const float2 d3 = ladd(lfma(f.sx, bc<float2>(Twx), lmul(f.sy, bc<float2>(Twy))), bc<float2>(Twz));
+  f.c_d = make_float2(f.use3d[0] ? d3.x : Twz, f.use3d[1] ? d3.y : Twz);
+  const float2 power = lmul(bc<float2>(-0.5f), rho);
+  f.G = make_float2(splat_exp(power.x), splat_exp(power.y));
+  const float2 oa = lmul(bc<float2>(r2.w), f.G);
+  f.alpha = make_float2(fminf(0.99f, oa.x), fminf(0.99f, oa.y));
+  f.live[0] = f.live[0] && !(f.c_d.x < kNearP0) && !(power.x > 0.0f) && !(f.alpha.x < 1.0f / 255.0f);
+  f.live[1] = f.live[1] && !(f.c_d.y < kNearP0) && !(power.y > 0.0f) && !(f.alpha.y < 1.0f / 255.0f);
+}
+
+// Stage 3: both pixels' recurrences and their summed share of the entry's
+// 18 gradient values (gv), P0/cr/backward.cu:337-440.
+__device__ __forceinline__ void bwd_update2(BwdPair& q, const BwdGeom2& f, const float4& r1, const float4& r2,
+                                            const float4& r3, const float4& r4, int pos, float (&gv)[32]) {
+  const bool l0 = f.live[0], l1 = f.live[1];
+  const float2 one = bc<float2>(1.0f), zero = bc<float2>(0.0f);
+  const float2 alpha = sel2(l0, l1, f.alpha, zero);
+  const float2 G = f.G, c_d = f.c_d;
+  const float2 oma = lfma(alpha, bc<float2>(-1.0f), one);                       // 1 - alpha
+  const float2 inv_1ma = make_float2(blend_rcp(oma.x), blend_rcp(oma.y));
+  const float2 T = sel2(l0, l1, lmul(q.T, inv_1ma), q.T);
+  q.T = T;
+  const float2 wgt = lmul(alpha, T);                                            // zero where not live
+  const float2 oml = lfma(q.last_alpha, bc<float2>(-1.0f), one);               // 1 - last_alpha
+  // colour recurrence on its dot product with dL/dpixel
+  const float2 cd = lfma(bc<float2>(r4.z), q.dL_dpixel[2],
+                         lfma(bc<float2>(r4.y), q.dL_dpixel[1], lmul(bc<float2>(r4.x), q.dL_dpixel[0])));
+  const float2 rec = lfma(q.last_alpha, q.last_col_dot, lmul(oml, q.rec_dot));
+  q.rec_dot = sel2(l0, l1, rec, q.rec_dot);
+  q.last_col_dot = sel2(l0, l1, cd, q.last_col_dot);
+  float2 dL_dalpha = ladd(cd, make_float2(-rec.x, -rec.y));
+  // depth distortion (mapped depth and its derivative)
+  const float2 inv_d = make_float2(blend_rcp(c_d.x), blend_rcp(c_d.y));
+  const float2 m_d = lmul(bc<float2>(kFarP0 / (kFarP0 - kNearP0)), lfma(bc<float2>(-kNearP0), inv_d, one));
+  const float2 dmd_dd = lmul(bc<float2>((kFarP0 * kNearP0) / (kFarP0 - kNearP0)), lmul(inv_d, inv_d));
+  float2 dL_dz = make_float2(pos == q.median_contributor[0] - 1 ? q.dL_dmedian.x : 0.0f,
+                             pos == q.median_contributor[1] - 1 ? q.dL_dmedian.y : 0.0f);
+  // final_D2 + m^2 final_A - 2 m final_D
+  const float2 reg = lfma(m_d, lfma(m_d, q.final_A, lmul(bc<float2>(-2.0f), q.final_D)), q.final_D2);
+  const float2 dL_dweight = lmul(reg, q.dL_dreg);
+  dL_dalpha = ladd(dL_dalpha, ladd(dL_dweight, make_float2(-q.last_dL_dT.x, -q.last_dL_dT.y)));
+  const float2 ldt = lfma(dL_dweight, alpha, lmul(lfma(alpha, bc<float2>(-1.0f), one), q.last_dL_dT));
+  q.last_dL_dT = sel2(l0, l1, ldt, q.last_dL_dT);
+  const float2 dL_dmd = lmul(lmul(bc<float2>(2.0f), wgt),
+                             lmul(lfma(m_d, q.final_A, make_float2(-q.final_D.x, -q.final_D.y)), q.dL_dreg));
+  dL_dz = lfma(dL_dmd, dmd_dd, dL_dz);
+  const float2 acd = lfma(q.last_alpha, q.last_depth, lmul(oml, q.accum_depth));
+  q.accum_depth = sel2(l0, l1, acd, q.accum_depth);
+  q.last_depth = sel2(l0, l1, c_d, q.last_depth);
+  dL_dalpha = lfma(ladd(c_d, make_float2(-acd.x, -acd.y)), q.dL_ddepth, dL_dalpha);
+  // accum_alpha = last_alpha + (1 - last_alpha) accum_alpha, one rounding each
+  const float2 aca = ladd(q.last_alpha, lmul(oml, q.accum_alpha));
+  q.accum_alpha = sel2(l0, l1, aca, q.accum_alpha);
+  dL_dalpha = lfma(lfma(aca, bc<float2>(-1.0f), one), q.dL_daccum, dL_dalpha);
+  // normal recurrence on its dot product with dL/dnormal
+  const float2 nd = lfma(bc<float2>(r3.z), q.dL_dnormal2D[2],
+                         lfma(bc<float2>(r3.y), q.dL_dnormal2D[1], lmul(bc<float2>(r3.x), q.dL_dnormal2D[0])));
+  const float2 nrec = lfma(q.last_alpha, q.last_nrm_dot, lmul(oml, q.nrm_dot));
+  q.nrm_dot = sel2(l0, l1, nrec, q.nrm_dot);
+  q.last_nrm_dot = sel2(l0, l1, nd, q.last_nrm_dot);
+  dL_dalpha = ladd(dL_dalpha, ladd(nd, make_float2(-nrec.x, -nrec.y)));
+  dL_dalpha = lmul(dL_dalpha, T);
+  q.last_alpha = sel2(l0, l1, alpha, q.last_alpha);
+  dL_dalpha = lfma(lmul(make_float2(-q.T_final.x, -q.T_final.y), inv_1ma), q.bg_dot, dL_dalpha);
+  dL_dalpha = sel2(l0, l1, dL_dalpha, zero);
+  dL_dz = sel2(l0, l1, lfma(wgt, q.dL_ddepth, dL_dz), zero);
+  const float2 dL_dG = lmul(bc<float2>(r2.w), dL_dalpha);
+  // per-value sums over the two pixels
+#pragma unroll
+  for (int ch = 0; ch < 3; ++ch) {
+    const float2 c = lmul(wgt, q.dL_dpixel[ch]);
+    gv[14 + ch] += c.x + c.y;
+    const float2 n = lmul(wgt, q.dL_dnormal2D[ch]);
+    gv[11 + ch] += n.x + n.y;
+  }
+  const float2 gG = lmul(G, dL_dalpha);
+  gv[17] += gG.x + gG.y;
+  // 3D branch (ray-splat intersection) where use3d, 2D (filter) branch elsewhere
+  const bool u0 = f.use3d[0], u1 = f.use3d[1];
+  const float2 dG3 = sel2(u0, u1, dL_dG, zero), dz3 = sel2(u0, u1, dL_dz, zero);
+  const float2 nG = make_float2(-G.x, -G.y);
+  const float2 dsx = lmul(lfma(lmul(dG3, nG), f.sx, lmul(dz3, bc<float2>(r1.z))), f.iz);
+  const float2 dsy = lmul(lfma(lmul(dG3, nG), f.sy, lmul(dz3, bc<float2>(r1.w))), f.iz);
+  const float2 dpz = lfma(dsx, make_float2(-f.sx.x, -f.sx.y), lmul(dsy, make_float2(-f.sy.x, -f.sy.y)));
+  // dL/dk = l x dL/dp, dL/dl = dL/dp x k
+  const FragGeom<float2>& g = f.g;
+  const float2 dkx = lfma(g.ly, dpz, lmul(make_float2(-g.lz.x, -g.lz.y), dsy));
+  const float2 dky = lfma(g.lz, dsx, lmul(make_float2(-g.lx.x, -g.lx.y), dpz));
+  const float2 dkz = lfma(g.lx, dsy, lmul(make_float2(-g.ly.x, -g.ly.y), dsx));
+  const float2 dlx = lfma(dsy, g.kz, lmul(make_float2(-dpz.x, -dpz.y), g.ky));
+  const float2 dly = lfma(dpz, g.kx, lmul(make_float2(-dsx.x, -dsx.y), g.kz));
+  const float2 dlz = lfma(dsx, g.ky, lmul(make_float2(-dsy.x, -dsy.y), g.kx));
+  gv[0] -= dkx.x + dkx.y;
+  gv[1] -= dky.x + dky.y;
+  gv[2] -= dkz.x + dkz.y;
+  gv[3] -= dlx.x + dlx.y;
+  gv[4] -= dly.x + dly.y;
+  gv[5] -= dlz.x + dlz.y;
+  const float2 px2 = bc<float2>(q.pxf);
+  const float2 u6 = lfma(px2, dkx, lfma(q.pyf, dlx, lmul(dz3, f.sx)));
+  const float2 u7 = lfma(px2, dky, lfma(q.pyf, dly, lmul(dz3, f.sy)));
+  const float2 dz2 = sel2(u0, u1, zero, dL_dz);
+  const float2 u8 = lfma(px2, dkz, lfma(q.pyf, dlz, ladd(dz3, dz2)));
+  gv[6] += u6.x + u6.y;
+  gv[7] += u7.x + u7.y;
+  gv[8] += u8.x + u8.y;
+  const float2 dG2 = sel2(u0, u1, zero, dL_dG);
+  const float2 kG = lmul(dG2, lmul(nG, bc<float2>(kFilterInvSquareP0)));
+  const float2 u9 = lmul(kG, g.dx), u10 = lmul(kG, g.dy);
+  gv[9] += u9.x + u9.y;
+  gv[10] += u10.x + u10.y;
+}
+
 // Resident CTAs per SM the plain backward is compiled for (registers per
 // thread = 65536 / (128 threads x this)).
 #ifndef SGR_BWD_MIN_CTAS
@@ -921,6 +1229,10 @@ __device__ __forceinline__ void render_bwd_tile(const sgr_batch& b, const GeomVi
 #endif
     thread_max = max(thread_max, Q.last_contributor);
   }
+  // the two pixels of a plain thread as packed lanes
+  constexpr bool PACKED = SGR_BWD_PACKED && VARIANT == SGR_VARIANT_PLAIN && PX == 2 && SPLIT == 1;
+  BwdPair qp;
+  if constexpr (PACKED) qp = to_pair(q);
 
   int warp_max = thread_max;
 #pragma unroll
@@ -980,6 +1292,19 @@ __device__ __forceinline__ void render_bwd_tile(const sgr_batch& b, const GeomVi
       for (int u = 0; u < 32; ++u) gv[u] = 0.f;
       const float4 r0 = s_rec[0][j], r1 = s_rec[1][j], r2 = s_rec[2][j];
       const float reach = s_rec[3][j].w;
+      if constexpr (PACKED) {
+        BwdGeom2 f2;
+        if (!__any_sync(0xffffffffu, bwd_reach2(qp, r0, r1, r2, reach, pos, f2))) continue;   // uniform
+        bwd_alpha2(r1, r2, f2);
+        const bool ok2 = f2.live[0] || f2.live[1];
+        if (!__any_sync(0xffffffffu, ok2)) continue;
+        const float4 r3 = s_rec[3][j], r4 = s_rec[4][j];
+        if (ok2) bwd_update2(qp, f2, r1, r2, r3, r4, pos, gv);
+        int which;
+        const float total = warp_sum18(gv, lane, which);
+        if (which >= 0 && total != 0.f) atomicAdd(grads + (size_t)s_id[j] * kGradF + which, total);
+        continue;
+      }
       BwdGeom f[PX];
       bool may = false;
 #pragma unroll
@@ -991,7 +1316,7 @@ __device__ __forceinline__ void render_bwd_tile(const sgr_batch& b, const GeomVi
       bool ok = false;
 #pragma unroll
       for (int i = 0; i < PX; ++i) {
-        if (SPLIT == 1 || ((rows_live >> i) & 1u)) bwd_alpha(r1, r2, f[i]);   // uniform
+        if (SPLIT == 1 || ((rows_live >> i) & 1u)) bwd_alpha<VARIANT>(r1, r2, f[i]);   // uniform
         ok |= f[i].live;
       }
       if (!__any_sync(0xffffffffu, ok)) continue;
