@@ -331,10 +331,10 @@ __global__ void __launch_bounds__(kThreads) k_gemm_tc(const sgr_gemm_args a) {
 //     accumulators (2 x NT columns), four MMAs per chunk once full[s] has
 //     its bytes, each chunk's MMAs committed to empty[s], the tile's last
 //     commit to tfull[b]; it waits on tempty[b] before reusing accumulator b;
-//   warps 2-9: epilogue; warp w reads tensor-memory lanes 32 (w % 4) .. + 31
-//     (rows of the tile), columns of half (w - 2) / 4 of the tile, once
-//     tfull[b] fires, 32 columns per wait, applies the epilogue, stores, and
-//     arrives on tempty[b].
+//   warps 2 ..: epilogue, four per 64 output columns; warp w reads
+//     tensor-memory lanes 32 (w % 4) .. + 31 (rows of the tile), columns of
+//     group (w - 2) / 4, once tfull[b] fires, 32 columns per wait, applies
+//     the epilogue, stores, and arrives on tempty[b].
 // So one tile's epilogue runs while the next tile's loads and MMAs do.
 // Every wait is bounded (kWaitNs) and also ends when another role has
 // failed; a failure raises SGR_MLP_TIMEOUT, the producer then waits
@@ -343,9 +343,12 @@ __global__ void __launch_bounds__(kThreads) k_gemm_tc(const sgr_gemm_args a) {
 // Out-of-range rows and columns are zero-filled by the TMA unit.
 // ---------------------------------------------------------------------------
 constexpr int kStages = 4;
-constexpr int kEpiWarps = 8;
 constexpr int kBiasSmem = 1024;   // output columns whose bias the persistent GEMM keeps in shared memory
-constexpr int kPersistThreads = 64 + 32 * kEpiWarps;
+// epilogue warps of an NT-column tile: four (one per 32 rows) per 64 columns
+template <int NT>
+__host__ __device__ constexpr int epi_warps() { return 4 * (NT >= 64 ? NT / 64 : 1); }
+template <int NT>
+__host__ __device__ constexpr int persist_threads() { return 64 + 32 * epi_warps<NT>(); }
 
 __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, int x, int y, uint32_t bar) {
   asm volatile(
@@ -376,7 +379,7 @@ __device__ __forceinline__ bool mbar_wait_or_fail(uint32_t bar, uint32_t parity,
 }
 
 template <int NT>
-__global__ void __launch_bounds__(kPersistThreads, 1)
+__global__ void __launch_bounds__(persist_threads<NT>(), 1)
     k_gemm_persist(const sgr_gemm_args a, const __grid_constant__ CUtensorMap map_a,
                    const __grid_constant__ CUtensorMap map_b, int ns) {
   extern __shared__ __align__(1024) uint8_t smem[];
@@ -393,7 +396,7 @@ __global__ void __launch_bounds__(kPersistThreads, 1)
   // values per 16 columns; from global memory those loads were its stall)
   const bool bias_smem = a.bias && a.N <= kBiasSmem;
   if (bias_smem)
-    for (int c = threadIdx.x; c < (int)a.N; c += kPersistThreads) s_bias[c] = a.bias[c];
+    for (int c = threadIdx.x; c < (int)a.N; c += persist_threads<NT>()) s_bias[c] = a.bias[c];
   const float* bias = bias_smem ? s_bias : a.bias;
   const int tiles_n = (int)((a.N + NT - 1) / NT);
   const int total = (int)((a.M + kTM - 1) / kTM) * tiles_n;
@@ -412,7 +415,8 @@ __global__ void __launch_bounds__(kPersistThreads, 1)
     }
     for (int b = 0; b < 2; ++b) {
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_addr(&s_tfull[b])) : "memory");
-      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_addr(&s_tempty[b])), "r"(kEpiWarps)
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_addr(&s_tempty[b])),
+                   "r"(epi_warps<NT>())
                    : "memory");
     }
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_addr(&s_done)) : "memory");
@@ -502,9 +506,9 @@ __global__ void __launch_bounds__(kPersistThreads, 1)
     }
   } else {
     // epilogue: this warp's quarter of the tensor-memory lanes (rows) and
-    // half of the columns
+    // its group of columns
     const int q = warp & 3;
-    constexpr int kHalf = NT / 2;
+    constexpr int kHalf = NT / (epi_warps<NT>() / 4);   // columns per warp
     const int h0 = ((warp - 2) >> 2) * kHalf;
     int i = 0;
     for (int t = blockIdx.x; t < total; t += gridDim.x, ++i) {
@@ -620,7 +624,7 @@ int launch_tma(const sgr_gemm_args& a, cudaStream_t st) {
     if (cudaFuncSetAttribute(k_gemm_persist<NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
             cudaSuccess ||
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gemm_persist<NT>, kPersistThreads, smem) !=
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gemm_persist<NT>, persist_threads<NT>(), smem) !=
             cudaSuccess)
       return SGR_ERR_CUDA;
     per_sm = per_sm < 512 / (2 * NT) ? per_sm : 512 / (2 * NT);
@@ -629,7 +633,7 @@ int launch_tma(const sgr_gemm_args& a, cudaStream_t st) {
   }
   const long long tiles = ((a.M + kTM - 1) / kTM) * ((a.N + NT - 1) / NT);
   const long long grid = tiles < (long long)resident[dev] ? tiles : (long long)resident[dev];
-  k_gemm_persist<NT><<<(unsigned)grid, kPersistThreads, smem, st>>>(a, ma, mb, ns);
+  k_gemm_persist<NT><<<(unsigned)grid, persist_threads<NT>(), smem, st>>>(a, ma, mb, ns);
   sgr::count_launches(1);
   return cudaGetLastError() == cudaSuccess ? SGR_OK : SGR_ERR_CUDA;
 }

@@ -1,9 +1,15 @@
 """What the trained proposal network gains over the reference's block
 initialisation (k-means blocks, identity rotation, fixed size), on seeded
 held-out synthetic scenes: the shipped weights (trained on the GPU by the
-project's own kernels, partgs_gb300/train_proposal.py) propose
-superquadric sets whose surfaces are closer to the truth, and block fits
-started from them reach the plain fit's final Chamfer distance sooner."""
+project's own kernels on block-fit labels, partgs_gb300/train_proposal.py)
+propose superquadric sets whose surfaces are closer to the truth, and over
+the 32 held-out scenes of the committed time-to-Chamfer record
+(profiles/time_to_chamfer_32.json: seed 4242, 300 iterations) the block fit
+started from them reaches the plain fit's final Chamfer in most scenes,
+in about half the plain fit's time in the median scene.  The benchmark spec's
+target, a third of the time, is not met; the test asserts the measured
+figures (with margin for the run-to-run spread of the fits), not the
+target."""
 import os
 
 import numpy as np
@@ -39,17 +45,21 @@ def test_proposal_init_is_closer_than_the_plain_init(sgr_lib):
     assert (cp < cn).mean() >= 0.6, (cp < cn).mean()
 
 
-def test_block_fit_from_the_proposal_reaches_the_plain_fit_sooner(sgr_lib):
+def test_time_to_chamfer_over_the_held_out_scenes(sgr_lib):
+    """All 32 scenes count: one whose proposal fit never reaches the plain
+    fit's level has ratio infinity.  Measured: 23 of 32 reach it, median
+    ratio 0.49 (profiles/time_to_chamfer_32.json)."""
     from partgs_gb300 import sq_data as D
-    from partgs_gb300.block_fit import time_to_chamfer
+    from partgs_gb300.block_fit import summarize, time_to_chamfer
     from partgs_gb300.train_proposal import load_npz
     net = load_npz(_weights())
-    b = D.sample_sq_batch(6, torch.Generator().manual_seed(77))
-    pts, _ = D.SceneRenderer(res=96).points(b, seed=77)
-    res = time_to_chamfer(net, b, pts, iters=150)
+    b = D.sample_sq_batch(32, torch.Generator().manual_seed(4242))
+    pts, _ = D.SceneRenderer(res=96).points(b, seed=4242)
+    res = time_to_chamfer(net, b, pts, iters=300)
     for r in res:
         assert np.isfinite(r["plain_final"]) and r["plain_final"] < r["plain_start"]
-    reached = [r for r in res if r["proposal_time"] is not None]
-    assert len(reached) >= 4, res
-    ratio = np.median([r["proposal_time"] / r["plain_time"] for r in reached])
-    assert ratio < 1.0, res
+    s = summarize(res, 300)
+    print({k: v for k, v in s.items() if k != "per_scene"})
+    assert s["reached"] >= 19, s["reached"]
+    assert s["time_ratio_median_all"] is not None and s["time_ratio_median_all"] <= 0.65, s["time_ratio_median_all"]
+    assert s["proposal_start_chamfer"] < s["plain_start_chamfer"]
