@@ -196,7 +196,10 @@ def roofline_report(workload, phases, dom, tr, P, V, H, W, keys, nbins, dev):
         e = {"ms": round(ms, 4)}
         if name in FLOPS_PER_FRAGMENT:
             frags = frag_fwd if name == "blend_fwd" else frag_bwd
-            inst = tj.get(name + "_warp_inst")
+            # warp instructions per launch: ncu's count per fragment on a smaller case of the same scene
+            # distribution (profiles/roofline_traffic.json) times this run's device-counted fragments
+            ipf = tj.get(name + "_warp_inst_per_fragment")
+            inst = ipf * frags if ipf else tj.get(name + "_warp_inst")
             e.update(bound="issue", fragments=int(frags),
                      fp32_effective={"achieved": round(FLOPS_PER_FRAGMENT[name] * frags / t / 1e12, 3),
                                      "peak": round(fp32_peak / 1e12, 2), "unit": "TFLOP/s",

@@ -56,6 +56,17 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint3
          ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
 }
 
+// The same descriptor for the 128-byte swizzled K-major layout: rows of
+// 128 bytes (64 bf16 of K), 8-row groups 1024 bytes apart (SBO), the
+// leading offset unused (1); the 16-byte chunks of row r are XOR-permuted by
+// r % 8, as the TMA unit writes them with CU_TENSOR_MAP_SWIZZLE_128B.  The
+// tile must start on a 1024-byte boundary; a K step of 16 advances the start
+// address by 32 bytes.
+__device__ __forceinline__ uint64_t smem_desc_sw128(uint32_t addr) {
+  return (uint64_t)((addr & 0x3FFFFu) >> 4) | (1ull << 16) | ((uint64_t)(1024u >> 4) << 32) | (1ull << 46) |
+         (2ull << 61);
+}
+
 // Instruction descriptor of kind::f16: fp32 accumulator, bf16 A and B, both
 // K-major, M = 128, N = n.
 __host__ __device__ constexpr uint32_t instr_desc(int n) {
@@ -343,6 +354,12 @@ __global__ void __launch_bounds__(kThreads) k_gemm_tc(const sgr_gemm_args a) {
 // Out-of-range rows and columns are zero-filled by the TMA unit.
 // ---------------------------------------------------------------------------
 constexpr int kStages = 4;
+// SGR_MLP_SW128 1: the persistent GEMM loads each K chunk of 64 as one
+// 128-byte swizzled TMA box per operand (64 columns x rows); 0: as eight
+// no-swizzle boxes of 8 columns (16-byte rows).
+#ifndef SGR_MLP_SW128
+#define SGR_MLP_SW128 1
+#endif
 constexpr int kBiasSmem = 1024;   // output columns whose bias the persistent GEMM keeps in shared memory
 // epilogue warps of an NT-column tile: four (one per 32 rows) per 64 columns
 template <int NT>
@@ -427,7 +444,8 @@ __global__ void __launch_bounds__(persist_threads<NT>(), 1)
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
   const uint32_t tmem = s_tmem;
-  const uint32_t base = (smem_addr(smem) + 127u) & ~127u;   // TMA destinations: 128-byte aligned
+  // TMA destinations: 1024-byte aligned (the swizzle atom; stages are multiples of it)
+  const uint32_t base = (smem_addr(smem) + 1023u) & ~1023u;
 
   int issued = 0;                                    // producer: chunks whose loads were issued
   if (warp == 0) {
@@ -446,10 +464,15 @@ __global__ void __launch_bounds__(persist_threads<NT>(), 1)
           const uint32_t full = smem_addr(&s_full[st]);
           mbar_expect(full, kStage);
           const uint32_t sa = base + st * kStage, sb = sa + kBytesA;
+#if SGR_MLP_SW128
+          tma_load_2d(sa, &map_a, c * kKC, m0, full);
+          tma_load_2d(sb, &map_b, c * kKC, n0, full);
+#else
           for (int kb = 0; kb < kKC / 8; ++kb) {
             tma_load_2d(sa + kb * kTM * 16, &map_a, c * kKC + kb * 8, m0, full);
             tma_load_2d(sb + kb * NT * 16, &map_b, c * kKC + kb * 8, n0, full);
           }
+#endif
           issued = g + 1;
         }
       }
@@ -478,8 +501,13 @@ __global__ void __launch_bounds__(persist_threads<NT>(), 1)
           const uint32_t sa = base + st * kStage, sb = sa + kBytesA;
 #pragma unroll
           for (int s = 0; s < kKC / 16; ++s) {
+#if SGR_MLP_SW128
+            const uint64_t da = smem_desc_sw128(sa + 32u * s);
+            const uint64_t db = smem_desc_sw128(sb + 32u * s);
+#else
             const uint64_t da = smem_desc(sa + 2u * s * kTM * 16, kTM * 16, 128u);
             const uint64_t db = smem_desc(sb + 2u * s * NT * 16, NT * 16, 128u);
+#endif
             const uint32_t acc = (c > 0 || s > 0) ? 1u : 0u;
             asm volatile(
                 "{\n .reg .pred p;\n setp.ne.u32 p, %4, 0;\n"
@@ -598,10 +626,17 @@ bool make_map(CUtensorMap* m, const void* base, long long rows, long long cols, 
   if (!enc) return false;
   const cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
   const cuuint64_t strides[1] = {(cuuint64_t)ld * 2};
+#if SGR_MLP_SW128
+  // boxes of 64 columns (128 bytes, the swizzle span) x box_rows
+  const cuuint32_t box[2] = {(cuuint32_t)kKC, (cuuint32_t)box_rows};
+  const CUtensorMapSwizzle swz = CU_TENSOR_MAP_SWIZZLE_128B;
+#else
   const cuuint32_t box[2] = {8u, (cuuint32_t)box_rows};
+  const CUtensorMapSwizzle swz = CU_TENSOR_MAP_SWIZZLE_NONE;
+#endif
   const cuuint32_t estr[2] = {1u, 1u};
   return enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box, estr,
-             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+             CU_TENSOR_MAP_INTERLEAVE_NONE, swz, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
@@ -610,7 +645,7 @@ int launch_tma(const sgr_gemm_args& a, cudaStream_t st) {
   alignas(64) CUtensorMap ma, mb;
   if (!make_map(&ma, a.A, a.M, a.K, a.lda, kTM) || !make_map(&mb, a.B, a.N, a.K, a.ldb, NT)) return SGR_ERR_CUDA;
   const int ns = kStages;
-  const size_t smem = (size_t)ns * (kTM + NT) * kKC * 2 + 128;
+  const size_t smem = (size_t)ns * (kTM + NT) * kKC * 2 + 1024;
   // per device, once: the shared-memory attribute and the resident CTAs (by
   // registers and shared memory, and by tensor memory: 512 columns per SM,
   // 2 NT per CTA; a CTA beyond that would wait in its allocation until

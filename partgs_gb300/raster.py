@@ -226,7 +226,7 @@ def forward(variant, means3D, opacities, shs, colors_precomp, scales, rotations,
     semantic = None
     if variant == L.SGR_VARIANT_PART:
         semantic = torch.empty((V, b.semantic_channels, H, W), dtype=torch.float32, device=device)
-    radii = torch.zeros(b.num_records, dtype=torch.int32, device=device)
+    radii = torch.empty(b.num_records, dtype=torch.int32, device=device)     # the library writes every record
     out = L.FwdOutputs(color.data_ptr(), others.data_ptr(), _ptr(semantic), radii.data_ptr())
     L.check(lib.sgr_forward_raster(C.byref(b), geom.data_ptr(), bins.data_ptr(), cap, scratch.data_ptr(),
                                    s0.fwd_scratch_bytes, C.byref(out), st), "sgr_forward_raster")
