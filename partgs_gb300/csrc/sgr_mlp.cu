@@ -67,6 +67,13 @@ __device__ __forceinline__ uint64_t smem_desc_sw128(uint32_t addr) {
          (2ull << 61);
 }
 
+// The 32-byte swizzled form, for K chunks of 16: rows of 32 bytes, 8-row
+// groups 256 bytes apart.
+__device__ __forceinline__ uint64_t smem_desc_sw32(uint32_t addr) {
+  return (uint64_t)((addr & 0x3FFFFu) >> 4) | (1ull << 16) | ((uint64_t)(256u >> 4) << 32) | (1ull << 46) |
+         (6ull << 61);
+}
+
 // Instruction descriptor of kind::f16: fp32 accumulator, bf16 A and B, both
 // K-major, M = 128, N = n.
 __host__ __device__ constexpr uint32_t instr_desc(int n) {
@@ -353,7 +360,8 @@ __global__ void __launch_bounds__(kThreads) k_gemm_tc(const sgr_gemm_args a) {
 // commit (all MMAs done), and only then is the tensor memory freed.
 // Out-of-range rows and columns are zero-filled by the TMA unit.
 // ---------------------------------------------------------------------------
-constexpr int kStages = 4;
+constexpr int kStages = 4;          // pipeline stages of K chunks of 64
+constexpr int kStages16 = 8;        // of K chunks of 16 (layers with K <= 16)
 // SGR_MLP_SW128 1: the persistent GEMM loads each K chunk of 64 as one
 // 128-byte swizzled TMA box per operand (64 columns x rows); 0: as eight
 // no-swizzle boxes of 8 columns (16-byte rows).
@@ -395,14 +403,16 @@ __device__ __forceinline__ bool mbar_wait_or_fail(uint32_t bar, uint32_t parity,
   }
 }
 
-template <int NT>
+// KC: K per chunk, 64 (128-byte swizzle) or 16 (32-byte swizzle, for K <= 16).
+template <int NT, int KC>
 __global__ void __launch_bounds__(persist_threads<NT>(), 1)
     k_gemm_persist(const sgr_gemm_args a, const __grid_constant__ CUtensorMap map_a,
                    const __grid_constant__ CUtensorMap map_b, int ns) {
   extern __shared__ __align__(1024) uint8_t smem[];
-  constexpr uint32_t kBytesA = kTM * kKC * 2, kBytesB = NT * kKC * 2, kStage = kBytesA + kBytesB;
+  constexpr uint32_t kBytesA = kTM * KC * 2, kBytesB = NT * KC * 2, kStage = kBytesA + kBytesB;
   constexpr uint32_t kCols = 2 * NT;                 // two accumulators
-  __shared__ __align__(8) uint64_t s_full[kStages], s_empty[kStages], s_tfull[2], s_tempty[2], s_done;
+  constexpr int kMaxStages = KC == 64 ? kStages : kStages16;
+  __shared__ __align__(8) uint64_t s_full[kMaxStages], s_empty[kMaxStages], s_tfull[2], s_tempty[2], s_done;
   __shared__ uint32_t s_tmem;
   __shared__ int s_fail;
   __shared__ float s_bias[kBiasSmem];
@@ -417,7 +427,7 @@ __global__ void __launch_bounds__(persist_threads<NT>(), 1)
   const float* bias = bias_smem ? s_bias : a.bias;
   const int tiles_n = (int)((a.N + NT - 1) / NT);
   const int total = (int)((a.M + kTM - 1) / kTM) * tiles_n;
-  const int chunks = (int)((a.K + kKC - 1) / kKC);
+  const int chunks = (int)((a.K + KC - 1) / KC);
 
   if (warp == 1) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_addr(&s_tmem)),
@@ -465,12 +475,12 @@ __global__ void __launch_bounds__(persist_threads<NT>(), 1)
           mbar_expect(full, kStage);
           const uint32_t sa = base + st * kStage, sb = sa + kBytesA;
 #if SGR_MLP_SW128
-          tma_load_2d(sa, &map_a, c * kKC, m0, full);
-          tma_load_2d(sb, &map_b, c * kKC, n0, full);
+          tma_load_2d(sa, &map_a, c * KC, m0, full);
+          tma_load_2d(sb, &map_b, c * KC, n0, full);
 #else
-          for (int kb = 0; kb < kKC / 8; ++kb) {
-            tma_load_2d(sa + kb * kTM * 16, &map_a, c * kKC + kb * 8, m0, full);
-            tma_load_2d(sb + kb * NT * 16, &map_b, c * kKC + kb * 8, n0, full);
+          for (int kb = 0; kb < KC / 8; ++kb) {
+            tma_load_2d(sa + kb * kTM * 16, &map_a, c * KC + kb * 8, m0, full);
+            tma_load_2d(sb + kb * NT * 16, &map_b, c * KC + kb * 8, n0, full);
           }
 #endif
           issued = g + 1;
@@ -500,10 +510,10 @@ __global__ void __launch_bounds__(persist_threads<NT>(), 1)
           asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
           const uint32_t sa = base + st * kStage, sb = sa + kBytesA;
 #pragma unroll
-          for (int s = 0; s < kKC / 16; ++s) {
+          for (int s = 0; s < KC / 16; ++s) {
 #if SGR_MLP_SW128
-            const uint64_t da = smem_desc_sw128(sa + 32u * s);
-            const uint64_t db = smem_desc_sw128(sb + 32u * s);
+            const uint64_t da = KC == 64 ? smem_desc_sw128(sa + 32u * s) : smem_desc_sw32(sa);
+            const uint64_t db = KC == 64 ? smem_desc_sw128(sb + 32u * s) : smem_desc_sw32(sb);
 #else
             const uint64_t da = smem_desc(sa + 2u * s * kTM * 16, kTM * 16, 128u);
             const uint64_t db = smem_desc(sb + 2u * s * NT * 16, NT * 16, 128u);
@@ -621,15 +631,16 @@ EncodeTiled encode_fn() {
 
 // Tensor map of a row-major bf16 matrix [rows, cols] (ld elements per row)
 // read in boxes of 8 columns x box_rows rows.
-bool make_map(CUtensorMap* m, const void* base, long long rows, long long cols, long long ld, int box_rows) {
+bool make_map(CUtensorMap* m, const void* base, long long rows, long long cols, long long ld, int box_rows,
+              int kc = kKC) {
   EncodeTiled enc = encode_fn();
   if (!enc) return false;
   const cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
   const cuuint64_t strides[1] = {(cuuint64_t)ld * 2};
 #if SGR_MLP_SW128
-  // boxes of 64 columns (128 bytes, the swizzle span) x box_rows
-  const cuuint32_t box[2] = {(cuuint32_t)kKC, (cuuint32_t)box_rows};
-  const CUtensorMapSwizzle swz = CU_TENSOR_MAP_SWIZZLE_128B;
+  // boxes of kc columns (the swizzle span: 128 bytes for 64, 32 for 16) x box_rows
+  const cuuint32_t box[2] = {(cuuint32_t)kc, (cuuint32_t)box_rows};
+  const CUtensorMapSwizzle swz = kc == 64 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_32B;
 #else
   const cuuint32_t box[2] = {8u, (cuuint32_t)box_rows};
   const CUtensorMapSwizzle swz = CU_TENSOR_MAP_SWIZZLE_NONE;
@@ -640,12 +651,13 @@ bool make_map(CUtensorMap* m, const void* base, long long rows, long long cols, 
              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-template <int NT>
-int launch_tma(const sgr_gemm_args& a, cudaStream_t st) {
+template <int NT, int KC>
+int launch_persist(const sgr_gemm_args& a, cudaStream_t st) {
   alignas(64) CUtensorMap ma, mb;
-  if (!make_map(&ma, a.A, a.M, a.K, a.lda, kTM) || !make_map(&mb, a.B, a.N, a.K, a.ldb, NT)) return SGR_ERR_CUDA;
-  const int ns = kStages;
-  const size_t smem = (size_t)ns * (kTM + NT) * kKC * 2 + 1024;
+  if (!make_map(&ma, a.A, a.M, a.K, a.lda, kTM, KC) || !make_map(&mb, a.B, a.N, a.K, a.ldb, NT, KC))
+    return SGR_ERR_CUDA;
+  const int ns = KC == 64 ? kStages : kStages16;
+  const size_t smem = (size_t)ns * (kTM + NT) * KC * 2 + 1024;
   // per device, once: the shared-memory attribute and the resident CTAs (by
   // registers and shared memory, and by tensor memory: 512 columns per SM,
   // 2 NT per CTA; a CTA beyond that would wait in its allocation until
@@ -656,10 +668,10 @@ int launch_tma(const sgr_gemm_args& a, cudaStream_t st) {
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDev) return SGR_ERR_CUDA;
   if (resident[dev] == 0) {
     int sms = 0, per_sm = 0;
-    if (cudaFuncSetAttribute(k_gemm_persist<NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+    if (cudaFuncSetAttribute(k_gemm_persist<NT, KC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
             cudaSuccess ||
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gemm_persist<NT>, persist_threads<NT>(), smem) !=
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gemm_persist<NT, KC>, persist_threads<NT>(), smem) !=
             cudaSuccess)
       return SGR_ERR_CUDA;
     per_sm = per_sm < 512 / (2 * NT) ? per_sm : 512 / (2 * NT);
@@ -668,9 +680,19 @@ int launch_tma(const sgr_gemm_args& a, cudaStream_t st) {
   }
   const long long tiles = ((a.M + kTM - 1) / kTM) * ((a.N + NT - 1) / NT);
   const long long grid = tiles < (long long)resident[dev] ? tiles : (long long)resident[dev];
-  k_gemm_persist<NT><<<(unsigned)grid, persist_threads<NT>(), smem, st>>>(a, ma, mb, ns);
+  k_gemm_persist<NT, KC><<<(unsigned)grid, persist_threads<NT>(), smem, st>>>(a, ma, mb, ns);
   sgr::count_launches(1);
   return cudaGetLastError() == cudaSuccess ? SGR_OK : SGR_ERR_CUDA;
+}
+
+// K <= 16 (the first layer: 3 coordinates padded to 16) in chunks of 16,
+// everything else in chunks of 64.
+template <int NT>
+int launch_tma(const sgr_gemm_args& a, cudaStream_t st) {
+#if SGR_MLP_SW128
+  if (a.K <= 16) return launch_persist<NT, 16>(a, st);
+#endif
+  return launch_persist<NT, 64>(a, st);
 }
 
 template <int NT, bool A_T, bool B_T>
