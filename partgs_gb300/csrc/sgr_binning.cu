@@ -365,9 +365,12 @@ constexpr size_t kMaxDynSmem = 220 * 1024;
 constexpr size_t kAlignB = 256;
 size_t al(size_t x) { return (x + kAlignB - 1) & ~(kAlignB - 1); }
 
-// Staging area of the list writer, in entries: 6,144 (24 KB), less where
+// Staging area of the list writer, in entries (6,144: 24 KB), less where
 // the per-warp counts leave less room.
-constexpr long long kStageEntries = 6144;
+#ifndef SGR_CELL_STAGE
+#define SGR_CELL_STAGE 6144
+#endif
+constexpr long long kStageEntries = SGR_CELL_STAGE;
 
 size_t writer_smem(int warps, int ncell, int stage) {
   return ((size_t)warps * ncell + 2 * (size_t)ncell + 1 + (size_t)stage) * 4;

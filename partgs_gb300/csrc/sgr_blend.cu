@@ -191,6 +191,13 @@ template <class T> __device__ __forceinline__ T bc(float s);
 template <> __device__ __forceinline__ float bc<float>(float s) { return s; }
 template <> __device__ __forceinline__ float2 bc<float2>(float s) { return make_float2(s, s); }
 
+// -k for k = fma(px, w, -u): -k itself for one pixel, fma(px, -w, u) for a
+// pair (a packed negation would cost an instruction).
+__device__ __forceinline__ float negk(float, float, float, float k) { return -k; }
+__device__ __forceinline__ float2 negk(float2 px, float w, float u, float2) {
+  return lfma(px, bc<float2>(-w), bc<float2>(u));
+}
+
 template <class T>
 struct FragGeom {
   T kx, ky, kz, lx, ly, lz, px, py, pz, dx, dy, rho2d;
@@ -207,11 +214,12 @@ __device__ __forceinline__ void frag_intersect(T pxf, T pyf, T npx, T npy, const
   f.lx = lfma(pyf, bc<T>(r1.z), bc<T>(-r0.w));
   f.ly = lfma(pyf, bc<T>(r1.w), bc<T>(-r1.x));
   f.lz = lfma(pyf, bc<T>(r2.x), bc<T>(-r1.y));
-  // -(c d) as (-c) d: -k by the same fma with negated operands (rounding is
-  // symmetric), so no product is negated
-  const T nkx = lfma(pxf, bc<T>(-r1.z), bc<T>(r0.x));
-  const T nky = lfma(pxf, bc<T>(-r1.w), bc<T>(r0.y));
-  const T nkz = lfma(pxf, bc<T>(-r2.x), bc<T>(r0.z));
+  // -(c d) as (-c) d with -k: a negation for one pixel (free as an operand
+  // modifier), the same fma with negated operands for two (rounding is
+  // symmetric, so both give exactly -k)
+  const T nkx = negk(pxf, r1.z, r0.x, f.kx);
+  const T nky = negk(pxf, r1.w, r0.y, f.ky);
+  const T nkz = negk(pxf, r2.x, r0.z, f.kz);
   f.px = lfma(f.ky, f.lz, lmul(nkz, f.ly));
   f.py = lfma(f.kz, f.lx, lmul(nkx, f.lz));
   f.pz = lfma(f.kx, f.ly, lmul(nky, f.lx));
