@@ -50,6 +50,28 @@ __device__ __forceinline__ uint32_t digit_of(K key, int shift, uint32_t dmask) {
   return (uint32_t)(key >> shift) & dmask;
 }
 
+// The lanes of the warp holding the same digit d (d <= kBins, kBins marking
+// an empty slot).  SGR_SORT_BALLOT 1: one ballot per digit bit (ten of
+// them), each lane keeping the lanes that agree with it on every bit;
+// 0: __match_any_sync.
+#ifndef SGR_SORT_BALLOT
+#define SGR_SORT_BALLOT 1
+#endif
+__device__ __forceinline__ unsigned digit_peers(uint32_t d) {
+#if SGR_SORT_BALLOT
+  unsigned m = 0xffffffffu;
+#pragma unroll
+  for (int b = 0; b <= kMaxDigitBits; ++b) {
+    const bool bit = (d >> b) & 1u;
+    const unsigned v = __ballot_sync(0xffffffffu, bit);
+    m &= bit ? v : ~v;
+  }
+  return m;
+#else
+  return __match_any_sync(0xffffffffu, d);
+#endif
+}
+
 // Exclusive scan of one value per thread over a 256-thread CTA; returns the
 // CTA total in `total`.  Uses s_warp[kSortWarps].
 template <class T>
@@ -110,7 +132,7 @@ __global__ void __launch_bounds__(kSortThreads) k_radix_hist(const K* __restrict
   }
 #pragma unroll
   for (int k = 0; k < kRadixItems; ++k) {
-    const unsigned peers = __match_any_sync(0xffffffffu, d[k]);
+    const unsigned peers = digit_peers(d[k]);
     if (d[k] < kBins && lane == __ffs(peers) - 1) atomicAdd(&s_cnt[d[k]], (uint32_t)__popc(peers));
   }
   __syncthreads();
@@ -190,7 +212,7 @@ __global__ void __launch_bounds__(kSortThreads) k_radix_scatter(const K* __restr
   for (int k = 0; k < kRadixItems; ++k) {
     const long long i = wbase + k * 32 + lane;
     const uint32_t d = i < n ? digit_of(key[k], shift, dmask) : (uint32_t)kBins;
-    const unsigned peers = __match_any_sync(0xffffffffu, d);
+    const unsigned peers = digit_peers(d);
     const int leader = __ffs(peers) - 1;
     uint32_t before = 0;
     if (lane == leader && d < kBins) {
