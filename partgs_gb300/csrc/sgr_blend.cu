@@ -1040,10 +1040,21 @@ __device__ __forceinline__ void bwd_alpha2(const float4& r1, const float4& r2, B
   f.alpha = make_float2(fminf(0.99f, oa.x), fminf(0.99f, oa.y));
   f.live[0] = f.live[0] && !(f.c_d.x < kNearP0) && !(power.x > 0.0f) && !(f.alpha.x < 1.0f / 255.0f);
   f.live[1] = f.live[1] && !(f.c_d.y < kNearP0) && !(power.y > 0.0f) && !(f.alpha.y < 1.0f / 255.0f);
+  // the splat-plane terms feed only the 3D branch's gradients: zero them on
+  // lanes that do not take it, where they may be infinite (a p.z too small
+  // for its reciprocal) and would turn the branch's zero weights into NaN
+  const bool k0 = f.live[0] && f.use3d[0], k1 = f.live[1] && f.use3d[1];
+  const float2 z2 = make_float2(0.0f, 0.0f);
+  f.sx = sel2(k0, k1, f.sx, z2);
+  f.sy = sel2(k0, k1, f.sy, z2);
+  f.iz = sel2(k0, k1, f.iz, z2);
 }
 
 // Stage 3: both pixels' recurrences and their summed share of the entry's
-// 18 gradient values (gv), P0/cr/backward.cu:337-440.
+// 18 gradient values, written to gv[0..17] (P0/cr/backward.cu:337-440).  A
+// lane whose fragments are not live keeps its state and writes zeros, so the
+// call needs no branch around it (the geometry of a non-live fragment is
+// finite: p.z is replaced by 1 in bwd_alpha2).
 __device__ __forceinline__ void bwd_update2(BwdPair& q, const BwdGeom2& f, const float4& r1, const float4& r2,
                                             const float4& r3, const float4& r4, int pos, float (&gv)[32]) {
   const bool l0 = f.live[0], l1 = f.live[1];
@@ -1103,12 +1114,12 @@ __device__ __forceinline__ void bwd_update2(BwdPair& q, const BwdGeom2& f, const
 #pragma unroll
   for (int ch = 0; ch < 3; ++ch) {
     const float2 c = lmul(wgt, q.dL_dpixel[ch]);
-    gv[14 + ch] += c.x + c.y;
+    gv[14 + ch] = c.x + c.y;
     const float2 n = lmul(wgt, q.dL_dnormal2D[ch]);
-    gv[11 + ch] += n.x + n.y;
+    gv[11 + ch] = n.x + n.y;
   }
   const float2 gG = lmul(G, dL_dalpha);
-  gv[17] += gG.x + gG.y;
+  gv[17] = gG.x + gG.y;
   // 3D branch (ray-splat intersection) where use3d, 2D (filter) branch elsewhere
   const bool u0 = f.use3d[0], u1 = f.use3d[1];
   const float2 dG3 = sel2(u0, u1, dL_dG, zero), dz3 = sel2(u0, u1, dL_dz, zero);
@@ -1124,25 +1135,25 @@ __device__ __forceinline__ void bwd_update2(BwdPair& q, const BwdGeom2& f, const
   const float2 dlx = lfma(dsy, g.kz, lmul(make_float2(-dpz.x, -dpz.y), g.ky));
   const float2 dly = lfma(dpz, g.kx, lmul(make_float2(-dsx.x, -dsx.y), g.kz));
   const float2 dlz = lfma(dsx, g.ky, lmul(make_float2(-dsy.x, -dsy.y), g.kx));
-  gv[0] -= dkx.x + dkx.y;
-  gv[1] -= dky.x + dky.y;
-  gv[2] -= dkz.x + dkz.y;
-  gv[3] -= dlx.x + dlx.y;
-  gv[4] -= dly.x + dly.y;
-  gv[5] -= dlz.x + dlz.y;
+  gv[0] = -(dkx.x + dkx.y);
+  gv[1] = -(dky.x + dky.y);
+  gv[2] = -(dkz.x + dkz.y);
+  gv[3] = -(dlx.x + dlx.y);
+  gv[4] = -(dly.x + dly.y);
+  gv[5] = -(dlz.x + dlz.y);
   const float2 px2 = bc<float2>(q.pxf);
   const float2 u6 = lfma(px2, dkx, lfma(q.pyf, dlx, lmul(dz3, f.sx)));
   const float2 u7 = lfma(px2, dky, lfma(q.pyf, dly, lmul(dz3, f.sy)));
   const float2 dz2 = sel2(u0, u1, zero, dL_dz);
   const float2 u8 = lfma(px2, dkz, lfma(q.pyf, dlz, ladd(dz3, dz2)));
-  gv[6] += u6.x + u6.y;
-  gv[7] += u7.x + u7.y;
-  gv[8] += u8.x + u8.y;
+  gv[6] = u6.x + u6.y;
+  gv[7] = u7.x + u7.y;
+  gv[8] = u8.x + u8.y;
   const float2 dG2 = sel2(u0, u1, zero, dL_dG);
   const float2 kG = lmul(dG2, lmul(nG, bc<float2>(kFilterInvSquareP0)));
   const float2 u9 = lmul(kG, g.dx), u10 = lmul(kG, g.dy);
-  gv[9] += u9.x + u9.y;
-  gv[10] += u10.x + u10.y;
+  gv[9] = u9.x + u9.y;
+  gv[10] = u10.x + u10.y;
 }
 
 // Resident CTAs per SM the plain backward is compiled for (registers per
@@ -1296,23 +1307,22 @@ __device__ __forceinline__ void render_bwd_tile(const sgr_batch& b, const GeomVi
       const uint32_t rows_live = (s_mask[j] >> (warp * SPLIT)) & ((1u << SPLIT) - 1u);   // which pixels may reach
       if (pos >= warp_max) continue;        // uniform: past every lane's last contributor
       float gv[32];
-#pragma unroll
-      for (int u = 0; u < 32; ++u) gv[u] = 0.f;
       const float4 r0 = s_rec[0][j], r1 = s_rec[1][j], r2 = s_rec[2][j];
       const float reach = s_rec[3][j].w;
       if constexpr (PACKED) {
         BwdGeom2 f2;
         if (!__any_sync(0xffffffffu, bwd_reach2(qp, r0, r1, r2, reach, pos, f2))) continue;   // uniform
         bwd_alpha2(r1, r2, f2);
-        const bool ok2 = f2.live[0] || f2.live[1];
-        if (!__any_sync(0xffffffffu, ok2)) continue;
+        if (!__any_sync(0xffffffffu, f2.live[0] || f2.live[1])) continue;
         const float4 r3 = s_rec[3][j], r4 = s_rec[4][j];
-        if (ok2) bwd_update2(qp, f2, r1, r2, r3, r4, pos, gv);
+        bwd_update2(qp, f2, r1, r2, r3, r4, pos, gv);   // every lane: non-live lanes write zeros
         int which;
         const float total = warp_sum18(gv, lane, which);
         if (which >= 0 && total != 0.f) atomicAdd(grads + (size_t)s_id[j] * kGradF + which, total);
         continue;
       }
+#pragma unroll
+      for (int u = 0; u < 32; ++u) gv[u] = 0.f;
       BwdGeom f[PX];
       bool may = false;
 #pragma unroll
