@@ -187,6 +187,10 @@ __device__ __forceinline__ float lfma(float a, float b, float c) { return __fmaf
 __device__ __forceinline__ float2 lfma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
 __device__ __forceinline__ float ladd(float a, float b) { return __fadd_rn(a, b); }
 __device__ __forceinline__ float2 ladd(float2 a, float2 b) { return __fadd2_rn(a, b); }
+// Per-lane select of a pair.
+__device__ __forceinline__ float2 sel2(bool a, bool b, float2 x, float2 y) {
+  return make_float2(a ? x.x : y.x, b ? x.y : y.y);
+}
 template <class T> __device__ __forceinline__ T bc(float s);
 template <> __device__ __forceinline__ float bc<float>(float s) { return s; }
 template <> __device__ __forceinline__ float2 bc<float2>(float s) { return make_float2(s, s); }
@@ -383,8 +387,14 @@ struct BlendShape {
 #ifndef SGR_PART_BWD_PX
 #define SGR_PART_BWD_PX 1
 #endif
+// SGR_FWD_PACKED 1: the plain forward gives each thread two pixels of one
+// column (a warp covers 16x4), their fragment geometry and accumulation as
+// the two lanes of packed FP32 operations (fwd_fragment2).
+#ifndef SGR_FWD_PACKED
+#define SGR_FWD_PACKED 1
+#endif
 template <int VARIANT, int WX = kTile>
-using FwdShapeT = BlendShape<1, WX>;
+using FwdShapeT = BlendShape<(SGR_FWD_PACKED && VARIANT == SGR_VARIANT_PLAIN) ? 2 : 1, WX>;
 template <int VARIANT, int WX = kTile>
 using BwdShapeT = BlendShape<(VARIANT == SGR_VARIANT_PLAIN) ? 2 : SGR_PART_BWD_PX, WX>;
 using FwdShape = BlendShape<1>;
@@ -536,11 +546,107 @@ __device__ __forceinline__ void fwd_fragment(FwdPixel<VARIANT>& q, const float4 
   q.last_contributor = contributor;
 }
 
-// Resident CTAs per SM the forward is compiled for: 4 for the plain variant
-// (64 registers), 3 for the part variant (80 registers; its semantic sums
-// and gradients live in shared memory).
+// Per-pixel state of the plain forward for a thread's two pixels, lane i =
+// pixel i (both in one column).
+struct FwdPair {
+  float pxf;
+  float2 pyf, npx, npy;
+  bool done[2];
+  float2 T;
+  uint32_t last_contributor[2];
+  float2 C[3], N[3];
+  float2 D, M1, M2, dist, med_depth;
+  int med_contrib[2];
+  uint32_t stop[2];
+};
+
+// One entry of the list for both pixels of a thread (fwd_fragment's
+// recurrences, P0/cr/forward.cu:349-430): the geometry in the explicit
+// sequence of frag_intersect, so every test decides as fwd_fragment and the
+// backward do; the accumulation as packed operations, zero-weighted on a lane
+// whose fragment does not count.
+__device__ __forceinline__ void fwd_fragment2(FwdPair& q, const float4 (*s_rec)[kBlock], int j,
+                                              uint32_t contributor) {
+  if (q.done[0] && q.done[1]) return;
+  const float4 r0 = s_rec[0][j], r1 = s_rec[1][j], r2 = s_rec[2][j];
+  const float reach = s_rec[3][j].w;
+  FragGeom<float2> f;
+  frag_intersect<float2>(make_float2(q.pxf, q.pxf), q.pyf, q.npx, q.npy, r0, r1, r2, f);
+  float2 pxy2, rpz2;
+  frag_reach_terms(f, reach, pxy2, rpz2);
+  bool a0 = !q.done[0] && f.pz.x != 0.0f && !(f.rho2d.x > reach && pxy2.x > rpz2.x);
+  bool a1 = !q.done[1] && f.pz.y != 0.0f && !(f.rho2d.y > reach && pxy2.y > rpz2.y);
+  if (!a0 && !a1) return;
+  const float Twx = r1.z, Twy = r1.w, Twz = r2.x;
+  const float2 iz = make_float2(splat_rcp(a0 ? f.pz.x : 1.0f), splat_rcp(a1 ? f.pz.y : 1.0f));
+  const float2 sx = lmul(f.px, iz), sy = lmul(f.py, iz);
+  const float2 rho3d = lfma(sx, sx, lmul(sy, sy));
+  const float2 d3 = ladd(lfma(sx, bc<float2>(Twx), lmul(sy, bc<float2>(Twy))), bc<float2>(Twz));
+  const float2 depth = make_float2(rho3d.x <= f.rho2d.x ? d3.x : Twz, rho3d.y <= f.rho2d.y ? d3.y : Twz);
+  a0 = a0 && !(depth.x < kNearP0);
+  a1 = a1 && !(depth.y < kNearP0);
+  const float2 power =
+      lmul(bc<float2>(-0.5f), make_float2(fminf(rho3d.x, f.rho2d.x), fminf(rho3d.y, f.rho2d.y)));
+  a0 = a0 && !(power.x > 0.0f);
+  a1 = a1 && !(power.y > 0.0f);
+  const float2 oa = lmul(bc<float2>(r2.w), make_float2(splat_exp(power.x), splat_exp(power.y)));
+  const float2 alpha = make_float2(fminf(0.99f, oa.x), fminf(0.99f, oa.y));
+  a0 = a0 && !(alpha.x < 1.0f / 255.0f);
+  a1 = a1 && !(alpha.y < 1.0f / 255.0f);
+  if (!a0 && !a1) return;
+  const float2 one = bc<float2>(1.0f), zero = bc<float2>(0.0f);
+  const float2 test_T = lmul(q.T, lfma(alpha, bc<float2>(-1.0f), one));     // T (1 - alpha)
+  if (a0 && test_T.x < 0.0001f) {
+    q.done[0] = true;
+    q.stop[0] = contributor;
+    a0 = false;
+  }
+  if (a1 && test_T.y < 0.0001f) {
+    q.done[1] = true;
+    q.stop[1] = contributor;
+    a1 = false;
+  }
+  if (!a0 && !a1) return;
+  const float4 r3 = s_rec[3][j], r4 = s_rec[4][j];
+  const float2 w = sel2(a0, a1, lmul(alpha, q.T), zero);
+  // a lane that does not accumulate gets a finite depth (its weight is zero)
+  const float2 dep = sel2(a0, a1, depth, one);
+  const float2 A = lfma(q.T, bc<float2>(-1.0f), one);                        // 1 - T
+  const float2 inv_d = make_float2(blend_rcp(dep.x), blend_rcp(dep.y));
+  const float2 m = lmul(bc<float2>(kFarP0 / (kFarP0 - kNearP0)), lfma(bc<float2>(-kNearP0), inv_d, one));
+  const float2 mm = lmul(m, m);
+  // m^2 A + M2 - 2 m M1
+  const float2 e = lfma(lmul(bc<float2>(-2.0f), m), q.M1, lfma(mm, A, q.M2));
+  q.dist = lfma(e, w, q.dist);
+  q.D = lfma(dep, w, q.D);
+  q.M1 = lfma(m, w, q.M1);
+  q.M2 = lfma(mm, w, q.M2);
+  if (a0 && q.T.x > 0.5f) {
+    q.med_depth.x = depth.x;
+    q.med_contrib[0] = (int)contributor;
+  }
+  if (a1 && q.T.y > 0.5f) {
+    q.med_depth.y = depth.y;
+    q.med_contrib[1] = (int)contributor;
+  }
+  q.N[0] = lfma(bc<float2>(r3.x), w, q.N[0]);
+  q.N[1] = lfma(bc<float2>(r3.y), w, q.N[1]);
+  q.N[2] = lfma(bc<float2>(r3.z), w, q.N[2]);
+  q.C[0] = lfma(bc<float2>(r4.x), w, q.C[0]);
+  q.C[1] = lfma(bc<float2>(r4.y), w, q.C[1]);
+  q.C[2] = lfma(bc<float2>(r4.z), w, q.C[2]);
+  q.T = sel2(a0, a1, test_T, q.T);
+  if (a0) q.last_contributor[0] = contributor;
+  if (a1) q.last_contributor[1] = contributor;
+}
+
+// Resident CTAs per SM the forward is compiled for.  Plain: 5 CTAs of 128
+// threads with two pixels each (96 registers, no spill; measured against 6,
+// the same time with a small spill, and 8, 43% slower with 128 bytes of
+// spill), or 4 of 256 threads with one pixel each (64 registers).  Part: 3
+// (80 registers; its semantic sums and gradients live in shared memory).
 #ifndef SGR_FWD_MIN_CTAS
-#define SGR_FWD_MIN_CTAS 4
+#define SGR_FWD_MIN_CTAS (SGR_FWD_PACKED ? 5 : 4)
 #endif
 #ifndef SGR_PART_FWD_MIN_CTAS
 #define SGR_PART_FWD_MIN_CTAS 3
@@ -602,6 +708,27 @@ __device__ __forceinline__ void render_fwd_tile(const sgr_batch& b, const GeomVi
     done = done && Q.done;
   }
 
+  // the two pixels of a plain thread as packed lanes
+  constexpr bool PACKED = VARIANT == SGR_VARIANT_PLAIN && PX == 2;
+  FwdPair qp;
+  if constexpr (PACKED) {
+    qp.pxf = q[0].pxf;
+    qp.pyf = make_float2(q[0].pyf, q[1].pyf);
+    qp.npx = make_float2(-q[0].pxf, -q[1].pxf);
+    qp.npy = make_float2(-q[0].pyf, -q[1].pyf);
+    qp.T = make_float2(1.0f, 1.0f);
+    const float2 z = make_float2(0.0f, 0.0f);
+    qp.C[0] = qp.C[1] = qp.C[2] = qp.N[0] = qp.N[1] = qp.N[2] = z;
+    qp.D = qp.M1 = qp.M2 = qp.dist = qp.med_depth = z;
+#pragma unroll
+    for (int i = 0; i < 2; ++i) {
+      qp.done[i] = q[i].done;
+      qp.last_contributor[i] = 0;
+      qp.med_contrib[i] = -1;
+      qp.stop[i] = 0;
+    }
+  }
+
   for (;; base += kBlock, head += kBlock) {
     if (__syncthreads_count(done) == NT) break;
     while (tail - head < kBlock && scanned < len) {   // refill the ring (CTA-uniform)
@@ -635,12 +762,39 @@ __device__ __forceinline__ void render_fwd_tile(const sgr_batch& b, const GeomVi
     for (int si = 0; !done && si < cnt; ++si) {
       const int j = s_list[warp][si];
       const uint32_t contributor = (uint32_t)(base + j + 1);
-      done = true;
+      if constexpr (PACKED) {
+        fwd_fragment2(qp, s_rec, j, contributor);
+        done = qp.done[0] && qp.done[1];
+      } else {
+        done = true;
 #pragma unroll
-      for (int i = 0; i < PX; ++i) {
-        fwd_fragment<VARIANT>(q[i], s_rec, s_sem4, j, contributor, S, sem_acc4);
-        done = done && q[i].done;
+        for (int i = 0; i < PX; ++i) {
+          fwd_fragment<VARIANT>(q[i], s_rec, s_sem4, j, contributor, S, sem_acc4);
+          done = done && q[i].done;
+        }
       }
+    }
+  }
+  if constexpr (PACKED) {   // back to the per-pixel state the outputs are written from
+#pragma unroll
+    for (int i = 0; i < 2; ++i) {
+      FwdPixel<VARIANT>& Q = q[i];
+      auto lane_of = [i](float2 x) { return i == 0 ? x.x : x.y; };
+      Q.done = qp.done[i];
+      Q.T = lane_of(qp.T);
+      Q.last_contributor = qp.last_contributor[i];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        Q.C[c] = lane_of(qp.C[c]);
+        Q.N[c] = lane_of(qp.N[c]);
+      }
+      Q.D = lane_of(qp.D);
+      Q.M1 = lane_of(qp.M1);
+      Q.M2 = lane_of(qp.M2);
+      Q.dist = lane_of(qp.dist);
+      Q.med_depth = lane_of(qp.med_depth);
+      Q.med_contrib = qp.med_contrib[i];
+      Q.stop = qp.stop[i];
     }
   }
 
@@ -699,7 +853,8 @@ __device__ __forceinline__ void render_fwd_tile(const sgr_batch& b, const GeomVi
 
 // One CTA per tile, or persistent CTAs taking tiles from a queue.
 template <int VARIANT, int WX>
-__global__ void __launch_bounds__(FwdShape::NT, (VARIANT == SGR_VARIANT_PLAIN) ? SGR_FWD_MIN_CTAS : SGR_PART_FWD_MIN_CTAS)
+__global__ void __launch_bounds__(FwdShapeT<VARIANT, WX>::NT,
+                                  (VARIANT == SGR_VARIANT_PLAIN) ? SGR_FWD_MIN_CTAS : SGR_PART_FWD_MIN_CTAS)
     k_render_fwd(const sgr_batch b, GeomView g, sgr_fwd_outputs out, TileQueue q) {
   __shared__ int s_item;
   for (int it = 0;; ++it) {
@@ -956,9 +1111,6 @@ __device__ __forceinline__ void bwd_update(BwdPixel<VARIANT>& q, const BwdGeom& 
 #define SGR_BWD_PACKED 1
 #endif
 
-__device__ __forceinline__ float2 sel2(bool a, bool b, float2 x, float2 y) {
-  return make_float2(a ? x.x : y.x, b ? x.y : y.y);
-}
 
 // Per-pixel state of the backward recurrences, lane i = pixel i.
 struct BwdPair {
@@ -1461,10 +1613,10 @@ void launch_fwd(const sgr_batch& b, const GeomView& g, const sgr_fwd_outputs& ou
   if (q.order) {
     k_tile_order<<<1, 1024, 0, st>>>(g, (int)tiles, 0, const_cast<uint32_t*>(q.order), q.next);
     count_launches();
-    const int r = resident_ctas(k, FwdShape::NT);
+    const int r = resident_ctas(k, FwdShapeT<VARIANT, WX>::NT);
     grid = r > 0 ? std::min<unsigned>(tiles, (unsigned)r) : tiles;
   }
-  k<<<grid, FwdShape::NT, 0, st>>>(b, g, out, q);
+  k<<<grid, FwdShapeT<VARIANT, WX>::NT, 0, st>>>(b, g, out, q);
 }
 
 template <int VARIANT, int WX>
