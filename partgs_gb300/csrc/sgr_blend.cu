@@ -1211,8 +1211,12 @@ __device__ __forceinline__ void bwd_update2(BwdPair& q, const BwdGeom2& f, const
                                             const float4& r3, const float4& r4, int pos, float (&gv)[32]) {
   const bool l0 = f.live[0], l1 = f.live[1];
   const float2 one = bc<float2>(1.0f), zero = bc<float2>(0.0f);
+  // A lane whose fragment does not count runs the update with alpha = 0 and a
+  // finite depth: every recurrence below is then exactly the identity in
+  // effect (its "last" terms enter the next update with weight 1 - 0), so only
+  // T and the gradients need masking.
   const float2 alpha = sel2(l0, l1, f.alpha, zero);
-  const float2 G = f.G, c_d = f.c_d;
+  const float2 G = f.G, c_d = sel2(l0, l1, f.c_d, one);
   const float2 oma = lfma(alpha, bc<float2>(-1.0f), one);                       // 1 - alpha
   const float2 inv_1ma = make_float2(blend_rcp(oma.x), blend_rcp(oma.y));
   const float2 T = sel2(l0, l1, lmul(q.T, inv_1ma), q.T);
@@ -1223,8 +1227,8 @@ __device__ __forceinline__ void bwd_update2(BwdPair& q, const BwdGeom2& f, const
   const float2 cd = lfma(bc<float2>(r4.z), q.dL_dpixel[2],
                          lfma(bc<float2>(r4.y), q.dL_dpixel[1], lmul(bc<float2>(r4.x), q.dL_dpixel[0])));
   const float2 rec = lfma(q.last_alpha, q.last_col_dot, lmul(oml, q.rec_dot));
-  q.rec_dot = sel2(l0, l1, rec, q.rec_dot);
-  q.last_col_dot = sel2(l0, l1, cd, q.last_col_dot);
+  q.rec_dot = rec;
+  q.last_col_dot = cd;
   float2 dL_dalpha = ladd(cd, make_float2(-rec.x, -rec.y));
   // depth distortion (mapped depth and its derivative)
   const float2 inv_d = make_float2(blend_rcp(c_d.x), blend_rcp(c_d.y));
@@ -1237,27 +1241,27 @@ __device__ __forceinline__ void bwd_update2(BwdPair& q, const BwdGeom2& f, const
   const float2 dL_dweight = lmul(reg, q.dL_dreg);
   dL_dalpha = ladd(dL_dalpha, ladd(dL_dweight, make_float2(-q.last_dL_dT.x, -q.last_dL_dT.y)));
   const float2 ldt = lfma(dL_dweight, alpha, lmul(lfma(alpha, bc<float2>(-1.0f), one), q.last_dL_dT));
-  q.last_dL_dT = sel2(l0, l1, ldt, q.last_dL_dT);
+  q.last_dL_dT = ldt;
   const float2 dL_dmd = lmul(lmul(bc<float2>(2.0f), wgt),
                              lmul(lfma(m_d, q.final_A, make_float2(-q.final_D.x, -q.final_D.y)), q.dL_dreg));
   dL_dz = lfma(dL_dmd, dmd_dd, dL_dz);
   const float2 acd = lfma(q.last_alpha, q.last_depth, lmul(oml, q.accum_depth));
-  q.accum_depth = sel2(l0, l1, acd, q.accum_depth);
-  q.last_depth = sel2(l0, l1, c_d, q.last_depth);
+  q.accum_depth = acd;
+  q.last_depth = c_d;
   dL_dalpha = lfma(ladd(c_d, make_float2(-acd.x, -acd.y)), q.dL_ddepth, dL_dalpha);
   // accum_alpha = last_alpha + (1 - last_alpha) accum_alpha, one rounding each
   const float2 aca = ladd(q.last_alpha, lmul(oml, q.accum_alpha));
-  q.accum_alpha = sel2(l0, l1, aca, q.accum_alpha);
+  q.accum_alpha = aca;
   dL_dalpha = lfma(lfma(aca, bc<float2>(-1.0f), one), q.dL_daccum, dL_dalpha);
   // normal recurrence on its dot product with dL/dnormal
   const float2 nd = lfma(bc<float2>(r3.z), q.dL_dnormal2D[2],
                          lfma(bc<float2>(r3.y), q.dL_dnormal2D[1], lmul(bc<float2>(r3.x), q.dL_dnormal2D[0])));
   const float2 nrec = lfma(q.last_alpha, q.last_nrm_dot, lmul(oml, q.nrm_dot));
-  q.nrm_dot = sel2(l0, l1, nrec, q.nrm_dot);
-  q.last_nrm_dot = sel2(l0, l1, nd, q.last_nrm_dot);
+  q.nrm_dot = nrec;
+  q.last_nrm_dot = nd;
   dL_dalpha = ladd(dL_dalpha, ladd(nd, make_float2(-nrec.x, -nrec.y)));
   dL_dalpha = lmul(dL_dalpha, T);
-  q.last_alpha = sel2(l0, l1, alpha, q.last_alpha);
+  q.last_alpha = alpha;
   dL_dalpha = lfma(lmul(make_float2(-q.T_final.x, -q.T_final.y), inv_1ma), q.bg_dot, dL_dalpha);
   dL_dalpha = sel2(l0, l1, dL_dalpha, zero);
   dL_dz = sel2(l0, l1, lfma(wgt, q.dL_ddepth, dL_dz), zero);
