@@ -387,17 +387,29 @@ struct BlendShape {
 #ifndef SGR_PART_BWD_PX
 #define SGR_PART_BWD_PX 1
 #endif
-// SGR_FWD_PACKED 1: the plain forward gives each thread two pixels of one
-// column (a warp covers 16x4), their fragment geometry and accumulation as
-// the two lanes of packed FP32 operations (fwd_fragment2).
+// SGR_FWD_PACKED 1: the forward gives each thread two pixels of one column
+// (a warp covers 16x4), their fragment geometry and accumulation as the two
+// lanes of packed FP32 operations (fwd_fragment2); SGR_BWD_PACKED 1 does the
+// same for the backward (bwd_update2).
 #ifndef SGR_FWD_PACKED
 #define SGR_FWD_PACKED 1
 #endif
+#ifndef SGR_BWD_PACKED
+#define SGR_BWD_PACKED 1
+#endif
+// SGR_PART_PACKED 1: the part variant's blends take the packed form too, its
+// semantic sums and gradients per pixel in shared memory; 0 keeps it at one
+// pixel per thread.
+#ifndef SGR_PART_PACKED
+#define SGR_PART_PACKED 1
+#endif
+template <int VARIANT>
+constexpr bool kPackedBlend = VARIANT == SGR_VARIANT_PLAIN || SGR_PART_PACKED;
 template <int VARIANT, int WX = kTile>
-using FwdShapeT = BlendShape<(SGR_FWD_PACKED && VARIANT == SGR_VARIANT_PLAIN) ? 2 : 1, WX>;
+using FwdShapeT = BlendShape<(SGR_FWD_PACKED && kPackedBlend<VARIANT>) ? 2 : 1, WX>;
 template <int VARIANT, int WX = kTile>
-using BwdShapeT = BlendShape<(VARIANT == SGR_VARIANT_PLAIN) ? 2 : SGR_PART_BWD_PX, WX>;
-using FwdShape = BlendShape<1>;
+using BwdShapeT = BlendShape<(SGR_BWD_PACKED && kPackedBlend<VARIANT>) ? 2 : (VARIANT == SGR_VARIANT_PLAIN) ? 2
+                                                                                      : SGR_PART_BWD_PX, WX>;
 template <int VARIANT>
 constexpr int kSemSlots = (VARIANT == SGR_VARIANT_PART) ? SGR_MAX_SEMANTICS : 1;
 
@@ -534,20 +546,20 @@ __device__ __forceinline__ void fwd_fragment(FwdPixel<VARIANT>& q, const float4 
     // four channels at a time; channels past S are zero in the staged values
     for (int g4 = 0; g4 < (S + 3) / 4; ++g4) {
       const float4 x = s_sem4[g4 * kBlock + j];
-      float4 a = sem_acc4[g4 * FwdShape::NT];
+      float4 a = sem_acc4[g4 * kBlock];
       a.x += x.x * alpha * q.T;
       a.y += x.y * alpha * q.T;
       a.z += x.z * alpha * q.T;
       a.w += x.w * alpha * q.T;
-      sem_acc4[g4 * FwdShape::NT] = a;
+      sem_acc4[g4 * kBlock] = a;
     }
   }
   q.T = test_T;
   q.last_contributor = contributor;
 }
 
-// Per-pixel state of the plain forward for a thread's two pixels, lane i =
-// pixel i (both in one column).
+// Per-pixel state of the forward for a thread's two pixels, lane i = pixel i
+// (both in one column).
 struct FwdPair {
   float pxf;
   float2 pyf, npx, npy;
@@ -555,18 +567,22 @@ struct FwdPair {
   float2 T;
   uint32_t last_contributor[2];
   float2 C[3], N[3];
-  float2 D, M1, M2, dist, med_depth;
+  float2 D, M1, M2, dist, med_depth, med_weight;
   int med_contrib[2];
   uint32_t stop[2];
 };
 
 // One entry of the list for both pixels of a thread (fwd_fragment's
-// recurrences, P0/cr/forward.cu:349-430): the geometry in the explicit
-// sequence of frag_intersect, so every test decides as fwd_fragment and the
-// backward do; the accumulation as packed operations, zero-weighted on a lane
-// whose fragment does not count.
+// recurrences, P0/cr/forward.cu:349-430 and P1/cr/forward.cu:350-440): the
+// geometry in the explicit sequence of frag_intersect, so every test decides
+// as the backward does; the accumulation as packed operations, zero-weighted
+// on a lane whose fragment does not count.  The part variant's semantic sums
+// sit in shared memory: pixel i of this thread at sem_acc4[g4 * kBlock + i *
+// NT] for channels 4 g4 .. 4 g4 + 3.
+template <int VARIANT, int NT>
 __device__ __forceinline__ void fwd_fragment2(FwdPair& q, const float4 (*s_rec)[kBlock], int j,
-                                              uint32_t contributor) {
+                                              uint32_t contributor, const float4* s_sem4, int S,
+                                              float4* sem_acc4) {
   if (q.done[0] && q.done[1]) return;
   const float4 r0 = s_rec[0][j], r1 = s_rec[1][j], r2 = s_rec[2][j];
   const float reach = s_rec[3][j].w;
@@ -613,7 +629,9 @@ __device__ __forceinline__ void fwd_fragment2(FwdPair& q, const float4 (*s_rec)[
   const float2 dep = sel2(a0, a1, depth, one);
   const float2 A = lfma(q.T, bc<float2>(-1.0f), one);                        // 1 - T
   const float2 inv_d = make_float2(blend_rcp(dep.x), blend_rcp(dep.y));
-  const float2 m = lmul(bc<float2>(kFarP0 / (kFarP0 - kNearP0)), lfma(bc<float2>(-kNearP0), inv_d, one));
+  const float2 m = (VARIANT == SGR_VARIANT_PLAIN)
+                       ? lmul(bc<float2>(kFarP0 / (kFarP0 - kNearP0)), lfma(bc<float2>(-kNearP0), inv_d, one))
+                       : lfma(bc<float2>(-kDmdP1f), inv_d, bc<float2>(kMdP1));   // mapped_depth_p1
   const float2 mm = lmul(m, m);
   // m^2 A + M2 - 2 m M1
   const float2 e = lfma(lmul(bc<float2>(-2.0f), m), q.M1, lfma(mm, A, q.M2));
@@ -623,11 +641,27 @@ __device__ __forceinline__ void fwd_fragment2(FwdPair& q, const float4 (*s_rec)[
   q.M2 = lfma(mm, w, q.M2);
   if (a0 && q.T.x > 0.5f) {
     q.med_depth.x = depth.x;
+    q.med_weight.x = w.x;
     q.med_contrib[0] = (int)contributor;
   }
   if (a1 && q.T.y > 0.5f) {
     q.med_depth.y = depth.y;
+    q.med_weight.y = w.y;
     q.med_contrib[1] = (int)contributor;
+  }
+  if (VARIANT == SGR_VARIANT_PART) {
+    // four channels at a time; channels past S are zero in the staged values
+    for (int g4 = 0; g4 < (S + 3) / 4; ++g4) {
+      const float4 x = s_sem4[g4 * kBlock + j];
+#pragma unroll
+      for (int i = 0; i < 2; ++i) {
+        if (!(i == 0 ? a0 : a1)) continue;
+        const float wi = i == 0 ? w.x : w.y;
+        float4& a = sem_acc4[g4 * kBlock + i * NT];
+        a = make_float4(__fmaf_rn(x.x, wi, a.x), __fmaf_rn(x.y, wi, a.y), __fmaf_rn(x.z, wi, a.z),
+                        __fmaf_rn(x.w, wi, a.w));
+      }
+    }
   }
   q.N[0] = lfma(bc<float2>(r3.x), w, q.N[0]);
   q.N[1] = lfma(bc<float2>(r3.y), w, q.N[1]);
@@ -649,7 +683,7 @@ __device__ __forceinline__ void fwd_fragment2(FwdPair& q, const float4 (*s_rec)[
 #define SGR_FWD_MIN_CTAS (SGR_FWD_PACKED ? 5 : 4)
 #endif
 #ifndef SGR_PART_FWD_MIN_CTAS
-#define SGR_PART_FWD_MIN_CTAS 3
+#define SGR_PART_FWD_MIN_CTAS (SGR_FWD_PACKED && SGR_PART_PACKED ? 4 : 3)
 #endif
 
 // The forward of one tile (all threads of the CTA).
@@ -657,7 +691,7 @@ template <int VARIANT, int WX>
 __device__ __forceinline__ void render_fwd_tile(const sgr_batch& b, const GeomView& g, const sgr_fwd_outputs& out,
                                                 const int tile) {
   using Shape = FwdShapeT<VARIANT, WX>;
-  constexpr int PX = Shape::PX, NT = Shape::NT, NW = Shape::NW, NS = kSemSlots<VARIANT>;
+  constexpr int PX = Shape::PX, NT = Shape::NT, NW = Shape::NW;
   const int tiles_per_view = g.tiles_x * g.tiles_y;
   const int v = tile / tiles_per_view;
   const int t = tile - v * tiles_per_view;
@@ -673,13 +707,16 @@ __device__ __forceinline__ void render_fwd_tile(const sgr_batch& b, const GeomVi
   __shared__ float4 s_rec[kRecF4 - 1][kBlock];
   __shared__ uint8_t s_mask[kBlock];
   __shared__ uint8_t s_list[NW][kBlock];
-  constexpr int NS4 = (NS + 3) / 4;
-  __shared__ float4 s_sem4[NS4 * kBlock];   // staged semantics, four channels per float4
   __shared__ uint32_t s_ring[kRing];
   __shared__ int s_count[32];
-  // part variant: each thread's semantic sums, one column per thread
-  __shared__ float4 s_semacc4[NS4][(VARIANT == SGR_VARIANT_PART) ? NT : 1];
-  float4* sem_acc4 = (VARIANT == SGR_VARIANT_PART) ? &s_semacc4[0][threadIdx.x] : nullptr;
+  // part variant, sized by S at launch (fwd_dynamic_smem): the staged
+  // semantics, four channels per float4, then every pixel's semantic sums
+  // (pixel i of a thread in column i * NT + thread); rows of kBlock float4
+  extern __shared__ float4 s_dyn4[];
+  static_assert(NT * PX == kBlock, "one column per pixel");
+  const int NS4 = (S + 3) / 4;
+  float4* const s_sem4 = s_dyn4;
+  float4* const sem_acc4 = (VARIANT == SGR_VARIANT_PART) ? s_dyn4 + NS4 * kBlock + threadIdx.x : nullptr;
 
   const uint32_t* list;
   int len;
@@ -704,12 +741,12 @@ __device__ __forceinline__ void render_fwd_tile(const sgr_batch& b, const GeomVi
     Q.med_contrib = -1;
     Q.stop = 0;
     if (VARIANT == SGR_VARIANT_PART)
-      for (int g4 = 0; g4 < (S + 3) / 4; ++g4) sem_acc4[g4 * NT] = make_float4(0.f, 0.f, 0.f, 0.f);
+      for (int g4 = 0; g4 < NS4; ++g4) sem_acc4[g4 * kBlock + i * NT] = make_float4(0.f, 0.f, 0.f, 0.f);
     done = done && Q.done;
   }
 
-  // the two pixels of a plain thread as packed lanes
-  constexpr bool PACKED = VARIANT == SGR_VARIANT_PLAIN && PX == 2;
+  // the two pixels of a thread as packed lanes
+  constexpr bool PACKED = PX == 2;
   FwdPair qp;
   if constexpr (PACKED) {
     qp.pxf = q[0].pxf;
@@ -719,7 +756,7 @@ __device__ __forceinline__ void render_fwd_tile(const sgr_batch& b, const GeomVi
     qp.T = make_float2(1.0f, 1.0f);
     const float2 z = make_float2(0.0f, 0.0f);
     qp.C[0] = qp.C[1] = qp.C[2] = qp.N[0] = qp.N[1] = qp.N[2] = z;
-    qp.D = qp.M1 = qp.M2 = qp.dist = qp.med_depth = z;
+    qp.D = qp.M1 = qp.M2 = qp.dist = qp.med_depth = qp.med_weight = z;
 #pragma unroll
     for (int i = 0; i < 2; ++i) {
       qp.done[i] = q[i].done;
@@ -763,7 +800,7 @@ __device__ __forceinline__ void render_fwd_tile(const sgr_batch& b, const GeomVi
       const int j = s_list[warp][si];
       const uint32_t contributor = (uint32_t)(base + j + 1);
       if constexpr (PACKED) {
-        fwd_fragment2(qp, s_rec, j, contributor);
+        fwd_fragment2<VARIANT, NT>(qp, s_rec, j, contributor, s_sem4, S, sem_acc4);
         done = qp.done[0] && qp.done[1];
       } else {
         done = true;
@@ -793,6 +830,7 @@ __device__ __forceinline__ void render_fwd_tile(const sgr_batch& b, const GeomVi
       Q.M2 = lane_of(qp.M2);
       Q.dist = lane_of(qp.dist);
       Q.med_depth = lane_of(qp.med_depth);
+      Q.med_weight = lane_of(qp.med_weight);
       Q.med_contrib = qp.med_contrib[i];
       Q.stop = qp.stop[i];
     }
@@ -845,8 +883,8 @@ __device__ __forceinline__ void render_fwd_tile(const sgr_batch& b, const GeomVi
     if (VARIANT == SGR_VARIANT_PART) {
       oth[pix + 7 * HW] = Q.med_weight;
       float* sem = out.semantic + (size_t)v * S * HW;
-      const float* acc = reinterpret_cast<const float*>(sem_acc4);   // thread column: float4 stride NT
-      for (int c = 0; c < S; ++c) sem[pix + c * HW] = acc[(c >> 2) * 4 * NT + (c & 3)];
+      const float* acc = reinterpret_cast<const float*>(sem_acc4 + i * NT);   // pixel column: float4 stride kBlock
+      for (int c = 0; c < S; ++c) sem[pix + c * HW] = acc[(c >> 2) * 4 * kBlock + (c & 3)];
     }
   }
 }
@@ -1100,16 +1138,13 @@ __device__ __forceinline__ void bwd_update(BwdPixel<VARIANT>& q, const BwdGeom& 
 }
 
 // ---------------------------------------------------------------------------
-// The plain backward's two pixels per thread as the two lanes of packed
-// FP32 operations (SGR_BWD_PACKED): the same recurrences as bwd_reach,
-// bwd_alpha and bwd_update, with the fragment geometry in the forward's
-// explicit sequence (frag_intersect), so the decisions -- which fragments
-// count -- are the forward's bit for bit.  A pixel that a fragment does not
-// reach keeps its state (per-lane selects) and adds nothing.
+// The backward's two pixels per thread as the two lanes of packed FP32
+// operations (SGR_BWD_PACKED): the same recurrences as bwd_reach, bwd_alpha
+// and bwd_update, with the fragment geometry in the forward's explicit
+// sequence (frag_intersect), so the decisions -- which fragments count -- are
+// the forward's bit for bit.  A pixel that a fragment does not reach keeps
+// its state and adds nothing.
 // ---------------------------------------------------------------------------
-#ifndef SGR_BWD_PACKED
-#define SGR_BWD_PACKED 1
-#endif
 
 
 // Per-pixel state of the backward recurrences, lane i = pixel i.
@@ -1119,12 +1154,14 @@ struct BwdPair {
   float2 T, T_final, final_A, final_D, final_D2, bg_dot;
   int last_contributor[2], median_contributor[2];
   float2 dL_dpixel[3], dL_dnormal2D[3];
-  float2 dL_ddepth, dL_daccum, dL_dreg, dL_dmedian;
+  float2 dL_ddepth, dL_daccum, dL_dreg, dL_dmedian, dL_dmaxw;
   float2 rec_dot, last_col_dot, nrm_dot, last_nrm_dot;
   float2 last_alpha, last_depth, accum_depth, accum_alpha, last_dL_dT;
+  float2 sem_w;   // part variant: alpha T of each pixel's fragment of the current entry, 0 where not live
 };
 
-__device__ __forceinline__ BwdPair to_pair(const BwdPixel<SGR_VARIANT_PLAIN> (&q)[2]) {
+template <int VARIANT>
+__device__ __forceinline__ BwdPair to_pair(const BwdPixel<VARIANT> (&q)[2]) {
   BwdPair p;
   auto f2 = [](float a, float b) { return make_float2(a, b); };
   p.pxf = q[0].pxf;
@@ -1149,7 +1186,9 @@ __device__ __forceinline__ BwdPair to_pair(const BwdPixel<SGR_VARIANT_PLAIN> (&q
   p.dL_daccum = f2(q[0].dL_daccum, q[1].dL_daccum);
   p.dL_dreg = f2(q[0].dL_dreg, q[1].dL_dreg);
   p.dL_dmedian = f2(q[0].dL_dmedian, q[1].dL_dmedian);
+  p.dL_dmaxw = f2(q[0].dL_dmaxw, q[1].dL_dmaxw);
   const float2 z = f2(0.f, 0.f);
+  p.sem_w = z;
   p.rec_dot = p.last_col_dot = p.nrm_dot = p.last_nrm_dot = z;
   p.last_alpha = p.last_depth = p.accum_depth = p.accum_alpha = p.last_dL_dT = z;
   return p;
@@ -1203,10 +1242,13 @@ __device__ __forceinline__ void bwd_alpha2(const float4& r1, const float4& r2, B
 }
 
 // Stage 3: both pixels' recurrences and their summed share of the entry's
-// 18 gradient values, written to gv[0..17] (P0/cr/backward.cu:337-440).  A
-// lane whose fragments are not live keeps its state and writes zeros, so the
-// call needs no branch around it (the geometry of a non-live fragment is
-// finite: p.z is replaced by 1 in bwd_alpha2).
+// 18 gradient values, written to gv[0..17] (P0/cr/backward.cu:337-440,
+// P1/cr/backward.cu:340-450).  A lane whose fragments are not live keeps its
+// state and writes zeros, so the call needs no branch around it (the
+// geometry of a non-live fragment is finite: p.z is replaced by 1 in
+// bwd_alpha2).  The part variant also keeps each fragment's weight for its
+// semantic gradients.
+template <int VARIANT>
 __device__ __forceinline__ void bwd_update2(BwdPair& q, const BwdGeom2& f, const float4& r1, const float4& r2,
                                             const float4& r3, const float4& r4, int pos, float (&gv)[32]) {
   const bool l0 = f.live[0], l1 = f.live[1];
@@ -1222,6 +1264,7 @@ __device__ __forceinline__ void bwd_update2(BwdPair& q, const BwdGeom2& f, const
   const float2 T = sel2(l0, l1, lmul(q.T, inv_1ma), q.T);
   q.T = T;
   const float2 wgt = lmul(alpha, T);                                            // zero where not live
+  if (VARIANT == SGR_VARIANT_PART) q.sem_w = wgt;
   const float2 oml = lfma(q.last_alpha, bc<float2>(-1.0f), one);               // 1 - last_alpha
   // colour recurrence on its dot product with dL/dpixel
   const float2 cd = lfma(bc<float2>(r4.z), q.dL_dpixel[2],
@@ -1232,13 +1275,19 @@ __device__ __forceinline__ void bwd_update2(BwdPair& q, const BwdGeom2& f, const
   float2 dL_dalpha = ladd(cd, make_float2(-rec.x, -rec.y));
   // depth distortion (mapped depth and its derivative)
   const float2 inv_d = make_float2(blend_rcp(c_d.x), blend_rcp(c_d.y));
-  const float2 m_d = lmul(bc<float2>(kFarP0 / (kFarP0 - kNearP0)), lfma(bc<float2>(-kNearP0), inv_d, one));
-  const float2 dmd_dd = lmul(bc<float2>((kFarP0 * kNearP0) / (kFarP0 - kNearP0)), lmul(inv_d, inv_d));
-  float2 dL_dz = make_float2(pos == q.median_contributor[0] - 1 ? q.dL_dmedian.x : 0.0f,
-                             pos == q.median_contributor[1] - 1 ? q.dL_dmedian.y : 0.0f);
+  constexpr bool PLAIN = VARIANT == SGR_VARIANT_PLAIN;
+  const float2 m_d = PLAIN ? lmul(bc<float2>(kFarP0 / (kFarP0 - kNearP0)), lfma(bc<float2>(-kNearP0), inv_d, one))
+                           : lfma(bc<float2>(-kDmdP1f), inv_d, bc<float2>(kMdP1));   // mapped_depth_p1
+  const float2 dmd_dd = lmul(bc<float2>(PLAIN ? (kFarP0 * kNearP0) / (kFarP0 - kNearP0) : kDmdP1f),
+                             lmul(inv_d, inv_d));
+  const bool med0 = pos == q.median_contributor[0] - 1, med1 = pos == q.median_contributor[1] - 1;
+  float2 dL_dz = make_float2(med0 ? q.dL_dmedian.x : 0.0f, med1 ? q.dL_dmedian.y : 0.0f);
   // final_D2 + m^2 final_A - 2 m final_D
   const float2 reg = lfma(m_d, lfma(m_d, q.final_A, lmul(bc<float2>(-2.0f), q.final_D)), q.final_D2);
-  const float2 dL_dweight = lmul(reg, q.dL_dreg);
+  // part: the median fragment's weight also carries the max-weight map's gradient
+  const float2 dL_dweight =
+      PLAIN ? lmul(reg, q.dL_dreg)
+            : lfma(reg, q.dL_dreg, make_float2(med0 ? q.dL_dmaxw.x : 0.0f, med1 ? q.dL_dmaxw.y : 0.0f));
   dL_dalpha = ladd(dL_dalpha, ladd(dL_dweight, make_float2(-q.last_dL_dT.x, -q.last_dL_dT.y)));
   const float2 ldt = lfma(dL_dweight, alpha, lmul(lfma(alpha, bc<float2>(-1.0f), one), q.last_dL_dT));
   q.last_dL_dT = ldt;
@@ -1319,7 +1368,7 @@ __device__ __forceinline__ void bwd_update2(BwdPair& q, const BwdGeom2& f, const
 #endif
 
 #ifndef SGR_PART_BWD_MIN_CTAS
-#define SGR_PART_BWD_MIN_CTAS 3
+#define SGR_PART_BWD_MIN_CTAS (SGR_BWD_PACKED && SGR_PART_PACKED ? 4 : 3)
 #endif
 
 // The backward of one tile (all threads of the CTA).
@@ -1348,7 +1397,7 @@ __device__ __forceinline__ void render_bwd_tile(const sgr_batch& b, const GeomVi
   __shared__ uint32_t s_id[kBlock];
   __shared__ uint8_t s_mask[kBlock];
   __shared__ uint8_t s_list[NW][kBlock];
-  __shared__ float s_dsem[NS][NT * PX];   // part variant: each pixel's dL/dpixel semantics
+  __shared__ __align__(16) float s_dsem[NS][NT * PX];   // part variant: each pixel's dL/dpixel semantics
   __shared__ int s_max[NW];
   __shared__ uint32_t s_ring[kRing];
   __shared__ int s_count[32];
@@ -1404,8 +1453,8 @@ __device__ __forceinline__ void render_bwd_tile(const sgr_batch& b, const GeomVi
 #endif
     thread_max = max(thread_max, Q.last_contributor);
   }
-  // the two pixels of a plain thread as packed lanes
-  constexpr bool PACKED = SGR_BWD_PACKED && VARIANT == SGR_VARIANT_PLAIN && PX == 2 && SPLIT == 1;
+  // the two pixels of a thread as packed lanes
+  constexpr bool PACKED = SGR_BWD_PACKED && kPackedBlend<VARIANT> && PX == 2 && SPLIT == 1;
   BwdPair qp;
   if constexpr (PACKED) qp = to_pair(q);
 
@@ -1471,10 +1520,35 @@ __device__ __forceinline__ void render_bwd_tile(const sgr_batch& b, const GeomVi
         bwd_alpha2(r1, r2, f2);
         if (!__any_sync(0xffffffffu, f2.live[0] || f2.live[1])) continue;
         const float4 r3 = s_rec[3][j], r4 = s_rec[4][j];
-        bwd_update2(qp, f2, r1, r2, r3, r4, pos, gv);   // every lane: non-live lanes write zeros
+        bwd_update2<VARIANT>(qp, f2, r1, r2, r3, r4, pos, gv);   // every lane: non-live lanes write zeros
         int which;
         const float total = warp_sum18(gv, lane, which);
-        if (which >= 0 && total != 0.f) atomicAdd(grads + (size_t)s_id[j] * kGradF + which, total);
+        const uint32_t r = s_id[j];
+        if (which >= 0 && total != 0.f) atomicAdd(grads + (size_t)r * kGradF + which, total);
+        if (VARIANT == SGR_VARIANT_PART && S > 0) {
+          // dL/dsemantic[c] = sum over the warp's pixels of weight x dL/dpixel semantic[c];
+          // sem_w is zero on a lane whose fragment is not live
+          float sv[32];
+          int ch;
+          float st;
+          const float2 sw = qp.sem_w;
+          if (S <= 8) {   // uniform: half the values and 9 shuffles instead of 16
+#pragma unroll
+            for (int c = 0; c < 8; ++c) {
+              const float2 d = c < S ? reinterpret_cast<const float2*>(s_dsem[c])[threadIdx.x] : make_float2(0.f, 0.f);
+              sv[c] = __fmaf_rn(sw.x, d.x, __fmul_rn(sw.y, d.y));
+            }
+            st = warp_sum8(sv, lane, ch);
+          } else {
+#pragma unroll
+            for (int c = 0; c < SGR_MAX_SEMANTICS; ++c) {
+              const float2 d = c < S ? reinterpret_cast<const float2*>(s_dsem[c])[threadIdx.x] : make_float2(0.f, 0.f);
+              sv[c] = __fmaf_rn(sw.x, d.x, __fmul_rn(sw.y, d.y));
+            }
+            st = warp_sum16(sv, lane, ch);
+          }
+          if (ch >= 0 && ch < S && st != 0.f) atomicAdd(dL_dsemantics + (size_t)(sid_base + (int)r) * S + ch, st);
+        }
         continue;
       }
 #pragma unroll
@@ -1591,36 +1665,60 @@ __global__ void __launch_bounds__(1024) k_tile_order(GeomView g, int n, int back
   for (int i = threadIdx.x; i < n; i += blockDim.x) order[atomicAdd(&s_pos[32 - __clz(cost(i))], 1u)] = (uint32_t)i;
 }
 
-// Resident CTAs per SM of a kernel on the current device (queried once per
-// kernel and device).
+// Resident CTAs of a kernel on the current device, with `rows` rows of
+// kBlock float4 of dynamic shared memory (queried once per kernel, device and
+// row count).
 template <class F>
-int resident_ctas(F kernel, int threads) {
-  constexpr int kMaxDev = 64;
-  static int cache[kMaxDev] = {};
+int resident_ctas(F kernel, int threads, int rows = 0) {
+  constexpr int kMaxDev = 64, kMaxRows = 2 * ((SGR_MAX_SEMANTICS + 3) / 4);
+  static int cache[kMaxDev][kMaxRows + 1] = {};
   int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDev) return 0;
-  if (cache[dev] == 0) {
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDev || rows < 0 || rows > kMaxRows) return 0;
+  if (cache[dev][rows] == 0) {
     int per_sm = 0, sms = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, 0) != cudaSuccess ||
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads,
+                                                      (size_t)rows * kBlock * sizeof(float4)) != cudaSuccess ||
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
       return 0;
-    cache[dev] = per_sm * sms;
+    cache[dev][rows] = per_sm * sms;
   }
-  return cache[dev];
+  return cache[dev][rows];
+}
+
+// Rows of kBlock float4 of the forward's dynamic shared memory: none for the
+// plain variant; the part variant's staged semantics and per-pixel sums,
+// (S + 3) / 4 rows each.
+inline int fwd_dynamic_rows(const sgr_batch& b) {
+  return b.variant == SGR_VARIANT_PART ? 2 * ((b.semantic_channels + 3) / 4) : 0;
+}
+
+// Lets a kernel take the largest dynamic shared memory the part variant asks
+// for (once per kernel and device).
+template <class F>
+void allow_dynamic_smem(F kernel) {
+  constexpr int kMaxDev = 64;
+  static bool done[kMaxDev] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDev || done[dev]) return;
+  cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       2 * ((SGR_MAX_SEMANTICS + 3) / 4) * kBlock * (int)sizeof(float4));
+  done[dev] = true;
 }
 
 template <int VARIANT, int WX>
 void launch_fwd(const sgr_batch& b, const GeomView& g, const sgr_fwd_outputs& out, TileQueue q, unsigned tiles,
                 cudaStream_t st) {
   auto* k = k_render_fwd<VARIANT, WX>;
+  const int rows = fwd_dynamic_rows(b);
+  if (VARIANT == SGR_VARIANT_PART) allow_dynamic_smem(k);
   unsigned grid = tiles;
   if (q.order) {
     k_tile_order<<<1, 1024, 0, st>>>(g, (int)tiles, 0, const_cast<uint32_t*>(q.order), q.next);
     count_launches();
-    const int r = resident_ctas(k, FwdShapeT<VARIANT, WX>::NT);
+    const int r = resident_ctas(k, FwdShapeT<VARIANT, WX>::NT, rows);
     grid = r > 0 ? std::min<unsigned>(tiles, (unsigned)r) : tiles;
   }
-  k<<<grid, FwdShapeT<VARIANT, WX>::NT, 0, st>>>(b, g, out, q);
+  k<<<grid, FwdShapeT<VARIANT, WX>::NT, (size_t)rows * kBlock * sizeof(float4), st>>>(b, g, out, q);
 }
 
 template <int VARIANT, int WX>
