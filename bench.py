@@ -356,14 +356,16 @@ def run_gpu(args):
         tr.raster.cell_tiles = args.cell_tiles
         tr.raster.blend_shape = args.blend_shape
         tr.raster.tile_schedule = args.tile_schedule
-    # cell size, warp footprint and tile schedule timed per workload unless
+        tr.raster.stage_entries = args.stage_entries
+    # cell size, warp footprint, tile schedule and staged batch timed per workload unless
     # given; the warm-up steps size the lists
     tr.capture(targets, warmup=3, autotune=not fixed)
     tuning = {}
     if not fixed:
         from partgs_gb300 import autotune as AT
         tuning = {"cells_ms": {str(k): round(v, 3) for k, v in AT.tune_cells.last_timings.items()},
-                  "blend_ms": {f"shape{k[0]}_sched{k[1]}": round(v, 3) for k, v in AT.tune_blend.last_timings.items()}}
+                  "blend_ms": {f"shape{k[0]}_sched{k[1]}_stage{k[2]}": round(v, 3)
+                               for k, v in AT.tune_blend.last_timings.items()}}
     launches_per_step = tr.launches_per_step
     for _ in range(args.warmup):
         tr.replay()
@@ -443,6 +445,7 @@ def run_gpu(args):
                            cell_list_capacity=tr.raster.bin_capacity, cell_tiles=tr.raster.cell_tiles,
                            blend_shape=["strip16", "patch8"][tr.raster.blend_shape],
                            tile_schedule=["grid", "queue"][tr.raster.tile_schedule],
+                           stage_entries=tr.raster.stage_entries or "library default (256 for plain)",
                            autotune_ms=tuning or None, parallelism=f"replicas x{ws}"),
             "e2e": {"value": ws / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(targets_host.numel() * 4),
                     "d2h_bytes_per_step": 4},
@@ -505,9 +508,10 @@ def run_multiscene(args):
     w_host = torch.randn(V, 10, H, W, generator=wg).pin_memory()
     w_dev = w_host.to(dev)
 
-    def make(cell, shape, sched):
+    def make(cell, shape, sched, stage=0):
         return MultiViewRasterizer(all_cams, [0, 0, 0], 3, scene_sizes=sizes, scene_views=[views] * n_scenes,
-                                   device=dev, cell_tiles=cell, blend_shape=shape, tile_schedule=sched)
+                                   device=dev, cell_tiles=cell, blend_shape=shape, tile_schedule=sched,
+                                   stage_entries=stage)
 
     def step(r, w):
         leaves = [t.detach().requires_grad_(True) for t in inputs]
@@ -526,19 +530,21 @@ def run_multiscene(args):
         torch.cuda.synchronize()
         return e0.elapsed_time(e1) / n
 
-    # autotune: cell edge (default footprint and schedule), then footprint x schedule
+    # autotune: cell edge (default footprint, schedule and staged batch),
+    # then footprint x schedule x staged batch
     tune = {}
     for cell in (2, 4, 8):
-        r = make(cell, 0, 0)
+        r = make(cell, 0, 0, L.SGR_STAGE_DEFAULT)
         step(r, w_dev)
-        tune[(cell, 0, 0)] = timed(lambda: step(r, w_dev), 2)
+        tune[(cell, 0, 0, L.SGR_STAGE_DEFAULT)] = timed(lambda: step(r, w_dev), 2)
     cell = min(tune, key=tune.get)[0]
     for shape in (0, 1):
         for sched in (0, 1):
-            if (cell, shape, sched) not in tune:
-                r = make(cell, shape, sched)
-                step(r, w_dev)
-                tune[(cell, shape, sched)] = timed(lambda: step(r, w_dev), 2)
+            for stage in (L.SGR_STAGE_DEFAULT, L.SGR_STAGE_SMALL):
+                if (cell, shape, sched, stage) not in tune:
+                    r = make(cell, shape, sched, stage)
+                    step(r, w_dev)
+                    tune[(cell, shape, sched, stage)] = timed(lambda: step(r, w_dev), 2)
     best = min(tune, key=tune.get)
     r = make(*best)
     for _ in range(args.warmup):
@@ -558,7 +564,7 @@ def run_multiscene(args):
 
     # the same work as 32 per-scene calls
     per = [MultiViewRasterizer(cams[s], [0, 0, 0], 3, num_surfels=sizes[s], device=dev, cell_tiles=best[0],
-                               blend_shape=best[1]) for s in range(n_scenes)]
+                               blend_shape=best[1], stage_entries=best[3]) for s in range(n_scenes)]
 
     def per_scene():
         for s in range(n_scenes):
@@ -576,8 +582,9 @@ def run_multiscene(args):
             "data": "synthetic (seeded scenes and loss weights)",
             "config": {"workload": MULTISCENE, "scenes": n_scenes, "surfels": offs[-1], "views_per_scene": views,
                        "height": H, "width": W, "cell_tiles": best[0], "blend_shape": best[1],
-                       "tile_schedule": best[2],
-                       "autotune_ms": {f"cell{c}_shape{sh}_sched{sc}": round(v, 3) for (c, sh, sc), v in tune.items()},
+                       "tile_schedule": best[2], "stage_entries": best[3],
+                       "autotune_ms": {f"cell{c}_shape{sh}_sched{sc}_stage{st}": round(v, 3)
+                                       for (c, sh, sc, st), v in tune.items()},
                        "l2": "per-step working set (3.7M surfels x 8 views of records, lists, images) far larger than "
                              "the 129 MB L2"},
             "e2e": {"value": 1.0 / e2e_s, "unit": "steps/s", "h2d_bytes_per_step": int(w_host.numel() * 4),
@@ -625,11 +632,13 @@ def main():
     ap.add_argument("--no-reference-cuda", action="store_true",
                     help="skip timing the reference's CUDA rasteriser on the same workload")
     ap.add_argument("--cell-tiles", type=int, default=0, choices=[0, 1, 2, 4, 8, 16],
-                    help="cell edge in tiles (0: cell edge, warp footprint and tile schedule autotuned)")
+                    help="cell edge in tiles (0: cell edge, warp footprint, tile schedule and staged batch autotuned)")
     ap.add_argument("--blend-shape", type=int, default=0, choices=[0, 1],
                     help="with --cell-tiles: the blends' warp footprint (0: 16x2 strips, 1: 8-wide patches)")
     ap.add_argument("--tile-schedule", type=int, default=0, choices=[0, 1],
                     help="with --cell-tiles: 0 a CTA per tile, 1 persistent CTAs on a tile queue")
+    ap.add_argument("--stage-entries", type=int, default=0, choices=[0, 128, 256],
+                    help="with --cell-tiles: list entries per staged batch of the blends (0: 256)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

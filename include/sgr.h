@@ -51,7 +51,7 @@
 extern "C" {
 #endif
 
-#define SGR_ABI_VERSION 3
+#define SGR_ABI_VERSION 4
 
 /* status codes returned by every entry point */
 #define SGR_OK 0
@@ -82,15 +82,22 @@ extern "C" {
                                          calls); that tile's gradients are incomplete */
 
 /* sgr_batch.blend_shape: the part of a 16x16 tile each warp of the blend
- * kernels owns.  STRIP16: 16-pixel-wide rows (16x2 in the forward, 16x4 in
- * the backward of the plain variant); PATCH8: 8-pixel-wide patches (8x4,
- * 8x8).  Only the grouping of pixels into warps changes: every pixel still
- * walks its 16x16 tile's list, so images and gradients are the same. */
+ * kernels owns.  STRIP16: 16-pixel-wide rows (16x4 at two pixels per
+ * thread); PATCH8: 8-pixel-wide patches (8x8).  Only the grouping of pixels
+ * into warps changes: every pixel still walks its 16x16 tile's list, so
+ * images and gradients are the same. */
 #define SGR_BLEND_STRIP16 0
 #define SGR_BLEND_PATCH8 1
 /* sgr_batch.tile_schedule */
 #define SGR_SCHEDULE_GRID 0
 #define SGR_SCHEDULE_QUEUE 1
+/* sgr_batch.stage_entries: tile-list entries the blends stage in shared
+ * memory per batch.  0 lets the library choose: SGR_STAGE_DEFAULT, or
+ * SGR_STAGE_SMALL for the part variant above 12 semantic channels (the
+ * smaller batch keeps its forward at 4 CTAs per SM).  Every pixel still walks
+ * the same entries in the same order, so images and gradients are the same. */
+#define SGR_STAGE_DEFAULT 256
+#define SGR_STAGE_SMALL 128
 
 #define SGR_VARIANT_PLAIN 0
 #define SGR_VARIANT_PART 1
@@ -152,6 +159,8 @@ typedef struct sgr_batch {
                                         SGR_BLEND_PATCH8 (results identical; speed depends on splat sizes) */
     int32_t tile_schedule;           /* SGR_SCHEDULE_GRID (one CTA per tile) or SGR_SCHEDULE_QUEUE (persistent
                                         CTAs take tiles from a device queue, longest estimated first) */
+    int32_t stage_entries;           /* 0 (the library's choice), SGR_STAGE_DEFAULT or SGR_STAGE_SMALL: list
+                                        entries per staged batch of the blends (results identical) */
 } sgr_batch;
 
 /* Workspace sizes and the layout of the geometry workspace. */

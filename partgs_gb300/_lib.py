@@ -14,7 +14,7 @@ LIB_PATH = _HERE / "_lib" / "libsgr.so"
 
 SGR_OK = 0
 SGR_ERR_CUDA = 6
-ABI_VERSION = 3
+ABI_VERSION = 4
 SGR_FLAG_KEY_OVERFLOW = 1
 SGR_FLAG_PREFILTERED = 2
 SGR_FLAG_BIN_OVERFLOW = 4
@@ -24,6 +24,8 @@ SGR_BLEND_STRIP16 = 0
 SGR_BLEND_PATCH8 = 1
 SGR_SCHEDULE_GRID = 0
 SGR_SCHEDULE_QUEUE = 1
+SGR_STAGE_DEFAULT = 256
+SGR_STAGE_SMALL = 128
 SGR_VARIANT_PLAIN = 0
 SGR_VARIANT_PART = 1
 SGR_MAX_SEMANTICS = 16
@@ -51,7 +53,7 @@ class Batch(C.Structure):
         ("scenes", _p), ("views", _p), ("viewmatrix", _p), ("projmatrix", _p), ("campos", _p),
         ("background", _p), ("means3D", _p), ("scales", _p), ("rotations", _p), ("opacities", _p),
         ("shs", _p), ("colors_precomp", _p), ("transmat_precomp", _p), ("semantics", _p), ("cell_tiles", _i),
-        ("blend_shape", _i), ("tile_schedule", _i),
+        ("blend_shape", _i), ("tile_schedule", _i), ("stage_entries", _i),
     ]
 
 

@@ -1,6 +1,6 @@
 """Workload autotuning of the rasteriser's launch shape.
 
-Three knobs change speed but not results:
+Four knobs change speed but not results:
 
 * the cell size.  Each blend CTA streams the list of the cell that holds its
   tile and keeps the entries whose rectangle holds the tile
@@ -12,11 +12,15 @@ Three knobs change speed but not results:
   it, at the price of more per-entry reach tests.
 * the tile schedule: one CTA per tile, or persistent CTAs taking tiles from
   a device queue in decreasing order of estimated cost (uneven scenes).
+* the staged batch (``stage_entries``): how many list entries the blends
+  copy into shared memory between two CTA barriers, 256 or 128.  Larger
+  batches mean fewer barriers; smaller ones less shared memory per CTA and
+  less waiting at each barrier for the warp with the most work.
 
 The best choice depends on the surfels' screen sizes, the image and the
 scene mix.  ``tune_cells`` times whole training steps of a ``SurfelTrainer``
-for each candidate cell edge, ``tune_blend`` then each footprint and
-schedule at that edge (parameters and optimiser state restored after each
+for each candidate cell edge, ``tune_blend`` then each footprint, schedule
+and staged batch at that edge (parameters and optimiser state restored after each
 trial); results are cached per workload shape for the process.
 """
 from __future__ import annotations
@@ -28,6 +32,7 @@ from . import _lib as L
 CANDIDATES = (2, 4, 8, 16)
 SHAPES = (L.SGR_BLEND_STRIP16, L.SGR_BLEND_PATCH8)
 SCHEDULES = (L.SGR_SCHEDULE_GRID, L.SGR_SCHEDULE_QUEUE)
+STAGES = (L.SGR_STAGE_DEFAULT, L.SGR_STAGE_SMALL)
 _CACHE: dict = {}
 
 
@@ -80,30 +85,32 @@ def tune_cells(trainer, targets, candidates=CANDIDATES, steps: int = 3, log=None
 tune_cells.last_timings = {}
 
 
-def tune_blend(trainer, targets, shapes=SHAPES, schedules=SCHEDULES, steps: int = 3, log=None) -> tuple:
-    """Sets ``trainer.raster.blend_shape`` and ``tile_schedule`` to the
-    fastest pair for this workload (at the current cell edge) and returns
-    it, with {(shape, schedule): ms per step} in ``last_timings``."""
+def tune_blend(trainer, targets, shapes=SHAPES, schedules=SCHEDULES, stages=STAGES, steps: int = 3,
+               log=None) -> tuple:
+    """Sets ``trainer.raster.blend_shape``, ``tile_schedule`` and
+    ``stage_entries`` to the fastest combination for this workload (at the
+    current cell edge) and returns it, with {(shape, schedule, stage): ms per
+    step} in ``last_timings``."""
     key = ("blend", trainer.raster.cell_tiles) + workload_key(trainer)
     r = trainer.raster
     if key in _CACHE:
-        r.blend_shape, r.tile_schedule = _CACHE[key]
+        r.blend_shape, r.tile_schedule, r.stage_entries = _CACHE[key]
         return _CACHE[key]
     state = trainer.snapshot()
     saved_capacity = r.bin_capacity
     timings = {}
-    pairs = [(shape, sched) for shape in shapes for sched in schedules]
-    for order in (pairs, pairs[::-1]):                 # two rounds, as tune_cells
-        for shape, sched in order:
-            r.blend_shape, r.tile_schedule = shape, sched
+    combos = [(shape, sched, stage) for shape in shapes for sched in schedules for stage in stages]
+    for order in (combos, combos[::-1]):               # two rounds, as tune_cells
+        for combo in order:
+            r.blend_shape, r.tile_schedule, r.stage_entries = combo
             r.set_capacity(None)
             t = _time_steps(trainer, targets, steps)
-            timings[(shape, sched)] = min(t, timings.get((shape, sched), t))
+            timings[combo] = min(t, timings.get(combo, t))
             trainer.restore(state)
             if log:
-                log(f"blend shape {shape}, schedule {sched}: {t:.2f} ms per step")
+                log(f"blend shape {combo[0]}, schedule {combo[1]}, stage {combo[2]}: {t:.2f} ms per step")
     best = min(timings, key=timings.get)
-    r.blend_shape, r.tile_schedule = best
+    r.blend_shape, r.tile_schedule, r.stage_entries = best
     r.set_capacity(saved_capacity)
     tune_blend.last_timings = timings
     _CACHE[key] = best

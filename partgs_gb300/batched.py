@@ -50,7 +50,7 @@ class MultiViewRasterizer:
 
     def __init__(self, cameras, bg, sh_degree=3, variant=L.SGR_VARIANT_PLAIN, bin_capacity=None,
                  scene_sizes=None, scene_views=None, num_surfels=None, device="cuda", cell_tiles=0, blend_shape=0,
-                 tile_schedule=0):
+                 tile_schedule=0, stage_entries=0):
         dev = torch.device(device)
         self.cameras = list(cameras)
         self.variant = variant
@@ -59,6 +59,7 @@ class MultiViewRasterizer:
         self.cell_tiles = cell_tiles
         self.blend_shape = blend_shape          # L.SGR_BLEND_*
         self.tile_schedule = tile_schedule      # L.SGR_SCHEDULE_*
+        self.stage_entries = stage_entries      # 0 or L.SGR_STAGE_*
         self.bg = torch.as_tensor(bg, dtype=torch.float32, device=dev)
         vm = torch.stack([torch.as_tensor(c.world_view_transform, dtype=torch.float32) for c in cameras])
         pm = torch.stack([torch.as_tensor(c.full_proj_transform, dtype=torch.float32) for c in cameras])
@@ -124,7 +125,7 @@ class MultiViewRasterizer:
             self.variant, means3D, opacities, shs, colors_precomp, scales, rotations, None, semantics, self.viewset,
             self.bg, self.sh_degree, 1.0, False, bin_capacity=self.bin_capacity, tables=self.tables,
             status_host=self.status, cell_tiles=self.cell_tiles, blend_shape=self.blend_shape,
-            tile_schedule=self.tile_schedule)
+            tile_schedule=self.tile_schedule, stage_entries=self.stage_entries)
         self.last_state = state                   # for inspection (bench counters)
         # sticky record of every forward since the last reset: flags OR-ed,
         # largest cell-list entry count (device side, so captured steps keep it)

@@ -26,6 +26,7 @@
 // backward's reciprocals are the hardware's approximate ones (splat_exp,
 // blend_rcp): a few 1e-7 relative on alpha, far inside the tolerances.
 #include <algorithm>
+#include <type_traits>
 
 #include "sgr_kernels.cuh"
 
@@ -34,8 +35,12 @@ namespace sgr {
 namespace {
 
 constexpr int kWarps = kBlock / 32;
-constexpr int kRing = 2048;            // ring of streamed list entries: >= kBlock + kChunk, a power of two
-static_assert(kRing >= kBlock + kChunk && (kRing & (kRing - 1)) == 0, "ring size");
+// Entries per staged batch of the blends (sgr_batch.stage_entries): the
+// default, and the smaller option.
+constexpr int kStageDefault = 256, kStageSmall = 128;
+constexpr int kRing = 2048;            // ring of streamed list entries: >= a batch + kChunk, a power of two
+static_assert(kRing >= kStageDefault + kChunk && (kRing & (kRing - 1)) == 0, "ring size");
+static_assert(kStageDefault <= 256 && kStageSmall <= kStageDefault, "staged slots are indexed by uint8_t");
 
 struct Strip {
   float x0, x1;       // pixel-centre x range of the tile
@@ -448,10 +453,10 @@ struct FwdPixel {
   uint32_t stop;   // list position (1-based) of the entry that ended the pixel, 0 while open
 };
 
-// One fragment of the forward for one pixel: entry j of the staged batch,
-// list position contributor - 1 (P0/cr/forward.cu:349-430).
-template <int VARIANT>
-__device__ __forceinline__ void fwd_fragment(FwdPixel<VARIANT>& q, const float4 (*s_rec)[kBlock],
+// One fragment of the forward for one pixel: entry j of the staged batch of
+// SB entries, list position contributor - 1 (P0/cr/forward.cu:349-430).
+template <int VARIANT, int SB>
+__device__ __forceinline__ void fwd_fragment(FwdPixel<VARIANT>& q, const float4 (*s_rec)[SB],
                                              const float4* s_sem4, int j, uint32_t contributor, int S,
                                              float4* sem_acc4) {
   if (q.done) return;
@@ -545,7 +550,7 @@ __device__ __forceinline__ void fwd_fragment(FwdPixel<VARIANT>& q, const float4 
     q.C[2] += r4.z * alpha * q.T;
     // four channels at a time; channels past S are zero in the staged values
     for (int g4 = 0; g4 < (S + 3) / 4; ++g4) {
-      const float4 x = s_sem4[g4 * kBlock + j];
+      const float4 x = s_sem4[g4 * SB + j];
       float4 a = sem_acc4[g4 * kBlock];
       a.x += x.x * alpha * q.T;
       a.y += x.y * alpha * q.T;
@@ -578,9 +583,10 @@ struct FwdPair {
 // as the backward does; the accumulation as packed operations, zero-weighted
 // on a lane whose fragment does not count.  The part variant's semantic sums
 // sit in shared memory: pixel i of this thread at sem_acc4[g4 * kBlock + i *
-// NT] for channels 4 g4 .. 4 g4 + 3.
-template <int VARIANT, int NT>
-__device__ __forceinline__ void fwd_fragment2(FwdPair& q, const float4 (*s_rec)[kBlock], int j,
+// NT] for channels 4 g4 .. 4 g4 + 3; the staged semantics of entry j at
+// s_sem4[g4 * SB + j].
+template <int VARIANT, int NT, int SB>
+__device__ __forceinline__ void fwd_fragment2(FwdPair& q, const float4 (*s_rec)[SB], int j,
                                               uint32_t contributor, const float4* s_sem4, int S,
                                               float4* sem_acc4) {
   if (q.done[0] && q.done[1]) return;
@@ -652,7 +658,7 @@ __device__ __forceinline__ void fwd_fragment2(FwdPair& q, const float4 (*s_rec)[
   if (VARIANT == SGR_VARIANT_PART) {
     // four channels at a time; channels past S are zero in the staged values
     for (int g4 = 0; g4 < (S + 3) / 4; ++g4) {
-      const float4 x = s_sem4[g4 * kBlock + j];
+      const float4 x = s_sem4[g4 * SB + j];
 #pragma unroll
       for (int i = 0; i < 2; ++i) {
         if (!(i == 0 ? a0 : a1)) continue;
@@ -687,7 +693,7 @@ __device__ __forceinline__ void fwd_fragment2(FwdPair& q, const float4 (*s_rec)[
 #endif
 
 // The forward of one tile (all threads of the CTA).
-template <int VARIANT, int WX>
+template <int VARIANT, int WX, int SB>
 __device__ __forceinline__ void render_fwd_tile(const sgr_batch& b, const GeomView& g, const sgr_fwd_outputs& out,
                                                 const int tile) {
   using Shape = FwdShapeT<VARIANT, WX>;
@@ -704,19 +710,20 @@ __device__ __forceinline__ void render_fwd_tile(const sgr_batch& b, const GeomVi
   const sgr_view_desc vd = b.views[v];
   const int sid_base = b.scenes[vd.scene].surfel_offset - vd.record_offset;
 
-  __shared__ float4 s_rec[kRecF4 - 1][kBlock];
-  __shared__ uint8_t s_mask[kBlock];
-  __shared__ uint8_t s_list[NW][kBlock];
+  __shared__ float4 s_rec[kRecF4 - 1][SB];
+  __shared__ uint8_t s_mask[SB];
+  __shared__ uint8_t s_list[NW][SB];
   __shared__ uint32_t s_ring[kRing];
   __shared__ int s_count[32];
-  // part variant, sized by S at launch (fwd_dynamic_smem): the staged
-  // semantics, four channels per float4, then every pixel's semantic sums
-  // (pixel i of a thread in column i * NT + thread); rows of kBlock float4
+  // part variant, sized by S at launch (fwd_dynamic_bytes): the staged
+  // semantics, four channels per float4 (rows of SB float4), then every
+  // pixel's semantic sums (rows of kBlock float4, pixel i of a thread in
+  // column i * NT + thread)
   extern __shared__ float4 s_dyn4[];
   static_assert(NT * PX == kBlock, "one column per pixel");
   const int NS4 = (S + 3) / 4;
   float4* const s_sem4 = s_dyn4;
-  float4* const sem_acc4 = (VARIANT == SGR_VARIANT_PART) ? s_dyn4 + NS4 * kBlock + threadIdx.x : nullptr;
+  float4* const sem_acc4 = (VARIANT == SGR_VARIANT_PART) ? s_dyn4 + NS4 * SB + threadIdx.x : nullptr;
 
   const uint32_t* list;
   int len;
@@ -766,15 +773,15 @@ __device__ __forceinline__ void render_fwd_tile(const sgr_batch& b, const GeomVi
     }
   }
 
-  for (;; base += kBlock, head += kBlock) {
+  for (;; base += SB, head += SB) {
     if (__syncthreads_count(done) == NT) break;
-    while (tail - head < kBlock && scanned < len) {   // refill the ring (CTA-uniform)
+    while (tail - head < SB && scanned < len) {   // refill the ring (CTA-uniform)
       int found;
       tail += stream_window<false, NT>(g, list, scanned, min(scanned + kChunk, len), (uint32_t)tx, (uint32_t)ty, 0,
                                        0, s_ring, tail, s_count, found);
       scanned = min(scanned + kChunk, len);
     }
-    const int n = min(kBlock, tail - head);
+    const int n = min(SB, tail - head);
     if (n <= 0) break;
     for (int e = threadIdx.x; e < n; e += NT) {
       const uint32_t r = s_ring[(head + e) & (kRing - 1)];
@@ -789,7 +796,7 @@ __device__ __forceinline__ void render_fwd_tile(const sgr_batch& b, const GeomVi
         const float* sem = b.semantics + (size_t)(sid_base + (int)r) * S;
         for (int g4 = 0; g4 < (S + 3) / 4; ++g4) {
           const int c = 4 * g4;
-          s_sem4[g4 * kBlock + e] = make_float4(sem[c], c + 1 < S ? sem[c + 1] : 0.f, c + 2 < S ? sem[c + 2] : 0.f,
+          s_sem4[g4 * SB + e] = make_float4(sem[c], c + 1 < S ? sem[c + 1] : 0.f, c + 2 < S ? sem[c + 2] : 0.f,
                                                 c + 3 < S ? sem[c + 3] : 0.f);
         }
       }
@@ -889,8 +896,9 @@ __device__ __forceinline__ void render_fwd_tile(const sgr_batch& b, const GeomVi
   }
 }
 
-// One CTA per tile, or persistent CTAs taking tiles from a queue.
-template <int VARIANT, int WX>
+// One CTA per tile, or persistent CTAs taking tiles from a queue; SB list
+// entries per staged batch.
+template <int VARIANT, int WX, int SB>
 __global__ void __launch_bounds__(FwdShapeT<VARIANT, WX>::NT,
                                   (VARIANT == SGR_VARIANT_PLAIN) ? SGR_FWD_MIN_CTAS : SGR_PART_FWD_MIN_CTAS)
     k_render_fwd(const sgr_batch b, GeomView g, sgr_fwd_outputs out, TileQueue q) {
@@ -907,7 +915,7 @@ __global__ void __launch_bounds__(FwdShapeT<VARIANT, WX>::NT,
       if (it > 0) return;
       tile = blockIdx.x;
     }
-    render_fwd_tile<VARIANT, WX>(b, g, out, tile);
+    render_fwd_tile<VARIANT, WX, SB>(b, g, out, tile);
   }
 }
 
@@ -1372,7 +1380,7 @@ __device__ __forceinline__ void bwd_update2(BwdPair& q, const BwdGeom2& f, const
 #endif
 
 // The backward of one tile (all threads of the CTA).
-template <int VARIANT, int WX>
+template <int VARIANT, int WX, int SB>
 __device__ __forceinline__ void render_bwd_tile(const sgr_batch& b, const GeomView& g, const sgr_bwd_inputs& in,
                                                 float* __restrict__ grads, float* __restrict__ dL_dsemantics,
                                                 const int tile) {
@@ -1393,10 +1401,10 @@ __device__ __forceinline__ void render_bwd_tile(const sgr_batch& b, const GeomVi
   const sgr_view_desc vd = b.views[v];
   const int sid_base = b.scenes[vd.scene].surfel_offset - vd.record_offset;
 
-  __shared__ float4 s_rec[kRecF4 - 1][kBlock];
-  __shared__ uint32_t s_id[kBlock];
-  __shared__ uint8_t s_mask[kBlock];
-  __shared__ uint8_t s_list[NW][kBlock];
+  __shared__ float4 s_rec[kRecF4 - 1][SB];
+  __shared__ uint32_t s_id[SB];
+  __shared__ uint8_t s_mask[SB];
+  __shared__ uint8_t s_list[NW][SB];
   __shared__ __align__(16) float s_dsem[NS][NT * PX];   // part variant: each pixel's dL/dpixel semantics
   __shared__ int s_max[NW];
   __shared__ uint32_t s_ring[kRing];
@@ -1477,8 +1485,8 @@ __device__ __forceinline__ void render_bwd_tile(const sgr_batch& b, const GeomVi
   int pos_end = (int)resume.y;                     // tile-list position after them
   const int top = min(block_max, pos_end);
   int head = 0, tail = 0;
-  for (int hi = top; hi > 0; hi -= kBlock, head += kBlock) {
-    while (tail - head < kBlock && scan_end > 0) {   // refill the ring (CTA-uniform)
+  for (int hi = top; hi > 0; hi -= SB, head += SB) {
+    while (tail - head < SB && scan_end > 0) {   // refill the ring (CTA-uniform)
       const int i0 = max(0, scan_end - kChunk);
       int found;
       tail += stream_window<true, NT>(g, list, i0, scan_end, (uint32_t)tx, (uint32_t)ty, pos_end, top, s_ring,
@@ -1486,7 +1494,7 @@ __device__ __forceinline__ void render_bwd_tile(const sgr_batch& b, const GeomVi
       pos_end -= found;
       scan_end = i0;
     }
-    const int n = min(kBlock, hi);
+    const int n = min(SB, hi);
     if (tail - head < n) {                         // index inconsistent with the rectangles: stop
       if (threadIdx.x == 0) atomicOr(&g.status->flags, SGR_FLAG_LIST_INCONSISTENT);
       break;
@@ -1609,7 +1617,7 @@ __device__ __forceinline__ void render_bwd_tile(const sgr_batch& b, const GeomVi
   }
 }
 
-template <int VARIANT, int WX>
+template <int VARIANT, int WX, int SB>
 __global__ void __launch_bounds__(BwdShapeT<VARIANT>::NT,
                                   (VARIANT == SGR_VARIANT_PLAIN) ? SGR_BWD_MIN_CTAS : SGR_PART_BWD_MIN_CTAS)
     k_render_bwd(const sgr_batch b, GeomView g, const sgr_bwd_inputs in, float* __restrict__ grads,
@@ -1627,7 +1635,7 @@ __global__ void __launch_bounds__(BwdShapeT<VARIANT>::NT,
       if (it > 0) return;
       tile = blockIdx.x;
     }
-    render_bwd_tile<VARIANT, WX>(b, g, in, grads, dL_dsemantics, tile);
+    render_bwd_tile<VARIANT, WX, SB>(b, g, in, grads, dL_dsemantics, tile);
   }
 }
 
@@ -1665,66 +1673,82 @@ __global__ void __launch_bounds__(1024) k_tile_order(GeomView g, int n, int back
   for (int i = threadIdx.x; i < n; i += blockDim.x) order[atomicAdd(&s_pos[32 - __clz(cost(i))], 1u)] = (uint32_t)i;
 }
 
-// Resident CTAs of a kernel on the current device, with `rows` rows of
-// kBlock float4 of dynamic shared memory (queried once per kernel, device and
-// row count).
+// Resident CTAs of a kernel on the current device with `dyn` bytes of
+// dynamic shared memory (queried once per kernel, device and size).
 template <class F>
-int resident_ctas(F kernel, int threads, int rows = 0) {
-  constexpr int kMaxDev = 64, kMaxRows = 2 * ((SGR_MAX_SEMANTICS + 3) / 4);
-  static int cache[kMaxDev][kMaxRows + 1] = {};
+int resident_ctas(F kernel, int threads, size_t dyn = 0) {
+  struct Entry {
+    const void* kernel;
+    int dev;
+    size_t dyn;
+    int ctas;
+  };
+  constexpr int kEntries = 256;
+  static Entry cache[kEntries] = {};
+  static int used = 0;
   int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDev || rows < 0 || rows > kMaxRows) return 0;
-  if (cache[dev][rows] == 0) {
-    int per_sm = 0, sms = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads,
-                                                      (size_t)rows * kBlock * sizeof(float4)) != cudaSuccess ||
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
-      return 0;
-    cache[dev][rows] = per_sm * sms;
-  }
-  return cache[dev][rows];
+  if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+  const void* key = reinterpret_cast<const void*>(kernel);
+  for (int i = 0; i < used; ++i)
+    if (cache[i].kernel == key && cache[i].dev == dev && cache[i].dyn == dyn) return cache[i].ctas;
+  int per_sm = 0, sms = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, dyn) != cudaSuccess ||
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+    return 0;
+  if (used < kEntries) cache[used++] = Entry{key, dev, dyn, per_sm * sms};
+  return per_sm * sms;
 }
 
-// Rows of kBlock float4 of the forward's dynamic shared memory: none for the
-// plain variant; the part variant's staged semantics and per-pixel sums,
-// (S + 3) / 4 rows each.
-inline int fwd_dynamic_rows(const sgr_batch& b) {
-  return b.variant == SGR_VARIANT_PART ? 2 * ((b.semantic_channels + 3) / 4) : 0;
+// Bytes of the forward's dynamic shared memory: none for the plain variant;
+// for the part variant, (S + 3) / 4 rows of SB float4 (staged semantics) and
+// as many rows of kBlock float4 (every pixel's semantic sums).
+template <int SB>
+size_t fwd_dynamic_bytes(const sgr_batch& b) {
+  const int rows = b.variant == SGR_VARIANT_PART ? (b.semantic_channels + 3) / 4 : 0;
+  return (size_t)rows * (SB + kBlock) * sizeof(float4);
 }
 
 // Lets a kernel take the largest dynamic shared memory the part variant asks
 // for (once per kernel and device).
 template <class F>
-void allow_dynamic_smem(F kernel) {
-  constexpr int kMaxDev = 64;
-  static bool done[kMaxDev] = {};
+void allow_dynamic_smem(F kernel, int bytes) {
+  struct Entry {
+    const void* kernel;
+    int dev;
+  };
+  constexpr int kEntries = 256;
+  static Entry done[kEntries] = {};
+  static int used = 0;
   int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDev || done[dev]) return;
-  cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       2 * ((SGR_MAX_SEMANTICS + 3) / 4) * kBlock * (int)sizeof(float4));
-  done[dev] = true;
+  if (cudaGetDevice(&dev) != cudaSuccess) return;
+  const void* key = reinterpret_cast<const void*>(kernel);
+  for (int i = 0; i < used; ++i)
+    if (done[i].kernel == key && done[i].dev == dev) return;
+  cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (used < kEntries) done[used++] = Entry{key, dev};
 }
 
-template <int VARIANT, int WX>
+template <int VARIANT, int WX, int SB>
 void launch_fwd(const sgr_batch& b, const GeomView& g, const sgr_fwd_outputs& out, TileQueue q, unsigned tiles,
                 cudaStream_t st) {
-  auto* k = k_render_fwd<VARIANT, WX>;
-  const int rows = fwd_dynamic_rows(b);
-  if (VARIANT == SGR_VARIANT_PART) allow_dynamic_smem(k);
+  auto* k = k_render_fwd<VARIANT, WX, SB>;
+  const size_t dyn = fwd_dynamic_bytes<SB>(b);
+  if (VARIANT == SGR_VARIANT_PART)
+    allow_dynamic_smem(k, (int)(((SGR_MAX_SEMANTICS + 3) / 4) * (SB + kBlock) * sizeof(float4)));
   unsigned grid = tiles;
   if (q.order) {
     k_tile_order<<<1, 1024, 0, st>>>(g, (int)tiles, 0, const_cast<uint32_t*>(q.order), q.next);
     count_launches();
-    const int r = resident_ctas(k, FwdShapeT<VARIANT, WX>::NT, rows);
+    const int r = resident_ctas(k, FwdShapeT<VARIANT, WX>::NT, dyn);
     grid = r > 0 ? std::min<unsigned>(tiles, (unsigned)r) : tiles;
   }
-  k<<<grid, FwdShapeT<VARIANT, WX>::NT, (size_t)rows * kBlock * sizeof(float4), st>>>(b, g, out, q);
+  k<<<grid, FwdShapeT<VARIANT, WX>::NT, dyn, st>>>(b, g, out, q);
 }
 
-template <int VARIANT, int WX>
+template <int VARIANT, int WX, int SB>
 void launch_bwd(const sgr_batch& b, const GeomView& g, const sgr_bwd_inputs& in, float* grads, float* dsem,
                 TileQueue q, unsigned tiles, cudaStream_t st) {
-  auto* k = k_render_bwd<VARIANT, WX>;
+  auto* k = k_render_bwd<VARIANT, WX, SB>;
   constexpr int NT = BwdShapeT<VARIANT>::NT;
   unsigned grid = tiles;
   if (q.order) {
@@ -1734,6 +1758,35 @@ void launch_bwd(const sgr_batch& b, const GeomView& g, const sgr_bwd_inputs& in,
     grid = r > 0 ? std::min<unsigned>(tiles, (unsigned)r) : tiles;
   }
   k<<<grid, NT, 0, st>>>(b, g, in, grads, dsem, q);
+}
+
+// Entries per staged batch for a batch's launch: as asked, or by default
+// 256, except 128 for the part variant above 12 semantic channels.  There
+// the 256-entry forward needs 62 KB of shared memory per CTA and fits 3 CTAs
+// per SM; the 128-entry one needs 43 KB and fits 4 (measured at 16 channels:
+// forward 19.4 -> 16.3 ms, backward unchanged).
+inline int stage_entries_of(const sgr_batch& b) {
+  if (b.stage_entries == SGR_STAGE_SMALL || b.stage_entries == SGR_STAGE_DEFAULT) return b.stage_entries;
+  return (b.variant == SGR_VARIANT_PART && b.semantic_channels > 12) ? SGR_STAGE_SMALL : SGR_STAGE_DEFAULT;
+}
+
+// Calls fn(variant, warp patch width, staged batch) as integral constants
+// for the batch's launch options.
+template <class Fn>
+void with_blend_shape(const sgr_batch& b, Fn&& fn) {
+  using std::integral_constant;
+  static_assert(kStageSmall == SGR_STAGE_SMALL && kStageDefault == SGR_STAGE_DEFAULT, "staged batch sizes");
+  const bool narrow = b.blend_shape == SGR_BLEND_PATCH8;
+  const bool small = stage_entries_of(b) == SGR_STAGE_SMALL;
+  auto by_stage = [&](auto variant, auto wx) {
+    small ? fn(variant, wx, integral_constant<int, kStageSmall>{})
+          : fn(variant, wx, integral_constant<int, kStageDefault>{});
+  };
+  auto by_width = [&](auto variant) {
+    narrow ? by_stage(variant, integral_constant<int, 8>{}) : by_stage(variant, integral_constant<int, kTile>{});
+  };
+  b.variant == SGR_VARIANT_PLAIN ? by_width(integral_constant<int, SGR_VARIANT_PLAIN>{})
+                                 : by_width(integral_constant<int, SGR_VARIANT_PART>{});
 }
 
 TileQueue tile_queue(const sgr_batch& b, const GeomView& g, unsigned tiles) {
@@ -1749,13 +1802,9 @@ void launch_render_fwd(const sgr_batch& b, const GeomView& g, const sgr_fwd_outp
   const unsigned tiles = (unsigned)(g.tiles_x * g.tiles_y) * (unsigned)b.num_views;
   if (tiles == 0) return;
   const TileQueue q = tile_queue(b, g, tiles);
-  const bool narrow = b.blend_shape == SGR_BLEND_PATCH8;
-  if (b.variant == SGR_VARIANT_PLAIN)
-    narrow ? launch_fwd<SGR_VARIANT_PLAIN, 8>(b, g, out, q, tiles, st)
-           : launch_fwd<SGR_VARIANT_PLAIN, kTile>(b, g, out, q, tiles, st);
-  else
-    narrow ? launch_fwd<SGR_VARIANT_PART, 8>(b, g, out, q, tiles, st)
-           : launch_fwd<SGR_VARIANT_PART, kTile>(b, g, out, q, tiles, st);
+  with_blend_shape(b, [&](auto variant, auto wx, auto sb) {
+    launch_fwd<decltype(variant)::value, decltype(wx)::value, decltype(sb)::value>(b, g, out, q, tiles, st);
+  });
   count_launches();
 }
 
@@ -1764,13 +1813,10 @@ void launch_render_bwd(const sgr_batch& b, const GeomView& g, const sgr_bwd_inpu
   const unsigned tiles = (unsigned)(g.tiles_x * g.tiles_y) * (unsigned)b.num_views;
   if (tiles == 0) return;
   const TileQueue q = tile_queue(b, g, tiles);
-  const bool narrow = b.blend_shape == SGR_BLEND_PATCH8;
-  if (b.variant == SGR_VARIANT_PLAIN)
-    narrow ? launch_bwd<SGR_VARIANT_PLAIN, 8>(b, g, in, grads, dL_dsemantics, q, tiles, st)
-           : launch_bwd<SGR_VARIANT_PLAIN, kTile>(b, g, in, grads, dL_dsemantics, q, tiles, st);
-  else
-    narrow ? launch_bwd<SGR_VARIANT_PART, 8>(b, g, in, grads, dL_dsemantics, q, tiles, st)
-           : launch_bwd<SGR_VARIANT_PART, kTile>(b, g, in, grads, dL_dsemantics, q, tiles, st);
+  with_blend_shape(b, [&](auto variant, auto wx, auto sb) {
+    launch_bwd<decltype(variant)::value, decltype(wx)::value, decltype(sb)::value>(b, g, in, grads, dL_dsemantics,
+                                                                                    q, tiles, st);
+  });
   count_launches();
 }
 

@@ -111,7 +111,7 @@ def _tables(variant, P, vs: ViewSet, device):
 
 def make_batch(variant, means3D, opacities, shs, colors_precomp, scales, rotations, transmat_precomp, semantics,
                vs: ViewSet, bg, sh_degree, scale_modifier, prefiltered, tables=None, cell_tiles=0, blend_shape=0,
-               tile_schedule=0):
+               tile_schedule=0, stage_entries=0):
     if means3D.dim() != 2 or means3D.shape[1] != 3:
         raise ValueError("means3D must have dimensions (num_points, 3)")
     if variant == L.SGR_VARIANT_PART and semantics is not None and semantics.dim() == 2 and \
@@ -164,6 +164,7 @@ def make_batch(variant, means3D, opacities, shs, colors_precomp, scales, rotatio
     b.cell_tiles = int(cell_tiles)
     b.blend_shape = int(blend_shape)
     b.tile_schedule = int(tile_schedule)
+    b.stage_entries = int(stage_entries)
     b.scale_modifier = float(scale_modifier)
     b.scenes = sct.data_ptr()
     b.views = vwt.data_ptr()
@@ -175,7 +176,7 @@ def make_batch(variant, means3D, opacities, shs, colors_precomp, scales, rotatio
 
 def forward(variant, means3D, opacities, shs, colors_precomp, scales, rotations, transmat_precomp, semantics,
             vs: ViewSet, bg, sh_degree=0, scale_modifier=1.0, prefiltered=False, bin_capacity=None, tables=None,
-            status_host=None, cell_tiles=0, blend_shape=0, tile_schedule=0):
+            status_host=None, cell_tiles=0, blend_shape=0, tile_schedule=0, stage_entries=0):
     """Rasterises every view of ``vs``.  Returns (color [V,3,H,W], others
     [V,7|8,H,W], semantic [V,S,H,W] or None, radii [R] int32, state).
 
@@ -190,12 +191,14 @@ def forward(variant, means3D, opacities, shs, colors_precomp, scales, rotations,
     default; ``autotune.tune_cells`` picks one per workload).  ``blend_shape``
     (SGR_BLEND_STRIP16 / SGR_BLEND_PATCH8) and ``tile_schedule``
     (SGR_SCHEDULE_GRID / SGR_SCHEDULE_QUEUE) choose how the blends group
-    pixels into warps and hand tiles to CTAs; results do not depend on them
+    pixels into warps and hand tiles to CTAs, ``stage_entries`` (0 /
+    SGR_STAGE_DEFAULT / SGR_STAGE_SMALL) how many list entries they stage in
+    shared memory at a time; results do not depend on them
     (``autotune.tune_blend`` picks them per workload)."""
     lib = L.load()
     b, keep, t = make_batch(variant, means3D, opacities, shs, colors_precomp, scales, rotations, transmat_precomp,
                             semantics, vs, bg, sh_degree, scale_modifier, prefiltered, tables, cell_tiles,
-                            blend_shape, tile_schedule)
+                            blend_shape, tile_schedule, stage_entries)
     device = means3D.device
     s0 = L.Sizes()
     L.check(lib.sgr_query_sizes(C.byref(b), 0, C.byref(s0)), "sgr_query_sizes")

@@ -2,7 +2,7 @@
 autograd, no loss kernels or optimiser) for either variant:
 
   python -m partgs_gb300.timing [--workload sq500k_16x800x600] [--semantics 8] [--steps 5]
-                                [--cell-tiles 2] [--blend-shape 0] [--tile-schedule 1]
+                                [--cell-tiles 2] [--blend-shape 0] [--tile-schedule 1] [--stage-entries 128]
 
 Prints one JSON line per variant with the library's CUDA-event phase times
 (ms per call).  The part variant gets ``--semantics`` channels of seeded
@@ -32,14 +32,15 @@ from .scenes import workload
 
 
 def time_variant(scene, cams, variant, semantics=None, steps=5, warmup=3, cell_tiles=0, blend_shape=0,
-                 tile_schedule=0):
+                 tile_schedule=0, stage_entries=0):
     dev = torch.device("cuda")
     lib = L.load()
     P = scene.P
     means, op = scene.means3D.to(dev), scene.opacities.to(dev)
     shs, sc, rot = scene.shs.to(dev), scene.scales.to(dev), scene.rotations.to(dev)
     r = MultiViewRasterizer(cams, [0, 0, 0], scene.sh_degree, variant=variant, num_surfels=P, device=dev,
-                            cell_tiles=cell_tiles, blend_shape=blend_shape, tile_schedule=tile_schedule)
+                            cell_tiles=cell_tiles, blend_shape=blend_shape, tile_schedule=tile_schedule,
+                            stage_entries=stage_entries)
 
     def step():
         m = means.clone().requires_grad_(True)
@@ -121,6 +122,7 @@ def main(argv=None):
     ap.add_argument("--cell-tiles", type=int, default=0)
     ap.add_argument("--blend-shape", type=int, default=0, help="0: 16-wide warp strips, 1: 8-wide patches")
     ap.add_argument("--tile-schedule", type=int, default=0, help="0: a CTA per tile, 1: persistent tile queue")
+    ap.add_argument("--stage-entries", type=int, default=0, help="list entries per staged batch: 0 (256) or 128")
     ap.add_argument("--multi-scene", action="store_true")
     ap.add_argument("--scenes", type=int, default=32)
     a = ap.parse_args(argv)
@@ -132,7 +134,7 @@ def main(argv=None):
     sem = torch.softmax(torch.randn(scene.P, a.semantics, generator=g) * 3, -1).cuda()
     for variant, name, s in ((L.SGR_VARIANT_PLAIN, "plain", None), (L.SGR_VARIANT_PART, "part", sem)):
         ph = time_variant(scene, cams, variant, s, a.steps, cell_tiles=a.cell_tiles, blend_shape=a.blend_shape,
-                          tile_schedule=a.tile_schedule)
+                          tile_schedule=a.tile_schedule, stage_entries=a.stage_entries)
         print(json.dumps({"variant": name, "workload": a.workload, "semantics": a.semantics if s is not None else 0,
                           "phase_ms": ph}), flush=True)
 

@@ -1,7 +1,8 @@
-"""The launch-shape autotuners: every candidate cell edge, warp footprint
-and tile schedule renders the same images (they only change how tiles find
-their lists and how pixels and tiles are handed to warps and CTAs), the
-tuners restore the parameters they trained through, and pick a candidate."""
+"""The launch-shape autotuners: every candidate cell edge, warp footprint,
+tile schedule and staged batch renders the same images (they only change
+how tiles find their lists, how pixels and tiles are handed to warps and
+CTAs, and how many list entries are staged at a time), the tuners restore
+the parameters they trained through, and pick a candidate."""
 import pytest
 import torch
 
@@ -40,9 +41,9 @@ def test_tuner_picks_a_candidate_and_restores_the_parameters(sgr_lib):
 
 
 def test_warp_footprint_and_schedule_do_not_change_the_results(sgr_lib):
-    """Both warp footprints and both tile schedules: identical images and
-    radii (every pixel walks the same list with the same arithmetic), and
-    gradients equal up to the order of the float atomics."""
+    """Both warp footprints, both tile schedules and both staged batches:
+    identical images and radii (every pixel walks the same list with the same
+    arithmetic), and gradients equal up to the order of the float atomics."""
     from partgs_gb300 import _lib as L
     from partgs_gb300.batched import MultiViewRasterizer
     from partgs_gb300.cameras import orbit_cameras
@@ -55,16 +56,53 @@ def test_warp_footprint_and_schedule_do_not_change_the_results(sgr_lib):
     outs = []
     for shape in (L.SGR_BLEND_STRIP16, L.SGR_BLEND_PATCH8):
         for sched in (L.SGR_SCHEDULE_GRID, L.SGR_SCHEDULE_QUEUE):
-            leaves = [t.clone().requires_grad_(True) for t in (sc.means3D, sc.opacities, sc.shs, sc.scales,
-                                                                sc.rotations)]
-            mv = MultiViewRasterizer(cams, [0.1, 0.2, 0.3], 3, num_surfels=3000, blend_shape=shape,
-                                     tile_schedule=sched)
-            img, amap, _, radii = mv(*leaves)
-            ((img * up_c).sum() + (amap * up_o).sum()).backward()
-            outs.append((img.detach(), amap.detach(), radii, [t.grad for t in leaves]))
+            for stage in (L.SGR_STAGE_DEFAULT, L.SGR_STAGE_SMALL):
+                leaves = [t.clone().requires_grad_(True) for t in (sc.means3D, sc.opacities, sc.shs, sc.scales,
+                                                                    sc.rotations)]
+                mv = MultiViewRasterizer(cams, [0.1, 0.2, 0.3], 3, num_surfels=3000, blend_shape=shape,
+                                         tile_schedule=sched, stage_entries=stage)
+                img, amap, _, radii = mv(*leaves)
+                ((img * up_c).sum() + (amap * up_o).sum()).backward()
+                outs.append((img.detach(), amap.detach(), radii, [t.grad for t in leaves]))
     for img, amap, radii, grads in outs[1:]:
         assert torch.equal(img, outs[0][0]) and torch.equal(amap, outs[0][1]) and torch.equal(radii, outs[0][2])
         for a, b in zip(grads, outs[0][3]):
+            assert float((a - b).norm() / b.norm()) < 1e-5
+
+
+@pytest.mark.parametrize("channels", [5, 16])
+def test_part_variant_launch_options_do_not_change_the_results(sgr_lib, channels):
+    """The part variant (semantic sums and staged semantics in shared memory
+    sized by the channel count and the staged batch): identical images,
+    semantics and radii for every footprint, schedule and staged batch;
+    gradients equal up to the order of the float atomics."""
+    from partgs_gb300 import _lib as L
+    from partgs_gb300.batched import MultiViewRasterizer
+    from partgs_gb300.cameras import orbit_cameras
+    from partgs_gb300.scenes import random_surfels
+    sc = random_surfels(3000, seed=53).to("cuda")
+    cams = orbit_cameras(2, 3.0, 80, 112, 55.0, seed=10)
+    g = torch.Generator(device="cuda").manual_seed(5)
+    sem0 = torch.softmax(torch.randn(3000, channels, device="cuda", generator=g) * 2, -1)
+    up_c = torch.randn(2, 3, 80, 112, device="cuda", generator=g)
+    up_o = torch.randn(2, 8, 80, 112, device="cuda", generator=g) * 0.1
+    up_s = torch.randn(2, channels, 80, 112, device="cuda", generator=g)
+    outs = []
+    for shape in (L.SGR_BLEND_STRIP16, L.SGR_BLEND_PATCH8):
+        for sched in (L.SGR_SCHEDULE_GRID, L.SGR_SCHEDULE_QUEUE):
+            for stage in (L.SGR_STAGE_DEFAULT, L.SGR_STAGE_SMALL):
+                leaves = [t.clone().requires_grad_(True) for t in (sc.means3D, sc.opacities, sc.shs, sc.scales,
+                                                                    sc.rotations)]
+                sem = sem0.clone().requires_grad_(True)
+                mv = MultiViewRasterizer(cams, [0.1, 0.2, 0.3], 3, variant=L.SGR_VARIANT_PART, num_surfels=3000,
+                                         blend_shape=shape, tile_schedule=sched, stage_entries=stage)
+                img, amap, smap, radii = mv(*leaves, semantics=sem)
+                ((img * up_c).sum() + (amap * up_o).sum() + (smap * up_s).sum()).backward()
+                outs.append((img.detach(), amap.detach(), smap.detach(), radii, [t.grad for t in leaves + [sem]]))
+    for img, amap, smap, radii, grads in outs[1:]:
+        assert torch.equal(img, outs[0][0]) and torch.equal(amap, outs[0][1])
+        assert torch.equal(smap, outs[0][2]) and torch.equal(radii, outs[0][3])
+        for a, b in zip(grads, outs[0][4]):
             assert float((a - b).norm() / b.norm()) < 1e-5
 
 
@@ -78,7 +116,7 @@ def test_blend_tuner_picks_a_pair(sgr_lib):
     tr = SurfelTrainer(scene, cams)
     before = [p.detach().clone() for p in tr.params()]
     best = autotune.tune_blend(tr, targets, steps=2)
-    assert best == (tr.raster.blend_shape, tr.raster.tile_schedule)
-    assert len(autotune.tune_blend.last_timings) == 4
+    assert best == (tr.raster.blend_shape, tr.raster.tile_schedule, tr.raster.stage_entries)
+    assert len(autotune.tune_blend.last_timings) == 8
     for p, q in zip(tr.params(), before):
         assert torch.equal(p.detach(), q)
