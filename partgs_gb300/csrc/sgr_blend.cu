@@ -147,7 +147,9 @@ __device__ __forceinline__ float blend_rcp(float x) {
 }
 
 // Sets sx, sy; returns the reciprocal of z it used (0 with divisions).
-__device__ __forceinline__ float splat_coords(float x, float y, float z, float& sx, float& sy) {
+// (The scalar helpers here serve the one-pixel-per-thread builds,
+// SGR_FWD_PACKED / SGR_PART_PACKED 0; the packed default leaves some unused.)
+[[maybe_unused]] __device__ __forceinline__ float splat_coords(float x, float y, float z, float& sx, float& sy) {
 #if SGR_SPLAT_DIV == 0
   sx = x / z;
   sy = y / z;
@@ -186,23 +188,23 @@ __device__ __forceinline__ float splat_rcp(float z) {
 // distance 2 (dx^2 + dy^2), s = p.xy / p.z by one approximate reciprocal,
 // rho3d = sx^2 + sy^2, depth (sx Tw.x + sy Tw.y) + Tw.z on the 3D branch.
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ float lmul(float a, float b) { return __fmul_rn(a, b); }
+[[maybe_unused]] __device__ __forceinline__ float lmul(float a, float b) { return __fmul_rn(a, b); }
 __device__ __forceinline__ float2 lmul(float2 a, float2 b) { return __fmul2_rn(a, b); }
-__device__ __forceinline__ float lfma(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+[[maybe_unused]] __device__ __forceinline__ float lfma(float a, float b, float c) { return __fmaf_rn(a, b, c); }
 __device__ __forceinline__ float2 lfma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
-__device__ __forceinline__ float ladd(float a, float b) { return __fadd_rn(a, b); }
+[[maybe_unused]] __device__ __forceinline__ float ladd(float a, float b) { return __fadd_rn(a, b); }
 __device__ __forceinline__ float2 ladd(float2 a, float2 b) { return __fadd2_rn(a, b); }
 // Per-lane select of a pair.
 __device__ __forceinline__ float2 sel2(bool a, bool b, float2 x, float2 y) {
   return make_float2(a ? x.x : y.x, b ? x.y : y.y);
 }
 template <class T> __device__ __forceinline__ T bc(float s);
-template <> __device__ __forceinline__ float bc<float>(float s) { return s; }
+template <> [[maybe_unused]] __device__ __forceinline__ float bc<float>(float s) { return s; }
 template <> __device__ __forceinline__ float2 bc<float2>(float s) { return make_float2(s, s); }
 
 // -k for k = fma(px, w, -u): -k itself for one pixel, fma(px, -w, u) for a
 // pair (a packed negation would cost an instruction).
-__device__ __forceinline__ float negk(float, float, float, float k) { return -k; }
+[[maybe_unused]] __device__ __forceinline__ float negk(float, float, float, float k) { return -k; }
 __device__ __forceinline__ float2 negk(float2 px, float w, float u, float2) {
   return lfma(px, bc<float2>(-w), bc<float2>(u));
 }
@@ -1557,60 +1559,60 @@ __device__ __forceinline__ void render_bwd_tile(const sgr_batch& b, const GeomVi
           }
           if (ch >= 0 && ch < S && st != 0.f) atomicAdd(dL_dsemantics + (size_t)(sid_base + (int)r) * S + ch, st);
         }
-        continue;
-      }
+      } else {
 #pragma unroll
-      for (int u = 0; u < 32; ++u) gv[u] = 0.f;
-      BwdGeom f[PX];
-      bool may = false;
+        for (int u = 0; u < 32; ++u) gv[u] = 0.f;
+        BwdGeom f[PX];
+        bool may = false;
 #pragma unroll
-      for (int i = 0; i < PX; ++i) {
-        f[i].live = false;
-        if (SPLIT == 1 || ((rows_live >> i) & 1u)) may |= bwd_reach<VARIANT>(q[i], r0, r1, r2, reach, pos, f[i]);
-      }
-      if (!__any_sync(0xffffffffu, may)) continue;  // uniform: no pixel of the warp within reach
-      bool ok = false;
+        for (int i = 0; i < PX; ++i) {
+          f[i].live = false;
+          if (SPLIT == 1 || ((rows_live >> i) & 1u)) may |= bwd_reach<VARIANT>(q[i], r0, r1, r2, reach, pos, f[i]);
+        }
+        if (!__any_sync(0xffffffffu, may)) continue;  // uniform: no pixel of the warp within reach
+        bool ok = false;
 #pragma unroll
-      for (int i = 0; i < PX; ++i) {
-        if (SPLIT == 1 || ((rows_live >> i) & 1u)) bwd_alpha<VARIANT>(r1, r2, f[i]);   // uniform
-        ok |= f[i].live;
-      }
-      if (!__any_sync(0xffffffffu, ok)) continue;
-      const float4 r3 = s_rec[3][j], r4 = s_rec[4][j];
+        for (int i = 0; i < PX; ++i) {
+          if (SPLIT == 1 || ((rows_live >> i) & 1u)) bwd_alpha<VARIANT>(r1, r2, f[i]);   // uniform
+          ok |= f[i].live;
+        }
+        if (!__any_sync(0xffffffffu, ok)) continue;
+        const float4 r3 = s_rec[3][j], r4 = s_rec[4][j];
 #pragma unroll
-      for (int i = 0; i < PX; ++i)
-        if (f[i].live) bwd_update<VARIANT>(q[i], f[i], r1, r2, r3, r4, pos, gv);
-      {
-        int which;
-        const float total = warp_sum18(gv, lane, which);
-        const uint32_t r = s_id[j];
-        if (which >= 0 && total != 0.f) atomicAdd(grads + (size_t)r * kGradF + which, total);
-        if (VARIANT == SGR_VARIANT_PART && S > 0) {
-          float sv[32];
-          int ch;
-          float st;
-          if (S <= 8) {   // uniform: half the values and 9 shuffles instead of 16
+        for (int i = 0; i < PX; ++i)
+          if (f[i].live) bwd_update<VARIANT>(q[i], f[i], r1, r2, r3, r4, pos, gv);
+        {
+          int which;
+          const float total = warp_sum18(gv, lane, which);
+          const uint32_t r = s_id[j];
+          if (which >= 0 && total != 0.f) atomicAdd(grads + (size_t)r * kGradF + which, total);
+          if (VARIANT == SGR_VARIANT_PART && S > 0) {
+            float sv[32];
+            int ch;
+            float st;
+            if (S <= 8) {   // uniform: half the values and 9 shuffles instead of 16
 #pragma unroll
-            for (int c = 0; c < 8; ++c) {
-              float t = 0.f;
+              for (int c = 0; c < 8; ++c) {
+                float t = 0.f;
 #pragma unroll
-              for (int i = 0; i < PX; ++i)
-                if (f[i].live && c < S) t += q[i].sem_w * s_dsem[c][threadIdx.x * PX + i];
-              sv[c] = t;
+                for (int i = 0; i < PX; ++i)
+                  if (f[i].live && c < S) t += q[i].sem_w * s_dsem[c][threadIdx.x * PX + i];
+                sv[c] = t;
+              }
+              st = warp_sum8(sv, lane, ch);
+            } else {
+#pragma unroll
+              for (int c = 0; c < SGR_MAX_SEMANTICS; ++c) {
+                float t = 0.f;
+#pragma unroll
+                for (int i = 0; i < PX; ++i)
+                  if (f[i].live && c < S) t += q[i].sem_w * s_dsem[c][threadIdx.x * PX + i];
+                sv[c] = t;
+              }
+              st = warp_sum16(sv, lane, ch);
             }
-            st = warp_sum8(sv, lane, ch);
-          } else {
-#pragma unroll
-            for (int c = 0; c < SGR_MAX_SEMANTICS; ++c) {
-              float t = 0.f;
-#pragma unroll
-              for (int i = 0; i < PX; ++i)
-                if (f[i].live && c < S) t += q[i].sem_w * s_dsem[c][threadIdx.x * PX + i];
-              sv[c] = t;
-            }
-            st = warp_sum16(sv, lane, ch);
+            if (ch >= 0 && ch < S && st != 0.f) atomicAdd(dL_dsemantics + (size_t)(sid_base + (int)r) * S + ch, st);
           }
-          if (ch >= 0 && ch < S && st != 0.f) atomicAdd(dL_dsemantics + (size_t)(sid_base + (int)r) * S + ch, st);
         }
       }
     }
