@@ -27,6 +27,7 @@
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdint>
 #include <mutex>
 
@@ -374,6 +375,11 @@ template <int NT>
 __host__ __device__ constexpr int epi_warps() { return 4 * (NT >= 64 ? NT / 64 : 1); }
 template <int NT>
 __host__ __device__ constexpr int persist_threads() { return 64 + 32 * epi_warps<NT>(); }
+// CTAs per SM the persistent GEMM is compiled for: as many as tensor memory
+// holds (512 columns, 2 NT per CTA), at most 4 (so 64-column tiles keep their
+// registers at 85 or fewer)
+template <int NT>
+__host__ __device__ constexpr int persist_min_ctas() { return 512 / (2 * NT) < 4 ? 512 / (2 * NT) : 4; }
 
 __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, int x, int y, uint32_t bar) {
   asm volatile(
@@ -405,7 +411,7 @@ __device__ __forceinline__ bool mbar_wait_or_fail(uint32_t bar, uint32_t parity,
 
 // KC: K per chunk, 64 (128-byte swizzle) or 16 (32-byte swizzle, for K <= 16).
 template <int NT, int KC>
-__global__ void __launch_bounds__(persist_threads<NT>(), 1)
+__global__ void __launch_bounds__(persist_threads<NT>(), persist_min_ctas<NT>())
     k_gemm_persist(const sgr_gemm_args a, const __grid_constant__ CUtensorMap map_a,
                    const __grid_constant__ CUtensorMap map_b, int ns) {
   extern __shared__ __align__(1024) uint8_t smem[];
@@ -656,30 +662,52 @@ int launch_persist(const sgr_gemm_args& a, cudaStream_t st) {
   alignas(64) CUtensorMap ma, mb;
   if (!make_map(&ma, a.A, a.M, a.K, a.lda, kTM, KC) || !make_map(&mb, a.B, a.N, a.K, a.ldb, NT, KC))
     return SGR_ERR_CUDA;
-  const int ns = KC == 64 ? kStages : kStages16;
+  // ring stages: a layer whose K is one chunk needs two (the next tile's
+  // operands load while this tile's MMA runs; two accumulators do the rest),
+  // which leaves shared memory for more resident CTAs
+  const long long chunks = (a.K + KC - 1) / KC;
+  const int ns = chunks <= 1 ? 2 : (KC == 64 ? kStages : kStages16);
   const size_t smem = (size_t)ns * (kTM + NT) * KC * 2 + 1024;
-  // per device, once: the shared-memory attribute and the resident CTAs (by
-  // registers and shared memory, and by tensor memory: 512 columns per SM,
-  // 2 NT per CTA; a CTA beyond that would wait in its allocation until
-  // another finished)
+  // per device and ring size, once: the shared-memory attribute and the
+  // resident CTAs per SM, from the kernel's registers and static shared
+  // memory and the SM's limits (register file in 256-register warp
+  // allocations, shared memory with the per-CTA reserve, threads), and from
+  // tensor memory (512 columns, 2 NT per CTA; a CTA beyond that would wait in
+  // its allocation until another finished).  Counted here rather than by the
+  // occupancy calculator, which answered 1 CTA per SM for this kernel where
+  // the SMs ran 3 (ncu: 456 CTAs of the 64-column tile resident at once,
+  // warps active 9% -> 26%, layer time -20%).
   constexpr int kMaxDev = 64;
-  static int resident[kMaxDev] = {};
+  static int resident[kMaxDev][2] = {};
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDev) return SGR_ERR_CUDA;
-  if (resident[dev] == 0) {
-    int sms = 0, per_sm = 0;
-    if (cudaFuncSetAttribute(k_gemm_persist<NT, KC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
-            cudaSuccess ||
+  int& res = resident[dev][ns == 2 ? 0 : 1];
+  if (res == 0) {
+    const int full = KC == 64 ? kStages : kStages16;   // the attribute covers the largest ring
+    cudaFuncAttributes fa{};
+    int sms = 0, smem_sm = 0, reserve = 0, regs_sm = 0, threads_sm = 0;
+    if (cudaFuncSetAttribute(k_gemm_persist<NT, KC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)((size_t)full * (kTM + NT) * KC * 2 + 1024)) != cudaSuccess ||
+        cudaFuncSetAttribute(k_gemm_persist<NT, KC>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                             (int)cudaSharedmemCarveoutMaxShared) != cudaSuccess ||
+        cudaFuncGetAttributes(&fa, k_gemm_persist<NT, KC>) != cudaSuccess ||
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gemm_persist<NT, KC>, persist_threads<NT>(), smem) !=
-            cudaSuccess)
+        cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&reserve, cudaDevAttrReservedSharedMemoryPerBlock, dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&threads_sm, cudaDevAttrMaxThreadsPerMultiProcessor, dev) != cudaSuccess)
       return SGR_ERR_CUDA;
-    per_sm = per_sm < 512 / (2 * NT) ? per_sm : 512 / (2 * NT);
+    constexpr int threads = persist_threads<NT>();
+    const int warp_regs = (fa.numRegs * 32 + 255) / 256 * 256;
+    int per_sm = 512 / (2 * NT);
+    per_sm = std::min(per_sm, regs_sm / std::max(1, warp_regs * (threads / 32)));
+    per_sm = std::min(per_sm, smem_sm / (int)(fa.sharedSizeBytes + smem + (size_t)reserve));
+    per_sm = std::min(per_sm, threads_sm / threads);
     if (per_sm < 1) return SGR_ERR_UNSUPPORTED;
-    resident[dev] = sms * per_sm;
+    res = sms * per_sm;
   }
   const long long tiles = ((a.M + kTM - 1) / kTM) * ((a.N + NT - 1) / NT);
-  const long long grid = tiles < (long long)resident[dev] ? tiles : (long long)resident[dev];
+  const long long grid = tiles < (long long)res ? tiles : (long long)res;
   k_gemm_persist<NT, KC><<<(unsigned)grid, persist_threads<NT>(), smem, st>>>(a, ma, mb, ns);
   sgr::count_launches(1);
   return cudaGetLastError() == cudaSuccess ? SGR_OK : SGR_ERR_CUDA;
