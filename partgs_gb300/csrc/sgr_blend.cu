@@ -166,8 +166,8 @@ __device__ __forceinline__ float blend_rcp(float x) {
 #endif
 }
 
-// The reciprocal of p.z the plain variant's explicit geometry uses: the
-// approximate one (SGR_SPLAT_DIV 2) or the correctly rounded one (0, 1).
+// The reciprocal of p.z the explicit geometry uses: the approximate one
+// (SGR_SPLAT_DIV 2) or the correctly rounded one (0, 1).
 __device__ __forceinline__ float splat_rcp(float z) {
 #if SGR_SPLAT_DIV == 2
   return __fdividef(1.0f, z);
@@ -177,12 +177,13 @@ __device__ __forceinline__ float splat_rcp(float z) {
 }
 
 // ---------------------------------------------------------------------------
-// Fragment geometry of the plain variant in an explicit order of IEEE
-// round-to-nearest operations, for one pixel (float) or for a thread's two
-// pixels at once (float2: the packed FP32 instructions, __ffma2_rn and
-// friends).  Both forms give identical results element by element, so the
-// forward (one pixel per thread) and the packed backward (two) make the
-// same decisions -- the near-plane, power and alpha tests -- bit for bit.
+// Fragment geometry in an explicit order of IEEE round-to-nearest
+// operations, for one pixel (float) or for a thread's two pixels at once
+// (float2: the packed FP32 instructions, __ffma2_rn and friends).  Both forms
+// give identical results element by element, so a forward and a backward in
+// either form make the same decisions -- the near-plane, power and alpha
+// tests -- bit for bit.  The packed blends of both variants use it, and the
+// plain variant's one-pixel forms too.
 // The operations follow P0/cr/forward.cu:349-378: k = px Tw - Tu,
 // l = py Tw - Tv, p = k x l (each component fma(a, b, -(c d))), the filter
 // distance 2 (dx^2 + dy^2), s = p.xy / p.z by one approximate reciprocal,
@@ -371,13 +372,14 @@ __device__ __forceinline__ void cell_list(const GeomView& g, int v, int tx, int 
 // ---------------------------------------------------------------------------
 // CTA shapes.  A thread owns PX pixels of one column, two rows apart, so a
 // warp covers a 16 x (2 PX) strip and a CTA of 256 / PX threads the tile.
-// The backward of the plain variant uses PX = 2: per-entry work (shared-
-// memory loads, the loop, the warp reduction of the gradients) is shared by
-// two pixels.  The forward keeps PX = 1: its pixels terminate independently
-// and it has no reduction to share.  The part variant's backward keeps
-// PX = 1 as well: at 3 CTAs of 256 threads it beats two pixels per thread
-// at 3 or 4 CTAs of 128 (49.5 ms against 56.3 and 50.7 on 500k surfels x 16
-// views, 8 semantic channels).
+// The packed blends (the default, both variants, both directions) use
+// PX = 2: per-entry work (shared-memory loads, the loop, the backward's warp
+// reduction) is shared by two pixels, whose arithmetic runs as the two lanes
+// of FP32x2 instructions.  With packing switched off the forward uses
+// PX = 1 (its pixels terminate independently), the plain backward PX = 2,
+// and the part backward PX = 1 (SGR_PART_BWD_PX): unpacked, 3 CTAs of 256
+// threads beat two pixels per thread at 3 or 4 CTAs of 128 (49.5 ms against
+// 56.3 and 50.7 on 500k surfels x 16 views, 8 semantic channels).
 // ---------------------------------------------------------------------------
 template <int PX_, int WX_ = kTile>
 struct BlendShape {
@@ -1371,8 +1373,8 @@ __device__ __forceinline__ void bwd_update2(BwdPair& q, const BwdGeom2& f, const
   gv[10] = u10.x + u10.y;
 }
 
-// Resident CTAs per SM the plain backward is compiled for (registers per
-// thread = 65536 / (128 threads x this)).
+// Resident CTAs per SM the backward is compiled for (registers per thread =
+// 65536 / (128 threads x this)); the part variant's, packed, as many.
 #ifndef SGR_BWD_MIN_CTAS
 #define SGR_BWD_MIN_CTAS 4
 #endif
