@@ -332,6 +332,84 @@ def time_reference_cuda(workload_name, steps=3, warmup=1, device=None):
                     "GaussianRasterizer, one view at a time; loss and Adam in PyTorch"}
 
 
+def time_part_variant(workload_name, cell_tiles, blend_shape, tile_schedule, semantics=8, steps=3, warmup=1,
+                      with_reference=True, device=None):
+    """The part variant, the rasteriser behind PartGS's ``render_part``
+    (renderer/gaussian_renderer_2d/__init__.py:11-149): this library's and
+    the reference's own (``diff_surfel_rasterization_part``, compiled
+    unmodified by ``oracle/ref_build.py``), forward + backward of every view
+    of the workload against fixed upstream gradients on the colour,
+    auxiliary and semantic maps, with ``semantics`` channels of seeded
+    softmax weights.  This library renders all views in one batched call at
+    the given launch shape; the reference one view at a time, as
+    ``render_part`` calls it.  Returns ms per pass over all views."""
+    import torch
+    from partgs_gb300 import _lib as L
+    from partgs_gb300.batched import MultiViewRasterizer
+    from partgs_gb300.scenes import workload
+    dev = device or torch.device("cuda")
+    scene, cams = workload(workload_name, 0)
+    V, H, W, S = len(cams), cams[0].height, cams[0].width, semantics
+    g = torch.Generator().manual_seed(1)
+    sem = torch.softmax(torch.randn(scene.P, S, generator=g) * 3, -1)
+    inputs = [t.to(dev) for t in (scene.means3D, scene.opacities, scene.shs, scene.scales, scene.rotations, sem)]
+    gr = torch.Generator(device=dev).manual_seed(3)
+    up_c = torch.randn(V, 3, H, W, device=dev, generator=gr)
+    up_o = torch.randn(V, 8, H, W, device=dev, generator=gr) * 0.1
+    up_s = torch.randn(V, S, H, W, device=dev, generator=gr)
+
+    def timed(fn, n):
+        fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(n):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / n
+
+    r = MultiViewRasterizer(cams, [0.0, 0.0, 0.0], scene.sh_degree, variant=L.SGR_VARIANT_PART, num_surfels=scene.P,
+                            device=dev, cell_tiles=cell_tiles, blend_shape=blend_shape, tile_schedule=tile_schedule)
+    leaves = [t.clone().requires_grad_(True) for t in inputs]
+
+    def ours():
+        col, oth, smap, _ = r(leaves[0], leaves[1], leaves[2], leaves[3], leaves[4], semantics=leaves[5])
+        ((col * up_c).sum() + (oth * up_o).sum() + (smap * up_s).sum()).backward()
+
+    for _ in range(warmup):
+        ours()
+    out = {"semantics": S, "views": V, "ours_ms": timed(ours, steps)}
+    if not with_reference:
+        return out
+    from oracle import ref_build, ref_cuda
+    try:
+        if not ref_cuda.available():
+            ref_build.build()
+        mod = ref_cuda.load("part")
+    except Exception as ex:   # sources not staged
+        out["reference_unavailable"] = str(ex)[:200]
+        return out
+    sets = [ref_cuda.settings(mod, c, [0.0, 0.0, 0.0], scene.sh_degree) for c in cams]
+    rl = [t.clone().requires_grad_(True) for t in inputs]
+
+    def reference():
+        for v in range(V):
+            m2 = torch.zeros_like(rl[0], requires_grad=True)
+            color, semantic, _, allmap = mod.GaussianRasterizer(sets[v])(
+                means3D=rl[0], means2D=m2, opacities=rl[1], semantics=rl[5], shs=rl[2], colors_precomp=None,
+                scales=rl[3], rotations=rl[4])
+            ((color * up_c[v]).sum() + (allmap * up_o[v]).sum() + (semantic * up_s[v]).sum()).backward()
+
+    for _ in range(warmup):
+        reference()
+    out["reference_ms"] = timed(reference, steps)
+    out["speedup"] = out["reference_ms"] / out["ours_ms"]
+    out["what"] = ("part rasteriser alone, forward + backward of all views; reference "
+                   "diff_surfel_rasterization_part (unmodified, nvcc -O3 sm_103a), one view at a time")
+    return out
+
+
 def run_gpu(args):
     import torch
     ws, rank, local = _dist()
@@ -459,6 +537,10 @@ def run_gpu(args):
             rc.update(ours_step_ms=ms_per_step, ours_raster_ms=raster_ms,
                       step_speedup=rc["step_ms"] / ms_per_step, raster_speedup=rc["raster_ms"] / raster_ms)
             line["reference_cuda"] = {k: (round(v, 4) if isinstance(v, float) else v) for k, v in rc.items()}
+    if rank == 0 and ws == 1 and not args.no_part:
+        pv = time_part_variant(args.workload, tr.raster.cell_tiles, tr.raster.blend_shape, tr.raster.tile_schedule,
+                               with_reference=not args.no_reference_cuda, device=dev)
+        line["part_variant"] = {k: (round(v, 4) if isinstance(v, float) else v) for k, v in pv.items()}
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         from oracle import cpu_baseline as CB
         procs = os.cpu_count() or 1
@@ -631,6 +713,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-reference-cuda", action="store_true",
                     help="skip timing the reference's CUDA rasteriser on the same workload")
+    ap.add_argument("--no-part", action="store_true",
+                    help="skip timing the part variant's rasteriser (and the reference's) on the same workload")
     ap.add_argument("--cell-tiles", type=int, default=0, choices=[0, 1, 2, 4, 8, 16],
                     help="cell edge in tiles (0: cell edge, warp footprint, tile schedule and staged batch autotuned)")
     ap.add_argument("--blend-shape", type=int, default=0, choices=[0, 1],
