@@ -26,6 +26,7 @@
 // backward's reciprocals are the hardware's approximate ones (splat_exp,
 // blend_rcp): a few 1e-7 relative on alpha, far inside the tolerances.
 #include <algorithm>
+#include <mutex>
 #include <type_traits>
 
 #include "sgr_kernels.cuh"
@@ -1677,6 +1678,13 @@ __global__ void __launch_bounds__(1024) k_tile_order(GeomView g, int n, int back
   for (int i = threadIdx.x; i < n; i += blockDim.x) order[atomicAdd(&s_pos[32 - __clz(cost(i))], 1u)] = (uint32_t)i;
 }
 
+// Host-side launch caches below are shared by every thread that calls the
+// library (ctypes callers run without the interpreter lock).
+std::mutex& launch_cache_mutex() {
+  static std::mutex m;
+  return m;
+}
+
 // Resident CTAs of a kernel on the current device with `dyn` bytes of
 // dynamic shared memory (queried once per kernel, device and size).
 template <class F>
@@ -1693,6 +1701,7 @@ int resident_ctas(F kernel, int threads, size_t dyn = 0) {
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return 0;
   const void* key = reinterpret_cast<const void*>(kernel);
+  std::lock_guard<std::mutex> lock(launch_cache_mutex());
   for (int i = 0; i < used; ++i)
     if (cache[i].kernel == key && cache[i].dev == dev && cache[i].dyn == dyn) return cache[i].ctas;
   int per_sm = 0, sms = 0;
@@ -1726,6 +1735,7 @@ void allow_dynamic_smem(F kernel, int bytes) {
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return;
   const void* key = reinterpret_cast<const void*>(kernel);
+  std::lock_guard<std::mutex> lock(launch_cache_mutex());
   for (int i = 0; i < used; ++i)
     if (done[i].kernel == key && done[i].dev == dev) return;
   cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);

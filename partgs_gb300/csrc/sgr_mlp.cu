@@ -679,8 +679,10 @@ int launch_persist(const sgr_gemm_args& a, cudaStream_t st) {
   // warps active 9% -> 26%, layer time -20%).
   constexpr int kMaxDev = 64;
   static int resident[kMaxDev][2] = {};
+  static std::mutex resident_mutex;   // callers may launch from several host threads
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDev) return SGR_ERR_CUDA;
+  std::unique_lock<std::mutex> lock(resident_mutex);
   int& res = resident[dev][ns == 2 ? 0 : 1];
   if (res == 0) {
     const int full = KC == 64 ? kStages : kStages16;   // the attribute covers the largest ring
@@ -706,8 +708,10 @@ int launch_persist(const sgr_gemm_args& a, cudaStream_t st) {
     if (per_sm < 1) return SGR_ERR_UNSUPPORTED;
     res = sms * per_sm;
   }
+  const int resident_ctas = res;
+  lock.unlock();
   const long long tiles = ((a.M + kTM - 1) / kTM) * ((a.N + NT - 1) / NT);
-  const long long grid = tiles < (long long)res ? tiles : (long long)res;
+  const long long grid = tiles < (long long)resident_ctas ? tiles : (long long)resident_ctas;
   k_gemm_persist<NT, KC><<<(unsigned)grid, persist_threads<NT>(), smem, st>>>(a, ma, mb, ns);
   sgr::count_launches(1);
   return cudaGetLastError() == cudaSuccess ? SGR_OK : SGR_ERR_CUDA;
