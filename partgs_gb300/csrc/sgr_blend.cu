@@ -1738,7 +1738,9 @@ void allow_dynamic_smem(F kernel, int bytes) {
   std::lock_guard<std::mutex> lock(launch_cache_mutex());
   for (int i = 0; i < used; ++i)
     if (done[i].kernel == key && done[i].dev == dev) return;
-  cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  // on failure nothing is recorded: the launch then fails and reports it, and
+  // the next launch tries again
+  if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes) != cudaSuccess) return;
   if (used < kEntries) done[used++] = Entry{key, dev};
 }
 
