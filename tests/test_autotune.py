@@ -120,3 +120,36 @@ def test_blend_tuner_picks_a_pair(sgr_lib):
     assert len(autotune.tune_blend.last_timings) == 8
     for p, q in zip(tr.params(), before):
         assert torch.equal(p.detach(), q)
+
+
+def test_part_variant_without_semantics_matches_with(sgr_lib):
+    """The part variant with no semantic channels (no dynamic shared memory,
+    every semantic loop skipped) renders the same colour and auxiliary maps
+    as with 5 channels, whose weights do not enter them, for every staged
+    batch; gradients of the shared inputs agree up to the order of the float
+    atomics."""
+    from partgs_gb300 import _lib as L
+    from partgs_gb300.batched import MultiViewRasterizer
+    from partgs_gb300.cameras import orbit_cameras
+    from partgs_gb300.scenes import random_surfels
+    sc = random_surfels(3000, seed=54).to("cuda")
+    cams = orbit_cameras(2, 3.0, 80, 112, 55.0, seed=11)
+    g = torch.Generator(device="cuda").manual_seed(6)
+    sem0 = torch.softmax(torch.randn(3000, 5, device="cuda", generator=g) * 2, -1)
+    up_c = torch.randn(2, 3, 80, 112, device="cuda", generator=g)
+    up_o = torch.randn(2, 8, 80, 112, device="cuda", generator=g) * 0.1
+    for stage in (L.SGR_STAGE_DEFAULT, L.SGR_STAGE_SMALL):
+        outs = []
+        for sem in (None, sem0):
+            leaves = [t.clone().requires_grad_(True) for t in (sc.means3D, sc.opacities, sc.shs, sc.scales,
+                                                                sc.rotations)]
+            mv = MultiViewRasterizer(cams, [0.1, 0.2, 0.3], 3, variant=L.SGR_VARIANT_PART, num_surfels=3000,
+                                     tile_schedule=L.SGR_SCHEDULE_QUEUE, stage_entries=stage)
+            img, amap, smap, radii = mv(*leaves, semantics=sem)
+            assert (smap is None) == (sem is None)
+            ((img * up_c).sum() + (amap * up_o).sum()).backward()
+            outs.append((img.detach(), amap.detach(), radii, [t.grad for t in leaves]))
+        (i0, a0, r0, g0), (i1, a1, r1, g1) = outs
+        assert torch.equal(i0, i1) and torch.equal(a0, a1) and torch.equal(r0, r1)
+        for a, b in zip(g0, g1):
+            assert float((a - b).norm() / b.norm()) < 1e-5
