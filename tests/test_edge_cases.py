@@ -1,6 +1,6 @@
-"""Edge cases the reference's API admits: empty inputs, nothing visible,
-precomputed colours and transMats, the scale modifier, the prefiltered
-contract, key-list overflow, near-plane visibility."""
+"""Edge cases the reference's API admits: empty inputs, nothing visible (both
+variants), precomputed colours and transMats, the scale modifier, the
+prefiltered contract, key-list overflow, near-plane visibility."""
 import numpy as np
 import pytest
 import torch
@@ -129,3 +129,38 @@ def test_mark_visible(base):
     vis = dsr.GaussianRasterizer(rs).markVisible(m.cuda()).cpu().numpy()
     np.testing.assert_array_equal(vis, O.mark_visible(m.numpy(), cam.world_view_transform.reshape(-1)))
     assert vis.dtype == bool and (~vis).sum() > 0
+
+
+def test_part_empty_scene_returns_zero_maps(base):
+    """The part drop-in with no surfels: zero colour, semantic and auxiliary
+    maps, no radii (the packed part kernels launch with every list empty)."""
+    import partgs_gb300.diff_surfel_rasterization_part as dsrp
+    _, cam = base
+    x = torch.zeros(0, 3, device="cuda")
+    img, sem, radii, allmap = _render(dsrp, cam, (0.5, 0.5, 0.5), means3D=x, means2D=x,
+                                      opacities=torch.zeros(0, 1, device="cuda"),
+                                      semantics=torch.zeros(0, 6, device="cuda"), colors_precomp=x,
+                                      scales=torch.zeros(0, 2, device="cuda"),
+                                      rotations=torch.zeros(0, 4, device="cuda"))
+    assert img.shape == (3, 64, 64) and float(img.abs().max()) == 0.0
+    assert sem.shape == (6, 64, 64) and float(sem.abs().max()) == 0.0
+    assert allmap.shape == (8, 64, 64) and radii.numel() == 0
+
+
+def test_part_everything_behind_the_camera_gives_background(base):
+    """The part drop-in with every surfel behind the camera: the background,
+    zero semantics and auxiliary maps, and zero gradients."""
+    import partgs_gb300.diff_surfel_rasterization_part as dsrp
+    scene, cam = base
+    sc = scene.to("cuda")
+    campos = torch.as_tensor(cam.camera_center, device="cuda")
+    behind = (campos * 2.0 + (sc.means3D * 0.01)).requires_grad_(True)
+    sem = torch.rand(sc.means3D.shape[0], 6, device="cuda").requires_grad_(True)
+    img, smap, radii, allmap = _render(dsrp, cam, (0.25, 0.5, 0.75), means3D=behind, means2D=torch.zeros_like(behind),
+                                       opacities=sc.opacities, semantics=sem, shs=sc.shs, scales=sc.scales,
+                                       rotations=sc.rotations)
+    assert int((radii > 0).sum()) == 0
+    np.testing.assert_allclose(img.detach().cpu().numpy().reshape(3, -1).mean(1), [0.25, 0.5, 0.75], atol=1e-7)
+    assert float(smap.detach().abs().max()) == 0.0 and float(allmap.detach().abs().max()) == 0.0
+    (img.sum() + smap.sum() + allmap.sum()).backward()
+    assert float(behind.grad.abs().max()) == 0.0 and float(sem.grad.abs().max()) == 0.0
