@@ -622,7 +622,7 @@ def run_multiscene(args):
     cell = min(tune, key=tune.get)[0]
     for shape in (0, 1):
         for sched in (0, 1):
-            for stage in (L.SGR_STAGE_DEFAULT, L.SGR_STAGE_SMALL):
+            for stage in (L.SGR_STAGE_DEFAULT, L.SGR_STAGE_SMALL, L.SGR_STAGE_TINY):
                 if (cell, shape, sched, stage) not in tune:
                     r = make(cell, shape, sched, stage)
                     step(r, w_dev)
@@ -721,7 +721,7 @@ def main():
                     help="with --cell-tiles: the blends' warp footprint (0: 16x2 strips, 1: 8-wide patches)")
     ap.add_argument("--tile-schedule", type=int, default=0, choices=[0, 1],
                     help="with --cell-tiles: 0 a CTA per tile, 1 persistent CTAs on a tile queue")
-    ap.add_argument("--stage-entries", type=int, default=0, choices=[0, 128, 256],
+    ap.add_argument("--stage-entries", type=int, default=0, choices=[0, 64, 128, 256],
                     help="with --cell-tiles: list entries per staged batch of the blends (0: 256)")
     args = ap.parse_args()
     if args.warmup < 3:

@@ -98,6 +98,7 @@ extern "C" {
  * the same entries in the same order, so images and gradients are the same. */
 #define SGR_STAGE_DEFAULT 256
 #define SGR_STAGE_SMALL 128
+#define SGR_STAGE_TINY 64
 
 #define SGR_VARIANT_PLAIN 0
 #define SGR_VARIANT_PART 1
@@ -159,8 +160,9 @@ typedef struct sgr_batch {
                                         SGR_BLEND_PATCH8 (results identical; speed depends on splat sizes) */
     int32_t tile_schedule;           /* SGR_SCHEDULE_GRID (one CTA per tile) or SGR_SCHEDULE_QUEUE (persistent
                                         CTAs take tiles from a device queue, longest estimated first) */
-    int32_t stage_entries;           /* 0 (the library's choice), SGR_STAGE_DEFAULT or SGR_STAGE_SMALL: list
-                                        entries per staged batch of the blends (results identical) */
+    int32_t stage_entries;           /* 0 (the library's choice), SGR_STAGE_DEFAULT, SGR_STAGE_SMALL or
+                                        SGR_STAGE_TINY: list entries per staged batch of the blends (results
+                                        identical) */
 } sgr_batch;
 
 /* Workspace sizes and the layout of the geometry workspace. */

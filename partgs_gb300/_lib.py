@@ -26,6 +26,7 @@ SGR_SCHEDULE_GRID = 0
 SGR_SCHEDULE_QUEUE = 1
 SGR_STAGE_DEFAULT = 256
 SGR_STAGE_SMALL = 128
+SGR_STAGE_TINY = 64
 SGR_VARIANT_PLAIN = 0
 SGR_VARIANT_PART = 1
 SGR_MAX_SEMANTICS = 16

@@ -13,7 +13,7 @@ Four knobs change speed but not results:
 * the tile schedule: one CTA per tile, or persistent CTAs taking tiles from
   a device queue in decreasing order of estimated cost (uneven scenes).
 * the staged batch (``stage_entries``): how many list entries the blends
-  copy into shared memory between two CTA barriers, 256 or 128.  Larger
+  copy into shared memory between two CTA barriers, 256, 128 or 64.  Larger
   batches mean fewer barriers; smaller ones less shared memory per CTA and
   less waiting at each barrier for the warp with the most work.
 
@@ -32,7 +32,7 @@ from . import _lib as L
 CANDIDATES = (2, 4, 8, 16)
 SHAPES = (L.SGR_BLEND_STRIP16, L.SGR_BLEND_PATCH8)
 SCHEDULES = (L.SGR_SCHEDULE_GRID, L.SGR_SCHEDULE_QUEUE)
-STAGES = (L.SGR_STAGE_DEFAULT, L.SGR_STAGE_SMALL)
+STAGES = (L.SGR_STAGE_DEFAULT, L.SGR_STAGE_SMALL, L.SGR_STAGE_TINY)
 _CACHE: dict = {}
 
 

@@ -58,7 +58,8 @@ int check_batch(const sgr_batch* b) {
   if (b->variant == SGR_VARIANT_PLAIN && b->semantic_channels != 0) return SGR_ERR_INVALID_ARGUMENT;
   if (b->blend_shape != SGR_BLEND_STRIP16 && b->blend_shape != SGR_BLEND_PATCH8) return SGR_ERR_INVALID_ARGUMENT;
   if (b->tile_schedule != SGR_SCHEDULE_GRID && b->tile_schedule != SGR_SCHEDULE_QUEUE) return SGR_ERR_INVALID_ARGUMENT;
-  if (b->stage_entries != 0 && b->stage_entries != SGR_STAGE_DEFAULT && b->stage_entries != SGR_STAGE_SMALL)
+  if (b->stage_entries != 0 && b->stage_entries != SGR_STAGE_DEFAULT && b->stage_entries != SGR_STAGE_SMALL &&
+      b->stage_entries != SGR_STAGE_TINY)
     return SGR_ERR_INVALID_ARGUMENT;
   if (!b->scenes || !b->views || !b->viewmatrix || !b->projmatrix || !b->campos || !b->background)
     return SGR_ERR_INVALID_ARGUMENT;

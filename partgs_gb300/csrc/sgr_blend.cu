@@ -37,11 +37,12 @@ namespace {
 
 constexpr int kWarps = kBlock / 32;
 // Entries per staged batch of the blends (sgr_batch.stage_entries): the
-// default, and the smaller option.
-constexpr int kStageDefault = 256, kStageSmall = 128;
+// default, and the smaller options.
+constexpr int kStageDefault = 256, kStageSmall = 128, kStageTiny = 64;
 constexpr int kRing = 2048;            // ring of streamed list entries: >= a batch + kChunk, a power of two
 static_assert(kRing >= kStageDefault + kChunk && (kRing & (kRing - 1)) == 0, "ring size");
-static_assert(kStageDefault <= 256 && kStageSmall <= kStageDefault, "staged slots are indexed by uint8_t");
+static_assert(kStageDefault <= 256 && kStageTiny <= kStageSmall && kStageSmall <= kStageDefault,
+              "staged slots are indexed by uint8_t");
 
 struct Strip {
   float x0, x1;       // pixel-centre x range of the tile
@@ -1782,7 +1783,8 @@ void launch_bwd(const sgr_batch& b, const GeomView& g, const sgr_bwd_inputs& in,
 // per SM; the 128-entry one needs 43 KB and fits 4 (measured at 16 channels:
 // forward 19.4 -> 16.3 ms, backward unchanged).
 inline int stage_entries_of(const sgr_batch& b) {
-  if (b.stage_entries == SGR_STAGE_SMALL || b.stage_entries == SGR_STAGE_DEFAULT) return b.stage_entries;
+  if (b.stage_entries == SGR_STAGE_SMALL || b.stage_entries == SGR_STAGE_DEFAULT || b.stage_entries == SGR_STAGE_TINY)
+    return b.stage_entries;
   return (b.variant == SGR_VARIANT_PART && b.semantic_channels > 12) ? SGR_STAGE_SMALL : SGR_STAGE_DEFAULT;
 }
 
@@ -1791,12 +1793,17 @@ inline int stage_entries_of(const sgr_batch& b) {
 template <class Fn>
 void with_blend_shape(const sgr_batch& b, Fn&& fn) {
   using std::integral_constant;
-  static_assert(kStageSmall == SGR_STAGE_SMALL && kStageDefault == SGR_STAGE_DEFAULT, "staged batch sizes");
+  static_assert(kStageSmall == SGR_STAGE_SMALL && kStageDefault == SGR_STAGE_DEFAULT && kStageTiny == SGR_STAGE_TINY,
+                "staged batch sizes");
   const bool narrow = b.blend_shape == SGR_BLEND_PATCH8;
-  const bool small = stage_entries_of(b) == SGR_STAGE_SMALL;
+  const int stage = stage_entries_of(b);
   auto by_stage = [&](auto variant, auto wx) {
-    small ? fn(variant, wx, integral_constant<int, kStageSmall>{})
-          : fn(variant, wx, integral_constant<int, kStageDefault>{});
+    if (stage == kStageSmall)
+      fn(variant, wx, integral_constant<int, kStageSmall>{});
+    else if (stage == kStageTiny)
+      fn(variant, wx, integral_constant<int, kStageTiny>{});
+    else
+      fn(variant, wx, integral_constant<int, kStageDefault>{});
   };
   auto by_width = [&](auto variant) {
     narrow ? by_stage(variant, integral_constant<int, 8>{}) : by_stage(variant, integral_constant<int, kTile>{});

@@ -122,7 +122,8 @@ def main(argv=None):
     ap.add_argument("--cell-tiles", type=int, default=0)
     ap.add_argument("--blend-shape", type=int, default=0, help="0: 16-wide warp strips, 1: 8-wide patches")
     ap.add_argument("--tile-schedule", type=int, default=0, help="0: a CTA per tile, 1: persistent tile queue")
-    ap.add_argument("--stage-entries", type=int, default=0, help="list entries per staged batch: 0 (256) or 128")
+    ap.add_argument("--stage-entries", type=int, default=0,
+                    help="list entries per staged batch: 0 (the library's choice), 256, 128 or 64")
     ap.add_argument("--multi-scene", action="store_true")
     ap.add_argument("--scenes", type=int, default=32)
     a = ap.parse_args(argv)

@@ -62,8 +62,9 @@ def test_invalid_arguments_rejected_without_touching_the_gpu(sgr_lib):
     b.scales = b.rotations = 16
     assert sgr_lib.sgr_query_sizes(C.byref(b), 0, C.byref(sizes)) == 2      # more than 16 SH coefficients
     b.sh_coeffs = 16
-    for stage, rc in ((64, 1), (512, 1), (L.SGR_STAGE_SMALL, 0), (L.SGR_STAGE_DEFAULT, 0), (0, 0)):
-        b.stage_entries = stage                                             # staged batch: 0, 256 or 128
+    for stage, rc in ((32, 1), (512, 1), (L.SGR_STAGE_TINY, 0), (L.SGR_STAGE_SMALL, 0), (L.SGR_STAGE_DEFAULT, 0),
+                      (0, 0)):
+        b.stage_entries = stage                                             # staged batch: 0, 256, 128 or 64
         assert sgr_lib.sgr_query_sizes(C.byref(b), 0, C.byref(sizes)) == rc, stage
     assert sgr_lib.sgr_mark_visible(-1, None, None, None, None, None) == 1
     assert sgr_lib.sgr_mark_visible(0, None, None, None, None, None) == 0

@@ -56,7 +56,7 @@ def test_warp_footprint_and_schedule_do_not_change_the_results(sgr_lib):
     outs = []
     for shape in (L.SGR_BLEND_STRIP16, L.SGR_BLEND_PATCH8):
         for sched in (L.SGR_SCHEDULE_GRID, L.SGR_SCHEDULE_QUEUE):
-            for stage in (L.SGR_STAGE_DEFAULT, L.SGR_STAGE_SMALL):
+            for stage in (L.SGR_STAGE_DEFAULT, L.SGR_STAGE_SMALL, L.SGR_STAGE_TINY):
                 leaves = [t.clone().requires_grad_(True) for t in (sc.means3D, sc.opacities, sc.shs, sc.scales,
                                                                     sc.rotations)]
                 mv = MultiViewRasterizer(cams, [0.1, 0.2, 0.3], 3, num_surfels=3000, blend_shape=shape,
@@ -90,7 +90,7 @@ def test_part_variant_launch_options_do_not_change_the_results(sgr_lib, channels
     outs = []
     for shape in (L.SGR_BLEND_STRIP16, L.SGR_BLEND_PATCH8):
         for sched in (L.SGR_SCHEDULE_GRID, L.SGR_SCHEDULE_QUEUE):
-            for stage in (L.SGR_STAGE_DEFAULT, L.SGR_STAGE_SMALL):
+            for stage in (L.SGR_STAGE_DEFAULT, L.SGR_STAGE_SMALL, L.SGR_STAGE_TINY):
                 leaves = [t.clone().requires_grad_(True) for t in (sc.means3D, sc.opacities, sc.shs, sc.scales,
                                                                     sc.rotations)]
                 sem = sem0.clone().requires_grad_(True)
@@ -117,7 +117,7 @@ def test_blend_tuner_picks_a_pair(sgr_lib):
     before = [p.detach().clone() for p in tr.params()]
     best = autotune.tune_blend(tr, targets, steps=2)
     assert best == (tr.raster.blend_shape, tr.raster.tile_schedule, tr.raster.stage_entries)
-    assert len(autotune.tune_blend.last_timings) == 8
+    assert len(autotune.tune_blend.last_timings) == 12
     for p, q in zip(tr.params(), before):
         assert torch.equal(p.detach(), q)
 
@@ -138,7 +138,7 @@ def test_part_variant_without_semantics_matches_with(sgr_lib):
     sem0 = torch.softmax(torch.randn(3000, 5, device="cuda", generator=g) * 2, -1)
     up_c = torch.randn(2, 3, 80, 112, device="cuda", generator=g)
     up_o = torch.randn(2, 8, 80, 112, device="cuda", generator=g) * 0.1
-    for stage in (L.SGR_STAGE_DEFAULT, L.SGR_STAGE_SMALL):
+    for stage in (L.SGR_STAGE_DEFAULT, L.SGR_STAGE_SMALL, L.SGR_STAGE_TINY):
         outs = []
         for sem in (None, sem0):
             leaves = [t.clone().requires_grad_(True) for t in (sc.means3D, sc.opacities, sc.shs, sc.scales,
